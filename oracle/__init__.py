@@ -1,0 +1,21 @@
+"""CPU oracle for the periodic GPW SCF hot path of hqc (ZihangL/hqc v0.1.12).
+
+TEST INFRASTRUCTURE ONLY.  Nothing in the ``hqc_gb300`` product imports this
+package; only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg
+of ``bench.py`` use it, and only as the checker.
+
+It is a NumPy float64 restatement of the reference algorithm, written in the
+streamed (real-space) form: AO values on the grid, rho(r) = sum_pq D_pq
+phi_p phi_q, FFT Poisson for Hartree, occupied-pair-density FFT exchange plus
+the reference's G=0 Madelung term, LDA xc, and the reference's DIIS / fixed
+point SCF with its smearing and chemical-potential search quirks.  On the odd
+grids the reference supports, this form is identical by Parseval to the
+reference's rhoG/ERI formulation (``hqc/pbc/solver.py:391-479``).
+
+Parity pin: ``tests/golden/*.npz`` hold outputs of the reference's own
+unmodified source, executed by ``tests/golden/make_golden.py`` over a NumPy
+stand-in for the JAX API subset it uses.  ``tests/test_oracle_golden.py``
+checks this oracle against those vectors.  The features the reference lacks
+(GGA-PBE, analytic forces) are checked by internal identities only (central
+finite differences, the uniform-gas limit) and are "parity unpinned".
+"""

@@ -1,0 +1,201 @@
+"""Generate golden vectors by running the reference ``hqc`` package itself.
+
+The reference (ZihangL/hqc v0.1.12) is pure Python on top of JAX.  jaxlib is
+not installable here, so this script puts ``tests/golden/_jaxshim`` (a NumPy
+stand-in for the JAX API subset the reference uses, see its ``_core.py``) in
+front of ``sys.path`` and imports the reference's unmodified sources from the
+read-only checkout.  Every number written below is therefore produced by the
+reference's own code path: ``hqc/pbc/solver.py`` (make_solver and its
+hf_gamma / dft_gamma / hf_kpt / dft_kpt drivers), ``hqc/pbc/scf.py``,
+``hqc/tools/smearing.py``, ``hqc/tools/excor.py``, ``hqc/pbc/gto.py``,
+``hqc/pbc/potential.py``, ``hqc/pbc/lcao.py`` and ``hqc/pbc/pes.py``.
+
+Positions come from ``numpy.random.default_rng(seed)`` (JAX's PRNG stream is
+not reproducible without jaxlib).  Output: one ``.npz`` per case in this
+folder plus ``manifest.json``.  Run from the repository root:
+
+    python tests/golden/make_golden.py [case-name ...]
+"""
+import json
+import os
+import sys
+import time
+import warnings
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REFERENCE = "/root/reference"
+sys.path.insert(0, os.path.join(HERE, "_jaxshim"))
+sys.path.insert(0, REFERENCE)
+warnings.filterwarnings("ignore")
+
+import jax.numpy as jnp  # noqa: E402  (the stand-in)
+from hqc.pbc.solver import make_solver  # noqa: E402
+from hqc.pbc.lcao import make_lcao  # noqa: E402
+from hqc.pbc.pes import make_pes  # noqa: E402
+from hqc.pbc.gto import make_pbc_gto  # noqa: E402
+from hqc.pbc.potential import potential_energy_pp  # noqa: E402
+
+
+def box(n):
+    return (4.0 / 3.0 * np.pi * n) ** (1.0 / 3.0)
+
+
+def uniform_positions(n, seed):
+    return np.random.default_rng(seed).uniform(0.0, box(n), (n, 3))
+
+
+def bcc_positions(ncell):
+    """bcc lattice, ``ncell``^3 conventional cells, in rs units."""
+    n = 2 * ncell ** 3
+    a = box(n) / ncell
+    pts = []
+    for i in range(ncell):
+        for j in range(ncell):
+            for k in range(ncell):
+                pts.append([i, j, k])
+                pts.append([i + 0.5, j + 0.5, k + 0.5])
+    return np.array(pts) * a
+
+
+SOLVER_KEYS = ("mo_coeff", "dm", "bands", "E", "Ki", "Vep", "Vee", "Se", "converged")
+
+# name -> (factory, n, rs, basis, seed, kwargs)
+SOLVER_CASES = {
+    "hf_szv_diis": ("solver", 4, 1.5, "gth-szv", 42, dict(grid_length=0.12, tol=1e-8)),
+    "hf_dzv_diis": ("solver", 4, 1.5, "gth-dzv", 42, dict(grid_length=0.12, tol=1e-8)),
+    "hf_dzvp_diis": ("solver", 4, 1.5, "gth-dzvp", 42, dict(grid_length=0.12, tol=1e-8)),
+    "hf_dzv_fp": ("solver", 4, 1.5, "gth-dzv", 42,
+                  dict(grid_length=0.12, tol=1e-10, diis=False)),
+    "hf_dzv_fermi_bisect": ("solver", 4, 1.5, "gth-dzv", 42,
+                            dict(grid_length=0.12, tol=1e-8, smearing=True,
+                                 smearing_method="fermi", smearing_sigma=0.1)),
+    "hf_dzv_gauss_bisect": ("solver", 4, 1.5, "gth-dzv", 42,
+                            dict(grid_length=0.12, tol=1e-8, smearing=True,
+                                 smearing_method="gauss", smearing_sigma=0.05)),
+    "hf_dzv_fermi_newton": ("lcao", 4, 1.5, "gth-dzv", 42,
+                            dict(grid_length=0.12, tol=1e-8, smearing=True,
+                                 smearing_method="fermi", smearing_sigma=0.1)),
+    "hf_h8_szv_41": ("solver", 8, 1.25, "gth-szv", 42,
+                     dict(grid_length=box(8) * 1.25 / 40.0, tol=1e-8)),
+    "dft_dzv_lda": ("solver", 4, 1.5, "gth-dzv", 42,
+                    dict(grid_length=0.2, tol=1e-8, dft=True, xc="lda,vwn")),
+    "dft_dzv_lda_fermi": ("solver", 4, 1.5, "gth-dzv", 42,
+                          dict(grid_length=0.2, tol=1e-8, dft=True, xc="lda,vwn",
+                               smearing=True, smearing_method="fermi",
+                               smearing_sigma=0.1)),
+    "dft_szv_lda_gauss": ("solver", 4, 1.5, "gth-szv", 7,
+                          dict(grid_length=0.2, tol=1e-8, dft=True, xc="lda,vwn",
+                               smearing=True, smearing_method="gauss",
+                               smearing_sigma=0.05)),
+    "dft_szv_lda_hl": ("solver", 4, 1.5, "gth-szv", 7,
+                       dict(grid_length=0.2, tol=1e-8, dft=True, xc="lda,hl")),
+    "dft_szv_lda_x": ("solver", 4, 1.5, "gth-szv", 7,
+                      dict(grid_length=0.2, tol=1e-8, dft=True, xc="lda,")),
+    "dft_dzvp_lda": ("solver", 4, 1.5, "gth-dzvp", 42,
+                     dict(grid_length=0.25, tol=1e-8, dft=True, xc="lda,vwn")),
+    "hf_h8_dzv_gauss_bisect": ("solver", 8, 1.4, "gth-dzv", 1,
+                               dict(grid_length=box(8) * 1.4 / 24.0, tol=1e-8,
+                                    smearing=True, smearing_method="gauss",
+                                    smearing_sigma=0.5 * 10000 / 157888.09)),
+    "pes_dev_hf_dzv": ("pes", 4, 1.5, "gth-dzv", 42,
+                       dict(grid_length=0.12, tol=1e-8, mode="dev")),
+    "hf_kpt_dzv": ("solver", 4, 1.5, "gth-dzv", 42,
+                   dict(grid_length=0.2, tol=1e-8, gamma=False)),
+    "dft_kpt_dzv": ("solver", 4, 1.5, "gth-dzv", 42,
+                    dict(grid_length=0.2, tol=1e-8, gamma=False, dft=True)),
+}
+
+
+def run_solver_case(name):
+    factory, n, rs, basis, seed, kw = SOLVER_CASES[name]
+    L = box(n)
+    xp = uniform_positions(n, seed)
+    kpt = None
+    if not kw.get("gamma", True):
+        kpt = np.random.default_rng(seed + 1).uniform(-np.pi / L / rs, np.pi / L / rs, 3)
+    t0 = time.time()
+    if factory == "solver":
+        f = make_solver(n, L, rs, basis, **kw)
+    elif factory == "lcao":
+        f = make_lcao(n, L, rs, basis, **kw)
+    else:
+        f = make_pes(n, L, rs, basis, **kw)
+    args = (jnp.array(xp.copy()),) if kpt is None else (jnp.array(xp.copy()), jnp.array(kpt))
+    out = f(*args)
+    rec = dict(xp=xp, n=n, rs=rs, L=L)
+    if kpt is not None:
+        rec["kpt"] = kpt
+    if factory == "solver":
+        for k, v in zip(SOLVER_KEYS, out):
+            rec[k] = np.asarray(v)
+    elif factory == "lcao":
+        for k, v in zip(("mo_coeff", "bands", "E"), out):
+            rec[k] = np.asarray(v)
+    else:
+        for k, v in zip(("Etot", "Ki", "Vep", "Vee", "Vpp", "Se", "converged"), out):
+            rec[k] = np.asarray(v)
+    meta = dict(factory=factory, n=n, rs=rs, basis=basis, seed=seed, kwargs=kw,
+                seconds=round(time.time() - t0, 2))
+    return rec, meta
+
+
+def run_gto_case():
+    """eval_pbc_ao values (``hqc/pbc/gto.py:357-369``) at random electrons."""
+    n, rs = 8, 1.5
+    L = box(n) * rs
+    rng = np.random.default_rng(43)
+    xp = rng.uniform(0.0, L, (n, 3))
+    xe = rng.uniform(0.0, L, (16, 3))
+    rec = dict(xp=xp, xe=xe, L=L)
+    for basis in ("gth-szv", "gth-dzv", "gth-dzvp"):
+        f = make_pbc_gto(basis, L)
+        vals = np.stack([np.asarray(f(jnp.array(xp), jnp.array(e))) for e in xe])
+        rec["ao_" + basis.replace("-", "_")] = vals
+    return rec, dict(n=n, rs=rs, seeds=43)
+
+
+def run_vpp_case():
+    """potential_energy_pp (``hqc/pbc/potential.py:103-130``)."""
+    rec = {}
+    meta = {}
+    # (tag, positions (rs units), rs)
+    cases = [("n14", uniform_positions(14, 42), 1.31),
+             ("n1", np.array([[0.3, 0.2, 0.1]]), 1.0),
+             ("bcc16", bcc_positions(2), 1.31),
+             ("n8", uniform_positions(8, 5), 1.25)]
+    for tag, xp, rs in cases:
+        n = xp.shape[0]
+        L = box(n)
+        rec["xp_" + tag] = xp
+        rec["vpp_" + tag] = np.asarray(potential_energy_pp(jnp.array(xp.copy()), L, rs))
+        rec["rs_" + tag] = np.asarray(rs)
+        meta[tag] = dict(n=n, rs=rs)
+    return rec, meta
+
+
+def main(selected):
+    manifest_path = os.path.join(HERE, "manifest.json")
+    manifest = json.load(open(manifest_path)) if os.path.exists(manifest_path) else {}
+    jobs = list(SOLVER_CASES) + ["gto_values", "vpp"]
+    if selected:
+        jobs = [j for j in jobs if j in selected]
+    for name in jobs:
+        t0 = time.time()
+        if name == "gto_values":
+            rec, meta = run_gto_case()
+        elif name == "vpp":
+            rec, meta = run_vpp_case()
+        else:
+            rec, meta = run_solver_case(name)
+        np.savez(os.path.join(HERE, name + ".npz"), **rec)
+        manifest[name] = meta
+        print(f"{name}: {time.time() - t0:.1f}s", {k: rec[k] for k in ("E", "converged") if k in rec},
+              flush=True)
+        with open(manifest_path, "w") as fh:
+            json.dump(manifest, fh, indent=1, sort_keys=True)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])

@@ -1,0 +1,93 @@
+"""The CPU oracle against golden vectors produced by the reference's own code.
+
+Tolerances: the fixtures and the oracle are both float64 on the CPU, so the
+converged quantities agree to rounding plus SCF-stopping noise (tol 1e-8 in
+the fixtures): 1e-9 Ry in energies, 1e-7 in bands/dm.
+"""
+import numpy as np
+import pytest
+
+from conftest import load_golden
+from oracle.gpw import Solver, Setup
+from oracle.ewald import vpp
+
+CONVERGED = ["hf_szv_diis", "hf_dzv_diis", "hf_dzvp_diis", "hf_dzv_fp", "hf_dzv_fermi_bisect",
+             "hf_dzv_fermi_newton", "hf_h8_szv_41", "dft_dzv_lda", "dft_dzv_lda_fermi",
+             "dft_szv_lda_gauss", "dft_szv_lda_hl", "dft_szv_lda_x", "dft_dzvp_lda"]
+
+
+def run_case(name):
+    meta, z = load_golden(name)
+    kw = dict(meta["kwargs"])
+    kw.pop("mode", None)
+    if meta["factory"] == "lcao":
+        kw.setdefault("search_method", "newton")
+    s = Solver(meta["n"], float(z["L"]), meta["rs"], meta["basis"], **kw)
+    return s, s.solve(z["xp"]), z
+
+
+@pytest.mark.parametrize("name", CONVERGED)
+def test_solver_matches_reference(name):
+    s, out, z = run_case(name)
+    if "converged" in z.files:
+        assert bool(out[8]) == bool(z["converged"])
+    assert abs(out[3] - z["E"]) < 1e-9
+    np.testing.assert_allclose(out[2], z["bands"], atol=1e-7)
+    if "dm" in z.files:
+        np.testing.assert_allclose(out[1], z["dm"], atol=1e-7)
+        for k, i in (("Ki", 4), ("Vep", 5), ("Vee", 6), ("Se", 7)):
+            assert abs(out[i] - z[k]) < 1e-8, k
+
+
+@pytest.mark.parametrize("name", ["hf_dzv_gauss_bisect", "hf_h8_dzv_gauss_bisect"])
+def test_gauss_smearing_quirk_not_converged(name):
+    """Gaussian occupations are capped at 1 in the reference (smearing.py:52);
+    with HF these cases do not converge there (max_cycle reached), and the
+    oracle reports the same."""
+    s, out, z = run_case(name)
+    assert not bool(z["converged"]) and not bool(out[8])
+
+
+def test_pes_dev_matches_reference():
+    meta, z = load_golden("pes_dev_hf_dzv")
+    kw = dict(meta["kwargs"])
+    kw.pop("mode")
+    s = Solver(meta["n"], float(z["L"]), meta["rs"], meta["basis"], **kw)
+    out = s.solve(z["xp"])
+    v = vpp(z["xp"], float(z["L"]), meta["rs"])
+    assert abs(out[3] + v - z["Etot"]) < 1e-9
+    assert abs(v - z["Vpp"]) < 1e-10
+
+
+def test_gto_values_match_reference():
+    meta, z = load_golden("gto_values")
+    L = float(z["L"])
+    for basis in ("gth-szv", "gth-dzv", "gth-dzvp"):
+        st = Setup(meta["n"], L / meta["rs"], meta["rs"], basis, n_grid=5)
+        ref = z["ao_" + basis.replace("-", "_")]
+        b = st.basis
+        xp, xe = z["xp"], z["xe"]
+        # evaluate the lattice-summed AOs at arbitrary points
+        out = np.zeros_like(ref)
+        for e, r in enumerate(xe):
+            for A in range(xp.shape[0]):
+                u = r[:, None] - xp[A][:, None] - st.lat1d[None, :]  # (3, t)
+                g = np.exp(-b.alpha[None, :, None] * u[:, None, :] ** 2)  # (3,a,t)
+                g0 = g.sum(-1)
+                g1 = (g * u[:, None, :]).sum(-1)
+                for k in range(b.nao):
+                    f = [g0[d] if not (b.l[k] == 1 and b.cart[k] == d) else g1[d] for d in range(3)]
+                    out[e, A * b.nao + k] = np.sum(b.coef[k] * f[0] * f[1] * f[2])
+        np.testing.assert_allclose(out, ref, atol=1e-12, rtol=1e-10)
+
+
+def test_vpp_matches_reference_and_madelung():
+    _, z = load_golden("vpp")
+    box = lambda n: (4 / 3 * np.pi * n) ** (1 / 3)
+    for tag in ("n14", "n1", "bcc16", "n8"):
+        xp = z["xp_" + tag]
+        n = xp.shape[0]
+        assert abs(vpp(xp, box(n), float(z["rs_" + tag])) - z["vpp_" + tag]) < 1e-10
+    # known answers: simple-cubic and bcc Madelung energies
+    assert abs(z["vpp_n1"] - (-2.8372974794806 / box(1))) < 1e-9
+    assert abs(z["vpp_bcc16"] - (-16 * 1.791858520 / 1.31)) < 1e-6
