@@ -1,0 +1,93 @@
+"""ctypes binding of ``libhqcgb.so`` (the C ABI declared in ``include/hqcgb.h``).
+
+The product has no CPU fallback: if the library is missing or cannot be
+loaded, every entry point raises.  Build it with ``python -m hqc_gb300.build``
+(``__graft_entry__.build()`` does the same).
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libhqcgb.so")
+
+c_double_p = ctypes.POINTER(ctypes.c_double)
+c_int_p = ctypes.POINTER(ctypes.c_int)
+
+STATUS = {0: "OK", 1: "NOT_CONVERGED", 2: "BAD_ARG", 3: "CUDA_ERROR", 4: "EIG_FAIL", 5: "NAN",
+          6: "NO_STATE"}
+XC = {"lda,": 0, "lda,vwn": 1, "lda,hl": 2, "lda,hl71": 2, "lda,bh": 3, "lda,bh72": 3,
+      "lda,gl": 4, "lda,gl77": 4, "pbe": 10, "gga_x_pbe,gga_c_pbe": 10, "pbe,pbe": 10}
+
+
+class Params(ctypes.Structure):
+    _fields_ = [
+        ("n_atoms", ctypes.c_int), ("n_grid", ctypes.c_int), ("L", ctypes.c_double),
+        ("nao_atom", ctypes.c_int), ("n_prim", ctypes.c_int),
+        ("alpha", c_double_p), ("coef", c_double_p), ("ao_l", c_int_p), ("ao_cart", c_int_p),
+        ("n_lat1d", ctypes.c_int), ("lat1d", c_double_p),
+        ("n_lattice", ctypes.c_int), ("lattice", c_double_p),
+        ("dft", ctypes.c_int), ("xc", ctypes.c_int), ("smearing", ctypes.c_int),
+        ("smearing_method", ctypes.c_int), ("smearing_sigma", ctypes.c_double),
+        ("search_method", ctypes.c_int), ("search_cycle", ctypes.c_int),
+        ("search_tol", ctypes.c_double), ("tol", ctypes.c_double), ("max_cycle", ctypes.c_int),
+        ("diis", ctypes.c_int), ("diis_space", ctypes.c_int), ("diis_start_cycle", ctypes.c_int),
+        ("diis_damp", ctypes.c_double), ("precision", ctypes.c_int),
+        ("exx_occ_threshold", ctypes.c_double), ("want_forces", ctypes.c_int),
+    ]
+
+
+class ScfOut(ctypes.Structure):
+    _fields_ = [("mo_coeff", ctypes.c_void_p), ("dm", ctypes.c_void_p), ("bands", ctypes.c_void_p),
+                ("energies", ctypes.c_void_p), ("converged", ctypes.c_void_p),
+                ("iterations", ctypes.c_void_p)]
+
+
+EXPORTS = ("hqcgb_plan_create", "hqcgb_plan_destroy", "hqcgb_scf", "hqcgb_scf_batch",
+           "hqcgb_forces", "hqcgb_ewald", "hqcgb_plan_query", "hqcgb_last_error",
+           "hqcgb_launch_count")
+
+_lib = None
+
+
+class HqcgbError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"hqcgb {STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+def load():
+    """Load the engine; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: build the CUDA engine with "
+                           "`python -m hqc_gb300.build` (there is no CPU fallback)")
+    lib = ctypes.CDLL(LIB_PATH)
+    lib.hqcgb_plan_create.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(ctypes.c_void_p)]
+    lib.hqcgb_plan_destroy.argtypes = [ctypes.c_void_p]
+    lib.hqcgb_scf.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ScfOut),
+                              ctypes.c_void_p]
+    lib.hqcgb_scf_batch.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                    ctypes.POINTER(ScfOut), ctypes.c_void_p]
+    lib.hqcgb_forces.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    lib.hqcgb_ewald.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                ctypes.c_double, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                ctypes.c_void_p]
+    lib.hqcgb_plan_query.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p,
+                                     ctypes.c_size_t, ctypes.c_void_p]
+    lib.hqcgb_plan_query.restype = ctypes.c_longlong
+    lib.hqcgb_last_error.restype = ctypes.c_char_p
+    lib.hqcgb_launch_count.argtypes = [ctypes.c_int]
+    lib.hqcgb_launch_count.restype = ctypes.c_longlong
+    for name in EXPORTS:
+        getattr(lib, name)
+    _lib = lib
+    return lib
+
+
+def check(status, allow=(0,)):
+    if status not in allow:
+        msg = load().hqcgb_last_error().decode(errors="replace")
+        raise HqcgbError(status, msg)
+    return status

@@ -1,0 +1,26 @@
+"""``torch.autograd.Function`` over the engine's energy + adjoint-force ABI.
+
+``PesFunction.apply(xp, pes)`` returns E + Vpp (Rydberg) for a pes made with
+``make_pes(..., forces=True)``; its backward multiplies the incoming gradient
+by dE/dxp from ``hqcgb_forces`` + the Ewald gradient, so
+``torch.autograd.grad`` works through the SCF like ``jax.grad(make_pes(...))``
+does for the reference's differentiable parts.
+"""
+import torch
+
+
+class PesFunction(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, xp, pes):
+        E, g = pes.value_and_grad(xp)
+        ctx.save_for_backward(g.to(device=xp.device, dtype=xp.dtype))
+        return E.to(device=xp.device, dtype=xp.dtype)
+
+    @staticmethod
+    def backward(ctx, gout):
+        (g,) = ctx.saved_tensors
+        return gout * g, None
+
+
+def pes_energy(xp, pes):
+    return PesFunction.apply(xp, pes)

@@ -1,0 +1,73 @@
+// Shared helpers of the hqcgb engine (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <cstdio>
+#include <cmath>
+
+#include "../../include/hqcgb.h"
+
+namespace hqcgb {
+
+void set_error(const std::string &msg);
+void count_launch(long long k = 1);
+
+struct Error {
+  int status;
+  std::string msg;
+};
+
+#define HQ_CUDA(call)                                                               \
+  do {                                                                              \
+    cudaError_t _e = (call);                                                        \
+    if (_e != cudaSuccess)                                                          \
+      throw ::hqcgb::Error{HQCGB_CUDA_ERROR, std::string(#call) + ": " +            \
+                                                cudaGetErrorString(_e)};            \
+  } while (0)
+
+#define HQ_LAUNCH_CHECK()                                                           \
+  do {                                                                              \
+    ::hqcgb::count_launch();                                                        \
+    cudaError_t _e = cudaGetLastError();                                            \
+    if (_e != cudaSuccess)                                                          \
+      throw ::hqcgb::Error{HQCGB_CUDA_ERROR,                                        \
+                           std::string("launch in ") + __func__ + ": " +             \
+                               cudaGetErrorString(_e)};                             \
+  } while (0)
+
+#define HQ_REQUIRE(cond, msg)                                                       \
+  do {                                                                              \
+    if (!(cond)) throw ::hqcgb::Error{HQCGB_BAD_ARG, msg};                          \
+  } while (0)
+
+inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+constexpr int kMaxGrid = 255;        // points per axis handled by the direct DFT passes
+constexpr int kMaxNao = 1024;        // AOs per configuration
+
+// ---------------------------------------------------------------------------
+// block reductions
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ inline T warp_sum(T v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Sum over the block; result valid in thread 0. blockDim.x multiple of 32.
+template <typename T>
+__device__ inline T block_sum(T v, T *sh /* >= 32 */) {
+  v = warp_sum(v);
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  int nw = (blockDim.x + 31) >> 5;
+  v = (threadIdx.x < nw) ? sh[threadIdx.x] : T(0);
+  if (w == 0) v = warp_sum(v);
+  __syncthreads();
+  return v;
+}
+
+}  // namespace hqcgb

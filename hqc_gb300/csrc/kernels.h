@@ -1,0 +1,85 @@
+// Host-side launchers of the hqcgb kernels (internal header).
+#pragma once
+#include <cuda_runtime.h>
+
+namespace hqcgb {
+
+// grid_fp64.cu
+void launch_gto1d(const double *xp, int n_atoms, int ng, double L, const double *alpha, int nprim,
+                  const double *lat1d, int nlat, double *F, cudaStream_t st);
+void launch_phi(const double *F, const double *coef, const int *ao_l, const int *ao_cart,
+                int nao_atom, int nprim, int nao, int ng, double *phi, double *dphi,
+                cudaStream_t st);
+void launch_density(const double *phi, const double *dphi, const double *D, int nao, long long N,
+                    double *rho, double *grho, double *Xout, cudaStream_t st);
+int quad_chunks(long long N);
+void launch_quadrature(const double *A, const double *B, const double *w, int nao, long long N,
+                       bool sym, double scale, bool accumulate, double *partial, double *M,
+                       cudaStream_t st);
+int xc_blocks(long long N);
+void launch_xc_pointwise(int kind, const double *rho, const double *grho, const double *vh,
+                         long long N, double dV, double *w, double *vxc_out, double *u,
+                         double *part, cudaStream_t st);
+void launch_gga_operand(const double *phi, const double *dphi, const double *w, const double *u,
+                        int nao, long long N, double dV, double *Z, cudaStream_t st);
+void launch_sum_partials(const double *part, int nblk, int stride, int nout, double scale,
+                         double *out, bool accumulate, cudaStream_t st);
+
+// fft_fp64.cu
+void launch_fft3d(double2 *c, int ng, int batch, const double2 *tw, bool inverse, cudaStream_t st);
+void launch_real_to_complex(const double *a, const double *s, long long N, int batch, double2 *c,
+                            cudaStream_t st);
+void launch_scale_complex(double2 *c, const double *k, long long N, int batch, cudaStream_t st);
+void launch_complex_real(const double2 *c, long long total, double scale, double *out,
+                         cudaStream_t st);
+void launch_coulomb_table(int ng, double L, double *kern, cudaStream_t st);
+void launch_vloc_G(const double *xp, int n_atoms, int ng, double L, double2 *ph, double2 *out,
+                   cudaStream_t st);
+int vloc_force_blocks(long long N);
+void launch_vloc_force(const double2 *ph, const double2 *F, int n_atoms, int ng, double L,
+                       double *part, cudaStream_t st);
+
+// linalg_fp64.cu
+void gemm(bool ta, bool tb, int M, int N, int K, double alpha, const double *A, int lda,
+          const double *B, int ldb, const double *d, double beta, double *C, int ldc,
+          cudaStream_t st);
+void axpby(int n, double a, const double *X, double b, const double *Y, bool transY, double *out,
+           cudaStream_t st);
+void dot(long long n, const double *A, const double *B, double scale, double *out, bool accumulate,
+         cudaStream_t st);
+void jacobi_eigh(int n, int batch, double *A, double *V, double *w, double *tmp, int *status,
+                 cudaStream_t st);
+void diis_extrapolate(int space, int n, const double *Fk, const double *ek, int last, double damp,
+                      double *B, double *c, double *F, cudaStream_t st);
+void occupations(int n_elec, int nmo, int smearing, int method, double sigma, int search, int cycle,
+                 double tol, double shift, const double *w, double *f, double *mu, cudaStream_t st);
+void entropy(int n, const double *f, double *out, cudaStream_t st);
+void inv_sqrt_cols(int n, const double *U, const double *w, double *v, int *bad, cudaStream_t st);
+void antisym(int n, const double *X, double *e, cudaStream_t st);
+
+// integrals_fp64.cu
+void launch_overlap_kinetic(const double *xp, int n, int nb, int nprim, const double *alpha,
+                            const double *coef, const int *ao_l, const int *ao_cart,
+                            const double *lattice, int nlat, double *S, double *T, const double *D,
+                            const double *W, double *gpart, double *grad, cudaStream_t st);
+void launch_ewald(const double *xp, int n, double L, double rs, double kappa, int gmax,
+                  double *pair_e, double *pair_g, double *energy, double *grad, cudaStream_t st);
+
+// forces_fp64.cu / exchange
+void launch_psi(const double *C, int nao, int col, const double *phi, long long N, double *psi,
+                cudaStream_t st);
+void launch_axpy_grid(long long total, long long N, double a, const double *s, const double *X,
+                      double *Z, cudaStream_t st);
+int force_grid_blocks(long long N);
+void launch_force_grid(const double *F1d, const double *coef, const int *ao_l, const int *ao_cart,
+                       int nao_atom, int nprim, int nao, int ng, const double *veff,
+                       const double *X, const double *u, const double *DPsi, const double *Z,
+                       double dV, double *part, cudaStream_t st);
+void launch_force_grid_reduce(const double *part, int nao, int nao_atom, int nblk, double *grad,
+                              cudaStream_t st);
+void launch_gga_psi(const double *dphi, const double *u, int nao, long long N, double *Psi,
+                    cudaStream_t st);
+void launch_add3(long long N, const double *a, const double *b, const double *c, double *out,
+                 cudaStream_t st);
+
+}  // namespace hqcgb

@@ -1,0 +1,641 @@
+// C ABI and host-side SCF driver of the hqcgb engine.
+//
+// hqcgb_plan_create replaces the factory-time part of make_solver
+// (hqc/pbc/solver.py:61-231); hqcgb_scf replaces one call of the jitted
+// hf_gamma / dft_gamma closure (solver.py:705-767, 839-899) including the
+// DIIS / fixed-point loops of hqc/pbc/scf.py.  The loop control runs on the
+// host; every array operation is a kernel on the caller's stream.
+#include <atomic>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <cmath>
+
+#include "common.cuh"
+#include "kernels.h"
+
+namespace hqcgb {
+static thread_local std::string g_err;
+static std::atomic<long long> g_launches{0};
+void set_error(const std::string &m) { g_err = m; }
+void count_launch(long long k) { g_launches += k; }
+}  // namespace hqcgb
+
+using namespace hqcgb;
+
+static constexpr double kMadelungSC = 0.22578495;  // solver.py:404
+
+struct hqcgb_plan {
+  hqcgb_params P{};
+  std::vector<double> h_alpha, h_coef, h_lat1d, h_lattice;
+  std::vector<int> h_l, h_cart;
+  int n = 0, nb = 0, nao = 0, ng = 0, nprim = 0;
+  long long N = 0;
+  double L = 0, Omega = 0, dV = 0;
+  bool gga = false, need_dphi = false, hf = false;
+  std::vector<void *> allocs;
+
+  // constant tables
+  double *alpha = nullptr, *coef = nullptr, *lat1d = nullptr, *lattice = nullptr;
+  int *ao_l = nullptr, *ao_cart = nullptr;
+  double2 *tw = nullptr;
+  double *coul = nullptr;
+  // geometry
+  double *xp = nullptr, *F1d = nullptr, *phi = nullptr, *dphi = nullptr;
+  double2 *ph = nullptr;
+  double *S = nullptr, *T = nullptr, *V = nullptr, *H = nullptr, *St = nullptr, *vorth = nullptr;
+  // scf matrices
+  double *F = nullptr, *F2e = nullptr, *K = nullptr, *Fp = nullptr, *C = nullptr, *c1 = nullptr,
+         *w = nullptr, *occ = nullptr, *D = nullptr, *t1 = nullptr, *t2 = nullptr, *err = nullptr,
+         *Fk = nullptr, *ek = nullptr, *Bm = nullptr, *dc = nullptr, *jtmp = nullptr,
+         *jA = nullptr, *ws = nullptr, *mu = nullptr;
+  int *jstat = nullptr, *ibad = nullptr;
+  // grid
+  double *rho = nullptr, *grho = nullptr, *vh = nullptr, *wq = nullptr, *vxc = nullptr,
+         *u = nullptr, *vloc = nullptr, *veff = nullptr, *X = nullptr, *Z = nullptr,
+         *DPsi = nullptr, *W = nullptr, *psi = nullptr;
+  double2 *cbuf = nullptr;
+  long long cbuf_batch = 0;
+  double *qpart = nullptr, *xpart = nullptr, *fpart = nullptr, *gpart = nullptr, *vpart = nullptr;
+  double *scal = nullptr;  // device scalars
+  double *hscal = nullptr; // pinned host mirror
+  // last state
+  bool have_state = false;
+  std::vector<double> h_occ;
+
+  template <class T>
+  T *alloc(size_t count) {
+    void *p = nullptr;
+    if (count == 0) count = 1;
+    HQ_CUDA(cudaMalloc(&p, count * sizeof(T)));
+    allocs.push_back(p);
+    return (T *)p;
+  }
+  ~hqcgb_plan() {
+    for (void *p : allocs) cudaFree(p);
+    if (hscal) cudaFreeHost(hscal);
+  }
+};
+
+// scal slots
+enum { S_TRHD = 0, S_EXC = 1, S_VHRHO = 2, S_TRKD = 3, S_ERR2 = 4, S_SE = 5, S_KI = 6, S_VEP = 7,
+       S_NSLOT = 16 };
+
+static void upload(void *dst, const void *src, size_t bytes) {
+  HQ_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
+}
+
+static double occ_shift(const hqcgb_plan *p) {
+  const hqcgb_params &P = p->P;
+  if (!P.smearing) return 0.0;
+  double n = P.n_atoms, nmo = p->nao;
+  if (P.smearing_method == HQCGB_SMEAR_FERMI) return -P.smearing_sigma * std::log(2 * nmo / n - 1);
+  // erfinv(1 - n/nmo) by Newton on erf (host, once)
+  double y = 1.0 - n / nmo, x = 0.0;
+  for (int it = 0; it < 200; ++it) {
+    double f = std::erf(x) - y;
+    double d = 2.0 / std::sqrt(M_PI) * std::exp(-x * x);
+    double dx = f / d;
+    x -= dx;
+    if (std::fabs(dx) < 1e-16 * (1 + std::fabs(x))) break;
+  }
+  return -P.smearing_sigma * x;
+}
+
+static void create(const hqcgb_params *in, hqcgb_plan *p) {
+  const hqcgb_params &P = *in;
+  HQ_REQUIRE(P.n_atoms >= 1, "n_atoms must be >= 1");
+  HQ_REQUIRE(P.n_grid >= 3 && P.n_grid <= kMaxGrid, "n_grid out of range");
+  HQ_REQUIRE(P.nao_atom >= 1 && P.n_prim >= 1, "empty basis");
+  HQ_REQUIRE(P.L > 0, "L must be positive");
+  HQ_REQUIRE(P.n_atoms * P.nao_atom <= kMaxNao, "too many AOs");
+  HQ_REQUIRE(P.diis_space >= 1 && P.diis_space <= 32, "diis_space must be in [1, 32]");
+  HQ_REQUIRE(P.max_cycle >= 0, "max_cycle must be >= 0");
+  HQ_REQUIRE(!P.smearing || P.smearing_sigma > 0, "smearing_sigma must be > 0 with smearing");
+  HQ_REQUIRE(P.n_atoms * P.nao_atom >= P.n_atoms / 2, "n_mo < n/2");
+  HQ_REQUIRE(P.precision == HQCGB_PREC_FP64 || P.precision == HQCGB_PREC_MIXED, "bad precision");
+  p->P = P;
+  p->n = P.n_atoms;
+  p->nb = P.nao_atom;
+  p->nao = p->n * p->nb;
+  p->ng = P.n_grid;
+  p->nprim = P.n_prim;
+  p->N = (long long)p->ng * p->ng * p->ng;
+  p->L = P.L;
+  p->Omega = P.L * P.L * P.L;
+  p->dV = p->Omega / (double)p->N;
+  p->hf = !P.dft;
+  p->gga = P.dft && P.xc == HQCGB_XC_PBE;
+  p->need_dphi = p->gga || P.want_forces;
+  p->h_alpha.assign(P.alpha, P.alpha + P.n_prim);
+  p->h_coef.assign(P.coef, P.coef + P.nao_atom * P.n_prim);
+  p->h_l.assign(P.ao_l, P.ao_l + P.nao_atom);
+  p->h_cart.assign(P.ao_cart, P.ao_cart + P.nao_atom);
+  for (int k = 0; k < P.nao_atom; ++k) {
+    HQ_REQUIRE(p->h_l[k] == 0 || p->h_l[k] == 1, "only s and p AOs are supported");
+    HQ_REQUIRE(p->h_cart[k] >= 0 && p->h_cart[k] < 3, "bad cartesian index");
+  }
+  p->h_lat1d.assign(P.lat1d, P.lat1d + P.n_lat1d);
+  p->h_lattice.assign(P.lattice, P.lattice + 3 * P.n_lattice);
+  int n = p->n, nao = p->nao;
+  long long N = p->N;
+  size_t nn = (size_t)nao * nao;
+
+  p->alpha = p->alloc<double>(P.n_prim);
+  upload(p->alpha, P.alpha, sizeof(double) * P.n_prim);
+  p->coef = p->alloc<double>(P.nao_atom * P.n_prim);
+  upload(p->coef, P.coef, sizeof(double) * P.nao_atom * P.n_prim);
+  p->ao_l = p->alloc<int>(P.nao_atom);
+  upload(p->ao_l, P.ao_l, sizeof(int) * P.nao_atom);
+  p->ao_cart = p->alloc<int>(P.nao_atom);
+  upload(p->ao_cart, P.ao_cart, sizeof(int) * P.nao_atom);
+  p->lat1d = p->alloc<double>(P.n_lat1d);
+  upload(p->lat1d, P.lat1d, sizeof(double) * P.n_lat1d);
+  p->lattice = p->alloc<double>(3 * P.n_lattice);
+  upload(p->lattice, P.lattice, sizeof(double) * 3 * P.n_lattice);
+  std::vector<double2> tw(p->ng);
+  for (int k = 0; k < p->ng; ++k) {
+    double a = -2.0 * M_PI * k / p->ng;
+    tw[k] = make_double2(std::cos(a), std::sin(a));
+  }
+  p->tw = p->alloc<double2>(p->ng);
+  upload(p->tw, tw.data(), sizeof(double2) * p->ng);
+  p->coul = p->alloc<double>(N);
+  launch_coulomb_table(p->ng, p->L, p->coul, 0);
+
+  p->xp = p->alloc<double>(3 * n);
+  p->F1d = p->alloc<double>((size_t)n * 3 * p->ng * P.n_prim * 6);
+  p->phi = p->alloc<double>((size_t)nao * N);
+  if (p->need_dphi) p->dphi = p->alloc<double>((size_t)3 * nao * N);
+  p->ph = p->alloc<double2>((size_t)n * 3 * p->ng);
+  for (double **m : {&p->S, &p->T, &p->V, &p->H, &p->St, &p->vorth, &p->F, &p->F2e, &p->K, &p->Fp,
+                     &p->C, &p->c1, &p->D, &p->t1, &p->t2, &p->err, &p->jtmp, &p->jA})
+    *m = p->alloc<double>(nn);
+  p->w = p->alloc<double>(nao);
+  p->ws = p->alloc<double>(nao);
+  p->occ = p->alloc<double>(nao);
+  p->mu = p->alloc<double>(1);
+  p->Fk = p->alloc<double>((size_t)P.diis_space * nn);
+  p->ek = p->alloc<double>((size_t)P.diis_space * nn);
+  p->Bm = p->alloc<double>((size_t)P.diis_space * P.diis_space);
+  p->dc = p->alloc<double>(P.diis_space);
+  p->jstat = p->alloc<int>(1);
+  p->ibad = p->alloc<int>(1);
+  p->rho = p->alloc<double>(N);
+  p->vh = p->alloc<double>(N);
+  p->wq = p->alloc<double>(N);
+  p->vxc = p->alloc<double>(N);
+  p->vloc = p->alloc<double>(N);
+  p->veff = p->alloc<double>(N);
+  p->psi = p->alloc<double>(N);
+  if (p->gga) {
+    p->grho = p->alloc<double>(3 * N);
+    p->u = p->alloc<double>(3 * N);
+    p->Z = p->alloc<double>((size_t)nao * N);
+  }
+  if (P.want_forces || p->hf) {
+    p->X = p->alloc<double>((size_t)nao * N);
+    if (!p->Z) p->Z = p->alloc<double>((size_t)nao * N);
+  }
+  if (P.want_forces && p->gga) p->DPsi = p->alloc<double>((size_t)nao * N);
+  p->cbuf_batch = p->hf ? nao : 1;
+  if (p->hf) p->W = p->alloc<double>((size_t)nao * N);
+  p->cbuf = p->alloc<double2>((size_t)p->cbuf_batch * N);
+  p->qpart = p->alloc<double>((size_t)quad_chunks(N) * nn);
+  p->xpart = p->alloc<double>((size_t)2 * xc_blocks(N));
+  if (P.want_forces) {
+    p->fpart = p->alloc<double>((size_t)nao * force_grid_blocks(N) * 3);
+    p->gpart = p->alloc<double>((size_t)n * n * p->nb * p->nb * 3);
+    p->vpart = p->alloc<double>((size_t)vloc_force_blocks(N) * n * 3);
+  }
+  p->scal = p->alloc<double>(S_NSLOT);
+  HQ_CUDA(cudaMallocHost(&p->hscal, S_NSLOT * sizeof(double)));
+  HQ_CUDA(cudaDeviceSynchronize());
+}
+
+// ---------------------------------------------------------------------------
+struct Ctx {
+  hqcgb_plan *p;
+  cudaStream_t st;
+};
+
+static void sync_scalars(Ctx &c) {
+  HQ_CUDA(cudaMemcpyAsync(c.p->hscal, c.p->scal, S_NSLOT * sizeof(double), cudaMemcpyDeviceToHost,
+                          c.st));
+  HQ_CUDA(cudaStreamSynchronize(c.st));
+}
+
+static void eigh(Ctx &c, const double *A, double *vecs, double *vals) {
+  hqcgb_plan *p = c.p;
+  int n = p->nao;
+  HQ_CUDA(cudaMemcpyAsync(p->jA, A, sizeof(double) * n * n, cudaMemcpyDeviceToDevice, c.st));
+  jacobi_eigh(n, 1, p->jA, vecs, vals, p->jtmp, p->jstat, c.st);
+}
+
+// C, w from a Fock matrix: F' = v^T F v, eigh, C = v c'
+static void diagonalize(Ctx &c, const double *Fm) {
+  hqcgb_plan *p = c.p;
+  int n = p->nao;
+  gemm(false, false, n, n, n, 1.0, Fm, n, p->vorth, n, nullptr, 0.0, p->t1, n, c.st);
+  gemm(true, false, n, n, n, 1.0, p->vorth, n, p->t1, n, nullptr, 0.0, p->Fp, n, c.st);
+  eigh(c, p->Fp, p->c1, p->w);
+  gemm(false, false, n, n, n, 1.0, p->vorth, n, p->c1, n, nullptr, 0.0, p->C, n, c.st);
+}
+
+static void density_matrix(Ctx &c) {
+  hqcgb_plan *p = c.p;
+  const hqcgb_params &P = p->P;
+  int n = p->nao;
+  occupations(P.n_atoms, n, P.smearing, P.smearing_method, P.smearing_sigma, P.search_method,
+              P.search_cycle, P.search_tol, occ_shift(p), p->w, p->occ, p->mu, c.st);
+  gemm(false, true, n, n, n, 1.0, p->C, n, p->C, n, p->occ, 0.0, p->D, n, c.st);
+}
+
+static void poisson(Ctx &c, const double *src, double *dst, bool keep_spectrum = false) {
+  hqcgb_plan *p = c.p;
+  launch_real_to_complex(src, nullptr, p->N, 1, p->cbuf, c.st);
+  launch_fft3d(p->cbuf, p->ng, 1, p->tw, false, c.st);
+  (void)keep_spectrum;
+  launch_scale_complex(p->cbuf, p->coul, p->N, 1, c.st);
+  launch_fft3d(p->cbuf, p->ng, 1, p->tw, true, c.st);
+  launch_complex_real(p->cbuf, p->N, 1.0, dst, c.st);
+}
+
+// Exact exchange K (with the Madelung G=0 term), solver.py:430-431, 604-614.
+// With Zacc != nullptr also accumulates the orbital force operand
+// Z_p += f_j psi_j (D W_j)_p.
+static void exchange(Ctx &c, double *Zacc) {
+  hqcgb_plan *p = c.p;
+  int n = p->nao;
+  long long N = p->N;
+  p->h_occ.resize(n);
+  HQ_CUDA(cudaMemcpyAsync(p->h_occ.data(), p->occ, sizeof(double) * n, cudaMemcpyDeviceToHost, c.st));
+  HQ_CUDA(cudaStreamSynchronize(c.st));
+  HQ_CUDA(cudaMemsetAsync(p->K, 0, sizeof(double) * n * n, c.st));
+  for (int i = 0; i < n; ++i) {
+    double f = p->h_occ[i];
+    if (!(f > p->P.exx_occ_threshold)) continue;
+    launch_psi(p->C, n, i, p->phi, N, p->psi, c.st);
+    launch_real_to_complex(p->phi, p->psi, N, n, p->cbuf, c.st);
+    launch_fft3d(p->cbuf, p->ng, n, p->tw, false, c.st);
+    launch_scale_complex(p->cbuf, p->coul, N, n, c.st);
+    launch_fft3d(p->cbuf, p->ng, n, p->tw, true, c.st);
+    launch_complex_real(p->cbuf, (long long)n * N, 1.0, p->W, c.st);
+    launch_quadrature(p->phi, p->W, p->psi, n, N, false, f * p->dV, true, p->qpart, p->K, c.st);
+    if (Zacc) {
+      launch_density(p->W, nullptr, p->D, n, N, p->vh /*scratch*/, nullptr, p->X, c.st);
+      launch_axpy_grid((long long)n * N, N, f, p->psi, p->X, Zacc, c.st);
+    }
+  }
+  axpby(n, 0.5, p->K, 0.5, p->K, true, p->t1, c.st);
+  double cM = 4.0 * M_PI / p->L * kMadelungSC;
+  gemm(false, false, n, n, n, 1.0, p->St, n, p->D, n, nullptr, 0.0, p->t2, n, c.st);
+  gemm(false, false, n, n, n, 1.0, p->t2, n, p->St, n, nullptr, 0.0, p->K, n, c.st);
+  axpby(n, 1.0, p->t1, cM, p->K, false, p->K, c.st);
+}
+
+// Two-electron part of the Fock matrix and the energy pieces for density D.
+// Leaves F = H + F2e in p->F; scalars in p->scal.
+static double fock(Ctx &c) {
+  hqcgb_plan *p = c.p;
+  const hqcgb_params &P = p->P;
+  int n = p->nao;
+  long long N = p->N;
+  launch_density(p->phi, p->gga ? p->dphi : nullptr, p->D, n, N, p->rho, p->gga ? p->grho : nullptr,
+                 nullptr, c.st);
+  poisson(c, p->rho, p->vh);
+  int kind = P.dft ? P.xc : -1;
+  launch_xc_pointwise(kind, p->rho, p->gga ? p->grho : nullptr, p->vh, N, p->dV, p->wq, p->vxc,
+                      p->gga ? p->u : nullptr, p->xpart, c.st);
+  launch_sum_partials(p->xpart, xc_blocks(N), 2, 2, 1.0, p->scal + S_EXC, false, c.st);
+  if (p->gga) {
+    launch_gga_operand(p->phi, p->dphi, p->wq, p->u, n, N, p->dV, p->Z, c.st);
+    launch_quadrature(p->Z, p->phi, nullptr, n, N, false, 1.0, false, p->qpart, p->t1, c.st);
+    axpby(n, 1.0, p->t1, 1.0, p->t1, true, p->F2e, c.st);
+  } else {
+    launch_quadrature(p->phi, p->phi, p->wq, n, N, true, 1.0, false, p->qpart, p->F2e, c.st);
+  }
+  if (p->hf) {
+    exchange(c, nullptr);
+    dot((long long)n * n, p->K, p->D, 1.0, p->scal + S_TRKD, false, c.st);
+    axpby(n, 1.0, p->F2e, -0.5, p->K, false, p->F2e, c.st);
+  }
+  axpby(n, 1.0, p->H, 1.0, p->F2e, false, p->F, c.st);
+  dot((long long)n * n, p->H, p->D, 1.0, p->scal + S_TRHD, false, c.st);
+  sync_scalars(c);
+  const double *s = p->hscal;
+  double E = s[S_TRHD] + 0.5 * p->dV * s[S_VHRHO];
+  E += P.dft ? p->dV * s[S_EXC] : -0.25 * s[S_TRKD];
+  return E;
+}
+
+static double err_vector(Ctx &c, double *e) {
+  hqcgb_plan *p = c.p;
+  int n = p->nao;
+  gemm(false, false, n, n, n, 1.0, p->S, n, p->D, n, nullptr, 0.0, p->t1, n, c.st);
+  gemm(false, false, n, n, n, 1.0, p->t1, n, p->F, n, nullptr, 0.0, p->t2, n, c.st);
+  antisym(n, p->t2, e, c.st);
+  dot((long long)n * n, e, e, 1.0, p->scal + S_ERR2, false, c.st);
+  sync_scalars(c);
+  return std::sqrt(p->hscal[S_ERR2]);
+}
+
+static void check_eig(Ctx &c) {
+  int st = 0;
+  HQ_CUDA(cudaMemcpyAsync(&st, c.p->jstat, sizeof(int), cudaMemcpyDeviceToHost, c.st));
+  HQ_CUDA(cudaStreamSynchronize(c.st));
+  if (st < 0) throw Error{HQCGB_EIG_FAIL, "Jacobi eigensolver did not converge"};
+}
+
+static void geometry(Ctx &c, const double *xp_dev) {
+  hqcgb_plan *p = c.p;
+  const hqcgb_params &P = p->P;
+  int n = p->nao;
+  long long N = p->N;
+  HQ_CUDA(cudaMemcpyAsync(p->xp, xp_dev, sizeof(double) * 3 * p->n, cudaMemcpyDeviceToDevice, c.st));
+  launch_gto1d(p->xp, p->n, p->ng, p->L, p->alpha, p->nprim, p->lat1d, P.n_lat1d, p->F1d, c.st);
+  launch_phi(p->F1d, p->coef, p->ao_l, p->ao_cart, p->nb, p->nprim, n, p->ng, p->phi, p->dphi, c.st);
+  launch_overlap_kinetic(p->xp, p->n, p->nb, p->nprim, p->alpha, p->coef, p->ao_l, p->ao_cart,
+                         p->lattice, P.n_lattice, p->S, p->T, nullptr, nullptr, nullptr, nullptr,
+                         c.st);
+  launch_vloc_G(p->xp, p->n, p->ng, p->L, p->ph, p->cbuf, c.st);
+  launch_fft3d(p->cbuf, p->ng, 1, p->tw, true, c.st);
+  launch_complex_real(p->cbuf, N, 1.0, p->vloc, c.st);
+  launch_quadrature(p->phi, p->phi, p->vloc, n, N, true, p->dV, false, p->qpart, p->V, c.st);
+  axpby(n, 1.0, p->T, 1.0, p->V, false, p->H, c.st);
+  if (p->hf) launch_quadrature(p->phi, p->phi, nullptr, n, N, true, p->dV, false, p->qpart, p->St, c.st);
+  // S^{-1/2} as U w^{-1/2} (solver.py:729-730)
+  HQ_CUDA(cudaMemsetAsync(p->ibad, 0, sizeof(int), c.st));
+  eigh(c, p->S, p->c1, p->ws);
+  inv_sqrt_cols(n, p->c1, p->ws, p->vorth, p->ibad, c.st);
+  int bad = 0;
+  HQ_CUDA(cudaMemcpyAsync(&bad, p->ibad, sizeof(int), cudaMemcpyDeviceToHost, c.st));
+  HQ_CUDA(cudaStreamSynchronize(c.st));
+  check_eig(c);
+  if (bad) throw Error{HQCGB_NAN, "overlap matrix is not positive definite (coincident atoms?)"};
+}
+
+static int scf_one(hqcgb_plan *p, const double *xp_dev, const hqcgb_scf_out *out, cudaStream_t st) {
+  Ctx c{p, st};
+  const hqcgb_params &P = p->P;
+  int n = p->nao;
+  size_t nn = (size_t)n * n;
+  p->have_state = false;
+  geometry(c, xp_dev);
+  // Hcore guess (solver.py:739-745)
+  diagonalize(c, p->H);
+  density_matrix(c);
+  double E0 = 0.0, E1 = 1.0;
+  int loop = 0;
+  if (P.diis) {
+    int sp = P.diis_space;
+    fock(c);
+    err_vector(c, p->err);
+    for (int k = 0; k < sp; ++k) {
+      HQ_CUDA(cudaMemcpyAsync(p->Fk + k * nn, p->F, nn * 8, cudaMemcpyDeviceToDevice, st));
+      HQ_CUDA(cudaMemcpyAsync(p->ek + k * nn, p->err, nn * 8, cudaMemcpyDeviceToDevice, st));
+    }
+    int head = sp - 1;
+    double enorm = 0.0;
+    auto step = [&](const double *Fin) {
+      diagonalize(c, Fin);
+      density_matrix(c);
+      double En = fock(c);
+      head = (head + 1) % sp;
+      HQ_CUDA(cudaMemcpyAsync(p->Fk + head * nn, p->F, nn * 8, cudaMemcpyDeviceToDevice, st));
+      enorm = err_vector(c, p->ek + head * nn);
+      E0 = E1;
+      E1 = En;
+      ++loop;
+    };
+    while (loop < P.diis_start_cycle + sp) step(p->Fk + head * nn);
+    E0 = E1 - 1.0;
+    while ((std::fabs(E1 - E0) > P.tol || enorm > 10.0 * P.tol) && loop < P.max_cycle) {
+      diis_extrapolate(sp, n, p->Fk, p->ek, head, P.diis_damp, p->Bm, p->dc, p->t1, st);
+      HQ_CUDA(cudaMemcpyAsync(p->Fp, p->t1, nn * 8, cudaMemcpyDeviceToDevice, st));
+      step(p->Fp);
+      if (!std::isfinite(E1)) throw Error{HQCGB_NAN, "non-finite energy in the SCF"};
+    }
+  } else {
+    while (std::fabs(E1 - E0) > P.tol && loop < P.max_cycle) {
+      double En = fock(c);
+      diagonalize(c, p->F);
+      density_matrix(c);
+      E0 = E1;
+      E1 = En;
+      ++loop;
+      if (!std::isfinite(E1)) throw Error{HQCGB_NAN, "non-finite energy in the SCF"};
+    }
+  }
+  check_eig(c);
+  int converged = (loop != P.max_cycle) ? 1 : 0;
+  // post-processing (solver.py:758-767 / 890-899)
+  density_matrix(c);
+  fock(c);
+  dot((long long)nn, p->T, p->D, 1.0, p->scal + S_KI, false, st);
+  dot((long long)nn, p->V, p->D, 1.0, p->scal + S_VEP, false, st);
+  entropy(n, p->occ, p->scal + S_SE, st);
+  sync_scalars(c);
+  const double *s = p->hscal;
+  double Exc = P.dft ? p->dV * s[S_EXC] : -0.25 * s[S_TRKD];
+  double Vee = 0.5 * p->dV * s[S_VHRHO] + Exc;
+  double en[5] = {E1, s[S_KI], s[S_VEP], Vee, s[S_SE]};
+  if (out) {
+    if (out->mo_coeff) HQ_CUDA(cudaMemcpyAsync(out->mo_coeff, p->C, nn * 8, cudaMemcpyDeviceToDevice, st));
+    if (out->dm) HQ_CUDA(cudaMemcpyAsync(out->dm, p->D, nn * 8, cudaMemcpyDeviceToDevice, st));
+    if (out->bands) HQ_CUDA(cudaMemcpyAsync(out->bands, p->w, n * 8, cudaMemcpyDeviceToDevice, st));
+    if (out->energies) HQ_CUDA(cudaMemcpyAsync(out->energies, en, sizeof(en), cudaMemcpyHostToDevice, st));
+    if (out->converged) HQ_CUDA(cudaMemcpyAsync(out->converged, &converged, sizeof(int), cudaMemcpyHostToDevice, st));
+    if (out->iterations) HQ_CUDA(cudaMemcpyAsync(out->iterations, &loop, sizeof(int), cudaMemcpyHostToDevice, st));
+    HQ_CUDA(cudaStreamSynchronize(st));
+  }
+  p->have_state = true;
+  return converged ? HQCGB_OK : HQCGB_NOT_CONVERGED;
+}
+
+static void forces(hqcgb_plan *p, double *grad, cudaStream_t st) {
+  Ctx c{p, st};
+  const hqcgb_params &P = p->P;
+  HQ_REQUIRE(P.want_forces, "plan was created without want_forces");
+  if (!p->have_state) throw Error{HQCGB_NO_STATE, "hqcgb_forces called before a successful SCF"};
+  int n = p->nao;
+  long long N = p->N;
+  HQ_CUDA(cudaMemsetAsync(grad, 0, sizeof(double) * 3 * p->n, st));
+  // energy-weighted density W = C diag(f eps) C^T  -> t2
+  launch_add3(n, nullptr, nullptr, nullptr, p->psi, st);  // psi[0..n) scratch = 0
+  launch_axpy_grid(n, n, 1.0, p->occ, p->w, p->psi, st);   // psi = f * eps
+  gemm(false, true, n, n, n, 1.0, p->C, n, p->C, n, p->psi, 0.0, p->t2, n, st);
+  launch_overlap_kinetic(p->xp, p->n, p->nb, p->nprim, p->alpha, p->coef, p->ao_l, p->ao_cart,
+                         p->lattice, P.n_lattice, nullptr, nullptr, p->D, p->t2, p->gpart, grad, st);
+  // density, X = D phi, Hartree, structure-factor term
+  launch_density(p->phi, p->gga ? p->dphi : nullptr, p->D, n, N, p->rho, p->gga ? p->grho : nullptr,
+                 p->X, st);
+  launch_real_to_complex(p->rho, nullptr, N, 1, p->cbuf, st);
+  launch_fft3d(p->cbuf, p->ng, 1, p->tw, false, st);
+  launch_vloc_force(p->ph, p->cbuf, p->n, p->ng, p->L, p->vpart, st);
+  launch_sum_partials(p->vpart, vloc_force_blocks(N), 3 * p->n, 3 * p->n, 1.0, grad, true, st);
+  launch_scale_complex(p->cbuf, p->coul, N, 1, st);
+  launch_fft3d(p->cbuf, p->ng, 1, p->tw, true, st);
+  launch_complex_real(p->cbuf, N, 1.0, p->vh, st);
+  const double *uu = nullptr;
+  if (P.dft) {
+    launch_xc_pointwise(P.xc, p->rho, p->gga ? p->grho : nullptr, p->vh, N, p->dV, p->wq, p->vxc,
+                        p->gga ? p->u : nullptr, p->xpart, st);
+    launch_add3(N, p->vloc, p->vh, p->vxc, p->veff, st);
+    if (p->gga) {
+      launch_gga_psi(p->dphi, p->u, n, N, p->Z, st);
+      launch_density(p->Z, nullptr, p->D, n, N, p->wq /*scratch*/, nullptr, p->DPsi, st);
+      uu = p->u;
+    }
+  } else {
+    launch_add3(N, p->vloc, p->vh, nullptr, p->veff, st);
+    HQ_CUDA(cudaMemsetAsync(p->Z, 0, sizeof(double) * n * N, st));
+    // X is reused inside exchange(); keep a copy of D phi in DPsi-free form:
+    // recompute X after the exchange pass.
+    exchange(c, p->Z);
+    // Madelung term c dV (D S~ D phi)_p  folded into Z with weight cM
+    gemm(false, false, n, n, n, 1.0, p->D, n, p->St, n, nullptr, 0.0, p->t1, n, st);
+    gemm(false, false, n, n, n, 1.0, p->t1, n, p->D, n, nullptr, 0.0, p->t2, n, st);
+    launch_density(p->phi, nullptr, p->t2, n, N, p->wq, nullptr, p->X, st);
+    double cM = 4.0 * M_PI / p->L * kMadelungSC;
+    launch_axpy_grid((long long)n * N, N, cM, nullptr, p->X, p->Z, st);
+    launch_density(p->phi, nullptr, p->D, n, N, p->rho, nullptr, p->X, st);
+  }
+  launch_force_grid(p->F1d, p->coef, p->ao_l, p->ao_cart, p->nb, p->nprim, n, p->ng, p->veff, p->X,
+                    uu, p->DPsi, p->hf ? p->Z : nullptr, p->dV, p->fpart, st);
+  launch_force_grid_reduce(p->fpart, n, p->nb, force_grid_blocks(N), grad, st);
+  HQ_CUDA(cudaStreamSynchronize(st));
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+#define HQ_GUARD(...)                                     \
+  try {                                                   \
+    __VA_ARGS__;                                          \
+  } catch (const Error &e) {                              \
+    set_error(e.msg);                                     \
+    return e.status;                                      \
+  } catch (const std::exception &e) {                     \
+    set_error(e.what());                                  \
+    return HQCGB_CUDA_ERROR;                              \
+  }
+
+extern "C" {
+
+int hqcgb_plan_create(const hqcgb_params *params, hqcgb_plan **plan) {
+  HQ_GUARD({
+    HQ_REQUIRE(params && plan, "null argument");
+    hqcgb_plan *p = new hqcgb_plan();
+    try {
+      create(params, p);
+    } catch (...) {
+      delete p;
+      throw;
+    }
+    *plan = p;
+    return HQCGB_OK;
+  });
+}
+
+int hqcgb_plan_destroy(hqcgb_plan *plan) {
+  HQ_GUARD({
+    delete plan;
+    return HQCGB_OK;
+  });
+}
+
+int hqcgb_scf(hqcgb_plan *plan, const double *xp, const hqcgb_scf_out *out, void *stream) {
+  HQ_GUARD({
+    HQ_REQUIRE(plan && xp, "null argument");
+    return scf_one(plan, xp, out, (cudaStream_t)stream);
+  });
+}
+
+int hqcgb_scf_batch(hqcgb_plan *plan, int n_cfg, const double *xp, const hqcgb_scf_out *out,
+                    void *stream) {
+  HQ_GUARD({
+    HQ_REQUIRE(plan && xp && out && n_cfg >= 0, "null argument");
+    int worst = HQCGB_OK;
+    size_t nn = (size_t)plan->nao * plan->nao;
+    for (int b = 0; b < n_cfg; ++b) {
+      hqcgb_scf_out o = *out;
+      if (o.mo_coeff) o.mo_coeff += b * nn;
+      if (o.dm) o.dm += b * nn;
+      if (o.bands) o.bands += (size_t)b * plan->nao;
+      if (o.energies) o.energies += 5 * b;
+      if (o.converged) o.converged += b;
+      if (o.iterations) o.iterations += b;
+      int s = scf_one(plan, xp + (size_t)b * 3 * plan->n, &o, (cudaStream_t)stream);
+      if (s > worst) worst = s;
+    }
+    return worst;
+  });
+}
+
+int hqcgb_forces(hqcgb_plan *plan, double *grad, void *stream) {
+  HQ_GUARD({
+    HQ_REQUIRE(plan && grad, "null argument");
+    forces(plan, grad, (cudaStream_t)stream);
+    return HQCGB_OK;
+  });
+}
+
+int hqcgb_ewald(const double *xp, int n, double L, double rs, double kappa, int gmax,
+                double *energy, double *grad, void *stream) {
+  HQ_GUARD({
+    HQ_REQUIRE(xp && energy && n >= 1 && L > 0 && rs > 0 && kappa > 0 && gmax >= 1, "bad argument");
+    cudaStream_t st = (cudaStream_t)stream;
+    int npair = n * (n - 1) / 2;
+    double *pe = nullptr, *pg = nullptr;
+    HQ_CUDA(cudaMallocAsync(&pe, sizeof(double) * (npair + 1), st));
+    HQ_CUDA(cudaMallocAsync(&pg, sizeof(double) * 3 * (npair + 1), st));
+    launch_ewald(xp, n, L, rs, kappa, gmax, pe, pg, energy, grad, st);
+    HQ_CUDA(cudaFreeAsync(pe, st));
+    HQ_CUDA(cudaFreeAsync(pg, st));
+    return HQCGB_OK;
+  });
+}
+
+long long hqcgb_plan_query(hqcgb_plan *p, const char *name, void *dst, size_t bytes, void *stream) {
+  try {
+    if (!p || !name) return -1;
+    size_t nn = (size_t)p->nao * p->nao * 8;
+    size_t ng = (size_t)p->N * 8;
+    const void *src = nullptr;
+    size_t sz = 0;
+    std::string k(name);
+    if (k == "S") { src = p->S; sz = nn; }
+    else if (k == "T") { src = p->T; sz = nn; }
+    else if (k == "V") { src = p->V; sz = nn; }
+    else if (k == "H") { src = p->H; sz = nn; }
+    else if (k == "fock") { src = p->F; sz = nn; }
+    else if (k == "J") { src = p->F2e; sz = nn; }
+    else if (k == "K") { src = p->K; sz = nn; }
+    else if (k == "D") { src = p->D; sz = nn; }
+    else if (k == "St") { src = p->St; sz = nn; }
+    else if (k == "phi") { src = p->phi; sz = ng * p->nao; }
+    else if (k == "rho") { src = p->rho; sz = ng; }
+    else if (k == "vh") { src = p->vh; sz = ng; }
+    else if (k == "vloc") { src = p->vloc; sz = ng; }
+    else return -2;
+    if (!dst) return (long long)sz;
+    if (bytes < sz) return -3;
+    HQ_CUDA(cudaMemcpyAsync(dst, src, sz, cudaMemcpyDeviceToDevice, (cudaStream_t)stream));
+    HQ_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    return (long long)sz;
+  } catch (const Error &e) {
+    set_error(e.msg);
+    return -4;
+  }
+}
+
+const char *hqcgb_last_error(void) { return g_err.c_str(); }
+
+long long hqcgb_launch_count(int reset) {
+  long long v = g_launches.load();
+  if (reset) g_launches = 0;
+  return v;
+}
+
+}  // extern "C"

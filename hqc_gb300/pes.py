@@ -1,0 +1,44 @@
+"""``make_pes``: potential energy surface factory (hqc/pbc/pes.py:10-152).
+
+``pes(xp)`` returns E + Vpp in Rydberg (mode 'default') or the 7-tuple
+(E + Vpp, Ki, Vep, Vee, Vpp, Se, converged) in mode 'dev'.  With
+``forces=True``, ``pes.value_and_grad(xp)`` returns (E + Vpp, d/dxp) in
+Rydberg per rs unit from the engine's adjoint (absent from the reference;
+under Fermi smearing the electronic part is the gradient of E - sigma*Se).
+"""
+from .solver import make_solver
+from .potential import potential_energy_pp_and_grad
+
+
+def make_pes(n, L, rs, basis, rcut=24, tol=1e-7, max_cycle=100, grid_length=0.12, diis=True,
+             diis_space=8, diis_start_cycle=1, diis_damp=0., use_jit=True, dft=False,
+             xc='lda,vwn', smearing=False, smearing_method='fermi', smearing_sigma=0.,
+             search_method='bisect', search_cycle=100, search_tol=1e-7, gamma=True, Gmax=15,
+             kappa=10, mode='default', precision='fp64', forces=False, n_grid=None,
+             exx_occ_threshold=0.0):
+    if mode not in ("default", "dev"):
+        raise ValueError(f"Invalid mode: {mode}.")
+    solver = make_solver(n, L, rs, basis, rcut=rcut, tol=tol, max_cycle=max_cycle,
+                         grid_length=grid_length, diis=diis, diis_space=diis_space,
+                         diis_start_cycle=diis_start_cycle, diis_damp=diis_damp, use_jit=use_jit,
+                         dft=dft, xc=xc, smearing=smearing, smearing_method=smearing_method,
+                         smearing_sigma=smearing_sigma, search_method=search_method,
+                         search_cycle=search_cycle, search_tol=search_tol, gamma=gamma,
+                         precision=precision, forces=forces, n_grid=n_grid,
+                         exx_occ_threshold=exx_occ_threshold)
+
+    def pes(xp):
+        _, _, _, E, Ki, Vep, Vee, Se, conv = solver(xp)
+        Vpp, _ = potential_energy_pp_and_grad(xp, L, rs, kappa=kappa, Gmax=Gmax)
+        if mode == "dev":
+            return E + Vpp, Ki, Vep, Vee, Vpp, Se, conv
+        return E + Vpp
+
+    def value_and_grad(xp):
+        out = solver(xp)
+        Vpp, gpp = potential_energy_pp_and_grad(xp, L, rs, kappa=kappa, Gmax=Gmax)
+        return out[3] + Vpp, solver.grad() + gpp
+
+    pes.solver = solver
+    pes.value_and_grad = value_and_grad
+    return pes

@@ -1,0 +1,136 @@
+/*
+ * hqcgb.h -- C ABI of the GB300 (sm_103a) periodic GPW SCF engine.
+ *
+ * Drop-in boundary for the hot path of hqc (ZihangL/hqc v0.1.12), whose
+ * public entry points are Python factories returning jitted closures:
+ *
+ *   make_solver(n, L, rs, basis, ...) -> solver(xp)      hqc/pbc/solver.py:14-32, 705-978
+ *   make_lcao(...)  -> lcao(xp) = (mo_coeff, bands, E)   hqc/pbc/lcao.py:11-78
+ *   make_pes(...)   -> pes(xp)  = E + Vpp                hqc/pbc/pes.py:10-152
+ *   potential_energy_pp(xp, L, rs, kappa, Gmax)          hqc/pbc/potential.py:103-130
+ *
+ * The factory's table building is hqcgb_plan_create; one call of the jitted
+ * closure is hqcgb_scf (+ hqcgb_ewald for make_pes).  Everything below works
+ * on caller-owned DEVICE buffers and a caller stream; the plan owns its
+ * workspace.  All functions return an hqcgb_status; a non-zero status leaves
+ * a message for hqcgb_last_error().  Energies are in Hartree (the Python
+ * layer converts to Rydberg like the reference), lengths in Bohr.
+ */
+#ifndef HQCGB_H
+#define HQCGB_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  HQCGB_OK = 0,
+  HQCGB_NOT_CONVERGED = 1,   /* SCF reached max_cycle (reference: converged=False) */
+  HQCGB_BAD_ARG = 2,
+  HQCGB_CUDA_ERROR = 3,
+  HQCGB_EIG_FAIL = 4,        /* Jacobi sweep limit reached */
+  HQCGB_NAN = 5,             /* non-finite energy or Fock matrix */
+  HQCGB_NO_STATE = 6         /* forces requested before an SCF */
+} hqcgb_status;
+
+enum { HQCGB_XC_LDA_X = 0, HQCGB_XC_LDA_VWN = 1, HQCGB_XC_LDA_HL = 2, HQCGB_XC_LDA_BH = 3,
+       HQCGB_XC_LDA_GL = 4, HQCGB_XC_PBE = 10 };
+enum { HQCGB_SMEAR_FERMI = 0, HQCGB_SMEAR_GAUSS = 1 };
+enum { HQCGB_SEARCH_BISECT = 0, HQCGB_SEARCH_NEWTON = 1 };
+enum { HQCGB_PREC_FP64 = 0, HQCGB_PREC_MIXED = 1 };
+
+typedef struct {
+  /* system (hqc/pbc/solver.py:14-32, 153-176) */
+  int n_atoms;
+  int n_grid;              /* points per axis; odd for reference parity */
+  double L;                /* box side, Bohr */
+  /* basis, one hydrogen's AOs (hqc/pbc/solver.py:64-151, hqc/pbc/gto.py:72-300) */
+  int nao_atom;
+  int n_prim;
+  const double *alpha;     /* [n_prim] primitive exponents */
+  const double *coef;      /* [nao_atom][n_prim] contraction * cart2sph factor */
+  const int *ao_l;         /* [nao_atom] 0 or 1 */
+  const int *ao_cart;      /* [nao_atom] cartesian direction of a p AO */
+  int n_lat1d;
+  const double *lat1d;     /* [n_lat1d] 1D lattice translations of the grid GTOs */
+  int n_lattice;
+  const double *lattice;   /* [n_lattice][3] lattice sphere of the S/T sums */
+  /* method */
+  int dft;                 /* 0: Hartree-Fock, 1: Kohn-Sham */
+  int xc;                  /* HQCGB_XC_* */
+  int smearing;
+  int smearing_method;     /* HQCGB_SMEAR_* */
+  double smearing_sigma;   /* Hartree */
+  int search_method;       /* HQCGB_SEARCH_* */
+  int search_cycle;
+  double search_tol;
+  double tol;
+  int max_cycle;
+  int diis;
+  int diis_space;
+  int diis_start_cycle;
+  double diis_damp;
+  int precision;           /* HQCGB_PREC_* */
+  double exx_occ_threshold;/* skip orbitals with occupation <= this in exchange */
+  int want_forces;         /* keep derivative tables for hqcgb_forces */
+} hqcgb_params;
+
+typedef struct {
+  double *mo_coeff;   /* [nao][nao], AO rows, MO columns (device) */
+  double *dm;         /* [nao][nao] (device) */
+  double *bands;      /* [nao] Hartree (device) */
+  double *energies;   /* [5]: E, Ki, Vep, Vee (Hartree), Se (device) */
+  int *converged;     /* [1] (device) */
+  int *iterations;    /* [1] (device), may be NULL */
+} hqcgb_scf_out;
+
+typedef struct hqcgb_plan hqcgb_plan;
+
+/* Factory: validates the parameters and allocates the workspace.
+ * Replaces the table-building part of make_solver (hqc/pbc/solver.py:61-231). */
+int hqcgb_plan_create(const hqcgb_params *params, hqcgb_plan **plan);
+
+/* Frees everything the plan owns. */
+int hqcgb_plan_destroy(hqcgb_plan *plan);
+
+/* One SCF at the proton positions xp [n_atoms][3] (Bohr, device).
+ * Replaces hf_gamma / dft_gamma (hqc/pbc/solver.py:705-767, 839-899). */
+int hqcgb_scf(hqcgb_plan *plan, const double *xp, const hqcgb_scf_out *out, void *stream);
+
+/* Batched SCF over n_cfg configurations of the same plan: xp is
+ * [n_cfg][n_atoms][3], every output pointer is strided by its per-config size.
+ * The reference batches with jax.vmap (test/test.py:157). */
+int hqcgb_scf_batch(hqcgb_plan *plan, int n_cfg, const double *xp, const hqcgb_scf_out *out,
+                    void *stream);
+
+/* Nuclear gradient dE/dR [n_atoms][3] (Hartree/Bohr, device) of the last SCF.
+ * No counterpart in the reference (forces are absent there,
+ * doc/solver_algorithm.md:1210); with Fermi smearing it is the gradient of
+ * E - sigma*Se. */
+int hqcgb_forces(hqcgb_plan *plan, double *grad, void *stream);
+
+/* Proton-proton Ewald energy (Rydberg) and its gradient (Rydberg per rs unit).
+ * xp [n][3] in rs units, L in rs units: hqc/pbc/potential.py:103-130.
+ * grad may be NULL. */
+int hqcgb_ewald(const double *xp, int n, double L, double rs, double kappa, int gmax,
+                double *energy, double *grad, void *stream);
+
+/* Copy an internal buffer of the last SCF into dst (device), for tests and
+ * tools: "S", "T", "V", "phi", "rho", "vH", "vloc", "fock", "J", "K".
+ * Returns the number of bytes copied (or needed when dst is NULL), < 0 on error. */
+long long hqcgb_plan_query(hqcgb_plan *plan, const char *name, void *dst, size_t bytes,
+                           void *stream);
+
+/* Human-readable description of the last error on this host thread. */
+const char *hqcgb_last_error(void);
+
+/* Kernel launches issued on behalf of the caller since the last reset. */
+long long hqcgb_launch_count(int reset);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HQCGB_H */

@@ -1,0 +1,78 @@
+"""CPU-side checks of the product: the C-ABI library loads and exports every
+symbol declared in include/hqcgb.h; the basis parser and the host tables
+match the oracle.  No GPU compute is called here."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+def header_symbols():
+    text = open(os.path.join(ROOT, "include", "hqcgb.h")).read()
+    return sorted(set(re.findall(r"\b(hqcgb_[a-z_]+)\s*\(", text)))
+
+
+def test_header_symbols_exported():
+    from hqc_gb300 import build, _lib
+    build.build()
+    lib = ctypes.CDLL(_lib.LIB_PATH)
+    syms = header_symbols()
+    assert len(syms) >= 9
+    for s in syms:
+        assert hasattr(lib, s), s
+    assert set(syms) <= set(_lib.EXPORTS)
+
+
+def test_last_error_and_bad_args_without_gpu():
+    from hqc_gb300 import _lib
+    lib = _lib.load()
+    P = _lib.Params()
+    P.n_atoms = 0
+    h = ctypes.c_void_p()
+    st = lib.hqcgb_plan_create(ctypes.byref(P), ctypes.byref(h))
+    assert st == 2  # HQCGB_BAD_ARG, validated before any device call
+    assert b"n_atoms" in lib.hqcgb_last_error()
+
+
+@pytest.mark.parametrize("basis", ["gth-szv", "gth-dzv", "gth-dzvp", "gth-tzv2p", "gth-qzv2p"])
+def test_basis_tables_match_oracle(basis):
+    from hqc_gb300.basis import basis_tables
+    from oracle.basis import Basis
+    a, c, l, cart = basis_tables(basis)
+    B = Basis(basis)
+    np.testing.assert_allclose(a, B.alpha, rtol=0, atol=0)
+    np.testing.assert_allclose(c, B.coef, rtol=1e-14, atol=1e-15)
+    assert list(l) == list(B.l) and list(cart) == list(B.cart)
+
+
+def test_basis_errors_like_reference():
+    from hqc_gb300.basis import basis_tables, load_as_str
+    with pytest.raises(ValueError):
+        basis_tables("gth-cc-tzvp")  # d functions: l_max > 1 (solver.py:85-86)
+    with pytest.raises(FileNotFoundError):
+        load_as_str("H", "no-such-basis")
+
+
+def test_grid_and_lattice_rules():
+    from hqc_gb300.solver import grid_size, lattice_1d, lattice_sphere
+    from oracle.gpw import Setup
+    for n, rs, gl in [(4, 1.5, 0.12), (8, 1.25, None), (54, 1.31, None)]:
+        L = (4 / 3 * np.pi * n) ** (1 / 3)
+        gl = gl or L * rs / 80
+        st = Setup(n, L, rs, "gth-szv", grid_length=gl)
+        assert grid_size(L * rs, gl) == st.ng
+        np.testing.assert_array_equal(lattice_1d(L * rs), st.lat1d)
+        assert lattice_sphere(L * rs, 24.0).shape == st.lattice.shape
+
+
+def test_xc_codes_and_reference_errors():
+    from hqc_gb300.solver import xc_code
+    assert xc_code("lda,vwn") == 1 and xc_code("pbe") == 10
+    with pytest.raises(NameError):
+        xc_code("lda,pz81")
+    with pytest.raises(ValueError):
+        xc_code("b3lyp,x")
