@@ -44,7 +44,8 @@ class ScfOut(ctypes.Structure):
 
 EXPORTS = ("hqcgb_plan_create", "hqcgb_plan_destroy", "hqcgb_scf", "hqcgb_scf_batch",
            "hqcgb_forces", "hqcgb_ewald", "hqcgb_plan_query", "hqcgb_last_error",
-           "hqcgb_launch_count")
+           "hqcgb_launch_count", "hqcgb_profile", "hqcgb_stage_stats")
+N_STAGES = 13
 
 _lib = None
 
@@ -80,6 +81,10 @@ def load():
     lib.hqcgb_last_error.restype = ctypes.c_char_p
     lib.hqcgb_launch_count.argtypes = [ctypes.c_int]
     lib.hqcgb_launch_count.restype = ctypes.c_longlong
+    lib.hqcgb_profile.argtypes = [ctypes.c_int]
+    lib.hqcgb_stage_stats.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_char_p),
+                                      ctypes.POINTER(ctypes.c_longlong),
+                                      ctypes.POINTER(ctypes.c_double)]
     for name in EXPORTS:
         getattr(lib, name)
     _lib = lib
@@ -91,3 +96,20 @@ def check(status, allow=(0,)):
         msg = load().hqcgb_last_error().decode(errors="replace")
         raise HqcgbError(status, msg)
     return status
+
+
+def stage_stats():
+    """{stage name: (launches, device ms)} since the last profile(1)."""
+    lib = load()
+    out = {}
+    for k in range(N_STAGES):
+        name = ctypes.c_char_p()
+        cnt = ctypes.c_longlong()
+        ms = ctypes.c_double()
+        check(lib.hqcgb_stage_stats(k, ctypes.byref(name), ctypes.byref(cnt), ctypes.byref(ms)))
+        out[name.value.decode()] = (cnt.value, ms.value)
+    return out
+
+
+def profile(enable):
+    check(load().hqcgb_profile(int(enable)))

@@ -14,6 +14,19 @@ namespace hqcgb {
 void set_error(const std::string &msg);
 void count_launch(long long k = 1);
 
+// Per-stage device timing (CUDA events on the launching stream), enabled by
+// hqcgb_profile(1).  Stage names are listed in plan.cu (kStageNames).
+enum Stage { ST_GTO = 0, ST_PHI, ST_DENSITY, ST_QUAD, ST_FFT, ST_XC, ST_JACOBI, ST_GEMM_SMALL,
+             ST_OVERLAP, ST_FORCE_GRID, ST_EXCHANGE, ST_EWALD, ST_OTHER, ST_COUNT };
+void stage_mark(int stage, cudaStream_t st, bool begin);
+struct StageScope {
+  int s;
+  cudaStream_t st;
+  StageScope(int s_, cudaStream_t st_) : s(s_), st(st_) { stage_mark(s, st, true); }
+  ~StageScope() { stage_mark(s, st, false); }
+};
+#define HQ_STAGE(stage, stream) ::hqcgb::StageScope _hq_scope_##__LINE__(stage, stream)
+
 struct Error {
   int status;
   std::string msg;

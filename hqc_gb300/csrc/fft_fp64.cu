@@ -102,6 +102,7 @@ __global__ void k_dft_pass(double2 *__restrict__ c, int ng, int axis, const doub
 }
 
 void launch_fft3d(double2 *c, int ng, int batch, const double2 *tw, bool inverse, cudaStream_t st) {
+  HQ_STAGE(ST_FFT, st);
   HQ_REQUIRE(ng <= kMaxGrid, "grid too large for the direct DFT passes");
   long long N = (long long)ng * ng * ng;
   size_t smem = ((size_t)ng * 32 + ng) * sizeof(double2);
@@ -227,6 +228,7 @@ __global__ void k_vloc_G(const double2 *__restrict__ ph, int n_atoms, int ng, do
 
 void launch_vloc_G(const double *xp, int n_atoms, int ng, double L, double2 *ph, double2 *out,
                    cudaStream_t st) {
+  HQ_STAGE(ST_OTHER, st);
   k_phases<<<ceil_div(n_atoms * 3 * ng, 128), 128, 0, st>>>(xp, n_atoms, ng, L, ph);
   HQ_LAUNCH_CHECK();
   long long N = (long long)ng * ng * ng;
@@ -280,6 +282,7 @@ int vloc_force_blocks(long long N) { return ceil_div(N, 256); }
 
 void launch_vloc_force(const double2 *ph, const double2 *F, int n_atoms, int ng, double L,
                        double *part, cudaStream_t st) {
+  HQ_STAGE(ST_FORCE_GRID, st);
   long long N = (long long)ng * ng * ng;
   k_vloc_force<<<vloc_force_blocks(N), 256, 0, st>>>(ph, F, n_atoms, ng, L, part);
   HQ_LAUNCH_CHECK();

@@ -25,6 +25,7 @@ __global__ void k_psi(const double *__restrict__ C, int nao, int col, const doub
 
 void launch_psi(const double *C, int nao, int col, const double *phi, long long N, double *psi,
                 cudaStream_t st) {
+  HQ_STAGE(ST_EXCHANGE, st);
   k_psi<<<ceil_div(N, 256), 256, 0, st>>>(C, nao, col, phi, N, psi);
   HQ_LAUNCH_CHECK();
 }
@@ -68,6 +69,7 @@ __global__ void k_gga_psi(const double *__restrict__ dphi, const double *__restr
 
 void launch_gga_psi(const double *dphi, const double *u, int nao, long long N, double *Psi,
                     cudaStream_t st) {
+  HQ_STAGE(ST_FORCE_GRID, st);
   k_gga_psi<<<ceil_div((long long)nao * N, 256), 256, 0, st>>>(dphi, u, nao, N, Psi);
   HQ_LAUNCH_CHECK();
 }
@@ -137,6 +139,7 @@ void launch_force_grid(const double *F1d, const double *coef, const int *ao_l, c
                        int nao_atom, int nprim, int nao, int ng, const double *veff,
                        const double *X, const double *u, const double *DPsi, const double *Z,
                        double dV, double *part, cudaStream_t st) {
+  HQ_STAGE(ST_FORCE_GRID, st);
   long long N = (long long)ng * ng * ng;
   dim3 grid(force_grid_blocks(N), nao);
   k_force_grid<<<grid, 256, 0, st>>>(F1d, coef, ao_l, ao_cart, nao_atom, nprim, nao, ng, veff, X, u,

@@ -54,6 +54,7 @@ __global__ void k_gto1d(const double *__restrict__ xp, int n_atoms, int ng, doub
 
 void launch_gto1d(const double *xp, int n_atoms, int ng, double L, const double *alpha, int nprim,
                   const double *lat1d, int nlat, double *F, cudaStream_t st) {
+  HQ_STAGE(ST_GTO, st);
   long long total = (long long)n_atoms * 3 * ng * nprim;
   k_gto1d<<<ceil_div(total, 256), 256, 0, st>>>(xp, n_atoms, ng, L, alpha, nprim, lat1d, nlat, F);
   HQ_LAUNCH_CHECK();
@@ -100,6 +101,7 @@ __global__ void k_phi(const double *__restrict__ F, const double *__restrict__ c
 void launch_phi(const double *F, const double *coef, const int *ao_l, const int *ao_cart,
                 int nao_atom, int nprim, int nao, int ng, double *phi, double *dphi,
                 cudaStream_t st) {
+  HQ_STAGE(ST_PHI, st);
   long long total = (long long)nao * ng * ng * ng;
   k_phi<<<ceil_div(total, 256), 256, 0, st>>>(F, coef, ao_l, ao_cart, nao_atom, nprim, nao, ng, phi,
                                                dphi);
@@ -151,6 +153,7 @@ __global__ void k_density(const double *__restrict__ phi, const double *__restri
 
 void launch_density(const double *phi, const double *dphi, const double *D, int nao, long long N,
                     double *rho, double *grho, double *Xout, cudaStream_t st) {
+  HQ_STAGE(ST_DENSITY, st);
   size_t smem = ((size_t)nao * 32 + 8 * 4 * 32) * sizeof(double);
   HQ_REQUIRE(smem <= 227 * 1024, "too many AOs for the FP64 density tile");
   static bool attr_set = false;
@@ -222,6 +225,7 @@ int quad_chunks(long long N) { return ceil_div(N, kQuadChunk); }
 void launch_quadrature(const double *A, const double *B, const double *w, int nao, long long N,
                        bool sym, double scale, bool accumulate, double *partial, double *M,
                        cudaStream_t st) {
+  HQ_STAGE(ST_QUAD, st);
   int nt = ceil_div(nao, 32);
   int nchunk = quad_chunks(N);
   dim3 grid(nt, nt, nchunk);
@@ -279,6 +283,7 @@ int xc_blocks(long long N) { return ceil_div(N, 256); }
 void launch_xc_pointwise(int kind, const double *rho, const double *grho, const double *vh,
                          long long N, double dV, double *w, double *vxc_out, double *u,
                          double *part, cudaStream_t st) {
+  HQ_STAGE(ST_XC, st);
   k_xc_pointwise<<<xc_blocks(N), 256, 0, st>>>(kind, rho, grho, vh, N, dV, w, vxc_out, u, part);
   HQ_LAUNCH_CHECK();
 }
@@ -298,6 +303,7 @@ __global__ void k_gga_operand(const double *__restrict__ phi, const double *__re
 
 void launch_gga_operand(const double *phi, const double *dphi, const double *w, const double *u,
                         int nao, long long N, double dV, double *Z, cudaStream_t st) {
+  HQ_STAGE(ST_XC, st);
   k_gga_operand<<<ceil_div((long long)nao * N, 256), 256, 0, st>>>(phi, dphi, w, u, nao, N, dV, Z);
   HQ_LAUNCH_CHECK();
 }

@@ -122,6 +122,7 @@ void launch_overlap_kinetic(const double *xp, int n, int nb, int nprim, const do
                             const double *coef, const int *ao_l, const int *ao_cart,
                             const double *lattice, int nlat, double *S, double *T, const double *D,
                             const double *W, double *gpart, double *grad, cudaStream_t st) {
+  HQ_STAGE(ST_OVERLAP, st);
   long long total = (long long)n * n * nb * nb;
   k_overlap_kinetic<<<ceil_div(total, 128), 128, 0, st>>>(xp, n, nb, nprim, alpha, coef, ao_l,
                                                           ao_cart, lattice, nlat, S, T, D, W, gpart);
@@ -220,6 +221,7 @@ __global__ void k_ewald_finish(const double *__restrict__ pair_e, const double *
 
 void launch_ewald(const double *xp, int n, double L, double rs, double kappa, int gmax,
                   double *pair_e, double *pair_g, double *energy, double *grad, cudaStream_t st) {
+  HQ_STAGE(ST_EWALD, st);
   int npair = n * (n - 1) / 2;
   if (npair > 0) {
     k_ewald_pairs<<<npair, 256, 0, st>>>(xp, n, L, kappa, gmax, pair_e, pair_g);

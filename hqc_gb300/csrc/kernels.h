@@ -49,6 +49,8 @@ void dot(long long n, const double *A, const double *B, double scale, double *ou
          cudaStream_t st);
 void jacobi_eigh(int n, int batch, double *A, double *V, double *w, double *tmp, int *status,
                  cudaStream_t st);
+void eigh_tql(int n, int batch, double *A, double *V, double *w, double *work, int *status,
+              cudaStream_t st);
 void diis_extrapolate(int space, int n, const double *Fk, const double *ek, int last, double damp,
                       double *B, double *c, double *F, cudaStream_t st);
 void occupations(int n_elec, int nmo, int smearing, int method, double sigma, int search, int cycle,

@@ -57,6 +57,7 @@ __global__ void k_gemm(int ta, int tb, int M, int N, int K, double alpha,
 void gemm(bool ta, bool tb, int M, int N, int K, double alpha, const double *A, int lda,
           const double *B, int ldb, const double *d, double beta, double *C, int ldc,
           cudaStream_t st) {
+  HQ_STAGE(ST_GEMM_SMALL, st);
   dim3 grid(ceil_div(N, 32), ceil_div(M, 32));
   k_gemm<<<grid, 256, 0, st>>>(ta, tb, M, N, K, alpha, A, lda, B, ldb, d, beta, C, ldc);
   HQ_LAUNCH_CHECK();
@@ -210,6 +211,7 @@ __global__ void __launch_bounds__(1024) k_jacobi(int n, double *__restrict__ Ab,
 
 void jacobi_eigh(int n, int batch, double *A, double *V, double *w, double *tmp, int *status,
                  cudaStream_t st) {
+  HQ_STAGE(ST_JACOBI, st);
   int m = n + (n & 1);
   size_t smem = (size_t)(m / 2) * (2 * sizeof(double) + 2 * sizeof(int));
   k_jacobi<<<batch, 1024, smem, st>>>(n, A, V, w, tmp, 60, 1e-14, status);
@@ -282,6 +284,7 @@ __global__ void k_diis_extrapolate(int space, long long nn, const double *__rest
 
 void diis_extrapolate(int space, int n, const double *Fk, const double *ek, int last, double damp,
                       double *B, double *c, double *F, cudaStream_t st) {
+  HQ_STAGE(ST_GEMM_SMALL, st);
   HQ_REQUIRE(space <= 32, "diis_space > 32");
   long long nn = (long long)n * n;
   k_diis_B<<<space * space, 256, 0, st>>>(space, nn, ek, B);
@@ -380,6 +383,7 @@ __global__ void k_occupations(OccParams P, const double *__restrict__ w, double 
 
 void occupations(int n_elec, int nmo, int smearing, int method, double sigma, int search, int cycle,
                  double tol, double shift, const double *w, double *f, double *mu, cudaStream_t st) {
+  HQ_STAGE(ST_OTHER, st);
   OccParams P{n_elec, nmo, smearing, method, search, cycle, sigma, tol, shift};
   k_occupations<<<1, 32, 0, st>>>(P, w, f, mu);
   HQ_LAUNCH_CHECK();

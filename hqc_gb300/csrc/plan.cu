@@ -19,6 +19,44 @@ static thread_local std::string g_err;
 static std::atomic<long long> g_launches{0};
 void set_error(const std::string &m) { g_err = m; }
 void count_launch(long long k) { g_launches += k; }
+
+static const char *kStageNames[ST_COUNT] = {"gto1d", "phi", "density", "quadrature", "fft", "xc",
+                                            "jacobi", "gemm_small", "overlap", "force_grid",
+                                            "exchange", "ewald", "other"};
+struct StageRec {
+  int stage;
+  cudaEvent_t a, b;
+};
+static bool g_profile = false;
+static std::vector<StageRec> g_recs;
+static std::vector<cudaEvent_t> g_event_pool;
+static int g_open[ST_COUNT];
+static cudaEvent_t g_open_ev[ST_COUNT];
+
+static cudaEvent_t take_event() {
+  if (!g_event_pool.empty()) {
+    cudaEvent_t e = g_event_pool.back();
+    g_event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  return e;
+}
+
+void stage_mark(int stage, cudaStream_t st, bool begin) {
+  if (!g_profile) return;
+  if (begin) {
+    if (g_open[stage]++ > 0) return;  // nested scopes of one stage count once
+    g_open_ev[stage] = take_event();
+    cudaEventRecord(g_open_ev[stage], st);
+  } else {
+    if (--g_open[stage] > 0) return;
+    cudaEvent_t b = take_event();
+    cudaEventRecord(b, st);
+    g_recs.push_back({stage, g_open_ev[stage], b});
+  }
+}
 }  // namespace hqcgb
 
 using namespace hqcgb;
@@ -225,11 +263,20 @@ static void sync_scalars(Ctx &c) {
   HQ_CUDA(cudaStreamSynchronize(c.st));
 }
 
+// Symmetric eigensolver: Householder + QL (eigh_fp64.cu); the Jacobi solver
+// is kept as the fallback when a QL sweep limit is hit.
 static void eigh(Ctx &c, const double *A, double *vecs, double *vals) {
   hqcgb_plan *p = c.p;
   int n = p->nao;
   HQ_CUDA(cudaMemcpyAsync(p->jA, A, sizeof(double) * n * n, cudaMemcpyDeviceToDevice, c.st));
-  jacobi_eigh(n, 1, p->jA, vecs, vals, p->jtmp, p->jstat, c.st);
+  eigh_tql(n, 1, p->jA, vecs, vals, p->jtmp, p->jstat, c.st);
+  int stt = 0;
+  HQ_CUDA(cudaMemcpyAsync(&stt, p->jstat, sizeof(int), cudaMemcpyDeviceToHost, c.st));
+  HQ_CUDA(cudaStreamSynchronize(c.st));
+  if (stt < 0) {
+    HQ_CUDA(cudaMemcpyAsync(p->jA, A, sizeof(double) * n * n, cudaMemcpyDeviceToDevice, c.st));
+    jacobi_eigh(n, 1, p->jA, vecs, vals, p->jtmp, p->jstat, c.st);
+  }
 }
 
 // C, w from a Fock matrix: F' = v^T F v, eigh, C = v c'
@@ -631,6 +678,40 @@ long long hqcgb_plan_query(hqcgb_plan *p, const char *name, void *dst, size_t by
 }
 
 const char *hqcgb_last_error(void) { return g_err.c_str(); }
+
+int hqcgb_profile(int enable) {
+  HQ_GUARD({
+    HQ_CUDA(cudaDeviceSynchronize());
+    for (auto &r : g_recs) {
+      g_event_pool.push_back(r.a);
+      g_event_pool.push_back(r.b);
+    }
+    g_recs.clear();
+    for (int k = 0; k < ST_COUNT; ++k) g_open[k] = 0;
+    g_profile = enable != 0;
+    return HQCGB_OK;
+  });
+}
+
+int hqcgb_stage_stats(int stage, const char **name, long long *count, double *ms) {
+  HQ_GUARD({
+    HQ_REQUIRE(stage >= 0 && stage < ST_COUNT, "stage out of range");
+    HQ_CUDA(cudaDeviceSynchronize());
+    long long c = 0;
+    double t = 0;
+    for (auto &r : g_recs) {
+      if (r.stage != stage) continue;
+      float f = 0;
+      HQ_CUDA(cudaEventElapsedTime(&f, r.a, r.b));
+      t += f;
+      ++c;
+    }
+    if (name) *name = kStageNames[stage];
+    if (count) *count = c;
+    if (ms) *ms = t;
+    return HQCGB_OK;
+  });
+}
 
 long long hqcgb_launch_count(int reset) {
   long long v = g_launches.load();

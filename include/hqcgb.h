@@ -129,6 +129,17 @@ const char *hqcgb_last_error(void);
 /* Kernel launches issued on behalf of the caller since the last reset. */
 long long hqcgb_launch_count(int reset);
 
+/* Stage timing: hqcgb_profile(1) clears the record and starts timing every
+ * stage (grid build, density, quadrature, FFT, xc, eigensolver, ...) with
+ * CUDA events on the launching stream; hqcgb_profile(0) clears and stops.
+ * No counterpart in the reference (its only timing is wall clock prints,
+ * test/test.py:71-78). */
+int hqcgb_profile(int enable);
+
+/* Launch count and summed device milliseconds of stage index `stage`
+ * (0 <= stage < 13) since hqcgb_profile(1); `name` receives its label. */
+int hqcgb_stage_stats(int stage, const char **name, long long *count, double *ms);
+
 #ifdef __cplusplus
 }
 #endif

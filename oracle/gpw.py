@@ -374,16 +374,22 @@ class Solver:
 
     # grid pieces --------------------------------------------------------
     def density(self, D, phi, grad=None):
-        X = np.einsum("pq,qijk->pijk", D, phi)
-        rho = np.einsum("pijk,pijk->ijk", phi, X)
+        """rho = sum_pq D_pq phi_p phi_q (solver.py:690), as X = D phi (BLAS)."""
+        shp = phi.shape
+        P = phi.reshape(shp[0], -1)
+        X = (D @ P)
+        rho = np.einsum("pg,pg->g", P, X).reshape(shp[1:])
+        X = X.reshape(shp)
         if grad is None:
             return rho, None, X
-        grho = 2 * np.einsum("dpijk,pijk->dijk", grad, X)
+        grho = 2 * np.einsum("dpg,pg->dg", grad.reshape(3, shp[0], -1),
+                             X.reshape(shp[0], -1)).reshape((3,) + shp[1:])
         return rho, grho, X
 
     def quadrature(self, w, phi):
         """V_pq = dV sum_r phi_p w phi_q (solver.py:693)."""
-        return self.st.dV * np.einsum("pijk,ijk,qijk->pq", phi, w, phi, optimize=True)
+        P = phi.reshape(phi.shape[0], -1)
+        return self.st.dV * ((P * w.reshape(1, -1)) @ P.T)
 
     def hartree(self, rho, phi):
         vh = self.st.poisson(rho)
@@ -400,7 +406,7 @@ class Solver:
             psi = np.einsum("p,pijk->ijk", C[:, i], phi)
             pair = phi * psi[None]
             W = st.poisson(pair)
-            K += occ[i] * st.dV * np.einsum("pijk,qijk->pq", pair, W, optimize=True)
+            K += occ[i] * st.dV * (pair.reshape(pair.shape[0], -1) @ W.reshape(W.shape[0], -1).T)
         K0 = 4 * np.pi / st.L * MADELUNG_SC * (Stilde @ D @ Stilde)
         return K + K0
 
@@ -411,8 +417,8 @@ class Solver:
         V = self.quadrature(vrho, phi)
         if self.xc.gga:
             u = 2 * vsig[None] * grho  # 2 v_sigma grad rho
-            Y = np.einsum("dijk,dpijk->pijk", u, grad)
-            M = self.st.dV * np.einsum("pijk,qijk->pq", Y, phi, optimize=True)
+            Y = np.einsum("dg,dpg->pg", u.reshape(3, -1), grad.reshape(3, grad.shape[1], -1))
+            M = self.st.dV * (Y @ phi.reshape(phi.shape[0], -1).T)
             V = V + M + M.T
         return Exc, V
 
@@ -425,8 +431,9 @@ class Solver:
         phi, grad, _ = st.ao_grid(xp, deriv=1 if need_grad else 0)
         vloc = st.vloc_grid(xp)
         V = self.quadrature(vloc, phi)
+        P = phi.reshape(phi.shape[0], -1)
         return dict(xp=xp, S=S, T=T, phi=phi, grad=grad, vloc=vloc, V=V,
-                    Stilde=st.dV * np.einsum("pijk,qijk->pq", phi, phi, optimize=True))
+                    Stilde=st.dV * (P @ P.T))
 
     def solve(self, xp_rs):
         g = self.setup_geometry(xp_rs)
