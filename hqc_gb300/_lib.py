@@ -44,7 +44,7 @@ class ScfOut(ctypes.Structure):
 
 EXPORTS = ("hqcgb_plan_create", "hqcgb_plan_destroy", "hqcgb_scf", "hqcgb_scf_batch",
            "hqcgb_forces", "hqcgb_ewald", "hqcgb_plan_query", "hqcgb_last_error",
-           "hqcgb_launch_count", "hqcgb_profile", "hqcgb_stage_stats")
+           "hqcgb_launch_count", "hqcgb_profile", "hqcgb_stage_stats", "hqcgb_eigh")
 N_STAGES = 13
 
 _lib = None
@@ -82,6 +82,8 @@ def load():
     lib.hqcgb_launch_count.argtypes = [ctypes.c_int]
     lib.hqcgb_launch_count.restype = ctypes.c_longlong
     lib.hqcgb_profile.argtypes = [ctypes.c_int]
+    lib.hqcgb_eigh.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                               ctypes.c_void_p, ctypes.c_void_p]
     lib.hqcgb_stage_stats.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_char_p),
                                       ctypes.POINTER(ctypes.c_longlong),
                                       ctypes.POINTER(ctypes.c_double)]
@@ -113,3 +115,21 @@ def stage_stats():
 
 def profile(enable):
     check(load().hqcgb_profile(int(enable)))
+
+
+def eigh(A):
+    """FP64 symmetric eigendecomposition on the GPU: (w ascending, V columns).
+
+    ``A`` is a float64 CUDA tensor of shape (n, n) or (batch, n, n)."""
+    import torch
+    lib = load()
+    A = A.contiguous()
+    single = A.dim() == 2
+    A3 = A.unsqueeze(0) if single else A
+    b, n, _ = A3.shape
+    w = torch.empty(b, n, dtype=torch.float64, device=A.device)
+    V = torch.empty(b, n, n, dtype=torch.float64, device=A.device)
+    st = ctypes.c_void_p(torch.cuda.current_stream(A.device).cuda_stream)
+    check(lib.hqcgb_eigh(n, b, ctypes.c_void_p(A3.data_ptr()), ctypes.c_void_p(w.data_ptr()),
+                         ctypes.c_void_p(V.data_ptr()), st))
+    return (w[0], V[0]) if single else (w, V)

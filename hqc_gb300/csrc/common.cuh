@@ -69,7 +69,8 @@ __device__ inline T warp_sum(T v) {
   return v;
 }
 
-// Sum over the block; result valid in thread 0. blockDim.x multiple of 32.
+// Sum over the block, returned to every thread. blockDim.x multiple of 32;
+// every thread of the block must call it.
 template <typename T>
 __device__ inline T block_sum(T v, T *sh /* >= 32 */) {
   v = warp_sum(v);
@@ -79,6 +80,10 @@ __device__ inline T block_sum(T v, T *sh /* >= 32 */) {
   int nw = (blockDim.x + 31) >> 5;
   v = (threadIdx.x < nw) ? sh[threadIdx.x] : T(0);
   if (w == 0) v = warp_sum(v);
+  __syncthreads();
+  if (threadIdx.x == 0) sh[0] = v;
+  __syncthreads();
+  v = sh[0];
   __syncthreads();
   return v;
 }

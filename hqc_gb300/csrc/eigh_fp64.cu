@@ -237,10 +237,10 @@ void eigh_tql(int n, int batch, double *A, double *V, double *w, double *work, i
   HQ_STAGE(ST_JACOBI, st);
   size_t smem = (size_t)7 * n * sizeof(double);
   HQ_REQUIRE(smem <= 200 * 1024, "matrix too large for the eigensolver");
-  static bool attr = false;
-  if (!attr) {
-    HQ_CUDA(cudaFuncSetAttribute(k_eigh_tql, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
-    attr = true;
+  static size_t attr = 0;
+  if (smem > attr) {
+    HQ_CUDA(cudaFuncSetAttribute(k_eigh_tql, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = smem;
   }
   k_eigh_tql<<<batch, kEigThreads, smem, st>>>(n, A, V, w, work, status);
   HQ_LAUNCH_CHECK();

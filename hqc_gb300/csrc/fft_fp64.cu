@@ -106,10 +106,10 @@ void launch_fft3d(double2 *c, int ng, int batch, const double2 *tw, bool inverse
   HQ_REQUIRE(ng <= kMaxGrid, "grid too large for the direct DFT passes");
   long long N = (long long)ng * ng * ng;
   size_t smem = ((size_t)ng * 32 + ng) * sizeof(double2);
-  static bool attr = false;
-  if (!attr) {
-    HQ_CUDA(cudaFuncSetAttribute(k_dft_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
-    attr = true;
+  static size_t attr = 0;
+  if (smem > attr) {
+    HQ_CUDA(cudaFuncSetAttribute(k_dft_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = smem;
   }
   int zb = (ng + 31) / 32;
   for (int axis = 2; axis >= 0; --axis) {

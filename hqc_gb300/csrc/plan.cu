@@ -677,6 +677,42 @@ long long hqcgb_plan_query(hqcgb_plan *p, const char *name, void *dst, size_t by
   }
 }
 
+int hqcgb_eigh(int n, int batch, const double *A, double *w, double *V, void *stream) {
+  HQ_GUARD({
+    HQ_REQUIRE(A && w && V && n >= 1 && n <= kMaxNao && batch >= 1, "bad argument");
+    cudaStream_t st = (cudaStream_t)stream;
+    size_t nn = (size_t)n * n * batch;
+    double *work = nullptr, *Ac = nullptr;
+    int *stat = nullptr;
+    HQ_CUDA(cudaMallocAsync(&work, nn * sizeof(double), st));
+    HQ_CUDA(cudaMallocAsync(&Ac, nn * sizeof(double), st));
+    HQ_CUDA(cudaMallocAsync(&stat, batch * sizeof(int), st));
+    HQ_CUDA(cudaMemcpyAsync(Ac, A, nn * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    eigh_tql(n, batch, Ac, V, w, work, stat, st);
+    std::vector<int> hs(batch);
+    HQ_CUDA(cudaMemcpyAsync(hs.data(), stat, batch * sizeof(int), cudaMemcpyDeviceToHost, st));
+    HQ_CUDA(cudaStreamSynchronize(st));
+    int status = HQCGB_OK;
+    for (int b = 0; b < batch; ++b) {
+      if (hs[b] < 0) {
+        HQ_CUDA(cudaMemcpyAsync(Ac + (size_t)b * n * n, A + (size_t)b * n * n,
+                                (size_t)n * n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+        jacobi_eigh(n, 1, Ac + (size_t)b * n * n, V + (size_t)b * n * n, w + (size_t)b * n,
+                    work, stat, st);
+        int js = 0;
+        HQ_CUDA(cudaMemcpyAsync(&js, stat, sizeof(int), cudaMemcpyDeviceToHost, st));
+        HQ_CUDA(cudaStreamSynchronize(st));
+        if (js < 0) status = HQCGB_EIG_FAIL;
+      }
+    }
+    HQ_CUDA(cudaFreeAsync(work, st));
+    HQ_CUDA(cudaFreeAsync(Ac, st));
+    HQ_CUDA(cudaFreeAsync(stat, st));
+    if (status != HQCGB_OK) throw Error{status, "eigensolver did not converge"};
+    return HQCGB_OK;
+  });
+}
+
 const char *hqcgb_last_error(void) { return g_err.c_str(); }
 
 int hqcgb_profile(int enable) {

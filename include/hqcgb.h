@@ -123,6 +123,13 @@ int hqcgb_ewald(const double *xp, int n, double L, double rs, double kappa, int 
 long long hqcgb_plan_query(hqcgb_plan *plan, const char *name, void *dst, size_t bytes,
                            void *stream);
 
+/* The engine's FP64 symmetric eigensolver (Householder tridiagonalisation +
+ * implicit QL, Jacobi fallback) on `batch` row-major n x n matrices A
+ * (device, not modified): ascending eigenvalues w [batch][n] and eigenvectors
+ * as the columns of V [batch][n][n].  Stands in for jnp.linalg.eigh as used
+ * at hqc/pbc/solver.py:729,741 and hqc/pbc/scf.py:69,138,198. */
+int hqcgb_eigh(int n, int batch, const double *A, double *w, double *V, void *stream);
+
 /* Human-readable description of the last error on this host thread. */
 const char *hqcgb_last_error(void);
 

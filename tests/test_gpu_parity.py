@@ -158,3 +158,42 @@ def test_coincident_atoms_raise():
     s = make_solver(n, L, rs, "gth-dzv", grid_length=0.3)
     with pytest.raises(HqcgbError):
         s(xp)
+
+
+@pytest.mark.parametrize("n,batch", [(1, 1), (2, 3), (33, 2), (160, 1), (270, 2)])
+def test_eigensolver_matches_lapack(n, batch):
+    import torch
+    from hqc_gb300._lib import eigh
+    rng = np.random.default_rng(n)
+    M = rng.normal(size=(batch, n, n))
+    M = M + np.transpose(M, (0, 2, 1))
+    if n >= 160:  # a clustered spectrum like a symmetric lattice's bands
+        Q = np.linalg.qr(rng.normal(size=(n, n)))[0]
+        lam = np.repeat(np.linspace(-2, 3, n // 10), 10)[:n] + 1e-9 * rng.normal(size=n)
+        M[0] = (Q * lam) @ Q.T
+        M[0] = 0.5 * (M[0] + M[0].T)
+    w, V = eigh(torch.as_tensor(M, device="cuda"))
+    w, V = _np(w), _np(V)
+    for b in range(batch):
+        np.testing.assert_allclose(w[b], np.linalg.eigvalsh(M[b]), atol=1e-12 * max(1, np.abs(M[b]).max()))
+        np.testing.assert_allclose(V[b].T @ V[b], np.eye(n), atol=1e-12)
+        np.testing.assert_allclose(M[b] @ V[b], V[b] * w[b], atol=1e-11 * max(1, np.abs(M[b]).max()))
+
+
+def test_h16_dzvp_pbe_forces_match_oracle():
+    """A system above one warp of AOs (80) exercising every block reduction."""
+    from hqc_gb300 import make_solver
+    from oracle.gpw import Solver
+    from oracle.forces import electronic_gradient
+    n, rs = 16, 1.31
+    L = (4 / 3 * np.pi * n) ** (1 / 3)
+    xp = np.random.default_rng(11).uniform(0, L, (n, 3))
+    kw = dict(grid_length=L * rs / 24, dft=True, xc="pbe", tol=1e-9, max_cycle=100)
+    s = make_solver(n, L, rs, "gth-dzvp", forces=True, **kw)
+    out = s(xp)
+    g = _np(s.plan.forces())
+    ref = Solver(n, L, rs, "gth-dzvp", **kw)
+    ro = ref.solve(xp)
+    assert abs(float(out[3]) - ro[3]) < 1e-8
+    np.testing.assert_allclose(_np(out[2]), ro[2], atol=1e-6)
+    np.testing.assert_allclose(g, electronic_gradient(ref), atol=1e-7)
