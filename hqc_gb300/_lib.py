@@ -44,7 +44,8 @@ class ScfOut(ctypes.Structure):
 
 EXPORTS = ("hqcgb_plan_create", "hqcgb_plan_destroy", "hqcgb_scf", "hqcgb_scf_batch",
            "hqcgb_forces", "hqcgb_ewald", "hqcgb_plan_query", "hqcgb_last_error",
-           "hqcgb_launch_count", "hqcgb_profile", "hqcgb_stage_stats", "hqcgb_eigh")
+           "hqcgb_launch_count", "hqcgb_profile", "hqcgb_stage_stats", "hqcgb_eigh",
+           "hqcgb_eigh_noalloc")
 N_STAGES = 13
 
 _lib = None
@@ -84,6 +85,8 @@ def load():
     lib.hqcgb_profile.argtypes = [ctypes.c_int]
     lib.hqcgb_eigh.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                ctypes.c_void_p, ctypes.c_void_p]
+    lib.hqcgb_eigh_noalloc.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.c_void_p, ctypes.c_void_p]
     lib.hqcgb_stage_stats.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_char_p),
                                       ctypes.POINTER(ctypes.c_longlong),
                                       ctypes.POINTER(ctypes.c_double)]
@@ -133,3 +136,27 @@ def eigh(A):
     check(lib.hqcgb_eigh(n, b, ctypes.c_void_p(A3.data_ptr()), ctypes.c_void_p(w.data_ptr()),
                          ctypes.c_void_p(V.data_ptr()), st))
     return (w[0], V[0]) if single else (w, V)
+
+
+EIGH_NOALLOC_MAX_N = 320
+
+
+def eigh_noalloc(A, w=None, V=None):
+    """``eigh`` of one (n, n) float64 CUDA matrix through ``hqcgb_eigh_noalloc``.
+
+    The engine call allocates nothing (its scratch is a static device array
+    shared by all calls on the device, n <= 320).  Callers that cannot
+    allocate pass preallocated ``w`` (n,) and ``V`` (n, n) buffers; otherwise
+    they are created here, on the torch side."""
+    import torch
+    lib = load()
+    A = A.contiguous()
+    n = A.shape[0]
+    if w is None:
+        w = torch.empty(n, dtype=torch.float64, device=A.device)
+    if V is None:
+        V = torch.empty(n, n, dtype=torch.float64, device=A.device)
+    st = ctypes.c_void_p(torch.cuda.current_stream(A.device).cuda_stream)
+    check(lib.hqcgb_eigh_noalloc(n, ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(w.data_ptr()),
+                                 ctypes.c_void_p(V.data_ptr()), st))
+    return w, V

@@ -130,6 +130,19 @@ long long hqcgb_plan_query(hqcgb_plan *plan, const char *name, void *dst, size_t
  * at hqc/pbc/solver.py:729,741 and hqc/pbc/scf.py:69,138,198. */
 int hqcgb_eigh(int n, int batch, const double *A, double *w, double *V, void *stream);
 
+/* Largest n accepted by hqcgb_eigh_noalloc. */
+#define HQCGB_EIGH_NOALLOC_MAX_N 320
+
+/* hqcgb_eigh for one matrix (n <= HQCGB_EIGH_NOALLOC_MAX_N) that allocates
+ * nothing: for callers that cannot allocate device memory, such as code
+ * inside a framework that owns every device buffer (an XLA custom call in a
+ * jitted program) or loops that must not wait on an allocation.  Its scratch
+ * is a static device array of about 1.6 MB per GPU, shared by every call on
+ * that device (calls whose device work overlaps race on it); the first call
+ * on a device looks the array up and should precede any stream capture.
+ * No counterpart in the reference. */
+int hqcgb_eigh_noalloc(int n, const double *A, double *w, double *V, void *stream);
+
 /* Human-readable description of the last error on this host thread. */
 const char *hqcgb_last_error(void);
 
