@@ -45,7 +45,7 @@ class ScfOut(ctypes.Structure):
 EXPORTS = ("hqcgb_plan_create", "hqcgb_plan_destroy", "hqcgb_scf", "hqcgb_scf_batch",
            "hqcgb_forces", "hqcgb_ewald", "hqcgb_plan_query", "hqcgb_last_error",
            "hqcgb_launch_count", "hqcgb_profile", "hqcgb_stage_stats", "hqcgb_eigh",
-           "hqcgb_eigh_noalloc")
+           "hqcgb_eigh_noalloc", "hqcgb_tc_quadrature", "hqcgb_tc_density")
 N_STAGES = 13
 
 _lib = None
@@ -85,6 +85,12 @@ def load():
     lib.hqcgb_profile.argtypes = [ctypes.c_int]
     lib.hqcgb_eigh.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                ctypes.c_void_p, ctypes.c_void_p]
+    lib.hqcgb_tc_quadrature.argtypes = [ctypes.c_int, ctypes.c_longlong, ctypes.c_longlong,
+                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                        ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    lib.hqcgb_tc_density.argtypes = [ctypes.c_int, ctypes.c_longlong, ctypes.c_longlong,
+                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_void_p, ctypes.c_void_p]
     lib.hqcgb_eigh_noalloc.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                        ctypes.c_void_p, ctypes.c_void_p]
     lib.hqcgb_stage_stats.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_char_p),
@@ -160,3 +166,30 @@ def eigh_noalloc(A, w=None, V=None):
     check(lib.hqcgb_eigh_noalloc(n, ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(w.data_ptr()),
                                  ctypes.c_void_p(V.data_ptr()), st))
     return w, V
+
+
+def tc_quadrature(phi32, w32, nsplit=2, drain=2):
+    """M = phi diag(w) phi^T on the tensor cores; phi32 (nao, ld), w32 (ld,) fp32 CUDA."""
+    import torch
+    lib = load()
+    nao, ld = phi32.shape
+    M = torch.empty(nao, nao, dtype=torch.float64, device=phi32.device)
+    st = ctypes.c_void_p(torch.cuda.current_stream(phi32.device).cuda_stream)
+    check(lib.hqcgb_tc_quadrature(nao, ld, ld, ctypes.c_void_p(phi32.data_ptr()),
+                                  ctypes.c_void_p(w32.data_ptr()), nsplit, drain,
+                                  ctypes.c_void_p(M.data_ptr()), st))
+    return M
+
+
+def tc_density(phi32, D32, N=None, nsplit=2, drain=1):
+    """rho[g] = sum_pq D[p][q] phi[p][g] phi[q][g] on the tensor cores."""
+    import torch
+    lib = load()
+    nao, ld = phi32.shape
+    N = ld if N is None else N
+    rho = torch.empty(N, dtype=torch.float64, device=phi32.device)
+    st = ctypes.c_void_p(torch.cuda.current_stream(phi32.device).cuda_stream)
+    check(lib.hqcgb_tc_density(nao, N, ld, ctypes.c_void_p(phi32.data_ptr()),
+                               ctypes.c_void_p(D32.data_ptr()), nsplit, drain,
+                               ctypes.c_void_p(rho.data_ptr()), st))
+    return rho

@@ -18,74 +18,87 @@ namespace hqcgb {
 
 constexpr int kEigThreads = 1024;
 
+__device__ inline double e_sqrt(double x) { return sqrt(x); }
+__device__ inline float e_sqrt(float x) { return sqrtf(x); }
+__device__ inline double e_hypot(double a, double b) { return hypot(a, b); }
+__device__ inline float e_hypot(float a, float b) { return hypotf(a, b); }
+__device__ inline double e_copysign(double a, double b) { return copysign(a, b); }
+__device__ inline float e_copysign(float a, float b) { return copysignf(a, b); }
+template <typename T> struct EigEps;
+template <> struct EigEps<double> { static constexpr double v = 1e-16; };
+template <> struct EigEps<float> { static constexpr float v = 6e-8f; };
+
+// T = double: the FP64 solver; T = float: the first stage of the mixed solver.
+template <typename T>
 __global__ void __launch_bounds__(kEigThreads)
-    k_eigh_tql(int n, double *__restrict__ Ab, double *__restrict__ Vb, double *__restrict__ wb,
-               double *__restrict__ workb, int *__restrict__ status) {
-  extern __shared__ double esh[];
-  double *d = esh;             // [n]
-  double *e = d + n;           // [n]
-  double *tau = e + n;         // [n]
-  double *v = tau + n;         // [n] current Householder vector
-  double *p = v + n;           // [n]
-  double *rc = p + n;          // [n] rotation cosines
-  double *rs = rc + n;         // [n] rotation sines
-  __shared__ double red[32];
+    k_eigh_tql(int n, T *__restrict__ Ab, T *__restrict__ Vb, T *__restrict__ wb,
+               T *__restrict__ workb, int *__restrict__ status) {
+  extern __shared__ __align__(16) unsigned char esh_raw[];
+  T *esh = reinterpret_cast<T *>(esh_raw);
+  T *d = esh;             // [n]
+  T *e = d + n;           // [n]
+  T *tau = e + n;         // [n]
+  T *v = tau + n;         // [n] current Householder vector
+  T *p = v + n;           // [n]
+  T *rc = p + n;          // [n] rotation cosines
+  T *rs = rc + n;         // [n] rotation sines
+  __shared__ T red[32];
   __shared__ int s_int[4];
-  __shared__ double s_dbl[4];
+  __shared__ T s_dbl[4];
   const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
-  double *A = Ab + (long long)blockIdx.x * n * n;
-  double *V = Vb + (long long)blockIdx.x * n * n;  // receives eigenvectors (columns)
-  double *w = wb + (long long)blockIdx.x * n;
-  double *Zt = workb + (long long)blockIdx.x * n * n;  // Zt[c][r] = Z[r][c]
+  T *A = Ab + (long long)blockIdx.x * n * n;
+  T *V = Vb + (long long)blockIdx.x * n * n;  // receives eigenvectors (columns)
+  T *w = wb + (long long)blockIdx.x * n;
+  T *Zt = workb + (long long)blockIdx.x * n * n;  // Zt[c][r] = Z[r][c]
   int fail = 0;
 
   // ---------------- 1. tridiagonalisation ----------------
   for (int k = 0; k < n - 2; ++k) {
     int m = n - k - 1;
-    const double *col = A + (long long)(k + 1) * n + k;  // A[k+1+i][k] = col[i*n]
-    double s2 = 0;
+    const T *col = A + (long long)(k + 1) * n + k;  // A[k+1+i][k] = col[i*n]
+    T s2 = 0;
     for (int i = 1 + tid; i < m; i += nt) {
-      double x = col[(long long)i * n];
+      T x = col[(long long)i * n];
       s2 += x * x;
     }
     s2 = block_sum(s2, red);
     if (tid == 0) {
-      double x0 = col[0];
-      if (s2 == 0.0) {
-        tau[k] = 0.0;
+      T x0 = col[0];
+      if (s2 == T(0)) {
+        tau[k] = T(0);
         e[k] = x0;
-        s_dbl[0] = 0.0;
+        s_dbl[0] = T(0);
       } else {
-        double beta = -copysign(sqrt(x0 * x0 + s2), x0);
+        T beta = -e_copysign(e_sqrt(x0 * x0 + s2), x0);
         tau[k] = (beta - x0) / beta;
         e[k] = beta;
-        s_dbl[0] = 1.0 / (x0 - beta);
+        s_dbl[0] = T(1) / (x0 - beta);
       }
     }
     __syncthreads();
-    double tk = tau[k];
-    if (tk == 0.0) {
-      for (int i = tid; i < m; i += nt) v[i] = (i == 0) ? 1.0 : 0.0;
+    T tk = tau[k];
+    if (tk == T(0)) {
+      for (int i = tid; i < m; i += nt) v[i] = (i == 0) ? T(1) : T(0);
       __syncthreads();
       continue;
     }
-    double sc = s_dbl[0];
-    for (int i = tid; i < m; i += nt) v[i] = (i == 0) ? 1.0 : col[(long long)i * n] * sc;
+    T sc = s_dbl[0];
+    for (int i = tid; i < m; i += nt) v[i] = (i == 0) ? T(1) : col[(long long)i * n] * sc;
     __syncthreads();
     // p = tau * A22 v  (one warp per row, coalesced over columns)
-    double *A22 = A + (long long)(k + 1) * n + (k + 1);
+    T *A22 = A + (long long)(k + 1) * n + (k + 1);
     for (int i = warp; i < m; i += nw) {
-      const double *row = A22 + (long long)i * n;
-      double s = 0;
+      const T *row = A22 + (long long)i * n;
+      T s = 0;
       for (int j = lane; j < m; j += 32) s += row[j] * v[j];
       s = warp_sum(s);
       if (lane == 0) p[i] = tk * s;
     }
     __syncthreads();
-    double pv = 0;
+    T pv = 0;
     for (int i = tid; i < m; i += nt) pv += p[i] * v[i];
     pv = block_sum(pv, red);
-    double alpha = -0.5 * tk * pv;
+    T alpha = T(-0.5) * tk * pv;
     for (int i = tid; i < m; i += nt) p[i] += alpha * v[i];  // p becomes w
     __syncthreads();
     for (long long idx = tid; idx < (long long)m * m; idx += nt) {
@@ -99,13 +112,13 @@ __global__ void __launch_bounds__(kEigThreads)
   for (int i = tid; i < n; i += nt) d[i] = A[(long long)i * n + i];
   if (tid == 0) {
     if (n >= 2) e[n - 2] = A[(long long)(n - 1) * n + (n - 2)];
-    e[n - 1] = 0.0;
-    if (n >= 2) tau[n - 2] = 0.0;
-    tau[n - 1] = 0.0;
+    e[n - 1] = T(0);
+    if (n >= 2) tau[n - 2] = T(0);
+    tau[n - 1] = T(0);
   }
   // Zt = I
   for (long long idx = tid; idx < (long long)n * n; idx += nt)
-    Zt[idx] = ((int)(idx / n) == (int)(idx % n)) ? 1.0 : 0.0;
+    Zt[idx] = ((int)(idx / n) == (int)(idx % n)) ? T(1) : T(0);
   __syncthreads();
 
   // ---------------- 2. implicit QL ----------------
@@ -115,8 +128,8 @@ __global__ void __launch_bounds__(kEigThreads)
       if (tid == 0) {
         int m;
         for (m = l; m < n - 1; ++m) {
-          double dd = fabs(d[m]) + fabs(d[m + 1]);
-          if (fabs(e[m]) <= 1e-16 * dd) break;
+          T dd = fabs(d[m]) + fabs(d[m + 1]);
+          if (fabs(e[m]) <= EigEps<T>::v * dd) break;
         }
         int nrot = 0, lo = l;
         if (m != l) {
@@ -124,26 +137,26 @@ __global__ void __launch_bounds__(kEigThreads)
             fail = 1;
             m = l;
           } else {
-            double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
-            double r = hypot(g, 1.0);
-            g = d[m] - d[l] + e[l] / (g + copysign(r, g));
-            double s = 1.0, c = 1.0, pp = 0.0;
+            T g = (d[l + 1] - d[l]) / (T(2) * e[l]);
+            T r = e_hypot(g, T(1));
+            g = d[m] - d[l] + e[l] / (g + e_copysign(r, g));
+            T s = T(1), c = T(1), pp = T(0);
             int i;
             bool early = false;
             for (i = m - 1; i >= l; --i) {
-              double f = s * e[i], b = c * e[i];
-              r = hypot(f, g);
+              T f = s * e[i], b = c * e[i];
+              r = e_hypot(f, g);
               e[i + 1] = r;
-              if (r == 0.0) {
+              if (r == T(0)) {
                 d[i + 1] -= pp;
-                e[m] = 0.0;
+                e[m] = T(0);
                 early = true;
                 break;
               }
               s = f / r;
               c = g / r;
               g = d[i + 1] - pp;
-              r = (d[i] - g) * s + 2.0 * c * b;
+              r = (d[i] - g) * s + T(2) * c * b;
               pp = s * r;
               d[i + 1] = g + pp;
               g = c * r - b;
@@ -155,7 +168,7 @@ __global__ void __launch_bounds__(kEigThreads)
             if (!early) {
               d[l] -= pp;
               e[l] = g;
-              e[m] = 0.0;
+              e[m] = T(0);
             }
           }
         }
@@ -170,14 +183,25 @@ __global__ void __launch_bounds__(kEigThreads)
       // apply the rotations of this sweep: rotation t acts on columns
       // (i, i+1) with i = m-1-t; thread k owns row k of Z
       if (nrot > 0) {
+        // batches of RB rotations: the RB loads of a batch are independent
+        // and issued together; the carried element stays in a register
+        constexpr int RB = sizeof(T) == 8 ? 16 : 32;
         for (int k = tid; k < n; k += nt) {
-          double cur = Zt[(long long)m * n + k];
-          for (int t = 0; t < nrot; ++t) {
-            int i = m - 1 - t;
-            double zi = Zt[(long long)i * n + k];
-            double c = rc[t], s = rs[t];
-            Zt[(long long)(i + 1) * n + k] = s * zi + c * cur;
-            cur = c * zi - s * cur;
+          T cur = Zt[(long long)m * n + k];
+          for (int t0 = 0; t0 < nrot; t0 += RB) {
+            T z[RB];
+#pragma unroll
+            for (int u = 0; u < RB; ++u)
+              if (t0 + u < nrot) z[u] = Zt[(long long)(m - 1 - t0 - u) * n + k];
+#pragma unroll
+            for (int u = 0; u < RB; ++u) {
+              if (t0 + u < nrot) {
+                int i = m - 1 - t0 - u;
+                T c = rc[t0 + u], s = rs[t0 + u];
+                Zt[(long long)(i + 1) * n + k] = s * z[u] + c * cur;
+                cur = c * z[u] - s * cur;
+              }
+            }
           }
           Zt[(long long)(m - nrot) * n + k] = cur;
         }
@@ -193,13 +217,13 @@ __global__ void __launch_bounds__(kEigThreads)
   for (int k = n - 3; k >= 0 && !fail; --k) {
     __syncthreads();
     int m = n - k - 1;
-    for (int i = tid; i < m; i += nt) v[i] = (i == 0) ? 1.0 : A[(long long)(k + 1 + i) * n + k];
-    double tk = tau[k];
+    for (int i = tid; i < m; i += nt) v[i] = (i == 0) ? T(1) : A[(long long)(k + 1 + i) * n + k];
+    T tk = tau[k];
     __syncthreads();
-    if (tk == 0.0) continue;
+    if (tk == T(0)) continue;
     for (int c = warp; c < n; c += nw) {
-      const double *zc = Zt + (long long)c * n + (k + 1);
-      double s = 0;
+      const T *zc = Zt + (long long)c * n + (k + 1);
+      T s = 0;
       for (int i = lane; i < m; i += 32) s += v[i] * zc[i];
       s = warp_sum(s);
       if (lane == 0) p[c] = tk * s;
@@ -214,14 +238,14 @@ __global__ void __launch_bounds__(kEigThreads)
 
   // ---------------- 4. sort ascending, write V[r][rank] = Z[r][c] ----------------
   for (int c = tid; c < n; c += nt) {
-    double lc = d[c];
+    T lc = d[c];
     int rank = 0;
     for (int j = 0; j < n; ++j) {
-      double lj = d[j];
+      T lj = d[j];
       rank += (lj < lc) || (lj == lc && j < c);
     }
     w[rank] = lc;
-    rc[c] = (double)rank;
+    rc[c] = (T)rank;
   }
   __syncthreads();
   for (long long idx = tid; idx < (long long)n * n; idx += nt) {
@@ -239,10 +263,30 @@ void eigh_tql(int n, int batch, double *A, double *V, double *w, double *work, i
   HQ_REQUIRE(smem <= 200 * 1024, "matrix too large for the eigensolver");
   static size_t attr = 0;
   if (smem > attr) {
-    HQ_CUDA(cudaFuncSetAttribute(k_eigh_tql, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    HQ_CUDA(cudaFuncSetAttribute(k_eigh_tql<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem));
     attr = smem;
   }
-  k_eigh_tql<<<batch, kEigThreads, smem, st>>>(n, A, V, w, work, status);
+  k_eigh_tql<double><<<batch, kEigThreads, smem, st>>>(n, A, V, w, work, status);
+  HQ_LAUNCH_CHECK();
+}
+
+}  // namespace hqcgb
+
+namespace hqcgb {
+
+void eigh_tql_f32(int n, int batch, float *A, float *V, float *w, float *work, int *status,
+                  cudaStream_t st) {
+  HQ_STAGE(ST_JACOBI, st);
+  size_t smem = (size_t)7 * n * sizeof(float);
+  HQ_REQUIRE(smem <= 200 * 1024, "matrix too large for the eigensolver");
+  static size_t attr = 0;
+  if (smem > attr) {
+    HQ_CUDA(cudaFuncSetAttribute(k_eigh_tql<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem));
+    attr = smem;
+  }
+  k_eigh_tql<float><<<batch, kEigThreads, smem, st>>>(n, A, V, w, work, status);
   HQ_LAUNCH_CHECK();
 }
 

@@ -17,18 +17,23 @@ namespace hqcgb {
 // base + l * line_stride; its elements are elem_stride apart.  When
 // line_stride == 1 the group is loaded element-major (coalesced across lines),
 // otherwise line-major (the lines are contiguous, elem_stride == 1).
-__global__ void k_dft_pass(double2 *__restrict__ c, int ng, int axis, const double2 *__restrict__ tw,
+// C = double2 (FP64 path) or float2 (mixed path; twiddles rounded from FP64).
+template <typename C>
+__global__ void k_dft_pass(C *__restrict__ c, int ng, int axis, const double2 *__restrict__ tw,
                            int inverse, long long N) {
-  extern __shared__ double2 sm[];  // [ng][32] data + [ng] twiddles
-  double2 *buf = sm;
-  double2 *w = sm + (size_t)ng * 32;
+  using R = decltype(C::x);
+  extern __shared__ __align__(16) unsigned char sm_raw[];
+  C *buf = reinterpret_cast<C *>(sm_raw);
+  C *w = buf + (size_t)ng * 32;
   int tid = threadIdx.x;
   for (int k = tid; k < ng; k += blockDim.x) {
     double2 t = tw[k];
-    if (inverse) t.y = -t.y;
-    w[k] = t;
+    C tt;
+    tt.x = (R)t.x;
+    tt.y = (R)(inverse ? -t.y : t.y);
+    w[k] = tt;
   }
-  double2 *data = c + (long long)blockIdx.y * N;
+  C *data = c + (long long)blockIdx.y * N;
   long long base;
   long long line_stride, elem_stride;
   int nlines;
@@ -54,35 +59,40 @@ __global__ void k_dft_pass(double2 *__restrict__ c, int ng, int axis, const doub
     }
     line_stride = 1;
   }
+  C zero;
+  zero.x = 0;
+  zero.y = 0;
   int total = ng * 32;
   if (line_stride == 1) {
     for (int f = tid; f < total; f += blockDim.x) {
       int j = f / 32, l = f % 32;
-      buf[j * 32 + l] = (l < nlines) ? data[base + l + (long long)j * elem_stride] : make_double2(0, 0);
+      buf[j * 32 + l] = (l < nlines) ? data[base + l + (long long)j * elem_stride] : zero;
     }
   } else {
     for (int f = tid; f < total; f += blockDim.x) {
       int l = f / ng, j = f % ng;
-      buf[j * 32 + l] = (l < nlines) ? data[base + (long long)l * line_stride + j] : make_double2(0, 0);
+      buf[j * 32 + l] = (l < nlines) ? data[base + (long long)l * line_stride + j] : zero;
     }
   }
   __syncthreads();
   // each thread: outputs (k, l) with l = tid % 32
   int l = tid & 31;
-  double2 res[16];  // ng <= 256 with 16 warps
+  C res[16];  // ng <= 256 with 16 warps
   int nk = 0;
   for (int k = tid >> 5; k < ng; k += (blockDim.x >> 5)) {
-    double re = 0, im = 0;
+    R re = 0, im = 0;
     int idx = 0;
     for (int j = 0; j < ng; ++j) {
-      double2 x = buf[j * 32 + l];
-      double2 t = w[idx];
+      C x = buf[j * 32 + l];
+      C t = w[idx];
       re += x.x * t.x - x.y * t.y;
       im += x.x * t.y + x.y * t.x;
       idx += k;
       if (idx >= ng) idx -= ng;
     }
-    res[nk++] = make_double2(re, im);
+    res[nk].x = re;
+    res[nk].y = im;
+    ++nk;
   }
   __syncthreads();
   nk = 0;
@@ -101,22 +111,64 @@ __global__ void k_dft_pass(double2 *__restrict__ c, int ng, int axis, const doub
   }
 }
 
-void launch_fft3d(double2 *c, int ng, int batch, const double2 *tw, bool inverse, cudaStream_t st) {
-  HQ_STAGE(ST_FFT, st);
+template <typename C>
+static void fft3d_impl(C *c, int ng, int batch, const double2 *tw, bool inverse, cudaStream_t st) {
   HQ_REQUIRE(ng <= kMaxGrid, "grid too large for the direct DFT passes");
   long long N = (long long)ng * ng * ng;
-  size_t smem = ((size_t)ng * 32 + ng) * sizeof(double2);
+  size_t smem = ((size_t)ng * 32 + ng) * sizeof(C);
   static size_t attr = 0;
   if (smem > attr) {
-    HQ_CUDA(cudaFuncSetAttribute(k_dft_pass, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    HQ_CUDA(cudaFuncSetAttribute(k_dft_pass<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr = smem;
   }
   int zb = (ng + 31) / 32;
   for (int axis = 2; axis >= 0; --axis) {
     dim3 grid(axis == 2 ? ceil_div((long long)ng * ng, 32) : ng * zb, batch);
-    k_dft_pass<<<grid, 512, smem, st>>>(c, ng, axis, tw, inverse ? 1 : 0, N);
+    k_dft_pass<C><<<grid, 512, smem, st>>>(c, ng, axis, tw, inverse ? 1 : 0, N);
     HQ_LAUNCH_CHECK();
   }
+}
+
+void launch_fft3d(double2 *c, int ng, int batch, const double2 *tw, bool inverse, cudaStream_t st) {
+  HQ_STAGE(ST_FFT, st);
+  fft3d_impl(c, ng, batch, tw, inverse, st);
+}
+
+void launch_fft3d_f32(float2 *c, int ng, int batch, const double2 *tw, bool inverse,
+                      cudaStream_t st) {
+  HQ_STAGE(ST_FFT, st);
+  fft3d_impl(c, ng, batch, tw, inverse, st);
+}
+
+// FP32 Poisson: out = ifft(kern * fft(src)), src/out FP64, transforms in FP32.
+__global__ void k_r2c32(const double *__restrict__ a, long long N, float2 *__restrict__ c) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < N) c[i] = make_float2((float)a[i], 0.f);
+}
+__global__ void k_scale_c32(float2 *__restrict__ c, const double *__restrict__ k, long long N) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < N) {
+    float f = (float)k[i];
+    float2 v = c[i];
+    c[i] = make_float2(v.x * f, v.y * f);
+  }
+}
+__global__ void k_c2r32(const float2 *__restrict__ c, long long N, double *__restrict__ out) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < N) out[i] = (double)c[i].x;
+}
+
+void launch_poisson_f32(const double *src, double *dst, float2 *cbuf, const double *kern, int ng,
+                        const double2 *tw, cudaStream_t st) {
+  long long N = (long long)ng * ng * ng;
+  k_r2c32<<<ceil_div(N, 256), 256, 0, st>>>(src, N, cbuf);
+  HQ_LAUNCH_CHECK();
+  launch_fft3d_f32(cbuf, ng, 1, tw, false, st);
+  k_scale_c32<<<ceil_div(N, 256), 256, 0, st>>>(cbuf, kern, N);
+  HQ_LAUNCH_CHECK();
+  launch_fft3d_f32(cbuf, ng, 1, tw, true, st);
+  k_c2r32<<<ceil_div(N, 256), 256, 0, st>>>(cbuf, N, dst);
+  HQ_LAUNCH_CHECK();
 }
 
 // c[b][g] = (a[b][g] * (s ? s[g] : 1), 0)

@@ -84,4 +84,47 @@ void launch_gga_psi(const double *dphi, const double *u, int nao, long long N, d
 void launch_add3(long long N, const double *a, const double *b, const double *c, double *out,
                  cudaStream_t st);
 
+// eigh_fp64.cu / eigh_mixed.cu
+void eigh_tql_f32(int n, int batch, float *A, float *V, float *w, float *work, int *status,
+                  cudaStream_t st);
+struct MixedEigWork {
+  float *A32, *V32, *w32, *work32;
+  double *T1, *S, *G, *E, *emax;
+  int *status;
+};
+void eigh_mixed(int n, const double *A, double *V, double *w, MixedEigWork &ws, cudaStream_t st);
+bool eigh_mixed_warm(int n, const double *A, const double *X0, double *V, double *w,
+                     MixedEigWork &ws, cudaStream_t st);
+
+// fft (FP32 transforms)
+void launch_fft3d_f32(float2 *c, int ng, int batch, const double2 *tw, bool inverse,
+                      cudaStream_t st);
+void launch_poisson_f32(const double *src, double *dst, float2 *cbuf, const double *kern, int ng,
+                        const double2 *tw, cudaStream_t st);
+
+// grid_mixed.cu
+void launch_phi32(const double *F, const double *coef, const int *ao_l, const int *ao_cart,
+                  int nao_atom, int nprim, int nao, int ng, long long ld, float *phi, float *dphi,
+                  cudaStream_t st);
+void launch_to_f32(const double *in, long long ldi, long long N, int rows, double scale, float *out,
+                   long long ldo, cudaStream_t st);
+
+// tc_gemm.cu (tcgen05, 3xTF32)
+int tc_quad_chunk();
+size_t tc_quad_partial_doubles(int nao, long long N);
+void launch_tc_gemm_nt(const float *A, const float *B, const float *w, int nao, long long N,
+                       long long ld, bool sym, bool add_transpose, double scale, double *partial,
+                       double *M, int *err, cudaStream_t st, int nsplit = 2, int drain = 4);
+void launch_tc_quadrature(const float *phi, const float *dphi, const float *w, const float *u,
+                          float dV, int nao, long long N, long long ld, bool gga, double scale,
+                          double *partial, double *M, int *err, cudaStream_t st, int nsplit = 2,
+                          int drain = 4, float *zbuf = nullptr);
+size_t tc_density_partial_doubles(int nao, long long ld, bool gga);
+int tc_ldk(int nao);
+void launch_transpose_phi(const float *phi, int nao, long long N, long long ld, float *phiT,
+                          cudaStream_t st);
+void launch_tc_density(const float *phi, const float *phiT, const float *dphi, const float *D32,
+                       int nao, long long N, long long ld, double *part, double *rho, double *grho,
+                       int *err, cudaStream_t st, int nsplit = 2, int drain = 3);
+
 }  // namespace hqcgb

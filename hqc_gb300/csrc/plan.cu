@@ -10,6 +10,8 @@
 #include <string>
 #include <vector>
 #include <cmath>
+#include <cstdlib>
+#include <algorithm>
 
 #include "common.cuh"
 #include "kernels.h"
@@ -63,6 +65,16 @@ using namespace hqcgb;
 
 static constexpr double kMadelungSC = 0.22578495;  // solver.py:404
 
+// HQCGB_TRACE=1 prints one line per SCF iteration (energy, error norm) to stderr.
+static bool trace_on() {
+  static int v = -1;
+  if (v < 0) {
+    const char *e = std::getenv("HQCGB_TRACE");
+    v = (e && e[0] == '1') ? 1 : 0;
+  }
+  return v == 1;
+}
+
 struct hqcgb_plan {
   hqcgb_params P{};
   std::vector<double> h_alpha, h_coef, h_lat1d, h_lattice;
@@ -95,6 +107,17 @@ struct hqcgb_plan {
   double2 *cbuf = nullptr;
   long long cbuf_batch = 0;
   double *qpart = nullptr, *xpart = nullptr, *fpart = nullptr, *gpart = nullptr, *vpart = nullptr;
+  // mixed-precision grid data (row stride ld floats)
+  bool mixed = false;
+  long long ld = 0;
+  float *phi32 = nullptr, *dphi32 = nullptr, *phiT32 = nullptr, *D32 = nullptr, *w32 = nullptr,
+        *u32 = nullptr, *z32 = nullptr;
+  double *tcq_part = nullptr, *tcd_part = nullptr;
+  float2 *cbuf32 = nullptr;
+  int *tc_err = nullptr;
+  MixedEigWork mew{};
+  double *c1_prev = nullptr;  // eigenvectors of the previous Fock diagonalisation
+  bool have_prev = false;
   double *scal = nullptr;  // device scalars
   double *hscal = nullptr; // pinned host mirror
   // last state
@@ -201,10 +224,43 @@ static void create(const hqcgb_params *in, hqcgb_plan *p) {
   p->coul = p->alloc<double>(N);
   launch_coulomb_table(p->ng, p->L, p->coul, 0);
 
+  p->mixed = P.precision == HQCGB_PREC_MIXED;
+  p->ld = (N + 63) / 64 * 64;
   p->xp = p->alloc<double>(3 * n);
   p->F1d = p->alloc<double>((size_t)n * 3 * p->ng * P.n_prim * 6);
-  p->phi = p->alloc<double>((size_t)nao * N);
-  if (p->need_dphi) p->dphi = p->alloc<double>((size_t)3 * nao * N);
+  // the FP64 AO grid is kept by the FP64 path, and by the mixed path for the
+  // parts it runs in FP64 (exact exchange, forces)
+  bool fp64_grid = !p->mixed || p->hf || P.want_forces;
+  if (fp64_grid) {
+    p->phi = p->alloc<double>((size_t)nao * N);
+    if (p->need_dphi) p->dphi = p->alloc<double>((size_t)3 * nao * N);
+  }
+  if (p->mixed) {
+    p->phi32 = p->alloc<float>((size_t)nao * p->ld);
+    if (p->gga) p->dphi32 = p->alloc<float>((size_t)3 * nao * p->ld);
+    p->phiT32 = p->alloc<float>((size_t)N * tc_ldk(nao));
+    p->D32 = p->alloc<float>((size_t)nao * tc_ldk(nao));
+    HQ_CUDA(cudaMemset(p->D32, 0, sizeof(float) * nao * tc_ldk(nao)));
+    if (p->gga) p->z32 = p->alloc<float>((size_t)nao * p->ld);
+    p->w32 = p->alloc<float>(p->ld);
+    p->u32 = p->alloc<float>(3 * p->ld);
+    p->tcq_part = p->alloc<double>(tc_quad_partial_doubles(nao, N));
+    p->tcd_part = p->alloc<double>(tc_density_partial_doubles(nao, p->ld, p->gga));
+    p->cbuf32 = p->alloc<float2>(N);
+    p->tc_err = p->alloc<int>(1);
+    HQ_CUDA(cudaMemset(p->tc_err, 0, sizeof(int)));
+    p->mew.A32 = p->alloc<float>(nn);
+    p->mew.V32 = p->alloc<float>(nn);
+    p->mew.w32 = p->alloc<float>(nao);
+    p->mew.work32 = p->alloc<float>(nn);
+    p->mew.T1 = p->alloc<double>(nn);
+    p->mew.S = p->alloc<double>(nn);
+    p->mew.G = p->alloc<double>(nn);
+    p->mew.E = p->alloc<double>(nn);
+    p->mew.status = p->alloc<int>(1);
+    p->mew.emax = p->alloc<double>(2);
+    p->c1_prev = p->alloc<double>(nn);
+  }
   p->ph = p->alloc<double2>((size_t)n * 3 * p->ng);
   for (double **m : {&p->S, &p->T, &p->V, &p->H, &p->St, &p->vorth, &p->F, &p->F2e, &p->K, &p->Fp,
                      &p->C, &p->c1, &p->D, &p->t1, &p->t2, &p->err, &p->jtmp, &p->jA})
@@ -268,6 +324,17 @@ static void sync_scalars(Ctx &c) {
 static void eigh(Ctx &c, const double *A, double *vecs, double *vals) {
   hqcgb_plan *p = c.p;
   int n = p->nao;
+  if (p->mixed) {
+    // FP32 Householder + QL, then FP64 Ogita-Aishima refinement
+    eigh_mixed(n, A, vecs, vals, p->mew, c.st);
+    int ms = 0;
+    HQ_CUDA(cudaMemcpyAsync(&ms, p->mew.status, sizeof(int), cudaMemcpyDeviceToHost, c.st));
+    HQ_CUDA(cudaStreamSynchronize(c.st));
+    if (ms >= 0) {
+      HQ_CUDA(cudaMemsetAsync(p->jstat, 0, sizeof(int), c.st));
+      return;
+    }
+  }
   HQ_CUDA(cudaMemcpyAsync(p->jA, A, sizeof(double) * n * n, cudaMemcpyDeviceToDevice, c.st));
   eigh_tql(n, 1, p->jA, vecs, vals, p->jtmp, p->jstat, c.st);
   int stt = 0;
@@ -285,7 +352,15 @@ static void diagonalize(Ctx &c, const double *Fm) {
   int n = p->nao;
   gemm(false, false, n, n, n, 1.0, Fm, n, p->vorth, n, nullptr, 0.0, p->t1, n, c.st);
   gemm(true, false, n, n, n, 1.0, p->vorth, n, p->t1, n, nullptr, 0.0, p->Fp, n, c.st);
-  eigh(c, p->Fp, p->c1, p->w);
+  bool done = false;
+  if (p->mixed && p->have_prev)
+    done = eigh_mixed_warm(n, p->Fp, p->c1_prev, p->c1, p->w, p->mew, c.st);
+  if (!done) eigh(c, p->Fp, p->c1, p->w);
+  if (p->mixed) {
+    HQ_CUDA(cudaMemcpyAsync(p->c1_prev, p->c1, sizeof(double) * n * n, cudaMemcpyDeviceToDevice,
+                            c.st));
+    p->have_prev = true;
+  }
   gemm(false, false, n, n, n, 1.0, p->vorth, n, p->c1, n, nullptr, 0.0, p->C, n, c.st);
 }
 
@@ -348,10 +423,25 @@ static double fock(Ctx &c) {
   const hqcgb_params &P = p->P;
   int n = p->nao;
   long long N = p->N;
+  int kind = P.dft ? P.xc : -1;
+  if (p->mixed) {
+    // tensor-core density (3xTF32, FP32 accumulation, FP64 sums), FP32
+    // Poisson, FP64 xc, tensor-core quadrature
+    launch_to_f32(p->D, n, n, n, 1.0, p->D32, tc_ldk(n), c.st);
+    launch_tc_density(p->phi32, p->phiT32, p->dphi32, p->D32, n, N, p->ld, p->tcd_part, p->rho,
+                      p->gga ? p->grho : nullptr, p->tc_err, c.st);
+    launch_poisson_f32(p->rho, p->vh, p->cbuf32, p->coul, p->ng, p->tw, c.st);
+    launch_xc_pointwise(kind, p->rho, p->gga ? p->grho : nullptr, p->vh, N, p->dV, p->wq, p->vxc,
+                        p->gga ? p->u : nullptr, p->xpart, c.st);
+    launch_sum_partials(p->xpart, xc_blocks(N), 2, 2, 1.0, p->scal + S_EXC, false, c.st);
+    launch_to_f32(p->wq, N, N, 1, 1.0, p->w32, p->ld, c.st);
+    if (p->gga) launch_to_f32(p->u, N, N, 3, 1.0, p->u32, p->ld, c.st);
+    launch_tc_quadrature(p->phi32, p->dphi32, p->w32, p->u32, (float)p->dV, n, N, p->ld, p->gga, 1.0,
+                         p->tcq_part, p->F2e, p->tc_err, c.st, 2, 4, p->z32);
+  } else {
   launch_density(p->phi, p->gga ? p->dphi : nullptr, p->D, n, N, p->rho, p->gga ? p->grho : nullptr,
                  nullptr, c.st);
   poisson(c, p->rho, p->vh);
-  int kind = P.dft ? P.xc : -1;
   launch_xc_pointwise(kind, p->rho, p->gga ? p->grho : nullptr, p->vh, N, p->dV, p->wq, p->vxc,
                       p->gga ? p->u : nullptr, p->xpart, c.st);
   launch_sum_partials(p->xpart, xc_blocks(N), 2, 2, 1.0, p->scal + S_EXC, false, c.st);
@@ -361,6 +451,7 @@ static double fock(Ctx &c) {
     axpby(n, 1.0, p->t1, 1.0, p->t1, true, p->F2e, c.st);
   } else {
     launch_quadrature(p->phi, p->phi, p->wq, n, N, true, 1.0, false, p->qpart, p->F2e, c.st);
+  }
   }
   if (p->hf) {
     exchange(c, nullptr);
@@ -401,14 +492,27 @@ static void geometry(Ctx &c, const double *xp_dev) {
   long long N = p->N;
   HQ_CUDA(cudaMemcpyAsync(p->xp, xp_dev, sizeof(double) * 3 * p->n, cudaMemcpyDeviceToDevice, c.st));
   launch_gto1d(p->xp, p->n, p->ng, p->L, p->alpha, p->nprim, p->lat1d, P.n_lat1d, p->F1d, c.st);
-  launch_phi(p->F1d, p->coef, p->ao_l, p->ao_cart, p->nb, p->nprim, n, p->ng, p->phi, p->dphi, c.st);
+  if (p->phi)
+    launch_phi(p->F1d, p->coef, p->ao_l, p->ao_cart, p->nb, p->nprim, n, p->ng, p->phi, p->dphi,
+               c.st);
+  if (p->mixed) {
+    launch_phi32(p->F1d, p->coef, p->ao_l, p->ao_cart, p->nb, p->nprim, n, p->ng, p->ld, p->phi32,
+                 p->dphi32, c.st);
+    launch_transpose_phi(p->phi32, n, N, p->ld, p->phiT32, c.st);
+  }
   launch_overlap_kinetic(p->xp, p->n, p->nb, p->nprim, p->alpha, p->coef, p->ao_l, p->ao_cart,
                          p->lattice, P.n_lattice, p->S, p->T, nullptr, nullptr, nullptr, nullptr,
                          c.st);
   launch_vloc_G(p->xp, p->n, p->ng, p->L, p->ph, p->cbuf, c.st);
   launch_fft3d(p->cbuf, p->ng, 1, p->tw, true, c.st);
   launch_complex_real(p->cbuf, N, 1.0, p->vloc, c.st);
-  launch_quadrature(p->phi, p->phi, p->vloc, n, N, true, p->dV, false, p->qpart, p->V, c.st);
+  if (p->mixed) {
+    launch_to_f32(p->vloc, N, N, 1, p->dV, p->w32, p->ld, c.st);
+    launch_tc_quadrature(p->phi32, nullptr, p->w32, nullptr, (float)p->dV, n, N, p->ld, false, 1.0,
+                         p->tcq_part, p->V, p->tc_err, c.st);
+  } else {
+    launch_quadrature(p->phi, p->phi, p->vloc, n, N, true, p->dV, false, p->qpart, p->V, c.st);
+  }
   axpby(n, 1.0, p->T, 1.0, p->V, false, p->H, c.st);
   if (p->hf) launch_quadrature(p->phi, p->phi, nullptr, n, N, true, p->dV, false, p->qpart, p->St, c.st);
   // S^{-1/2} as U w^{-1/2} (solver.py:729-730)
@@ -428,6 +532,7 @@ static int scf_one(hqcgb_plan *p, const double *xp_dev, const hqcgb_scf_out *out
   int n = p->nao;
   size_t nn = (size_t)n * n;
   p->have_state = false;
+  p->have_prev = false;
   geometry(c, xp_dev);
   // Hcore guess (solver.py:739-745)
   diagonalize(c, p->H);
@@ -454,17 +559,24 @@ static int scf_one(hqcgb_plan *p, const double *xp_dev, const hqcgb_scf_out *out
       E0 = E1;
       E1 = En;
       ++loop;
+      if (trace_on()) fprintf(stderr, "scf %3d E=%.12f dE=%.3e err=%.3e\n", loop, E1, E1 - E0, enorm);
     };
     while (loop < P.diis_start_cycle + sp) step(p->Fk + head * nn);
     E0 = E1 - 1.0;
-    while ((std::fabs(E1 - E0) > P.tol || enorm > 10.0 * P.tol) && loop < P.max_cycle) {
+    // The mixed path's Fock build carries noise (3xTF32, FP32 accumulation):
+    // its stopping tests are floored at that noise (|dE| 1e-6 Ha, commutator
+    // 2e-5) so that tol below the floor cannot make the loop spin to max_cycle.
+    const double etol = p->mixed ? std::max(P.tol, 2e-6) : P.tol;
+    const double errtol = p->mixed ? std::max(10.0 * P.tol, 2e-5) : 10.0 * P.tol;
+    while ((std::fabs(E1 - E0) > etol || enorm > errtol) && loop < P.max_cycle) {
       diis_extrapolate(sp, n, p->Fk, p->ek, head, P.diis_damp, p->Bm, p->dc, p->t1, st);
       HQ_CUDA(cudaMemcpyAsync(p->Fp, p->t1, nn * 8, cudaMemcpyDeviceToDevice, st));
       step(p->Fp);
       if (!std::isfinite(E1)) throw Error{HQCGB_NAN, "non-finite energy in the SCF"};
     }
   } else {
-    while (std::fabs(E1 - E0) > P.tol && loop < P.max_cycle) {
+    const double etol = p->mixed ? std::max(P.tol, 2e-6) : P.tol;
+    while (std::fabs(E1 - E0) > etol && loop < P.max_cycle) {
       double En = fock(c);
       diagonalize(c, p->F);
       density_matrix(c);
@@ -475,6 +587,15 @@ static int scf_one(hqcgb_plan *p, const double *xp_dev, const hqcgb_scf_out *out
     }
   }
   check_eig(c);
+  if (p->mixed) {
+    int te = 0;
+    HQ_CUDA(cudaMemcpyAsync(&te, p->tc_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    HQ_CUDA(cudaStreamSynchronize(st));
+    if (te) {
+      HQ_CUDA(cudaMemsetAsync(p->tc_err, 0, sizeof(int), st));
+      throw Error{HQCGB_CUDA_ERROR, "tensor-core pipeline wait limit hit (code " + std::to_string(te) + ")"};
+    }
+  }
   int converged = (loop != P.max_cycle) ? 1 : 0;
   // post-processing (solver.py:758-767 / 890-899)
   density_matrix(c);

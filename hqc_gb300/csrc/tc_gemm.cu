@@ -1,0 +1,816 @@
+// tcgen05 (5th-generation tensor core) grid contractions of the mixed path.
+//
+//   quadrature  M_pq = sum_g A_p(g) B_q(g)        A = phi * w (or the GGA
+//               operand), B = phi; K = grid split over CTAs, FP64 partial
+//               tiles reduced in FP64 (hqc/pbc/solver.py:693: Vxc, J, Vep);
+//   density     X = D phi (M = AO, N = grid, K = AO) with the fused epilogue
+//               rho(g) = sum_p phi_p(g) X_p(g) (+ grad rho for GGA)
+//               (hqc/pbc/solver.py:690).
+//
+// Precision.  Products: 3xTF32 -- each fp32 operand x is split into
+// hi = rna_tf32(x) and lo = x - hi and the MMA accumulates hi*hi + hi*lo +
+// lo*hi (kind::tf32, M = 128, N = 128, K = 8 per instruction).  Sums: the
+// tensor core accumulates in FP32 in TMEM only over a short K sub-chunk
+// (`drain` stages of K = 32); the epilogue threads then drain the sub-chunk
+// into register-resident compensated sums (Knuth's TwoSum in FP32, about 46
+// significant bits) while the MMA fills the other TMEM buffer.  Long sums
+// across CTAs are reduced in FP64.
+//
+// CTA layout (288 threads): warps 0-7 are producers (load fp32 tiles from
+// global memory, split hi/lo, store them in the UMMA canonical K-major
+// 128-byte-swizzled layout) and drain/epilogue threads (warp w owns TMEM
+// lanes 32(w%4).. and column half w/4); warp 8 allocates TMEM and one of its
+// threads issues the MMAs.  Two smem stages of K = 32, two TMEM accumulators
+// of 128 columns.  Every mbarrier wait has an iteration limit: on expiry the
+// kernel records an error code in *err, stops issuing work, waits (bounded)
+// for its MMAs, frees TMEM and returns.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace hqcgb {
+namespace tc {
+
+constexpr int kProducers = 128;          // warps 0-3: loads + TF32 split
+constexpr int kDrainers = 128;           // warps 4-7: TMEM drains + epilogue
+constexpr int kThreads = kProducers + kDrainers + 32;  // + MMA warp 8
+constexpr int kStageK = 32;              // fp32 elements per row per stage (128 bytes)
+constexpr int kM = 128, kN = 128;
+constexpr size_t kTile = 16384;          // 128 rows x 128 bytes
+constexpr int kMaxSplit = 2;             // pieces per operand (hi, lo)
+constexpr size_t kStageBytes = 2 * kMaxSplit * kTile;  // A pieces, then B pieces
+constexpr unsigned kSpinLimit = 1u << 26;
+
+__device__ inline uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ inline void mbar_init(uint64_t *bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ inline void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ inline bool mbar_try_wait(uint64_t *bar, unsigned parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, 100000;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait; returns false (and records `code`) when the limit is hit.
+__device__ inline bool mbar_wait(uint64_t *bar, unsigned parity, int *err, int code) {
+  for (unsigned it = 0; it < kSpinLimit; ++it)
+    if (mbar_try_wait(bar, parity)) return true;
+  if (err) atomicCAS(err, 0, code);
+  return false;
+}
+
+__device__ inline uint32_t tf32_rna(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+// Split fp32 x into two TF32 pieces, each rounded to nearest: x ~ hi + lo.
+__device__ __forceinline__ void split2(float x, float &hi, float &lo) {
+  hi = __uint_as_float(tf32_rna(x));
+  lo = __uint_as_float(tf32_rna(x - hi));
+}
+
+// UMMA shared-memory descriptor: K-major, 128-byte swizzle, 8-row groups
+// 1024 bytes apart (SBO), descriptor version 1.
+__device__ inline uint64_t sdesc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+  d |= (uint64_t)1 << 16;                 // LBO (unused for swizzled K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;       // SBO
+  d |= (uint64_t)1 << 46;                 // version
+  d |= (uint64_t)2 << 61;                 // SWIZZLE_128B
+  return d;
+}
+
+// Instruction descriptor: kind::tf32, D = F32, A = B = TF32, both K-major.
+__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) |
+         ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ inline void mma_tf32(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t idesc, int acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
+      ::"r"(dtmem), "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__device__ inline void mma_commit(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+               ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ inline void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ inline void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ inline void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+__device__ inline void tmem_alloc(uint32_t *dst_smem, int ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+               ::"r"(smem_u32(dst_smem)), "r"(ncols) : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+
+__device__ inline void tmem_dealloc(uint32_t taddr, int ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols)
+               : "memory");
+}
+
+// 32 lanes x 16 consecutive 32-bit columns
+__device__ inline void tmem_ld16(uint32_t taddr, float *v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15},"
+      " [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ inline void tmem_st16(uint32_t taddr, const float *v) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};"
+      ::"r"(taddr), "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+        "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
+        "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])), "r"(__float_as_uint(v[8])),
+        "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
+        "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])),
+        "r"(__float_as_uint(v[15]))
+      : "memory");
+}
+
+__device__ inline void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+__device__ inline void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// 32 lanes x 16 columns without the wait (several loads in flight, then one wait)
+__device__ inline void tmem_ld16_nowait(uint32_t taddr, uint32_t *r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15},"
+      " [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+
+// byte offset of the 16-byte chunk `c` of row `r` in a K-major SW128 tile
+__device__ inline uint32_t swz(int r, int c) { return (uint32_t)(r * 128 + ((c ^ (r & 7)) << 4)); }
+
+// Store the hi/lo pieces of 4 K-consecutive elements of row r (K chunk c);
+// the hi piece goes to `tiles`, the lo piece to `tiles + kTile`.
+__device__ __forceinline__ void store_split4(char *tiles, int r, int c, float4 v) {
+  float4 h, l;
+  split2(v.x, h.x, l.x);
+  split2(v.y, h.y, l.y);
+  split2(v.z, h.z, l.z);
+  split2(v.w, h.w, l.w);
+  uint32_t off = swz(r, c);
+  *reinterpret_cast<float4 *>(tiles + off) = h;
+  *reinterpret_cast<float4 *>(tiles + kTile + off) = l;
+}
+
+// MMAs of one stage (K = 32 -> 4 instructions of K = 8 per product pair):
+// lo*hi + hi*lo + hi*hi (small products first).  A 3-piece split (6
+// products) was measured to give no gain: the FP32 accumulation in TMEM, not
+// the operand representation, limits the accuracy, and the short drains
+// address that.
+__device__ __forceinline__ void issue_stage(uint32_t tmem_d, uint32_t base, uint32_t idesc,
+                                            bool first) {
+  const uint32_t Ah = base, Al = base + kTile, Bh = base + kMaxSplit * kTile,
+                 Bl = base + kMaxSplit * kTile + kTile;
+#pragma unroll
+  for (int ks = 0; ks < kStageK / 8; ++ks) {
+    uint32_t off = ks * 32;  // 8 tf32 = 32 bytes along K
+    mma_tf32(tmem_d, sdesc(Al + off), sdesc(Bh + off), idesc, (first && ks == 0) ? 0 : 1);
+    mma_tf32(tmem_d, sdesc(Ah + off), sdesc(Bl + off), idesc, 1);
+    mma_tf32(tmem_d, sdesc(Ah + off), sdesc(Bh + off), idesc, 1);
+  }
+}
+
+// Compensated accumulation (TwoSum): (s, c) += v
+__device__ inline void two_sum_add(float &s, float &c, float v) {
+  float t = s + v;
+  float z = t - s;
+  c += (s - (t - z)) + (v - z);
+  s = t;
+}
+
+// Shared skeleton: `fill(stage_index, smem_stage_base)` is executed by the
+// 256 worker threads; after every `drain` stages the workers add the TMEM
+// sub-chunk sum into (s[64], c[64]) -- their row (lane) and column half.
+constexpr int kRing = 3;
+struct Pipe {
+  uint64_t full_bar[kRing], empty_bar[kRing], acc_full[2], acc_empty[2];
+  uint32_t tmem_base;
+};
+
+// TMEM columns: [0,128) and [128,256) the two MMA accumulators, [256,384)
+// the compensated sums S, [384,512) their carries C.
+constexpr uint32_t kColS = 2 * kN, kColC = 3 * kN, kTmemCols = 4 * kN;
+
+// Drain the accumulator of sub-chunk j into (S, C): S, C += A_j (TwoSum).
+// Drainer warp w (4..7) owns TMEM lanes 32(w%4)..+31 and all 128 columns;
+// per round of 32 columns six TMEM loads are in flight before one wait.
+__device__ __forceinline__ bool drain_sub(Pipe &P, int j, int *err, int code) {
+  const int warp = threadIdx.x >> 5;
+  const uint32_t lane_off = (uint32_t)((warp & 3) * 32) << 16;
+  const int b = j & 1, use = j >> 1;
+  bool got = mbar_wait(&P.acc_full[b], use & 1, err, code);
+  tc_fence_after();
+  if (got) {
+#pragma unroll 1
+    for (int col = 0; col < kN; col += 32) {
+      uint32_t va[32], sa[32], ca[32];
+      tmem_ld16_nowait(P.tmem_base + lane_off + b * kN + col, va);
+      tmem_ld16_nowait(P.tmem_base + lane_off + b * kN + col + 16, va + 16);
+      if (j > 0) {
+        tmem_ld16_nowait(P.tmem_base + lane_off + kColS + col, sa);
+        tmem_ld16_nowait(P.tmem_base + lane_off + kColS + col + 16, sa + 16);
+        tmem_ld16_nowait(P.tmem_base + lane_off + kColC + col, ca);
+        tmem_ld16_nowait(P.tmem_base + lane_off + kColC + col + 16, ca + 16);
+      }
+      tmem_wait_ld();
+      float sv[32], cv[32];
+#pragma unroll
+      for (int i = 0; i < 32; ++i) {
+        float v = __uint_as_float(va[i]);
+        if (j == 0) {
+          sv[i] = v;
+          cv[i] = 0.f;
+        } else {
+          sv[i] = __uint_as_float(sa[i]);
+          cv[i] = __uint_as_float(ca[i]);
+          two_sum_add(sv[i], cv[i], v);
+        }
+      }
+      tmem_st16(P.tmem_base + lane_off + kColS + col, sv);
+      tmem_st16(P.tmem_base + lane_off + kColS + col + 16, sv + 16);
+      tmem_st16(P.tmem_base + lane_off + kColC + col, cv);
+      tmem_st16(P.tmem_base + lane_off + kColC + col + 16, cv + 16);
+    }
+    tmem_wait_st();
+  }
+  tc_fence_before();
+  mbar_arrive(&P.acc_empty[b]);
+  return got;
+}
+
+// Read back (S + C) of 16 columns (starting at col) of this drainer's row.
+__device__ __forceinline__ void read_sum16(const Pipe &P, int col, double *out) {
+  const int warp = threadIdx.x >> 5;
+  const uint32_t lane_off = (uint32_t)((warp & 3) * 32) << 16;
+  uint32_t sv[16], cv[16];
+  tmem_ld16_nowait(P.tmem_base + lane_off + kColS + col, sv);
+  tmem_ld16_nowait(P.tmem_base + lane_off + kColC + col, cv);
+  tmem_wait_ld();
+#pragma unroll
+  for (int i = 0; i < 16; ++i) out[i] = (double)__uint_as_float(sv[i]) + (double)__uint_as_float(cv[i]);
+}
+
+__device__ inline void cp_async16(uint32_t saddr, const void *g) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(saddr), "l"(g) : "memory");
+}
+__device__ inline void cp_async_zero16(uint32_t saddr, const void *g) {
+  // src-size 0: fills the 16 bytes with zeros without reading global memory
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, 0;" ::"r"(saddr), "l"(g) : "memory");
+}
+__device__ inline void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ inline void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// Generic K-major operand description: element (row, k) at ptr[row * ld + k];
+// rows >= rows_valid and k >= k_end read as zero.  Every row start and every
+// 4-element chunk is 16-byte aligned (ld % 4 == 0, k offsets multiples of 4).
+struct Operand {
+  const float *ptr;
+  long long ld;
+  int rows_valid;
+};
+
+constexpr int kStages = 3;  // smem ring depth; copies run 2 stages ahead
+
+// Producer/MMA/drain pipeline over `nstages` K-stages of 32 starting at k_begin.
+// Producer thread t copies (cp.async) and later splits, in place, the 16-byte
+// chunks t + 128 j (j = 0..7) of the A and B tiles -- all in K chunk t % 8 --
+// and the matching 4 weights w[k..k+3] (into its own smem slot).
+__device__ __forceinline__ bool run_pipe(Pipe &P, char *sm, float4 *wslot, const Operand &A,
+                                         int a_row0, const Operand &B, int b_row0, const float *w,
+                                         long long k_begin, long long k_end, int nstages, int drain,
+                                         int ns, int *err, int code0) {
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int nsub = (nstages + drain - 1) / drain;
+  bool ok = true;
+  if (warp < 4) {
+    const int cch = tid & 7;
+    // the 8 A rows and 8 B rows this thread copies never change
+    const float *arow[8], *brow[8];
+    uint32_t avalid = 0, bvalid = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      int r = (tid >> 3) + 16 * j;
+      int ra = a_row0 + r, rb = b_row0 + r;
+      arow[j] = A.ptr + (long long)(ra < A.rows_valid ? ra : 0) * A.ld + cch * 4;
+      brow[j] = B.ptr + (long long)(rb < B.rows_valid ? rb : 0) * B.ld + cch * 4;
+      avalid |= (ra < A.rows_valid ? 1u : 0u) << j;
+      bvalid |= (rb < B.rows_valid ? 1u : 0u) << j;
+    }
+    const uint32_t sbase = smem_u32(sm);
+    auto issue = [&](int st) {  // async copies of stage st into buffer st % kStages
+      const int buf = st % kStages;
+      const uint32_t base = sbase + buf * (uint32_t)kStageBytes;
+      long long kk = k_begin + (long long)st * kStageK;  // chunk start (without cch*4)
+      long long k = kk + cch * 4;
+      bool kin = k < k_end;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        int r = (tid >> 3) + 16 * j;
+        uint32_t off = swz(r, cch);
+        const float *ga = arow[j] + (kin ? kk : 0);
+        const float *gb = brow[j] + (kin ? kk : 0);
+        if (kin && ((avalid >> j) & 1u)) cp_async16(base + off, ga);
+        else cp_async_zero16(base + off, arow[j]);
+        if (kin && ((bvalid >> j) & 1u)) cp_async16(base + kMaxSplit * kTile + off, gb);
+        else cp_async_zero16(base + kMaxSplit * kTile + off, brow[j]);
+      }
+      if (w) {
+        uint32_t ws = smem_u32(&wslot[buf * kProducers + tid]);
+        if (kin) cp_async16(ws, w + k);
+        else cp_async_zero16(ws, w);
+      }
+      cp_async_commit();
+    };
+    auto split_stage = [&](int st) {  // in place: raw fp32 in piece 0 -> pieces
+      const int buf = st % kStages;
+      char *base = sm + buf * kStageBytes;
+      float4 wv = w ? wslot[buf * kProducers + tid] : make_float4(1.f, 1.f, 1.f, 1.f);
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        int r = (tid >> 3) + 16 * j;
+        uint32_t off = swz(r, cch);
+        float4 av = *reinterpret_cast<float4 *>(base + off);
+        av.x *= wv.x; av.y *= wv.y; av.z *= wv.z; av.w *= wv.w;
+        float4 bv = *reinterpret_cast<float4 *>(base + kMaxSplit * kTile + off);
+        store_split4(base, r, cch, av);
+        store_split4(base + kMaxSplit * kTile, r, cch, bv);
+      }
+    };
+    for (int st = 0; st < 2 && st < nstages; ++st) issue(st);
+    for (int stage = 0; stage < nstages; ++stage) {
+      // stage `stage` landed once at most one newer group is pending
+      if (stage + 1 < nstages) cp_async_wait<1>();
+      else cp_async_wait<0>();
+      if (ok) split_stage(stage);
+      fence_proxy_async();
+      mbar_arrive(&P.full_bar[stage % kStages]);
+      int nx = stage + 2;  // refill the buffer of stage - 1 once the MMA released it
+      if (nx < nstages) {
+        int use = nx / kStages;
+        if (ok && use > 0 && !mbar_wait(&P.empty_bar[nx % kStages], (use - 1) & 1, err, code0 + 1))
+          ok = false;
+        issue(nx);
+      }
+    }
+  } else if (warp < 8) {
+    for (int j = 0; j < nsub; ++j) ok = drain_sub(P, j, err, code0 + 3) && ok;
+  } else if (lane == 0) {
+    const uint32_t idesc = idesc_tf32(kM, kN);
+    int stage = 0;
+    for (int j = 0; j < nsub; ++j) {
+      int ab = j & 1, ause = j >> 1;
+      if (ok && ause > 0 && !mbar_wait(&P.acc_empty[ab], (ause - 1) & 1, err, code0 + 4)) ok = false;
+      tc_fence_after();
+      uint32_t tmem_d = P.tmem_base + (uint32_t)(ab * kN);
+      int s_end = min(nstages, (j + 1) * drain);
+      bool first = true;
+      for (; stage < s_end; ++stage) {
+        int b = stage % kStages, use = stage / kStages;
+        if (ok && !mbar_wait(&P.full_bar[b], use & 1, err, code0 + 2)) ok = false;
+        tc_fence_after();
+        if (ok) issue_stage(tmem_d, smem_u32(sm + b * kStageBytes), idesc, first);
+        first = false;
+        mma_commit(&P.empty_bar[b]);
+      }
+      mma_commit(&P.acc_full[ab]);
+    }
+  }
+  return ok;
+}
+
+__device__ inline void pipe_init(Pipe &P) {
+  if (threadIdx.x == 0) {
+    for (int b = 0; b < kStages; ++b) {
+      mbar_init(&P.full_bar[b], kProducers);
+      mbar_init(&P.empty_bar[b], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&P.acc_full[b], 1);
+      mbar_init(&P.acc_empty[b], kDrainers);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if ((threadIdx.x >> 5) == 8) tmem_alloc(&P.tmem_base, kTmemCols);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+}
+
+__device__ inline void pipe_finish(Pipe &P) {
+  tc_fence_before();
+  __syncthreads();
+  if ((threadIdx.x >> 5) == 8) {
+    tc_fence_after();
+    tmem_dealloc(P.tmem_base, kTmemCols);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Quadrature: grid (m_tiles, n_tiles, k_chunks); tile 128 x 128; FP64
+// partial tiles P[chunk][tile_m][tile_n][128][128] of sum_g A_p(g) w(g) B_q(g).
+// ---------------------------------------------------------------------------
+struct QuadArgs {
+  Operand A, B;
+  const float *w;
+  int nao, sym, drain, ns;
+  long long N;
+  int kchunk;
+  double *partial;
+  int *err;
+};
+
+constexpr size_t kWslotBytes = kStages * kProducers * sizeof(float4);
+constexpr size_t kQuadSmem = kStages * kStageBytes + kWslotBytes + 1024;
+
+__global__ void __launch_bounds__(kThreads, 1) k_tc_quadrature(QuadArgs a) {
+  extern __shared__ __align__(1024) char smraw[];
+  char *sm = (char *)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
+  __shared__ Pipe P;
+  const int mt = blockIdx.x, nt = blockIdx.y, chunk = blockIdx.z;
+  if (a.sym && nt < mt) return;  // whole CTA exits before any barrier use
+  pipe_init(P);
+  const long long k0 = (long long)chunk * a.kchunk;
+  const long long k1 = min(k0 + (long long)a.kchunk, a.N);
+  const int nstages = (int)((k1 - k0 + kStageK - 1) / kStageK);
+  const int tid = threadIdx.x;
+  float4 *wslot = reinterpret_cast<float4 *>(sm + kStages * kStageBytes);
+  bool ok = run_pipe(P, sm, wslot, a.A, mt * kM, a.B, nt * kN, a.w, k0, k1, nstages, a.drain, a.ns,
+                     a.err, 0);
+  const int warp = tid >> 5;
+  if (warp >= 4 && warp < 8) {
+    int row = (warp & 3) * 32 + (tid & 31);
+    double *out = a.partial + ((((long long)chunk * gridDim.x + mt) * gridDim.y + nt) * kM + row) * kN;
+#pragma unroll 1
+    for (int c0 = 0; c0 < kN; c0 += 16) {
+      double v[16];
+      read_sum16(P, c0, v);
+      if (ok)
+#pragma unroll
+        for (int i = 0; i < 16; ++i) out[c0 + i] = v[i];
+    }
+  }
+  pipe_finish(P);
+}
+
+// M[p][q] = scale * sum_chunks P  (+ mirror for sym; + transpose-add for GGA)
+__global__ void k_tc_quad_reduce(const double *__restrict__ P, int nchunk, int mtiles, int ntiles,
+                                 int nao, int sym, int add_transpose, double scale,
+                                 double *__restrict__ M) {
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= nao * nao) return;
+  int p = idx / nao, q = idx % nao;
+  auto get = [&](int pp, int qq) {
+    if (sym && (qq / kN) < (pp / kM)) { int t = pp; pp = qq; qq = t; }
+    int tm = pp / kM, tn = qq / kN, r = pp % kM, cc = qq % kN;
+    double s = 0;
+    for (int k = 0; k < nchunk; ++k)
+      s += P[((((long long)k * mtiles + tm) * ntiles + tn) * kM + r) * kN + cc];
+    return s;
+  };
+  double v = get(p, q);
+  if (add_transpose) v += get(q, p);
+  M[idx] = scale * v;
+}
+
+// ---------------------------------------------------------------------------
+// Density: X = D phi on tiles (128 AOs) x (128 grid points), K = AO, from the
+// K-major operands D[p][q] (row stride ldk) and phiT[g][q] (grid-major copy,
+// row stride ldk).  Epilogue: part[mt][g] = sum_{p in tile} phi_p(g) X_p(g)
+// and, for GGA, part_g[c][mt][g] = 2 sum_p dphi_c,p(g) X_p(g) (FP64).
+// ---------------------------------------------------------------------------
+struct DensArgs {
+  Operand D, phiT;
+  const float *phi, *dphi;  // AO-major (row stride ld) for the epilogue
+  int nao, kpad, drain, ns;
+  long long N, ld;
+  double *part, *part_g;
+  int *err;
+};
+
+constexpr int kProdLd = kN + 1;
+constexpr size_t kProdBytes = 2 * (size_t)kM * kProdLd * sizeof(float);
+constexpr size_t kDensSmem =
+    (kProdBytes > kStages * kStageBytes ? kProdBytes : kStages * kStageBytes) + kWslotBytes + 1024;
+
+__global__ void __launch_bounds__(kThreads, 1) k_tc_density(DensArgs a) {
+  extern __shared__ __align__(1024) char smraw[];
+  char *sm = (char *)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
+  __shared__ Pipe P;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int mt = blockIdx.x;
+  const long long g0 = (long long)blockIdx.y * kN;
+  const int mtiles = gridDim.x;
+  pipe_init(P);
+  const int nstages = a.kpad / kStageK;
+  const int p0 = mt * kM;
+  float4 *wslot = reinterpret_cast<float4 *>(
+      sm + (kProdBytes > kStages * kStageBytes ? kProdBytes : kStages * kStageBytes));
+  bool ok = run_pipe(P, sm, wslot, a.D, p0, a.phiT, (int)g0, nullptr, 0, a.nao, nstages, a.drain,
+                     a.ns, a.err, 10);
+
+  // epilogue: products with phi (and grad phi), column sums over the 128 AO rows
+  __syncthreads();  // all MMAs consumed and drained: the stage smem is free
+  float *prod = reinterpret_cast<float *>(sm);   // [128][129] sums
+  float *prodc = prod + kM * kProdLd;             // [128][129] compensations
+  int ncomp = a.part_g ? 4 : 1;
+  for (int comp = 0; comp < ncomp; ++comp) {
+    if (warp >= 4 && warp < 8) {
+      int row = (warp & 3) * 32 + (tid & 31), p = p0 + row;
+      const float *src = (comp == 0) ? a.phi + (long long)p * a.ld
+                                     : a.dphi + ((long long)(comp - 1) * a.nao + p) * a.ld;
+#pragma unroll 1
+      for (int c0 = 0; c0 < kN; c0 += 16) {
+        double x[16];
+        read_sum16(P, c0, x);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          int col = c0 + i;
+          long long g = g0 + col;
+          float f = (ok && p < a.nao && g < a.N) ? src[g] : 0.f;
+          // X * f as an unevaluated pair (hi, lo) of floats
+          float xs = (float)x[i];
+          float xc = (float)(x[i] - (double)xs);
+          float hi = xs * f;
+          float lo = fmaf(xs, f, -hi) + xc * f;
+          prod[row * kProdLd + col] = hi;
+          prodc[row * kProdLd + col] = lo;
+        }
+      }
+    }
+    __syncthreads();
+    if (tid < kN) {
+      long long g = g0 + tid;
+      float ss = 0.f, cc = 0.f;
+      for (int r = 0; r < kM; ++r) {
+        two_sum_add(ss, cc, prod[r * kProdLd + tid]);
+        cc += prodc[r * kProdLd + tid];
+      }
+      if (ok && g < a.N) {
+        double v = (double)ss + (double)cc;
+        if (comp == 0) a.part[(long long)mt * a.ld + g] = v;
+        else a.part_g[((long long)(comp - 1) * mtiles + mt) * a.ld + g] = 2.0 * v;
+      }
+    }
+    __syncthreads();
+  }
+  pipe_finish(P);
+}
+
+// rho[g] = sum_mt part[mt][g], grho similarly
+__global__ void k_tc_density_reduce(const double *__restrict__ part, const double *__restrict__ part_g,
+                                    int mtiles, long long N, long long ld, double *__restrict__ rho,
+                                    double *__restrict__ grho) {
+  long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= N) return;
+  double s = 0;
+  for (int m = 0; m < mtiles; ++m) s += part[(long long)m * ld + g];
+  rho[g] = s;
+  if (grho) {
+    for (int c = 0; c < 3; ++c) {
+      double t = 0;
+      for (int m = 0; m < mtiles; ++m) t += part_g[((long long)c * mtiles + m) * ld + g];
+      grho[(long long)c * N + g] = t;
+    }
+  }
+}
+
+// phiT[g][q] (row stride ldk) = phi[q][g] for g < N, q < nao; zero for q in [nao, ldk)
+__global__ void k_transpose_phi(const float *__restrict__ phi, int nao, long long N, long long ld,
+                                float *__restrict__ phiT, int ldk) {
+  __shared__ float t[32][33];
+  long long g0 = (long long)blockIdx.x * 32;
+  int q0 = blockIdx.y * 32;
+  int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 256 threads: 8 rows per pass
+  for (int r = ty; r < 32; r += 8) {
+    int q = q0 + r;
+    long long g = g0 + tx;
+    t[r][tx] = (q < nao && g < N) ? phi[(long long)q * ld + g] : 0.f;
+  }
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) {
+    long long g = g0 + r;
+    int q = q0 + tx;
+    if (g < N && q < ldk) phiT[g * ldk + q] = t[tx][r];
+  }
+}
+
+}  // namespace tc
+
+// ---------------------------------------------------------------------------
+int tc_quad_chunk() { return 8192; }
+
+size_t tc_quad_partial_doubles(int nao, long long N) {
+  int mt = ceil_div(nao, tc::kM), nt = ceil_div(nao, tc::kN);
+  long long chunks = ceil_div(N, tc_quad_chunk());
+  return (size_t)chunks * mt * nt * tc::kM * tc::kN;
+}
+
+// M = scale * sum_g A_p(g) w(g) B_q(g) (+ its transpose when add_transpose);
+// A, B fp32 [nao][ld]; w may be null.  sym: A == B with w symmetric use.
+void launch_tc_gemm_nt(const float *A, const float *B, const float *w, int nao, long long N,
+                       long long ld, bool sym, bool add_transpose, double scale, double *partial,
+                       double *M, int *err, cudaStream_t st, int nsplit, int drain) {
+  HQ_STAGE(ST_QUAD, st);
+  HQ_REQUIRE(ld % 4 == 0, "row stride must be a multiple of 4 floats");
+  HQ_REQUIRE(nsplit == 2, "nsplit must be 2 (3xTF32)");
+  HQ_REQUIRE(drain >= 1, "drain must be >= 1");
+  static bool attr = false;
+  if (!attr) {
+    HQ_CUDA(cudaFuncSetAttribute(tc::k_tc_quadrature, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)tc::kQuadSmem));
+    attr = true;
+  }
+  tc::QuadArgs a;
+  a.A = tc::Operand{A, ld, nao};
+  a.B = tc::Operand{B, ld, nao};
+  a.w = w; a.nao = nao; a.sym = sym ? 1 : 0; a.drain = drain; a.ns = nsplit; a.N = N;
+  a.kchunk = tc_quad_chunk(); a.partial = partial; a.err = err;
+  int mt = ceil_div(nao, tc::kM), nt = ceil_div(nao, tc::kN);
+  int chunks = ceil_div(N, a.kchunk);
+  dim3 grid(mt, nt, chunks);
+  tc::k_tc_quadrature<<<grid, tc::kThreads, tc::kQuadSmem, st>>>(a);
+  HQ_LAUNCH_CHECK();
+  tc::k_tc_quad_reduce<<<ceil_div((long long)nao * nao, 256), 256, 0, st>>>(
+      partial, chunks, mt, nt, nao, a.sym, add_transpose ? 1 : 0, scale, M);
+  HQ_LAUNCH_CHECK();
+}
+
+// Quadrature of the Fock build: LDA  M = phi diag(w) phi^T;  GGA  M = Z phi^T +
+// phi Z^T with the operand Z = 0.5 w phi + dV u.grad phi precomputed in `zbuf`.
+__global__ void k_gga_operand32(const float *__restrict__ phi, const float *__restrict__ dphi,
+                                const float *__restrict__ w, const float *__restrict__ u, int nao,
+                                long long ld, float dV, float *__restrict__ Z) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long NN = (long long)nao * ld;
+  if (i >= NN) return;
+  long long g = i % ld;
+  Z[i] = 0.5f * w[g] * phi[i] + dV * (u[g] * dphi[i] + u[ld + g] * dphi[NN + i] +
+                                      u[2 * ld + g] * dphi[2 * NN + i]);
+}
+
+void launch_tc_quadrature(const float *phi, const float *dphi, const float *w, const float *u,
+                          float dV, int nao, long long N, long long ld, bool gga, double scale,
+                          double *partial, double *M, int *err, cudaStream_t st, int nsplit,
+                          int drain, float *zbuf) {
+  if (!gga) {
+    launch_tc_gemm_nt(phi, phi, w, nao, N, ld, true, false, scale, partial, M, err, st, nsplit, drain);
+    return;
+  }
+  HQ_REQUIRE(zbuf && dphi && u, "GGA quadrature needs dphi, u and a Z buffer");
+  k_gga_operand32<<<ceil_div((long long)nao * ld, 256), 256, 0, st>>>(phi, dphi, w, u, nao, ld, dV,
+                                                                       zbuf);
+  HQ_LAUNCH_CHECK();
+  launch_tc_gemm_nt(zbuf, phi, nullptr, nao, N, ld, false, true, scale, partial, M, err, st, nsplit,
+                    drain);
+}
+
+size_t tc_density_partial_doubles(int nao, long long ld, bool gga) {
+  int mt = ceil_div(nao, tc::kM);
+  return (size_t)mt * ld * (gga ? 4 : 1);
+}
+
+int tc_ldk(int nao) { return ceil_div(nao, 32) * 32; }
+
+void launch_transpose_phi(const float *phi, int nao, long long N, long long ld, float *phiT,
+                          cudaStream_t st) {
+  int ldk = tc_ldk(nao);
+  dim3 grid(ceil_div(N, 32), ceil_div(ldk, 32));
+  tc::k_transpose_phi<<<grid, 256, 0, st>>>(phi, nao, N, ld, phiT, ldk);
+  HQ_LAUNCH_CHECK();
+}
+
+// D32: [nao][ldk] (zero columns beyond nao); phiT: [N][ldk] grid-major copy.
+void launch_tc_density(const float *phi, const float *phiT, const float *dphi, const float *D32,
+                       int nao, long long N, long long ld, double *part, double *rho, double *grho,
+                       int *err, cudaStream_t st, int nsplit, int drain) {
+  HQ_STAGE(ST_DENSITY, st);
+  HQ_REQUIRE(ld % 4 == 0, "row stride must be a multiple of 4 floats");
+  HQ_REQUIRE(nsplit == 2, "nsplit must be 2 (3xTF32)");
+  HQ_REQUIRE(drain >= 1, "drain must be >= 1");
+  static bool attr = false;
+  if (!attr) {
+    HQ_CUDA(cudaFuncSetAttribute(tc::k_tc_density, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)tc::kDensSmem));
+    attr = true;
+  }
+  int mt = ceil_div(nao, tc::kM);
+  int ldk = tc_ldk(nao);
+  tc::DensArgs a;
+  a.D = tc::Operand{D32, ldk, nao};
+  a.phiT = tc::Operand{phiT, ldk, (int)N};
+  a.phi = phi; a.dphi = grho ? dphi : nullptr; a.nao = nao;
+  a.kpad = ldk; a.drain = drain; a.ns = nsplit; a.N = N; a.ld = ld; a.part = part;
+  a.part_g = grho ? part + (size_t)mt * ld : nullptr; a.err = err;
+  dim3 grid(mt, ceil_div(N, tc::kN));
+  tc::k_tc_density<<<grid, tc::kThreads, tc::kDensSmem, st>>>(a);
+  HQ_LAUNCH_CHECK();
+  tc::k_tc_density_reduce<<<ceil_div(N, 256), 256, 0, st>>>(part, a.part_g, mt, N, ld, rho, grho);
+  HQ_LAUNCH_CHECK();
+}
+
+}  // namespace hqcgb
+
+// ---------------------------------------------------------------------------
+// C ABI: the two tensor-core contractions as library calls (tests and tools).
+// ---------------------------------------------------------------------------
+extern "C" int hqcgb_tc_quadrature(int nao, long long N, long long ld, const float *phi,
+                                   const float *w, int nsplit, int drain, double *M, void *stream) {
+  using namespace hqcgb;
+  cudaStream_t st = (cudaStream_t)stream;
+  try {
+    HQ_REQUIRE(nao >= 1 && N >= 1 && ld >= N && ld % 4 == 0 && phi && w && M, "bad argument");
+    double *part = nullptr;
+    int *err = nullptr;
+    HQ_CUDA(cudaMallocAsync(&part, tc_quad_partial_doubles(nao, N) * sizeof(double), st));
+    HQ_CUDA(cudaMallocAsync(&err, sizeof(int), st));
+    HQ_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
+    launch_tc_gemm_nt(phi, phi, w, nao, N, ld, true, false, 1.0, part, M, err, st, nsplit, drain);
+    int h = 0;
+    HQ_CUDA(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    HQ_CUDA(cudaFreeAsync(part, st));
+    HQ_CUDA(cudaFreeAsync(err, st));
+    HQ_CUDA(cudaStreamSynchronize(st));
+    if (h) throw Error{HQCGB_CUDA_ERROR, "tensor-core pipeline wait limit hit"};
+    return HQCGB_OK;
+  } catch (const Error &e) {
+    set_error(e.msg);
+    return e.status;
+  }
+}
+
+extern "C" int hqcgb_tc_density(int nao, long long N, long long ld, const float *phi,
+                                const float *D, int nsplit, int drain, double *rho, void *stream) {
+  using namespace hqcgb;
+  cudaStream_t st = (cudaStream_t)stream;
+  try {
+    HQ_REQUIRE(nao >= 1 && N >= 1 && ld >= N && ld % 4 == 0 && phi && D && rho, "bad argument");
+    int ldk = tc_ldk(nao);
+    double *part = nullptr;
+    float *phiT = nullptr, *D32 = nullptr;
+    int *err = nullptr;
+    HQ_CUDA(cudaMallocAsync(&part, tc_density_partial_doubles(nao, ld, false) * sizeof(double), st));
+    HQ_CUDA(cudaMallocAsync(&phiT, (size_t)N * ldk * sizeof(float), st));
+    HQ_CUDA(cudaMallocAsync(&D32, (size_t)nao * ldk * sizeof(float), st));
+    HQ_CUDA(cudaMallocAsync(&err, sizeof(int), st));
+    HQ_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
+    HQ_CUDA(cudaMemsetAsync(D32, 0, (size_t)nao * ldk * sizeof(float), st));
+    HQ_CUDA(cudaMemcpy2DAsync(D32, ldk * sizeof(float), D, nao * sizeof(float), nao * sizeof(float),
+                              nao, cudaMemcpyDeviceToDevice, st));
+    launch_transpose_phi(phi, nao, N, ld, phiT, st);
+    launch_tc_density(phi, phiT, nullptr, D32, nao, N, ld, part, rho, nullptr, err, st, nsplit, drain);
+    int h = 0;
+    HQ_CUDA(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    HQ_CUDA(cudaFreeAsync(part, st));
+    HQ_CUDA(cudaFreeAsync(phiT, st));
+    HQ_CUDA(cudaFreeAsync(D32, st));
+    HQ_CUDA(cudaFreeAsync(err, st));
+    HQ_CUDA(cudaStreamSynchronize(st));
+    if (h) throw Error{HQCGB_CUDA_ERROR, "tensor-core pipeline wait limit hit"};
+    return HQCGB_OK;
+  } catch (const Error &e) {
+    set_error(e.msg);
+    return e.status;
+  }
+}

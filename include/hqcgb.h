@@ -130,6 +130,18 @@ long long hqcgb_plan_query(hqcgb_plan *plan, const char *name, void *dst, size_t
  * at hqc/pbc/solver.py:729,741 and hqc/pbc/scf.py:69,138,198. */
 int hqcgb_eigh(int n, int batch, const double *A, double *w, double *V, void *stream);
 
+/* The tensor-core grid contractions of the mixed path as library calls
+ * (device pointers; fp32 inputs with row stride ld >= N, ld % 4 == 0, zero
+ * padding in [N, ld)).  nsplit = 2 (3xTF32; the only value accepted);
+ * drain = number of K sub-chunks of 32 points summed in TMEM before a
+ * compensated FP32 drain (1 = most accurate).
+ *   quadrature: M[p][q] = sum_g phi[p][g] w[g] phi[q][g]  (hqc/pbc/solver.py:693)
+ *   density:    rho[g]  = sum_pq D[p][q] phi[p][g] phi[q][g] (hqc/pbc/solver.py:690) */
+int hqcgb_tc_quadrature(int nao, long long N, long long ld, const float *phi, const float *w,
+                        int nsplit, int drain, double *M, void *stream);
+int hqcgb_tc_density(int nao, long long N, long long ld, const float *phi, const float *D,
+                     int nsplit, int drain, double *rho, void *stream);
+
 /* Largest n accepted by hqcgb_eigh_noalloc. */
 #define HQCGB_EIGH_NOALLOC_MAX_N 320
 
