@@ -45,7 +45,8 @@ class ScfOut(ctypes.Structure):
 EXPORTS = ("hqcgb_plan_create", "hqcgb_plan_destroy", "hqcgb_scf", "hqcgb_scf_batch",
            "hqcgb_forces", "hqcgb_ewald", "hqcgb_plan_query", "hqcgb_last_error",
            "hqcgb_launch_count", "hqcgb_profile", "hqcgb_stage_stats", "hqcgb_eigh",
-           "hqcgb_eigh_noalloc", "hqcgb_tc_quadrature", "hqcgb_tc_density")
+           "hqcgb_eigh_noalloc", "hqcgb_eigh_mixed", "hqcgb_tc_quadrature", "hqcgb_tc_density",
+           "hqcgb_tc_orbital_density")
 N_STAGES = 13
 
 _lib = None
@@ -91,6 +92,9 @@ def load():
     lib.hqcgb_tc_density.argtypes = [ctypes.c_int, ctypes.c_longlong, ctypes.c_longlong,
                                      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                      ctypes.c_void_p, ctypes.c_void_p]
+    lib.hqcgb_tc_orbital_density.argtypes = [ctypes.c_int, ctypes.c_longlong, ctypes.c_longlong] + \
+        [ctypes.c_void_p] * 4 + [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 3
+    lib.hqcgb_eigh_mixed.argtypes = [ctypes.c_int] + [ctypes.c_void_p] * 4
     lib.hqcgb_eigh_noalloc.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                        ctypes.c_void_p, ctypes.c_void_p]
     lib.hqcgb_stage_stats.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_char_p),
@@ -144,6 +148,21 @@ def eigh(A):
     return (w[0], V[0]) if single else (w, V)
 
 
+def eigh_mixed(A):
+    """The mixed-precision eigensolver (FP32 solve + FP64 refinement) on one
+    (n, n) float64 CUDA matrix: (w ascending, V columns)."""
+    import torch
+    lib = load()
+    A = A.contiguous()
+    n = A.shape[0]
+    w = torch.empty(n, dtype=torch.float64, device=A.device)
+    V = torch.empty(n, n, dtype=torch.float64, device=A.device)
+    st = ctypes.c_void_p(torch.cuda.current_stream(A.device).cuda_stream)
+    check(lib.hqcgb_eigh_mixed(n, ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(w.data_ptr()),
+                               ctypes.c_void_p(V.data_ptr()), st))
+    return w, V
+
+
 EIGH_NOALLOC_MAX_N = 320
 
 
@@ -193,3 +212,26 @@ def tc_density(phi32, D32, N=None, nsplit=2, drain=1):
                                ctypes.c_void_p(D32.data_ptr()), nsplit, drain,
                                ctypes.c_void_p(rho.data_ptr()), st))
     return rho
+
+
+def tc_orbital_density(phi32, C, occ, N=None, nuse=None, dphi32=None):
+    """rho = sum_k occ_k (sum_p C[p,k] phi_p)^2 (and grad rho with dphi32) on
+    the tensor cores; phi32 (nao, ld) fp32, C (nao, nmo) and occ (nmo,) fp64."""
+    import torch
+    lib = load()
+    nao, ld = phi32.shape
+    N = ld if N is None else N
+    nmo = C.shape[1]
+    nuse = nmo if nuse is None else nuse
+    dev = phi32.device
+    rho = torch.empty(N, dtype=torch.float64, device=dev)
+    grho = torch.empty(3, N, dtype=torch.float64, device=dev) if dphi32 is not None else None
+    C = C.contiguous()
+    occ = occ.contiguous()
+    st = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    check(lib.hqcgb_tc_orbital_density(
+        nao, N, ld, ctypes.c_void_p(phi32.data_ptr()),
+        ctypes.c_void_p(dphi32.data_ptr() if dphi32 is not None else 0),
+        ctypes.c_void_p(C.data_ptr()), ctypes.c_void_p(occ.data_ptr()), nmo, nuse,
+        ctypes.c_void_p(rho.data_ptr()), ctypes.c_void_p(grho.data_ptr() if grho is not None else 0), st))
+    return rho if grho is None else (rho, grho)

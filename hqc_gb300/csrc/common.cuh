@@ -88,4 +88,23 @@ __device__ inline T block_sum(T v, T *sh /* >= 32 */) {
   return v;
 }
 
+// Maximum over the block, returned to every thread (same contract).
+template <typename T>
+__device__ inline T block_max(T v, T *sh /* >= 32 */) {
+  for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  int nw = (blockDim.x + 31) >> 5;
+  if (w == 0) {
+    v = (lane < nw) ? sh[lane] : sh[0];
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if (lane == 0) sh[0] = v;
+  }
+  __syncthreads();
+  v = sh[0];
+  __syncthreads();
+  return v;
+}
+
 }  // namespace hqcgb

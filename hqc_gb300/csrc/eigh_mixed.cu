@@ -3,16 +3,17 @@
 // Stage 1 (FP32, one thread block): Householder tridiagonalisation, implicit
 // QL and back-transformation -- the FP64 algorithm of eigh_fp64.cu run in
 // FP32, 30-60x cheaper per operation on GB300.
-// Stage 2 (FP64): two iterations of the Ogita-Aishima refinement
+// Stage 2 (FP64): Ogita-Aishima refinement
 // (T. Ogita, K. Aishima, "Iterative refinement for symmetric eigenvalue
 // decomposition", Japan J. Indust. Appl. Math. 35 (2018) 1007-1035):
 //   R = I - X^T X,  S = X^T A X,  l_i = s_ii / (1 - r_ii),
 //   E_ij = (s_ij + l_j r_ij) / (l_j - l_i)   for |l_i - l_j| > delta,
 //   E_ij = r_ij / 2                            otherwise,
 //   X <- X + X E,
-// with delta = 2 (||S - diag(l)|| + ||A|| ||R||) (Frobenius norms).  Each
-// iteration squares the error, so FP32-accurate vectors become FP64-accurate
-// after two; all of it is FP64 GEMM work spread over many SMs.  The result
+// with delta = 2 (||S - diag(l)|| + ||A|| ||R||) (Frobenius norms), and the
+// clustered-eigenvalue extension of the same authors (below).  Each iteration
+// squares the error, so FP32-accurate vectors become FP64-accurate after two
+// or three; all of it is FP64 GEMM work spread over many SMs.  The result
 // stands in for jnp.linalg.eigh (hqc/pbc/scf.py:69,138,198).
 #include <cstdlib>
 
@@ -30,16 +31,37 @@ __global__ void k_f32_to_f64(long long n, const float *__restrict__ a, double *_
   if (i < n) b[i] = (double)a[i];
 }
 
-// One block: lambda, delta and the correction E from S and G = X^T X.
+// One block: lambda, delta, the clusters and the correction E from
+// S = X^T A X and G = X^T X.
+//
+// Clusters (Ogita, Aishima, "Iterative refinement for symmetric eigenvalue
+// decomposition II: clustered eigenvalues", Japan J. Indust. Appl. Math. 36
+// (2019) 435-459): eigenvalue estimates closer than delta form a cluster,
+// within which the basic update only re-orthogonalises.  Each cluster C is
+// therefore rotated first by the eigenvectors W_C of its block S_CC (cyclic
+// Jacobi, one thread per cluster): X_C <- X_C W_C, S <- W^T S W and
+// G <- W^T G W, after which the cluster's Ritz values are separated and the
+// next iteration converges quadratically again.  Clusters larger than
+// kMaxCluster are left unrotated and flagged in emax[2].
+// emax[0] = max |E|, emax[1] = ||S - diag(l)||_F / ||A||_F before the
+// update, emax[2] = 1 when a cluster was too large, emax[3] = cluster count.
+constexpr int kMaxCluster = 48;
+
 __global__ void __launch_bounds__(1024) k_oa_correction(int n, const double *__restrict__ A,
-                                                        const double *__restrict__ S,
-                                                        const double *__restrict__ G,
+                                                        double *__restrict__ S,
+                                                        double *__restrict__ G,
+                                                        double *__restrict__ X,
                                                         double *__restrict__ E,
                                                         double *__restrict__ lam,
-                                                        double *__restrict__ emax) {
+                                                        double *__restrict__ emax,
+                                                        int *__restrict__ iwork,
+                                                        double *__restrict__ wbuf) {
   __shared__ double red[32];
+  __shared__ int s_nclus, s_bad;
   const int tid = threadIdx.x, nt = blockDim.x;
   const long long nn = (long long)n * n;
+  int *order = iwork, *cid = iwork + n, *cstart = iwork + 2 * n, *csize = iwork + 3 * n,
+      *coff = iwork + 4 * n;
   for (int i = tid; i < n; i += nt) lam[i] = S[(long long)i * n + i] / (G[(long long)i * n + i]);
   __syncthreads();
   double a2 = 0, s2 = 0, r2 = 0;
@@ -55,19 +77,157 @@ __global__ void __launch_bounds__(1024) k_oa_correction(int n, const double *__r
   a2 = block_sum(a2, red);
   s2 = block_sum(s2, red);
   r2 = block_sum(r2, red);
-  double delta = 2.0 * (sqrt(s2) + sqrt(a2) * sqrt(r2));
-  if (tid == 0 && emax) emax[1] = sqrt(s2) / fmax(sqrt(a2), 1e-300);  // relative off-diagonal
+  // largest off-diagonal coupling |s_ij + l_j r_ij|
+  double cmax = 0;
+  for (long long k = tid; k < nn; k += nt) {
+    int i = (int)(k / n), j = (int)(k % n);
+    if (i != j) cmax = fmax(cmax, fabs(S[k] - lam[j] * G[k]));
+  }
+  cmax = block_max(cmax, red);
+  // Separation: pairs closer than 10x the largest coupling would get
+  // corrections |E_ij| > 0.1, outside the quadratic regime, so they are
+  // clustered instead; the floor (1e-6 of the mean eigenvalue scale) keeps
+  // pairs that are ill-determined at FP64 rounding in clusters as well.
+  // (The paper's bound 2(||S - diag(l)||_F + ||A||_F ||R||_F) is rigorous but
+  // lumps whole bands of a 270-AO Fock matrix into one cluster.)
+  const double delta = fmax(10.0 * cmax, 1e-6 * sqrt(a2 / n));
+  if (tid == 0 && emax) emax[1] = sqrt(s2) / fmax(sqrt(a2), 1e-300);
+
+  // ascending order of the estimates (ties by index)
+  for (int i = tid; i < n; i += nt) {
+    double li = lam[i];
+    int r = 0;
+    for (int j = 0; j < n; ++j) {
+      double lj = lam[j];
+      r += (lj < li) || (lj == li && j < i);
+    }
+    order[r] = i;
+  }
+  __syncthreads();
+  // clusters: maximal runs of the ordered estimates with gaps <= delta
+  if (tid == 0) {
+    int nclus = 0, bad = 0, off = 0;
+    for (int i = 0; i < n;) {
+      int j = i;
+      while (j + 1 < n && lam[order[j + 1]] - lam[order[j]] <= delta) ++j;
+      int k = j - i + 1;
+      if (k >= 2 && k <= kMaxCluster) {
+        cstart[nclus] = i;
+        csize[nclus] = k;
+        coff[nclus] = off;
+        off += 2 * k * k;
+        for (int m = i; m <= j; ++m) cid[order[m]] = nclus;
+        ++nclus;
+      } else {
+        if (k > kMaxCluster) bad = 1;
+        for (int m = i; m <= j; ++m) cid[order[m]] = -1;
+      }
+      i = j + 1;
+    }
+    s_nclus = nclus;
+    s_bad = bad;
+    if (emax) {
+      emax[2] = bad;
+      emax[3] = nclus;
+    }
+  }
+  __syncthreads();
+  const int nclus = s_nclus;
+
+  if (nclus > 0) {
+    // cyclic Jacobi on each cluster block B = S_CC; W accumulates the rotations
+    for (int c = tid; c < nclus; c += nt) {
+      const int k = csize[c], s0 = cstart[c];
+      double *B = wbuf + coff[c], *W = B + k * k;
+      for (int a = 0; a < k; ++a)
+        for (int b = 0; b < k; ++b) {
+          long long ia = order[s0 + a], ib = order[s0 + b];
+          B[a * k + b] = 0.5 * (S[ia * n + ib] + S[ib * n + ia]);
+          W[a * k + b] = (a == b) ? 1.0 : 0.0;
+        }
+      for (int sweep = 0; sweep < 40; ++sweep) {
+        double offd = 0, diag = 0;
+        for (int a = 0; a < k; ++a) {
+          diag += B[a * k + a] * B[a * k + a];
+          for (int b = a + 1; b < k; ++b) offd += B[a * k + b] * B[a * k + b];
+        }
+        if (offd <= 1e-34 * diag || offd == 0.0) break;
+        for (int a = 0; a < k - 1; ++a)
+          for (int b = a + 1; b < k; ++b) {
+            double bab = B[a * k + b];
+            if (bab == 0.0) continue;
+            double theta = (B[b * k + b] - B[a * k + a]) / (2.0 * bab);
+            double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+            double cs = 1.0 / sqrt(t * t + 1.0), sn = t * cs;
+            for (int m = 0; m < k; ++m) {  // B <- B J, W <- W J
+              double x = B[m * k + a], y = B[m * k + b];
+              B[m * k + a] = cs * x - sn * y;
+              B[m * k + b] = sn * x + cs * y;
+              x = W[m * k + a];
+              y = W[m * k + b];
+              W[m * k + a] = cs * x - sn * y;
+              W[m * k + b] = sn * x + cs * y;
+            }
+            for (int m = 0; m < k; ++m) {  // B <- J^T B
+              double x = B[a * k + m], y = B[b * k + m];
+              B[a * k + m] = cs * x - sn * y;
+              B[b * k + m] = sn * x + cs * y;
+            }
+          }
+      }
+    }
+    __syncthreads();
+    // columns: X_C <- X_C W_C, S_:C <- S_:C W_C, G_:C <- G_:C W_C
+    for (long long idx = tid; idx < (long long)n * nclus; idx += nt) {
+      const int r = (int)(idx % n), c = (int)(idx / n);
+      const int k = csize[c], s0 = cstart[c];
+      const double *W = wbuf + coff[c] + k * k;
+      double *mats[3] = {X, S, G};
+      for (int q = 0; q < 3; ++q) {
+        double *row = mats[q] + (long long)r * n;
+        double tmp[kMaxCluster];
+        for (int j = 0; j < k; ++j) {
+          double acc = 0;
+          for (int i = 0; i < k; ++i) acc += row[order[s0 + i]] * W[i * k + j];
+          tmp[j] = acc;
+        }
+        for (int j = 0; j < k; ++j) row[order[s0 + j]] = tmp[j];
+      }
+    }
+    __syncthreads();
+    // rows: S_C: <- W_C^T S_C:, G_C: <- W_C^T G_C:
+    for (long long idx = tid; idx < (long long)n * nclus; idx += nt) {
+      const int col = (int)(idx % n), c = (int)(idx / n);
+      const int k = csize[c], s0 = cstart[c];
+      const double *W = wbuf + coff[c] + k * k;
+      double *mats[2] = {S, G};
+      for (int q = 0; q < 2; ++q) {
+        double *m = mats[q];
+        double tmp[kMaxCluster];
+        for (int j = 0; j < k; ++j) {
+          double acc = 0;
+          for (int i = 0; i < k; ++i) acc += W[i * k + j] * m[(long long)order[s0 + i] * n + col];
+          tmp[j] = acc;
+        }
+        for (int j = 0; j < k; ++j) m[(long long)order[s0 + j] * n + col] = tmp[j];
+      }
+    }
+    __syncthreads();
+    for (int i = tid; i < n; i += nt) lam[i] = S[(long long)i * n + i] / (G[(long long)i * n + i]);
+    __syncthreads();
+  }
+
   double em = 0;
   for (long long k = tid; k < nn; k += nt) {
     int i = (int)(k / n), j = (int)(k % n);
     double r = (i == j ? 1.0 : 0.0) - G[k];
+    bool same = cid[i] >= 0 && cid[i] == cid[j];
     double e;
-    if (i != j && fabs(lam[i] - lam[j]) > delta) e = (S[k] + lam[j] * r) / (lam[j] - lam[i]);
+    if (i != j && !same && fabs(lam[i] - lam[j]) > delta) e = (S[k] + lam[j] * r) / (lam[j] - lam[i]);
     else e = 0.5 * r;
     E[k] = e;
     em = fmax(em, fabs(e));
   }
-  // block max through the sum helper's shared buffer
   __shared__ double mx[32];
   for (int o = 16; o > 0; o >>= 1) em = fmax(em, __shfl_xor_sync(0xffffffffu, em, o));
   if ((tid & 31) == 0) mx[tid >> 5] = em;
@@ -75,7 +235,7 @@ __global__ void __launch_bounds__(1024) k_oa_correction(int n, const double *__r
   if (tid < 32) {
     em = (tid < (nt >> 5)) ? mx[tid] : 0.0;
     for (int o = 16; o > 0; o >>= 1) em = fmax(em, __shfl_xor_sync(0xffffffffu, em, o));
-    if (tid == 0 && emax) *emax = em;
+    if (tid == 0 && emax) emax[0] = em;
   }
 }
 
@@ -112,23 +272,30 @@ static void sort_eigpairs(int n, double *w, double *X, MixedEigWork &ws, cudaStr
   HQ_LAUNCH_CHECK();
 }
 
+// One refinement step; returns ||X^T A X - diag|| / ||A|| before the update.
 static double oa_iteration(int n, const double *A, double *X, double *w, MixedEigWork &ws,
                            cudaStream_t st) {
   gemm(false, false, n, n, n, 1.0, A, n, X, n, nullptr, 0.0, ws.T1, n, st);    // A X
   gemm(true, false, n, n, n, 1.0, X, n, ws.T1, n, nullptr, 0.0, ws.S, n, st);  // X^T A X
   gemm(true, false, n, n, n, 1.0, X, n, X, n, nullptr, 0.0, ws.G, n, st);      // X^T X
-  k_oa_correction<<<1, 1024, 0, st>>>(n, A, ws.S, ws.G, ws.E, w, ws.emax);
+  k_oa_correction<<<1, 1024, 0, st>>>(n, A, ws.S, ws.G, X, ws.E, w, ws.emax, ws.iwork, ws.wbuf);
   HQ_LAUNCH_CHECK();
   gemm(false, false, n, n, n, 1.0, X, n, ws.E, n, nullptr, 0.0, ws.T1, n, st);  // X E
   axpby(n, 1.0, X, 1.0, ws.T1, false, X, st);                                  // X += X E
-  double em[2] = {0, 0};
-  HQ_CUDA(cudaMemcpyAsync(em, ws.emax, 2 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  double em[4] = {0, 0, 0, 0};
+  HQ_CUDA(cudaMemcpyAsync(em, ws.emax, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
   HQ_CUDA(cudaStreamSynchronize(st));
-  return em[1];  // relative off-diagonal norm of X^T A X before this update
+  if (std::getenv("HQCGB_TRACE"))
+    fprintf(stderr, "  oa off=%.3e max|E|=%.3e clusters=%g%s\n", em[1], em[0], em[3],
+            em[2] != 0 ? " (cluster too large)" : "");
+  return em[1];
 }
 
-// Full solve: FP32 stage + two refinements.
-void eigh_mixed(int n, const double *A, double *V, double *w, MixedEigWork &ws, cudaStream_t st) {
+// Full solve: FP32 stage, then refinement until the relative off-diagonal
+// norm measured before a step is at rounding level (1e-12).  Returns false
+// when the refinement does not get there within 8 steps (the caller then
+// uses the FP64 solver) or the FP32 stage failed.
+bool eigh_mixed(int n, const double *A, double *V, double *w, MixedEigWork &ws, cudaStream_t st) {
   HQ_STAGE(ST_JACOBI, st);
   long long nn = (long long)n * n;
   k_f64_to_f32<<<ceil_div(nn, 256), 256, 0, st>>>(nn, A, ws.A32);
@@ -136,32 +303,49 @@ void eigh_mixed(int n, const double *A, double *V, double *w, MixedEigWork &ws, 
   eigh_tql_f32(n, 1, ws.A32, ws.V32, ws.w32, ws.work32, ws.status, st);
   k_f32_to_f64<<<ceil_div(nn, 256), 256, 0, st>>>(nn, ws.V32, V);
   HQ_LAUNCH_CHECK();
-  for (int it = 0; it < 2; ++it) oa_iteration(n, A, V, w, ws, st);
-  sort_eigpairs(n, w, V, ws, st);
-}
-
-// Warm start from eigenvectors X0 of a nearby matrix (the previous SCF
-// iteration's Fock matrix): refinement only, while its corrections shrink
-// quadratically.  Returns false (V untouched semantics not guaranteed) when
-// the start is too far, so the caller runs the full solve.
-bool eigh_mixed_warm(int n, const double *A, const double *X0, double *V, double *w,
-                     MixedEigWork &ws, cudaStream_t st) {
-  HQ_STAGE(ST_JACOBI, st);
-  HQ_CUDA(cudaMemcpyAsync(V, X0, sizeof(double) * n * n, cudaMemcpyDeviceToDevice, st));
-  // off = ||X^T A X - diag|| / ||A|| of the start; the refinement converges
-  // quadratically only when the start is close, so far starts fall back.
-  double prev = 1e300;
-  for (int it = 0; it < 6; ++it) {
+  int hs = 0;
+  HQ_CUDA(cudaMemcpyAsync(&hs, ws.status, sizeof(int), cudaMemcpyDeviceToHost, st));
+  HQ_CUDA(cudaStreamSynchronize(st));
+  if (hs < 0) return false;
+  for (int it = 0; it < 8; ++it) {
     double off = oa_iteration(n, A, V, w, ws, st);
-    if (std::getenv("HQCGB_TRACE")) fprintf(stderr, "  warm it %d off=%.3e\n", it, off);
-    if (!(off < 2e-3) || (it > 0 && off > 0.25 * prev && off > 1e-12)) return false;
-    if (off < 1e-11) {  // this update took it to rounding level
+    if (off < 1e-12) {
       sort_eigpairs(n, w, V, ws, st);
       return true;
     }
-    prev = off;
   }
   return false;
 }
 
 }  // namespace hqcgb
+
+// C ABI: the mixed-precision solver on one matrix (workspace allocated per call).
+extern "C" int hqcgb_eigh_mixed(int n, const double *A, double *w, double *V, void *stream) {
+  using namespace hqcgb;
+  cudaStream_t st = (cudaStream_t)stream;
+  try {
+    HQ_REQUIRE(A && w && V && n >= 1 && n <= kMaxNao, "bad argument");
+    size_t nn = (size_t)n * n;
+    MixedEigWork ws{};
+    void *blk = nullptr;
+    size_t f32 = 3 * nn + 2 * (size_t)n + 64, f64 = 6 * nn + 64, i32 = 5 * (size_t)n + 64;
+    HQ_CUDA(cudaMallocAsync(&blk, f64 * sizeof(double) + f32 * sizeof(float) + i32 * sizeof(int), st));
+    double *d = reinterpret_cast<double *>(blk);
+    ws.T1 = d; ws.S = d + nn; ws.G = d + 2 * nn; ws.E = d + 3 * nn; ws.wbuf = d + 4 * nn;
+    ws.emax = d + 6 * nn;
+    float *f = reinterpret_cast<float *>(d + f64);
+    ws.A32 = f; ws.V32 = f + nn; ws.work32 = f + 2 * nn; ws.w32 = f + 3 * nn;
+    ws.status = reinterpret_cast<int *>(f + f32);
+    ws.iwork = ws.status + 64;
+    HQ_CUDA(cudaMemsetAsync(ws.status, 0, sizeof(int), st));
+    bool ok = eigh_mixed(n, A, V, w, ws, st);
+    HQ_CUDA(cudaFreeAsync(blk, st));
+    HQ_CUDA(cudaStreamSynchronize(st));
+    int hs = ok ? 0 : -1;
+    if (hs < 0) throw Error{HQCGB_EIG_FAIL, "eigensolver did not converge"};
+    return HQCGB_OK;
+  } catch (const Error &e) {
+    set_error(e.msg);
+    return e.status;
+  }
+}

@@ -89,12 +89,10 @@ void eigh_tql_f32(int n, int batch, float *A, float *V, float *w, float *work, i
                   cudaStream_t st);
 struct MixedEigWork {
   float *A32, *V32, *w32, *work32;
-  double *T1, *S, *G, *E, *emax;
-  int *status;
+  double *T1, *S, *G, *E, *emax, *wbuf;  // wbuf: 2 n^2 (cluster blocks); emax: 4
+  int *status, *iwork;                    // iwork: 5 n
 };
-void eigh_mixed(int n, const double *A, double *V, double *w, MixedEigWork &ws, cudaStream_t st);
-bool eigh_mixed_warm(int n, const double *A, const double *X0, double *V, double *w,
-                     MixedEigWork &ws, cudaStream_t st);
+bool eigh_mixed(int n, const double *A, double *V, double *w, MixedEigWork &ws, cudaStream_t st);
 
 // fft (FP32 transforms)
 void launch_fft3d_f32(float2 *c, int ng, int batch, const double2 *tw, bool inverse,
@@ -123,6 +121,12 @@ size_t tc_density_partial_doubles(int nao, long long ld, bool gga);
 int tc_ldk(int nao);
 void launch_transpose_phi(const float *phi, int nao, long long N, long long ld, float *phiT,
                           cudaStream_t st);
+int tc_psi_max(bool gga);
+int tc_psi_width(int nuse);
+void launch_psi_operand(const double *C, const double *occ, int nao, int nmo, int nuse, int ldk,
+                        float *Yhl, cudaStream_t st);
+void launch_tc_psi_density(const float *phiT, const float *dphiT, const float *Yhl, int npsi, int ldk,
+                           long long N, double *rho, double *grho, int *err, cudaStream_t st);
 void launch_tc_density(const float *phi, const float *phiT, const float *dphi, const float *D32,
                        int nao, long long N, long long ld, double *part, double *rho, double *grho,
                        int *err, cudaStream_t st, int nsplit = 2, int drain = 3);

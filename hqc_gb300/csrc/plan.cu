@@ -110,14 +110,14 @@ struct hqcgb_plan {
   // mixed-precision grid data (row stride ld floats)
   bool mixed = false;
   long long ld = 0;
+  float *dphiT32 = nullptr, *Yhl = nullptr;  // grid-major AO gradients; split Y^T
+  std::vector<double> hocc;                   // host copy of the occupations
   float *phi32 = nullptr, *dphi32 = nullptr, *phiT32 = nullptr, *D32 = nullptr, *w32 = nullptr,
         *u32 = nullptr, *z32 = nullptr;
   double *tcq_part = nullptr, *tcd_part = nullptr;
   float2 *cbuf32 = nullptr;
   int *tc_err = nullptr;
   MixedEigWork mew{};
-  double *c1_prev = nullptr;  // eigenvectors of the previous Fock diagonalisation
-  bool have_prev = false;
   double *scal = nullptr;  // device scalars
   double *hscal = nullptr; // pinned host mirror
   // last state
@@ -239,6 +239,9 @@ static void create(const hqcgb_params *in, hqcgb_plan *p) {
     p->phi32 = p->alloc<float>((size_t)nao * p->ld);
     if (p->gga) p->dphi32 = p->alloc<float>((size_t)3 * nao * p->ld);
     p->phiT32 = p->alloc<float>((size_t)N * tc_ldk(nao));
+    if (p->gga) p->dphiT32 = p->alloc<float>((size_t)3 * N * tc_ldk(nao));
+    p->Yhl = p->alloc<float>((size_t)2 * tc_psi_max(false) * tc_ldk(nao));
+    p->hocc.resize(nao);
     p->D32 = p->alloc<float>((size_t)nao * tc_ldk(nao));
     HQ_CUDA(cudaMemset(p->D32, 0, sizeof(float) * nao * tc_ldk(nao)));
     if (p->gga) p->z32 = p->alloc<float>((size_t)nao * p->ld);
@@ -258,8 +261,9 @@ static void create(const hqcgb_params *in, hqcgb_plan *p) {
     p->mew.G = p->alloc<double>(nn);
     p->mew.E = p->alloc<double>(nn);
     p->mew.status = p->alloc<int>(1);
-    p->mew.emax = p->alloc<double>(2);
-    p->c1_prev = p->alloc<double>(nn);
+    p->mew.emax = p->alloc<double>(4);
+    p->mew.wbuf = p->alloc<double>(2 * nn);
+    p->mew.iwork = p->alloc<int>(5 * (size_t)nao);
   }
   p->ph = p->alloc<double2>((size_t)n * 3 * p->ng);
   for (double **m : {&p->S, &p->T, &p->V, &p->H, &p->St, &p->vorth, &p->F, &p->F2e, &p->K, &p->Fp,
@@ -326,14 +330,11 @@ static void eigh(Ctx &c, const double *A, double *vecs, double *vals) {
   int n = p->nao;
   if (p->mixed) {
     // FP32 Householder + QL, then FP64 Ogita-Aishima refinement
-    eigh_mixed(n, A, vecs, vals, p->mew, c.st);
-    int ms = 0;
-    HQ_CUDA(cudaMemcpyAsync(&ms, p->mew.status, sizeof(int), cudaMemcpyDeviceToHost, c.st));
-    HQ_CUDA(cudaStreamSynchronize(c.st));
-    if (ms >= 0) {
+    if (eigh_mixed(n, A, vecs, vals, p->mew, c.st)) {
       HQ_CUDA(cudaMemsetAsync(p->jstat, 0, sizeof(int), c.st));
       return;
     }
+    if (trace_on()) fprintf(stderr, "eigh: mixed solve did not converge, FP64 solve\n");
   }
   HQ_CUDA(cudaMemcpyAsync(p->jA, A, sizeof(double) * n * n, cudaMemcpyDeviceToDevice, c.st));
   eigh_tql(n, 1, p->jA, vecs, vals, p->jtmp, p->jstat, c.st);
@@ -352,15 +353,11 @@ static void diagonalize(Ctx &c, const double *Fm) {
   int n = p->nao;
   gemm(false, false, n, n, n, 1.0, Fm, n, p->vorth, n, nullptr, 0.0, p->t1, n, c.st);
   gemm(true, false, n, n, n, 1.0, p->vorth, n, p->t1, n, nullptr, 0.0, p->Fp, n, c.st);
-  bool done = false;
-  if (p->mixed && p->have_prev)
-    done = eigh_mixed_warm(n, p->Fp, p->c1_prev, p->c1, p->w, p->mew, c.st);
-  if (!done) eigh(c, p->Fp, p->c1, p->w);
-  if (p->mixed) {
-    HQ_CUDA(cudaMemcpyAsync(p->c1_prev, p->c1, sizeof(double) * n * n, cudaMemcpyDeviceToDevice,
-                            c.st));
-    p->have_prev = true;
+  if (p->mixed) {  // exact symmetry for the refinement (rounding of the two GEMMs)
+    axpby(n, 0.5, p->Fp, 0.5, p->Fp, true, p->t1, c.st);
+    HQ_CUDA(cudaMemcpyAsync(p->Fp, p->t1, sizeof(double) * n * n, cudaMemcpyDeviceToDevice, c.st));
   }
+  eigh(c, p->Fp, p->c1, p->w);
   gemm(false, false, n, n, n, 1.0, p->vorth, n, p->c1, n, nullptr, 0.0, p->C, n, c.st);
 }
 
@@ -427,9 +424,22 @@ static double fock(Ctx &c) {
   if (p->mixed) {
     // tensor-core density (3xTF32, FP32 accumulation, FP64 sums), FP32
     // Poisson, FP64 xc, tensor-core quadrature
-    launch_to_f32(p->D, n, n, n, 1.0, p->D32, tc_ldk(n), c.st);
-    launch_tc_density(p->phi32, p->phiT32, p->dphi32, p->D32, n, N, p->ld, p->tcd_part, p->rho,
-                      p->gga ? p->grho : nullptr, p->tc_err, c.st);
+    // orbitals with a non-negligible occupation (sorted by energy, so first)
+    HQ_CUDA(cudaMemcpyAsync(p->hocc.data(), p->occ, sizeof(double) * n, cudaMemcpyDeviceToHost, c.st));
+    HQ_CUDA(cudaStreamSynchronize(c.st));
+    int nuse = 0;
+    for (int k = 0; k < n; ++k)
+      if (p->hocc[k] > 1e-14) nuse = k + 1;
+    if (nuse <= tc_psi_max(p->gga)) {
+      // rho = sum_k |psi_k|^2 from Y = C_occ sqrt(f) (n_use / n_ao of the work)
+      launch_psi_operand(p->C, p->occ, n, n, nuse, tc_ldk(n), p->Yhl, c.st);
+      launch_tc_psi_density(p->phiT32, p->dphiT32, p->Yhl, tc_psi_width(nuse), tc_ldk(n), N, p->rho,
+                            p->gga ? p->grho : nullptr, p->tc_err, c.st);
+    } else {
+      launch_to_f32(p->D, n, n, n, 1.0, p->D32, tc_ldk(n), c.st);
+      launch_tc_density(p->phi32, p->phiT32, p->dphi32, p->D32, n, N, p->ld, p->tcd_part, p->rho,
+                        p->gga ? p->grho : nullptr, p->tc_err, c.st);
+    }
     launch_poisson_f32(p->rho, p->vh, p->cbuf32, p->coul, p->ng, p->tw, c.st);
     launch_xc_pointwise(kind, p->rho, p->gga ? p->grho : nullptr, p->vh, N, p->dV, p->wq, p->vxc,
                         p->gga ? p->u : nullptr, p->xpart, c.st);
@@ -499,6 +509,10 @@ static void geometry(Ctx &c, const double *xp_dev) {
     launch_phi32(p->F1d, p->coef, p->ao_l, p->ao_cart, p->nb, p->nprim, n, p->ng, p->ld, p->phi32,
                  p->dphi32, c.st);
     launch_transpose_phi(p->phi32, n, N, p->ld, p->phiT32, c.st);
+    if (p->gga)
+      for (int d = 0; d < 3; ++d)
+        launch_transpose_phi(p->dphi32 + (size_t)d * n * p->ld, n, N, p->ld,
+                             p->dphiT32 + (size_t)d * N * tc_ldk(n), c.st);
   }
   launch_overlap_kinetic(p->xp, p->n, p->nb, p->nprim, p->alpha, p->coef, p->ao_l, p->ao_cart,
                          p->lattice, P.n_lattice, p->S, p->T, nullptr, nullptr, nullptr, nullptr,
@@ -532,7 +546,6 @@ static int scf_one(hqcgb_plan *p, const double *xp_dev, const hqcgb_scf_out *out
   int n = p->nao;
   size_t nn = (size_t)n * n;
   p->have_state = false;
-  p->have_prev = false;
   geometry(c, xp_dev);
   // Hcore guess (solver.py:739-745)
   diagonalize(c, p->H);
@@ -782,6 +795,8 @@ long long hqcgb_plan_query(hqcgb_plan *p, const char *name, void *dst, size_t by
     else if (k == "K") { src = p->K; sz = nn; }
     else if (k == "D") { src = p->D; sz = nn; }
     else if (k == "St") { src = p->St; sz = nn; }
+    else if (k == "Fp") { src = p->Fp; sz = nn; }
+    else if (k == "vorth") { src = p->vorth; sz = nn; }
     else if (k == "phi") { src = p->phi; sz = ng * p->nao; }
     else if (k == "rho") { src = p->rho; sz = ng; }
     else if (k == "vh") { src = p->vh; sz = ng; }

@@ -24,6 +24,8 @@
 // of 128 columns.  Every mbarrier wait has an iteration limit: on expiry the
 // kernel records an error code in *err, stops issuing work, waits (bounded)
 // for its MMAs, frees TMEM and returns.
+#include <algorithm>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -38,7 +40,7 @@ constexpr int kM = 128, kN = 128;
 constexpr size_t kTile = 16384;          // 128 rows x 128 bytes
 constexpr int kMaxSplit = 2;             // pieces per operand (hi, lo)
 constexpr size_t kStageBytes = 2 * kMaxSplit * kTile;  // A pieces, then B pieces
-constexpr unsigned kSpinLimit = 1u << 26;
+constexpr uint64_t kWaitNs = 4000000000ull;  // 4 s
 
 __device__ inline uint32_t smem_u32(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -56,7 +58,7 @@ __device__ inline bool mbar_try_wait(uint64_t *bar, unsigned parity) {
   uint32_t ok;
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, 100000;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, 20000;\n\t"
       "selp.u32 %0, 1, 0, p;\n\t}"
       : "=r"(ok)
       : "r"(smem_u32(bar)), "r"(parity)
@@ -64,10 +66,21 @@ __device__ inline bool mbar_try_wait(uint64_t *bar, unsigned parity) {
   return ok != 0;
 }
 
-// Bounded wait; returns false (and records `code`) when the limit is hit.
+__device__ inline uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Bounded wait: gives up after kWaitNs of wall time (no stage of these
+// kernels takes more than milliseconds), records `code` and returns false.
 __device__ inline bool mbar_wait(uint64_t *bar, unsigned parity, int *err, int code) {
-  for (unsigned it = 0; it < kSpinLimit; ++it)
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  for (;;) {
     if (mbar_try_wait(bar, parity)) return true;
+    if (global_ns() - t0 > kWaitNs) break;
+  }
   if (err) atomicCAS(err, 0, code);
   return false;
 }
@@ -509,7 +522,11 @@ __global__ void k_tc_quad_reduce(const double *__restrict__ P, int nchunk, int m
       s += P[((((long long)k * mtiles + tm) * ntiles + tn) * kM + r) * kN + cc];
     return s;
   };
-  double v = get(p, q);
+  // sym: the (p, q) and (q, p) elements of a diagonal tile round differently
+  // (the weight multiplies one operand before its TF32 split), so both are
+  // averaged -- the result is exactly symmetric, as every Fock piece must be
+  // before the orthogonalisation amplifies any asymmetry by 1/s_min(S).
+  double v = (sym && !add_transpose) ? 0.5 * (get(p, q) + get(q, p)) : get(p, q);
   if (add_transpose) v += get(q, p);
   M[idx] = scale * v;
 }
@@ -636,7 +653,333 @@ __global__ void k_transpose_phi(const float *__restrict__ phi, int nao, long lon
   }
 }
 
+// ---------------------------------------------------------------------------
+// Orbital density: psi_k(g) = sum_p phi_p(g) Y_pk with Y = C_occ sqrt(f)
+// (npsi <= kPsiMaxN columns, zero-padded), rho(g) = sum_k psi_k(g)^2 and,
+// for GGA, grad rho = 2 sum_k psi_k grad psi_k.  This is the density
+// sum_pq D_pq phi_p phi_q of D = C diag(f) C^T (hqc/pbc/solver.py:566-577,
+// 690) at npsi / n_ao of the GEMM work.
+//
+// Tiles: M = 128 grid points (A = rows of the grid-major phiT / dphiT,
+// K-major), N = npsi (B = the TF32 hi/lo pieces of Y^T, pre-split in global
+// memory), K = AO in stages of 32.  Persistent CTAs loop over grid tiles;
+// stage s of a CTA is (tile, component, K block).
+//
+// Accuracy.  The tensor core's FP32 accumulation truncates, so sums of many
+// MMAs drift low (about half an ulp per instruction).  Every stage therefore
+// accumulates in its own TMEM slot -- the large hi*hi products and the
+// 2^-11 smaller cross products in separate accumulators -- and the epilogue
+// warps drain each stage into compensated (TwoSum) FP32 sums S + C kept in
+// TMEM per component; psi = S + C is formed in FP64 at the end of a tile.
+// TMEM: a ring of RA stage slots of 2 npsi columns, then S and C
+// (ncomp npsi columns each).
+// ---------------------------------------------------------------------------
+constexpr int kPsiMaxN = 64;
+constexpr int kPsiRing = 4;
+constexpr size_t kPsiAPieces = 2 * kTile;                       // A hi, A lo
+constexpr size_t kPsiBPiece = (size_t)kPsiMaxN * 128;           // one B piece
+constexpr size_t kPsiStageBytes = kPsiAPieces + 2 * kPsiBPiece;  // 48 KB
+constexpr size_t kPsiSmem = kPsiRing * kPsiStageBytes + 1024;
+
+struct PsiArgs {
+  const float *phiT;   // [N][ldk]
+  const float *dphiT;  // [3][N][ldk] (GGA) or null
+  const float *Yhl;    // [2][npsi][ldk]: TF32 hi and lo pieces of Y^T
+  long long N;
+  int ldk, npsi, ncomp;
+  double *rho, *grho;  // [N], [3][N]
+  int *err;
+};
+
+// TMEM stage-slot ring depth for (npsi, ncomp); 0 when it does not fit.
+__host__ __device__ inline int psi_ring(int npsi, int ncomp) {
+  for (int ra = 4; ra >= 2; ra -= 2)
+    if (ra * 2 * npsi + 2 * ncomp * npsi <= 512) return ra;
+  return 0;
+}
+
+struct PsiPipe {
+  uint64_t full[kPsiRing], empty[kPsiRing], acc_full[4], acc_empty[4];
+  uint32_t tmem_base;
+};
+
+template <int NPSI>
+__global__ void __launch_bounds__(kThreads, 1) k_tc_psi_density(PsiArgs a) {
+  extern __shared__ __align__(1024) char smraw[];
+  char *sm = (char *)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
+  __shared__ PsiPipe P;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int nkb = a.ldk / kStageK;
+  const long long ntiles = (a.N + kM - 1) / kM;
+  const long long my_tiles = ntiles > blockIdx.x ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  const int per_tile = a.ncomp * nkb;
+  const long long S = my_tiles * per_tile;
+  const int RA = psi_ring(NPSI, a.ncomp);
+  const uint32_t colS = (uint32_t)(RA * 2 * NPSI), colC = colS + (uint32_t)(a.ncomp * NPSI);
+  const int ncols = (int)colC + a.ncomp * NPSI;
+  int tcols = 32;
+  while (tcols < ncols) tcols <<= 1;
+
+  if (tid == 0) {
+    for (int b = 0; b < kPsiRing; ++b) {
+      mbar_init(&P.full[b], kProducers);
+      mbar_init(&P.empty[b], 1);
+    }
+    for (int b = 0; b < 4; ++b) {
+      mbar_init(&P.acc_full[b], 1);
+      mbar_init(&P.acc_empty[b], kDrainers);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 8) tmem_alloc(&P.tmem_base, tcols);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+
+  bool ok = true;
+  if (warp < 4) {
+    // producer: A chunks (row (tid>>3) + 16 j, 16-byte chunk tid & 7), then
+    // this thread's share of the B piece chunks (rows of Y^T)
+    const int cch = tid & 7;
+    const int bchunks = NPSI * 8;  // per piece
+    const uint32_t sbase = smem_u32(sm);
+    auto issue = [&](long long st) {
+      const int slot = (int)(st % kPsiRing);
+      const uint32_t base = sbase + slot * (uint32_t)kPsiStageBytes;
+      const long long t = st / per_tile;
+      const int r = (int)(st % per_tile), comp = r / nkb, kb = r % nkb;
+      const long long g0 = (blockIdx.x + t * gridDim.x) * (long long)kM;
+      const float *src = comp == 0 ? a.phiT : a.dphiT + (long long)(comp - 1) * a.N * a.ldk;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        int row = (tid >> 3) + 16 * j;
+        long long g = g0 + row;
+        uint32_t off = swz(row, cch);
+        const float *gp = src + (g < a.N ? g : 0) * (long long)a.ldk + kb * kStageK + cch * 4;
+        if (g < a.N) cp_async16(base + off, gp);
+        else cp_async_zero16(base + off, src);
+      }
+      for (int c = tid; c < 2 * bchunks; c += kProducers) {
+        int piece = c / bchunks, cc = c % bchunks, row = cc >> 3, ch = cc & 7;
+        const float *gp = a.Yhl + ((long long)piece * NPSI + row) * a.ldk + kb * kStageK + ch * 4;
+        cp_async16(base + (uint32_t)(kPsiAPieces + piece * kPsiBPiece) + swz(row, ch), gp);
+      }
+    };
+    constexpr int L = kPsiRing - 1;  // copies in flight ahead of the split
+    for (int st = 0; st < L; ++st) {
+      if (st < S) issue(st);
+      cp_async_commit();
+    }
+    for (long long st = 0; st < S; ++st) {
+      cp_async_wait<L - 1>();
+      if (ok) {
+        char *base = sm + (st % kPsiRing) * kPsiStageBytes;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          int row = (tid >> 3) + 16 * j;
+          uint32_t off = swz(row, cch);
+          float4 v = *reinterpret_cast<float4 *>(base + off);
+          store_split4(base, row, cch, v);
+        }
+      }
+      fence_proxy_async();
+      mbar_arrive(&P.full[st % kPsiRing]);
+      long long nx = st + L;
+      if (nx < S) {
+        long long use = nx / kPsiRing;
+        if (ok && use > 0 && !mbar_wait(&P.empty[nx % kPsiRing], (unsigned)((use - 1) & 1), a.err, 21))
+          ok = false;
+        issue(nx);
+      }
+      cp_async_commit();
+    }
+    cp_async_wait<0>();
+  } else if (warp < 8) {
+    // drains and epilogue: thread = grid point (TMEM lane)
+    const int row = (warp & 3) * 32 + lane;
+    const uint32_t tbase = P.tmem_base + ((uint32_t)((warp & 3) * 32) << 16);
+    for (long long st = 0; st < S; ++st) {
+      const int b = (int)(st % RA);
+      const long long use = st / RA;
+      bool got = ok && mbar_wait(&P.acc_full[b], (unsigned)(use & 1), a.err, 23);
+      if (!got) ok = false;
+      tc_fence_after();
+      const int r = (int)(st % per_tile), comp = r / nkb, kb = r % nkb;
+      if (got) {
+        const uint32_t slot = tbase + (uint32_t)(b * 2 * NPSI);
+        const uint32_t sc = tbase + colS + (uint32_t)(comp * NPSI);
+        const uint32_t cc = tbase + colC + (uint32_t)(comp * NPSI);
+#pragma unroll
+        for (int c0 = 0; c0 < NPSI; c0 += 16) {
+          uint32_t vb[16], vs[16], ss[16], cs[16];
+          tmem_ld16_nowait(slot + c0, vb);
+          tmem_ld16_nowait(slot + NPSI + c0, vs);
+          if (kb > 0) {
+            tmem_ld16_nowait(sc + c0, ss);
+            tmem_ld16_nowait(cc + c0, cs);
+          }
+          tmem_wait_ld();
+          float so[16], co[16];
+#pragma unroll
+          for (int i = 0; i < 16; ++i) {
+            float big = __uint_as_float(vb[i]), small = __uint_as_float(vs[i]);
+            if (kb == 0) {
+              so[i] = big;
+              co[i] = small;
+            } else {
+              so[i] = __uint_as_float(ss[i]);
+              co[i] = __uint_as_float(cs[i]);
+              two_sum_add(so[i], co[i], big);
+              co[i] += small;
+            }
+          }
+          tmem_st16(sc + c0, so);
+          tmem_st16(cc + c0, co);
+        }
+        tmem_wait_st();
+      }
+      tc_fence_before();
+      mbar_arrive(&P.acc_empty[b]);
+      if (r == per_tile - 1) {  // tile complete: psi = S + C for every component
+        const long long t = st / per_tile;
+        const long long g = (blockIdx.x + t * gridDim.x) * (long long)kM + row;
+        if (ok) {
+          double psi[NPSI];
+          double rho = 0;
+#pragma unroll
+          for (int c0 = 0; c0 < NPSI; c0 += 16) {
+            double v[16];
+            uint32_t ss[16], cs[16];
+            tmem_ld16_nowait(tbase + colS + c0, ss);
+            tmem_ld16_nowait(tbase + colC + c0, cs);
+            tmem_wait_ld();
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+              v[i] = (double)__uint_as_float(ss[i]) + (double)__uint_as_float(cs[i]);
+              psi[c0 + i] = v[i];
+              rho += v[i] * v[i];
+            }
+          }
+          double gr[3] = {0, 0, 0};
+          for (int comp2 = 1; comp2 < a.ncomp; ++comp2) {
+#pragma unroll
+            for (int c0 = 0; c0 < NPSI; c0 += 16) {
+              uint32_t ss[16], cs[16];
+              tmem_ld16_nowait(tbase + colS + (uint32_t)(comp2 * NPSI + c0), ss);
+              tmem_ld16_nowait(tbase + colC + (uint32_t)(comp2 * NPSI + c0), cs);
+              tmem_wait_ld();
+#pragma unroll
+              for (int i = 0; i < 16; ++i)
+                gr[comp2 - 1] +=
+                    psi[c0 + i] * ((double)__uint_as_float(ss[i]) + (double)__uint_as_float(cs[i]));
+            }
+          }
+          if (g < a.N) {
+            a.rho[g] = rho;
+            if (a.ncomp > 1)
+              for (int c = 0; c < 3; ++c) a.grho[(long long)c * a.N + g] = 2.0 * gr[c];
+          }
+        }
+      }
+    }
+  } else if (lane == 0) {
+    const uint32_t idesc = idesc_tf32(kM, NPSI);
+    for (long long st = 0; st < S; ++st) {
+      const int slot = (int)(st % kPsiRing);
+      const int b = (int)(st % RA);
+      const long long ause = st / RA;
+      if (ok && ause > 0 && !mbar_wait(&P.acc_empty[b], (unsigned)((ause - 1) & 1), a.err, 24))
+        ok = false;
+      if (ok && !mbar_wait(&P.full[slot], (unsigned)((st / kPsiRing) & 1), a.err, 22)) ok = false;
+      tc_fence_after();
+      if (ok) {
+        const uint32_t dbig = P.tmem_base + (uint32_t)(b * 2 * NPSI), dsmall = dbig + NPSI;
+        const uint32_t base = smem_u32(sm + slot * kPsiStageBytes);
+        const uint32_t Ah = base, Al = base + kTile;
+        const uint32_t Bh = base + (uint32_t)kPsiAPieces, Bl = Bh + (uint32_t)kPsiBPiece;
+#pragma unroll
+        for (int ks = 0; ks < kStageK / 8; ++ks) {
+          uint32_t off = ks * 32;
+          mma_tf32(dsmall, sdesc(Al + off), sdesc(Bh + off), idesc, ks == 0 ? 0 : 1);
+          mma_tf32(dsmall, sdesc(Ah + off), sdesc(Bl + off), idesc, 1);
+          mma_tf32(dbig, sdesc(Ah + off), sdesc(Bh + off), idesc, ks == 0 ? 0 : 1);
+        }
+      }
+      mma_commit(&P.empty[slot]);
+      mma_commit(&P.acc_full[b]);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 8) {
+    tc_fence_after();
+    tmem_dealloc(P.tmem_base, tcols);
+  }
+}
+
+// Yhl[0][k][p], Yhl[1][k][p]: TF32 hi/lo pieces of C[p][k] sqrt(occ[k]) for
+// k < nuse, zero for k in [nuse, npsi) and p in [nao, ldk).
+__global__ void k_psi_operand(const double *__restrict__ C, const double *__restrict__ occ, int nao,
+                              int nmo, int nuse, int npsi, int ldk, float *__restrict__ Yhl) {
+  int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= npsi * ldk) return;
+  int k = idx / ldk, pp = idx % ldk;
+  float x = 0.f;
+  if (k < nuse && pp < nao) x = (float)(C[(long long)pp * nmo + k] * sqrt(fmax(occ[k], 0.0)));
+  float hi, lo;
+  split2(x, hi, lo);
+  Yhl[idx] = hi;
+  Yhl[(long long)npsi * ldk + idx] = lo;
+}
+
 }  // namespace tc
+
+// ---------------------------------------------------------------------------
+int tc_psi_max(bool gga) { return gga ? 32 : tc::kPsiMaxN; }
+int tc_psi_width(int nuse) { return ceil_div(nuse, 16) * 16; }
+
+void launch_psi_operand(const double *C, const double *occ, int nao, int nmo, int nuse, int ldk,
+                        float *Yhl, cudaStream_t st) {
+  int npsi = tc_psi_width(nuse);
+  tc::k_psi_operand<<<ceil_div(npsi * ldk, 256), 256, 0, st>>>(C, occ, nao, nmo, nuse, npsi, ldk, Yhl);
+  HQ_LAUNCH_CHECK();
+}
+
+// rho (and grad rho) from the grid-major AO values and the pre-split Y^T.
+void launch_tc_psi_density(const float *phiT, const float *dphiT, const float *Yhl, int npsi, int ldk,
+                           long long N, double *rho, double *grho, int *err, cudaStream_t st) {
+  HQ_STAGE(ST_DENSITY, st);
+  HQ_REQUIRE(npsi >= 16 && npsi <= tc::kPsiMaxN && npsi % 16 == 0, "orbital count out of range");
+  HQ_REQUIRE(tc::psi_ring(npsi, grho ? 4 : 1) > 0, "orbital count too large for the TMEM layout");
+  HQ_REQUIRE(ldk % tc::kStageK == 0, "AO stride must be a multiple of 32");
+  static int nsm = 0;
+  if (!nsm) {
+    HQ_CUDA(cudaFuncSetAttribute(tc::k_tc_psi_density<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)tc::kPsiSmem));
+    HQ_CUDA(cudaFuncSetAttribute(tc::k_tc_psi_density<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)tc::kPsiSmem));
+    HQ_CUDA(cudaFuncSetAttribute(tc::k_tc_psi_density<48>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)tc::kPsiSmem));
+    HQ_CUDA(cudaFuncSetAttribute(tc::k_tc_psi_density<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)tc::kPsiSmem));
+    int dev = 0;
+    HQ_CUDA(cudaGetDevice(&dev));
+    HQ_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  }
+  tc::PsiArgs a;
+  a.phiT = phiT; a.dphiT = grho ? dphiT : nullptr; a.Yhl = Yhl; a.N = N; a.ldk = ldk;
+  a.npsi = npsi; a.ncomp = grho ? 4 : 1; a.rho = rho; a.grho = grho; a.err = err;
+  HQ_REQUIRE(!grho || dphiT, "GGA density needs the gradient operand");
+  long long ntiles = ceil_div(N, tc::kM);
+  int grid = (int)std::min<long long>(ntiles, nsm);
+  switch (npsi) {
+    case 16: tc::k_tc_psi_density<16><<<grid, tc::kThreads, tc::kPsiSmem, st>>>(a); break;
+    case 32: tc::k_tc_psi_density<32><<<grid, tc::kThreads, tc::kPsiSmem, st>>>(a); break;
+    case 48: tc::k_tc_psi_density<48><<<grid, tc::kThreads, tc::kPsiSmem, st>>>(a); break;
+    default: tc::k_tc_psi_density<64><<<grid, tc::kThreads, tc::kPsiSmem, st>>>(a); break;
+  }
+  HQ_LAUNCH_CHECK();
+}
 
 // ---------------------------------------------------------------------------
 int tc_quad_chunk() { return 8192; }
@@ -805,6 +1148,49 @@ extern "C" int hqcgb_tc_density(int nao, long long N, long long ld, const float 
     HQ_CUDA(cudaFreeAsync(part, st));
     HQ_CUDA(cudaFreeAsync(phiT, st));
     HQ_CUDA(cudaFreeAsync(D32, st));
+    HQ_CUDA(cudaFreeAsync(err, st));
+    HQ_CUDA(cudaStreamSynchronize(st));
+    if (h) throw Error{HQCGB_CUDA_ERROR, "tensor-core pipeline wait limit hit"};
+    return HQCGB_OK;
+  } catch (const Error &e) {
+    set_error(e.msg);
+    return e.status;
+  }
+}
+
+// rho (and grad rho when dphi and grho are given) = sum_k occ_k |sum_p C_pk phi_p|^2
+// over the first nuse orbitals; C is [nao][nmo] row-major (FP64), phi and
+// dphi are AO-major fp32 with row stride ld.
+extern "C" int hqcgb_tc_orbital_density(int nao, long long N, long long ld, const float *phi,
+                                        const float *dphi, const double *C, const double *occ,
+                                        int nmo, int nuse, double *rho, double *grho, void *stream) {
+  using namespace hqcgb;
+  cudaStream_t st = (cudaStream_t)stream;
+  try {
+    HQ_REQUIRE(nao >= 1 && N >= 1 && ld >= N && ld % 4 == 0 && phi && C && occ && rho,
+               "bad argument");
+    HQ_REQUIRE(nuse >= 1 && nuse <= nmo && nuse <= tc_psi_max(dphi != nullptr), "orbital count out of range");
+    HQ_REQUIRE((dphi == nullptr) == (grho == nullptr), "dphi and grho go together");
+    int ldk = tc_ldk(nao);
+    int ncomp = dphi ? 4 : 1;
+    float *phiT = nullptr, *Yhl = nullptr;
+    int *err = nullptr;
+    HQ_CUDA(cudaMallocAsync(&phiT, (size_t)ncomp * N * ldk * sizeof(float), st));
+    HQ_CUDA(cudaMallocAsync(&Yhl, (size_t)2 * tc_psi_max(false) * ldk * sizeof(float), st));
+    HQ_CUDA(cudaMallocAsync(&err, sizeof(int), st));
+    HQ_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
+    launch_transpose_phi(phi, nao, N, ld, phiT, st);
+    if (dphi)
+      for (int d = 0; d < 3; ++d)
+        launch_transpose_phi(dphi + (size_t)d * nao * ld, nao, N, ld, phiT + (size_t)(d + 1) * N * ldk,
+                             st);
+    launch_psi_operand(C, occ, nao, nmo, nuse, ldk, Yhl, st);
+    launch_tc_psi_density(phiT, dphi ? phiT + (size_t)N * ldk : nullptr, Yhl, tc_psi_width(nuse), ldk,
+                          N, rho, grho, err, st);
+    int h = 0;
+    HQ_CUDA(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    HQ_CUDA(cudaFreeAsync(phiT, st));
+    HQ_CUDA(cudaFreeAsync(Yhl, st));
     HQ_CUDA(cudaFreeAsync(err, st));
     HQ_CUDA(cudaStreamSynchronize(st));
     if (h) throw Error{HQCGB_CUDA_ERROR, "tensor-core pipeline wait limit hit"};

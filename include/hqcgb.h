@@ -130,6 +130,12 @@ long long hqcgb_plan_query(hqcgb_plan *plan, const char *name, void *dst, size_t
  * at hqc/pbc/solver.py:729,741 and hqc/pbc/scf.py:69,138,198. */
 int hqcgb_eigh(int n, int batch, const double *A, double *w, double *V, void *stream);
 
+/* The mixed-precision eigensolver of the mixed SCF path on one matrix: an
+ * FP32 Householder + QL solve refined to FP64 accuracy by two Ogita-Aishima
+ * iterations (FP64 GEMMs).  Same arguments and outputs as hqcgb_eigh with
+ * batch = 1. */
+int hqcgb_eigh_mixed(int n, const double *A, double *w, double *V, void *stream);
+
 /* The tensor-core grid contractions of the mixed path as library calls
  * (device pointers; fp32 inputs with row stride ld >= N, ld % 4 == 0, zero
  * padding in [N, ld)).  nsplit = 2 (3xTF32; the only value accepted);
@@ -141,6 +147,15 @@ int hqcgb_tc_quadrature(int nao, long long N, long long ld, const float *phi, co
                         int nsplit, int drain, double *M, void *stream);
 int hqcgb_tc_density(int nao, long long N, long long ld, const float *phi, const float *D,
                      int nsplit, int drain, double *rho, void *stream);
+
+/* Orbital form of the density: rho(g) = sum_k occ_k |psi_k(g)|^2 with
+ * psi_k = sum_p C[p][k] phi_p over the first nuse (<= 64) orbitals, and
+ * with dphi (3 x [nao][ld]) also grad rho (3 x N) -- the density of
+ * D = C diag(occ) C^T (hqc/pbc/solver.py:566-577,690) at nuse/nao of the
+ * work.  C is [nao][nmo] row-major FP64; phi/dphi fp32 as above. */
+int hqcgb_tc_orbital_density(int nao, long long N, long long ld, const float *phi,
+                             const float *dphi, const double *C, const double *occ, int nmo,
+                             int nuse, double *rho, double *grho, void *stream);
 
 /* Largest n accepted by hqcgb_eigh_noalloc. */
 #define HQCGB_EIGH_NOALLOC_MAX_N 320
