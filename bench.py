@@ -132,7 +132,7 @@ def run_ours(args):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    precision = "fp64" if args.precision == "auto" else args.precision
+    precision = "mixed" if args.precision == "auto" else args.precision
     w0 = workload(7)
     n, L, rs = w0["n"], w0["L"], w0["rs"]
     kw = dict(dft=True, xc=w0["xc"], grid_length=w0["grid_length"], tol=1e-7, max_cycle=100,

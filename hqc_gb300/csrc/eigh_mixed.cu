@@ -15,6 +15,7 @@
 // squares the error, so FP32-accurate vectors become FP64-accurate after two
 // or three; all of it is FP64 GEMM work spread over many SMs.  The result
 // stands in for jnp.linalg.eigh (hqc/pbc/scf.py:69,138,198).
+#include <algorithm>
 #include <cstdlib>
 
 #include "common.cuh"
@@ -46,44 +47,78 @@ __global__ void k_f32_to_f64(long long n, const float *__restrict__ a, double *_
 // emax[0] = max |E|, emax[1] = ||S - diag(l)||_F / ||A||_F before the
 // update, emax[2] = 1 when a cluster was too large, emax[3] = cluster count.
 constexpr int kMaxCluster = 48;
+constexpr int kOaThreads = 256;
 
-__global__ void __launch_bounds__(1024) k_oa_correction(int n, const double *__restrict__ A,
-                                                        double *__restrict__ S,
-                                                        double *__restrict__ G,
-                                                        double *__restrict__ X,
-                                                        double *__restrict__ E,
-                                                        double *__restrict__ lam,
-                                                        double *__restrict__ emax,
-                                                        int *__restrict__ iwork,
-                                                        double *__restrict__ wbuf) {
-  __shared__ double red[32];
-  __shared__ int s_nclus, s_bad;
-  const int tid = threadIdx.x, nt = blockDim.x;
+// non-negative doubles compare like their bit patterns
+__device__ inline void atomic_max_nonneg(double *a, double v) {
+  atomicMax(reinterpret_cast<unsigned long long *>(a), (unsigned long long)__double_as_longlong(v));
+}
+
+// Pass 1 (grid): ||A||_F^2, ||S - diag(l)||_F^2, ||R||_F^2 and the largest
+// coupling max_{i != j} |s_ij - l_j g_ij| into red[0..3] (zeroed by the host).
+__global__ void __launch_bounds__(kOaThreads) k_oa_stats(int n, const double *__restrict__ A,
+                                                         const double *__restrict__ S,
+                                                         const double *__restrict__ G,
+                                                         double *__restrict__ red) {
+  __shared__ double sh[32];
   const long long nn = (long long)n * n;
-  int *order = iwork, *cid = iwork + n, *cstart = iwork + 2 * n, *csize = iwork + 3 * n,
-      *coff = iwork + 4 * n;
-  for (int i = tid; i < n; i += nt) lam[i] = S[(long long)i * n + i] / (G[(long long)i * n + i]);
-  __syncthreads();
-  double a2 = 0, s2 = 0, r2 = 0;
-  for (long long k = tid; k < nn; k += nt) {
+  double a2 = 0, s2 = 0, r2 = 0, cm = 0;
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < nn;
+       k += (long long)gridDim.x * blockDim.x) {
     int i = (int)(k / n), j = (int)(k % n);
     double a = A[k];
     a2 += a * a;
-    double r = (i == j ? 1.0 : 0.0) - G[k];
+    double g = G[k], r = (i == j ? 1.0 : 0.0) - g;
     r2 += r * r;
-    double sd = S[k] - (i == j ? lam[i] : 0.0);
-    s2 += sd * sd;
+    double lj = S[(long long)j * n + j] / G[(long long)j * n + j];
+    if (i == j) continue;
+    double sv = S[k];
+    s2 += sv * sv;
+    cm = fmax(cm, fabs(sv - lj * g));
   }
-  a2 = block_sum(a2, red);
-  s2 = block_sum(s2, red);
-  r2 = block_sum(r2, red);
-  // largest off-diagonal coupling |s_ij + l_j r_ij|
-  double cmax = 0;
-  for (long long k = tid; k < nn; k += nt) {
-    int i = (int)(k / n), j = (int)(k % n);
-    if (i != j) cmax = fmax(cmax, fabs(S[k] - lam[j] * G[k]));
+  a2 = block_sum(a2, sh);
+  s2 = block_sum(s2, sh);
+  r2 = block_sum(r2, sh);
+  cm = block_max(cm, sh);
+  if (threadIdx.x == 0) {
+    atomicAdd(&red[0], a2);
+    atomicAdd(&red[1], s2);
+    atomicAdd(&red[2], r2);
+    atomic_max_nonneg(&red[3], cm);
   }
-  cmax = block_max(cmax, red);
+}
+
+// Pass 2 (one block): estimates, separation, clusters and the Jacobi
+// rotations W_C of the cluster blocks.
+//
+// Clusters (Ogita, Aishima, "Iterative refinement for symmetric eigenvalue
+// decomposition II: clustered eigenvalues", Japan J. Indust. Appl. Math. 36
+// (2019) 435-459): estimates closer than delta form a cluster, within which
+// the basic update only re-orthogonalises.  Each cluster C is rotated first
+// by the eigenvectors W_C of its block S_CC (cyclic Jacobi, one thread per
+// cluster): X_C <- X_C W_C, S <- W^T S W and G <- W^T G W (passes 3 and 4),
+// after which the cluster's Ritz values are separated and the iteration
+// converges quadratically again.  Clusters larger than kMaxCluster are left
+// unrotated and flagged.
+// Outputs: emax[1] = ||S - diag(l)||_F / ||A||_F, emax[2] = 1 when a cluster
+// was too large, emax[3] = cluster count, emax[4] = delta; iwork = order,
+// cluster id, cluster start / size / wbuf offset, then the count at 5n.
+__global__ void __launch_bounds__(1024) k_oa_clusters(int n, const double *__restrict__ S,
+                                                      const double *__restrict__ G,
+                                                      const double *__restrict__ red,
+                                                      double *__restrict__ lam,
+                                                      double *__restrict__ emax,
+                                                      int *__restrict__ iwork,
+                                                      double *__restrict__ wbuf) {
+  __shared__ int s_nclus;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  int *order = iwork, *cid = iwork + n, *cstart = iwork + 2 * n, *csize = iwork + 3 * n,
+      *coff = iwork + 4 * n;
+  for (int i = tid; i < n; i += nt) lam[i] = S[(long long)i * n + i] / G[(long long)i * n + i];
+  __syncthreads();
+  // off-diagonal part of ||S - diag(l)||: the diagonal of S - diag(l) is
+  // s_ii (1 - 1/g_ii), negligible, and is left out
+  const double a2 = red[0], s2 = red[1], cmax = red[3];
   // Separation: pairs closer than 10x the largest coupling would get
   // corrections |E_ij| > 0.1, outside the quadratic regime, so they are
   // clustered instead; the floor (1e-6 of the mean eigenvalue scale) keeps
@@ -91,9 +126,6 @@ __global__ void __launch_bounds__(1024) k_oa_correction(int n, const double *__r
   // (The paper's bound 2(||S - diag(l)||_F + ||A||_F ||R||_F) is rigorous but
   // lumps whole bands of a 270-AO Fock matrix into one cluster.)
   const double delta = fmax(10.0 * cmax, 1e-6 * sqrt(a2 / n));
-  if (tid == 0 && emax) emax[1] = sqrt(s2) / fmax(sqrt(a2), 1e-300);
-
-  // ascending order of the estimates (ties by index)
   for (int i = tid; i < n; i += nt) {
     double li = lam[i];
     int r = 0;
@@ -104,7 +136,6 @@ __global__ void __launch_bounds__(1024) k_oa_correction(int n, const double *__r
     order[r] = i;
   }
   __syncthreads();
-  // clusters: maximal runs of the ordered estimates with gaps <= delta
   if (tid == 0) {
     int nclus = 0, bad = 0, off = 0;
     for (int i = 0; i < n;) {
@@ -125,118 +156,138 @@ __global__ void __launch_bounds__(1024) k_oa_correction(int n, const double *__r
       i = j + 1;
     }
     s_nclus = nclus;
-    s_bad = bad;
-    if (emax) {
-      emax[2] = bad;
-      emax[3] = nclus;
-    }
+    iwork[5 * n] = nclus;
+    emax[1] = sqrt(s2) / fmax(sqrt(a2), 1e-300);
+    emax[2] = bad;
+    emax[3] = nclus;
+    emax[4] = delta;
   }
   __syncthreads();
   const int nclus = s_nclus;
-
-  if (nclus > 0) {
-    // cyclic Jacobi on each cluster block B = S_CC; W accumulates the rotations
-    for (int c = tid; c < nclus; c += nt) {
-      const int k = csize[c], s0 = cstart[c];
-      double *B = wbuf + coff[c], *W = B + k * k;
-      for (int a = 0; a < k; ++a)
-        for (int b = 0; b < k; ++b) {
-          long long ia = order[s0 + a], ib = order[s0 + b];
-          B[a * k + b] = 0.5 * (S[ia * n + ib] + S[ib * n + ia]);
-          W[a * k + b] = (a == b) ? 1.0 : 0.0;
-        }
-      for (int sweep = 0; sweep < 40; ++sweep) {
-        double offd = 0, diag = 0;
-        for (int a = 0; a < k; ++a) {
-          diag += B[a * k + a] * B[a * k + a];
-          for (int b = a + 1; b < k; ++b) offd += B[a * k + b] * B[a * k + b];
-        }
-        if (offd <= 1e-34 * diag || offd == 0.0) break;
-        for (int a = 0; a < k - 1; ++a)
-          for (int b = a + 1; b < k; ++b) {
-            double bab = B[a * k + b];
-            if (bab == 0.0) continue;
-            double theta = (B[b * k + b] - B[a * k + a]) / (2.0 * bab);
-            double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-            double cs = 1.0 / sqrt(t * t + 1.0), sn = t * cs;
-            for (int m = 0; m < k; ++m) {  // B <- B J, W <- W J
-              double x = B[m * k + a], y = B[m * k + b];
-              B[m * k + a] = cs * x - sn * y;
-              B[m * k + b] = sn * x + cs * y;
-              x = W[m * k + a];
-              y = W[m * k + b];
-              W[m * k + a] = cs * x - sn * y;
-              W[m * k + b] = sn * x + cs * y;
-            }
-            for (int m = 0; m < k; ++m) {  // B <- J^T B
-              double x = B[a * k + m], y = B[b * k + m];
-              B[a * k + m] = cs * x - sn * y;
-              B[b * k + m] = sn * x + cs * y;
-            }
+  // cyclic Jacobi on each cluster block B = S_CC; W accumulates the rotations
+  for (int c = tid; c < nclus; c += nt) {
+    const int k = csize[c], s0 = cstart[c];
+    double *B = wbuf + coff[c], *W = B + k * k;
+    for (int a = 0; a < k; ++a)
+      for (int b = 0; b < k; ++b) {
+        long long ia = order[s0 + a], ib = order[s0 + b];
+        B[a * k + b] = 0.5 * (S[ia * n + ib] + S[ib * n + ia]);
+        W[a * k + b] = (a == b) ? 1.0 : 0.0;
+      }
+    for (int sweep = 0; sweep < 40; ++sweep) {
+      double offd = 0, diag = 0;
+      for (int a = 0; a < k; ++a) {
+        diag += B[a * k + a] * B[a * k + a];
+        for (int b = a + 1; b < k; ++b) offd += B[a * k + b] * B[a * k + b];
+      }
+      if (offd <= 1e-34 * diag || offd == 0.0) break;
+      for (int a = 0; a < k - 1; ++a)
+        for (int b = a + 1; b < k; ++b) {
+          double bab = B[a * k + b];
+          if (bab == 0.0) continue;
+          double theta = (B[b * k + b] - B[a * k + a]) / (2.0 * bab);
+          double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+          double cs = 1.0 / sqrt(t * t + 1.0), sn = t * cs;
+          for (int m = 0; m < k; ++m) {  // B <- B J, W <- W J
+            double x = B[m * k + a], y = B[m * k + b];
+            B[m * k + a] = cs * x - sn * y;
+            B[m * k + b] = sn * x + cs * y;
+            x = W[m * k + a];
+            y = W[m * k + b];
+            W[m * k + a] = cs * x - sn * y;
+            W[m * k + b] = sn * x + cs * y;
           }
-      }
-    }
-    __syncthreads();
-    // columns: X_C <- X_C W_C, S_:C <- S_:C W_C, G_:C <- G_:C W_C
-    for (long long idx = tid; idx < (long long)n * nclus; idx += nt) {
-      const int r = (int)(idx % n), c = (int)(idx / n);
-      const int k = csize[c], s0 = cstart[c];
-      const double *W = wbuf + coff[c] + k * k;
-      double *mats[3] = {X, S, G};
-      for (int q = 0; q < 3; ++q) {
-        double *row = mats[q] + (long long)r * n;
-        double tmp[kMaxCluster];
-        for (int j = 0; j < k; ++j) {
-          double acc = 0;
-          for (int i = 0; i < k; ++i) acc += row[order[s0 + i]] * W[i * k + j];
-          tmp[j] = acc;
+          for (int m = 0; m < k; ++m) {  // B <- J^T B
+            double x = B[a * k + m], y = B[b * k + m];
+            B[a * k + m] = cs * x - sn * y;
+            B[b * k + m] = sn * x + cs * y;
+          }
         }
-        for (int j = 0; j < k; ++j) row[order[s0 + j]] = tmp[j];
-      }
     }
-    __syncthreads();
-    // rows: S_C: <- W_C^T S_C:, G_C: <- W_C^T G_C:
-    for (long long idx = tid; idx < (long long)n * nclus; idx += nt) {
-      const int col = (int)(idx % n), c = (int)(idx / n);
-      const int k = csize[c], s0 = cstart[c];
-      const double *W = wbuf + coff[c] + k * k;
-      double *mats[2] = {S, G};
-      for (int q = 0; q < 2; ++q) {
-        double *m = mats[q];
-        double tmp[kMaxCluster];
-        for (int j = 0; j < k; ++j) {
-          double acc = 0;
-          for (int i = 0; i < k; ++i) acc += W[i * k + j] * m[(long long)order[s0 + i] * n + col];
-          tmp[j] = acc;
-        }
-        for (int j = 0; j < k; ++j) m[(long long)order[s0 + j] * n + col] = tmp[j];
-      }
-    }
-    __syncthreads();
-    for (int i = tid; i < n; i += nt) lam[i] = S[(long long)i * n + i] / (G[(long long)i * n + i]);
-    __syncthreads();
   }
+}
 
+// Pass 3 (grid): columns X_C <- X_C W_C, S_:C <- S_:C W_C, G_:C <- G_:C W_C.
+__global__ void __launch_bounds__(kOaThreads) k_oa_rotate_cols(int n, double *__restrict__ X,
+                                                               double *__restrict__ S,
+                                                               double *__restrict__ G,
+                                                               const int *__restrict__ iwork,
+                                                               const double *__restrict__ wbuf) {
+  const int nclus = iwork[5 * n];
+  const int *order = iwork, *cstart = iwork + 2 * n, *csize = iwork + 3 * n, *coff = iwork + 4 * n;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < 3LL * n * nclus;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(idx % n), q = (int)((idx / n) % 3), c = (int)(idx / (3LL * n));
+    const int k = csize[c], s0 = cstart[c];
+    const double *W = wbuf + coff[c] + k * k;
+    double *row = (q == 0 ? X : q == 1 ? S : G) + (long long)r * n;
+    double tmp[kMaxCluster];
+    for (int j = 0; j < k; ++j) {
+      double acc = 0;
+      for (int i = 0; i < k; ++i) acc += row[order[s0 + i]] * W[i * k + j];
+      tmp[j] = acc;
+    }
+    for (int j = 0; j < k; ++j) row[order[s0 + j]] = tmp[j];
+  }
+}
+
+// Pass 4 (grid): rows S_C: <- W_C^T S_C:, G_C: <- W_C^T G_C:.
+__global__ void __launch_bounds__(kOaThreads) k_oa_rotate_rows(int n, double *__restrict__ S,
+                                                               double *__restrict__ G,
+                                                               const int *__restrict__ iwork,
+                                                               const double *__restrict__ wbuf) {
+  const int nclus = iwork[5 * n];
+  const int *order = iwork, *cstart = iwork + 2 * n, *csize = iwork + 3 * n, *coff = iwork + 4 * n;
+  for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < 2LL * n * nclus;
+       idx += (long long)gridDim.x * blockDim.x) {
+    const int col = (int)(idx % n), q = (int)((idx / n) % 2), c = (int)(idx / (2LL * n));
+    const int k = csize[c], s0 = cstart[c];
+    const double *W = wbuf + coff[c] + k * k;
+    double *m = q == 0 ? S : G;
+    double tmp[kMaxCluster];
+    for (int j = 0; j < k; ++j) {
+      double acc = 0;
+      for (int i = 0; i < k; ++i) acc += W[i * k + j] * m[(long long)order[s0 + i] * n + col];
+      tmp[j] = acc;
+    }
+    for (int j = 0; j < k; ++j) m[(long long)order[s0 + j] * n + col] = tmp[j];
+  }
+}
+
+// Pass 5 (grid): l_i = s_ii / g_ii of the rotated S, G and the correction
+// E_ij = (s_ij + l_j r_ij) / (l_j - l_i) for separated pairs, r_ij / 2 within
+// a cluster or closer than delta; max |E| into red[4] (zeroed by the host).
+__global__ void __launch_bounds__(kOaThreads) k_oa_update(int n, const double *__restrict__ S,
+                                                          const double *__restrict__ G,
+                                                          const int *__restrict__ iwork,
+                                                          const double *__restrict__ emax,
+                                                          double *__restrict__ lam,
+                                                          double *__restrict__ E,
+                                                          double *__restrict__ red) {
+  extern __shared__ double sl[];  // [n]
+  __shared__ double sh[32];
+  const int *cid = iwork + n;
+  for (int i = threadIdx.x; i < n; i += blockDim.x)
+    sl[i] = S[(long long)i * n + i] / G[(long long)i * n + i];
+  __syncthreads();
+  if (blockIdx.x == 0)
+    for (int i = threadIdx.x; i < n; i += blockDim.x) lam[i] = sl[i];
+  const double delta = emax[4];
+  const long long nn = (long long)n * n;
   double em = 0;
-  for (long long k = tid; k < nn; k += nt) {
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < nn;
+       k += (long long)gridDim.x * blockDim.x) {
     int i = (int)(k / n), j = (int)(k % n);
     double r = (i == j ? 1.0 : 0.0) - G[k];
     bool same = cid[i] >= 0 && cid[i] == cid[j];
     double e;
-    if (i != j && !same && fabs(lam[i] - lam[j]) > delta) e = (S[k] + lam[j] * r) / (lam[j] - lam[i]);
+    if (i != j && !same && fabs(sl[i] - sl[j]) > delta) e = (S[k] + sl[j] * r) / (sl[j] - sl[i]);
     else e = 0.5 * r;
     E[k] = e;
     em = fmax(em, fabs(e));
   }
-  __shared__ double mx[32];
-  for (int o = 16; o > 0; o >>= 1) em = fmax(em, __shfl_xor_sync(0xffffffffu, em, o));
-  if ((tid & 31) == 0) mx[tid >> 5] = em;
-  __syncthreads();
-  if (tid < 32) {
-    em = (tid < (nt >> 5)) ? mx[tid] : 0.0;
-    for (int o = 16; o > 0; o >>= 1) em = fmax(em, __shfl_xor_sync(0xffffffffu, em, o));
-    if (tid == 0 && emax) emax[0] = em;
-  }
+  em = block_max(em, sh);
+  if (threadIdx.x == 0) atomic_max_nonneg(&red[4], em);
 }
 
 // Sort eigenpairs ascending (stable): w, and the columns of X via scratch T.
@@ -275,18 +326,31 @@ static void sort_eigpairs(int n, double *w, double *X, MixedEigWork &ws, cudaStr
 // One refinement step; returns ||X^T A X - diag|| / ||A|| before the update.
 static double oa_iteration(int n, const double *A, double *X, double *w, MixedEigWork &ws,
                            cudaStream_t st) {
+  const long long nn = (long long)n * n;
+  const int grid = (int)std::min<long long>(ceil_div(nn, kOaThreads), 148);
+  double *red = ws.emax + 8;  // [0..4] grid reductions
   gemm(false, false, n, n, n, 1.0, A, n, X, n, nullptr, 0.0, ws.T1, n, st);    // A X
   gemm(true, false, n, n, n, 1.0, X, n, ws.T1, n, nullptr, 0.0, ws.S, n, st);  // X^T A X
   gemm(true, false, n, n, n, 1.0, X, n, X, n, nullptr, 0.0, ws.G, n, st);      // X^T X
-  k_oa_correction<<<1, 1024, 0, st>>>(n, A, ws.S, ws.G, X, ws.E, w, ws.emax, ws.iwork, ws.wbuf);
+  HQ_CUDA(cudaMemsetAsync(red, 0, 5 * sizeof(double), st));
+  k_oa_stats<<<grid, kOaThreads, 0, st>>>(n, A, ws.S, ws.G, red);
+  HQ_LAUNCH_CHECK();
+  k_oa_clusters<<<1, 1024, 0, st>>>(n, ws.S, ws.G, red, w, ws.emax, ws.iwork, ws.wbuf);
+  HQ_LAUNCH_CHECK();
+  k_oa_rotate_cols<<<grid, kOaThreads, 0, st>>>(n, X, ws.S, ws.G, ws.iwork, ws.wbuf);
+  HQ_LAUNCH_CHECK();
+  k_oa_rotate_rows<<<grid, kOaThreads, 0, st>>>(n, ws.S, ws.G, ws.iwork, ws.wbuf);
+  HQ_LAUNCH_CHECK();
+  k_oa_update<<<grid, kOaThreads, n * sizeof(double), st>>>(n, ws.S, ws.G, ws.iwork, ws.emax, w, ws.E,
+                                                             red);
   HQ_LAUNCH_CHECK();
   gemm(false, false, n, n, n, 1.0, X, n, ws.E, n, nullptr, 0.0, ws.T1, n, st);  // X E
   axpby(n, 1.0, X, 1.0, ws.T1, false, X, st);                                  // X += X E
-  double em[4] = {0, 0, 0, 0};
-  HQ_CUDA(cudaMemcpyAsync(em, ws.emax, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  double em[13];
+  HQ_CUDA(cudaMemcpyAsync(em, ws.emax, 13 * sizeof(double), cudaMemcpyDeviceToHost, st));
   HQ_CUDA(cudaStreamSynchronize(st));
   if (std::getenv("HQCGB_TRACE"))
-    fprintf(stderr, "  oa off=%.3e max|E|=%.3e clusters=%g%s\n", em[1], em[0], em[3],
+    fprintf(stderr, "  oa off=%.3e max|E|=%.3e clusters=%g%s\n", em[1], em[8 + 4], em[3],
             em[2] != 0 ? " (cluster too large)" : "");
   return em[1];
 }
@@ -317,6 +381,29 @@ bool eigh_mixed(int n, const double *A, double *V, double *w, MixedEigWork &ws, 
   return false;
 }
 
+// Warm start from eigenvectors X0 of a nearby matrix (the previous SCF
+// iteration's orthogonalised Fock matrix): refinement only, accepted when it
+// reaches rounding level while contracting.  Returns false when the start is
+// too far (relative off-diagonal norm above 2e-3) or the iteration stalls; the
+// caller then runs the full solve.
+bool eigh_mixed_warm(int n, const double *A, const double *X0, double *V, double *w,
+                     MixedEigWork &ws, cudaStream_t st) {
+  HQ_STAGE(ST_JACOBI, st);
+  HQ_CUDA(cudaMemcpyAsync(V, X0, sizeof(double) * n * n, cudaMemcpyDeviceToDevice, st));
+  double prev = 1e300;
+  for (int it = 0; it < 8; ++it) {
+    double off = oa_iteration(n, A, V, w, ws, st);
+    if (!(off < 2e-3)) return false;
+    if (off < 1e-12) {
+      sort_eigpairs(n, w, V, ws, st);
+      return true;
+    }
+    if (it > 0 && off > 0.5 * prev) return false;
+    prev = off;
+  }
+  return false;
+}
+
 }  // namespace hqcgb
 
 // C ABI: the mixed-precision solver on one matrix (workspace allocated per call).
@@ -328,7 +415,7 @@ extern "C" int hqcgb_eigh_mixed(int n, const double *A, double *w, double *V, vo
     size_t nn = (size_t)n * n;
     MixedEigWork ws{};
     void *blk = nullptr;
-    size_t f32 = 3 * nn + 2 * (size_t)n + 64, f64 = 6 * nn + 64, i32 = 5 * (size_t)n + 64;
+    size_t f32 = 3 * nn + 2 * (size_t)n + 64, f64 = 6 * nn + 64, i32 = 5 * (size_t)n + 64;  // emax: 64
     HQ_CUDA(cudaMallocAsync(&blk, f64 * sizeof(double) + f32 * sizeof(float) + i32 * sizeof(int), st));
     double *d = reinterpret_cast<double *>(blk);
     ws.T1 = d; ws.S = d + nn; ws.G = d + 2 * nn; ws.E = d + 3 * nn; ws.wbuf = d + 4 * nn;

@@ -89,9 +89,11 @@ void eigh_tql_f32(int n, int batch, float *A, float *V, float *w, float *work, i
                   cudaStream_t st);
 struct MixedEigWork {
   float *A32, *V32, *w32, *work32;
-  double *T1, *S, *G, *E, *emax, *wbuf;  // wbuf: 2 n^2 (cluster blocks); emax: 4
-  int *status, *iwork;                    // iwork: 5 n
+  double *T1, *S, *G, *E, *emax, *wbuf;  // wbuf: 2 n^2 (cluster blocks); emax: 16
+  int *status, *iwork;                    // iwork: 5 n + 1
 };
+bool eigh_mixed_warm(int n, const double *A, const double *X0, double *V, double *w,
+                     MixedEigWork &ws, cudaStream_t st);
 bool eigh_mixed(int n, const double *A, double *V, double *w, MixedEigWork &ws, cudaStream_t st);
 
 // fft (FP32 transforms)

@@ -111,6 +111,8 @@ struct hqcgb_plan {
   bool mixed = false;
   long long ld = 0;
   float *dphiT32 = nullptr, *Yhl = nullptr;  // grid-major AO gradients; split Y^T
+  double *c1_prev = nullptr;                 // eigenvectors of the previous F'
+  bool have_prev = false;
   std::vector<double> hocc;                   // host copy of the occupations
   float *phi32 = nullptr, *dphi32 = nullptr, *phiT32 = nullptr, *D32 = nullptr, *w32 = nullptr,
         *u32 = nullptr, *z32 = nullptr;
@@ -261,9 +263,10 @@ static void create(const hqcgb_params *in, hqcgb_plan *p) {
     p->mew.G = p->alloc<double>(nn);
     p->mew.E = p->alloc<double>(nn);
     p->mew.status = p->alloc<int>(1);
-    p->mew.emax = p->alloc<double>(4);
+    p->mew.emax = p->alloc<double>(16);
     p->mew.wbuf = p->alloc<double>(2 * nn);
-    p->mew.iwork = p->alloc<int>(5 * (size_t)nao);
+    p->mew.iwork = p->alloc<int>(5 * (size_t)nao + 1);
+    p->c1_prev = p->alloc<double>(nn);
   }
   p->ph = p->alloc<double2>((size_t)n * 3 * p->ng);
   for (double **m : {&p->S, &p->T, &p->V, &p->H, &p->St, &p->vorth, &p->F, &p->F2e, &p->K, &p->Fp,
@@ -357,7 +360,15 @@ static void diagonalize(Ctx &c, const double *Fm) {
     axpby(n, 0.5, p->Fp, 0.5, p->Fp, true, p->t1, c.st);
     HQ_CUDA(cudaMemcpyAsync(p->Fp, p->t1, sizeof(double) * n * n, cudaMemcpyDeviceToDevice, c.st));
   }
-  eigh(c, p->Fp, p->c1, p->w);
+  // mixed: refine the previous iteration's eigenvectors when they are close
+  bool done = p->mixed && p->have_prev &&
+              eigh_mixed_warm(n, p->Fp, p->c1_prev, p->c1, p->w, p->mew, c.st);
+  if (!done) eigh(c, p->Fp, p->c1, p->w);
+  if (p->mixed) {
+    HQ_CUDA(cudaMemcpyAsync(p->c1_prev, p->c1, sizeof(double) * n * n, cudaMemcpyDeviceToDevice, c.st));
+    p->have_prev = true;
+  }
+  if (trace_on() && p->mixed) fprintf(stderr, "eigh: %s\n", done ? "warm start" : "full solve");
   gemm(false, false, n, n, n, 1.0, p->vorth, n, p->c1, n, nullptr, 0.0, p->C, n, c.st);
 }
 
@@ -546,6 +557,7 @@ static int scf_one(hqcgb_plan *p, const double *xp_dev, const hqcgb_scf_out *out
   int n = p->nao;
   size_t nn = (size_t)n * n;
   p->have_state = false;
+  p->have_prev = false;
   geometry(c, xp_dev);
   // Hcore guess (solver.py:739-745)
   diagonalize(c, p->H);
