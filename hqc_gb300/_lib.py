@@ -46,7 +46,7 @@ EXPORTS = ("hqcgb_plan_create", "hqcgb_plan_destroy", "hqcgb_scf", "hqcgb_scf_ba
            "hqcgb_forces", "hqcgb_ewald", "hqcgb_plan_query", "hqcgb_last_error",
            "hqcgb_launch_count", "hqcgb_profile", "hqcgb_stage_stats", "hqcgb_eigh",
            "hqcgb_eigh_noalloc", "hqcgb_eigh_mixed", "hqcgb_tc_quadrature", "hqcgb_tc_density",
-           "hqcgb_tc_orbital_density")
+           "hqcgb_tc_orbital_density", "hqcgb_plan_set_concurrency", "hqcgb_pes_batch")
 N_STAGES = 13
 
 _lib = None
@@ -74,6 +74,9 @@ def load():
     lib.hqcgb_scf_batch.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                     ctypes.POINTER(ScfOut), ctypes.c_void_p]
     lib.hqcgb_forces.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    lib.hqcgb_plan_set_concurrency.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.hqcgb_pes_batch.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+                                    ctypes.POINTER(ScfOut), ctypes.c_void_p, ctypes.c_void_p]
     lib.hqcgb_ewald.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                 ctypes.c_double, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                 ctypes.c_void_p]

@@ -6,6 +6,8 @@
 // DIIS / fixed-point loops of hqc/pbc/scf.py.  The loop control runs on the
 // host; every array operation is a kernel on the caller's stream.
 #include <atomic>
+#include <mutex>
+#include <thread>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -30,12 +32,14 @@ struct StageRec {
   cudaEvent_t a, b;
 };
 static bool g_profile = false;
+static std::mutex g_rec_mu;  // guards g_recs and g_event_pool (batch workers record too)
 static std::vector<StageRec> g_recs;
 static std::vector<cudaEvent_t> g_event_pool;
-static int g_open[ST_COUNT];
-static cudaEvent_t g_open_ev[ST_COUNT];
+static thread_local int g_open[ST_COUNT];
+static thread_local cudaEvent_t g_open_ev[ST_COUNT];
 
 static cudaEvent_t take_event() {
+  std::lock_guard<std::mutex> lock(g_rec_mu);
   if (!g_event_pool.empty()) {
     cudaEvent_t e = g_event_pool.back();
     g_event_pool.pop_back();
@@ -56,6 +60,7 @@ void stage_mark(int stage, cudaStream_t st, bool begin) {
     if (--g_open[stage] > 0) return;
     cudaEvent_t b = take_event();
     cudaEventRecord(b, st);
+    std::lock_guard<std::mutex> lock(g_rec_mu);
     g_recs.push_back({stage, g_open_ev[stage], b});
   }
 }
@@ -134,7 +139,14 @@ struct hqcgb_plan {
     allocs.push_back(p);
     return (T *)p;
   }
+  // concurrent batch workers: sub-plans with their own workspaces and streams
+  int concurrency = 1;
+  std::vector<hqcgb_plan *> workers;
+  std::vector<cudaStream_t> wstreams;
+
   ~hqcgb_plan() {
+    for (hqcgb_plan *w : workers) delete w;
+    for (cudaStream_t s : wstreams) cudaStreamDestroy(s);
     for (void *p : allocs) cudaFree(p);
     if (hscal) cudaFreeHost(hscal);
   }
@@ -701,6 +713,108 @@ static void forces(hqcgb_plan *p, double *grad, cudaStream_t st) {
 }
 
 // ---------------------------------------------------------------------------
+// Batches: configuration b runs SCF (+ forces) on one of `concurrency` plans
+// -- the plan itself on the caller's stream and clones with their own
+// workspaces and streams -- each driven by its own host thread, so that the
+// single-SM stages of one configuration (eigensolver, small FP64 linear
+// algebra, host-side loop control) overlap the grid kernels of the others.
+// The reference batches with jax.vmap over the same jitted SCF
+// (test/test.py:157).
+// ---------------------------------------------------------------------------
+static hqcgb_params params_of(const hqcgb_plan *p) {
+  hqcgb_params q = p->P;
+  q.alpha = p->h_alpha.data();
+  q.coef = p->h_coef.data();
+  q.ao_l = p->h_l.data();
+  q.ao_cart = p->h_cart.data();
+  q.lat1d = p->h_lat1d.data();
+  q.lattice = p->h_lattice.data();
+  return q;
+}
+
+static void ensure_workers(hqcgb_plan *p, int k) {
+  while ((int)p->workers.size() < k) {
+    hqcgb_params q = params_of(p);
+    hqcgb_plan *w = new hqcgb_plan();
+    try {
+      create(&q, w);
+    } catch (...) {
+      delete w;
+      throw;
+    }
+    cudaStream_t s;
+    HQ_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    p->workers.push_back(w);
+    p->wstreams.push_back(s);
+  }
+}
+
+static hqcgb_scf_out slice(const hqcgb_scf_out &o, int b, int nao) {
+  size_t nn = (size_t)nao * nao;
+  hqcgb_scf_out r = o;
+  if (r.mo_coeff) r.mo_coeff += b * nn;
+  if (r.dm) r.dm += b * nn;
+  if (r.bands) r.bands += (size_t)b * nao;
+  if (r.energies) r.energies += 5 * b;
+  if (r.converged) r.converged += b;
+  if (r.iterations) r.iterations += b;
+  return r;
+}
+
+static int run_batch(hqcgb_plan *p, int n_cfg, const double *xp, const hqcgb_scf_out *out,
+                     double *grad, cudaStream_t st) {
+  const int nthreads = std::min(p->concurrency, n_cfg);
+  if (nthreads <= 1) {
+    int worst = HQCGB_OK;
+    for (int b = 0; b < n_cfg; ++b) {
+      hqcgb_scf_out o = slice(*out, b, p->nao);
+      int s = scf_one(p, xp + (size_t)b * 3 * p->n, &o, st);
+      if (grad) forces(p, grad + (size_t)b * 3 * p->n, st);
+      worst = std::max(worst, s);
+    }
+    return worst;
+  }
+  ensure_workers(p, nthreads - 1);
+  int dev = 0;
+  HQ_CUDA(cudaGetDevice(&dev));
+  HQ_CUDA(cudaStreamSynchronize(st));  // inputs may still be in flight on the caller's stream
+  std::atomic<int> next{0};
+  std::vector<int> status(n_cfg, HQCGB_OK);
+  std::vector<std::string> msg(n_cfg);
+  auto work = [&](int t) {
+    hqcgb_plan *q = t == 0 ? p : p->workers[t - 1];
+    cudaStream_t qs = t == 0 ? st : p->wstreams[t - 1];
+    cudaSetDevice(dev);
+    for (int b = next++; b < n_cfg; b = next++) {
+      try {
+        hqcgb_scf_out o = slice(*out, b, p->nao);
+        status[b] = scf_one(q, xp + (size_t)b * 3 * p->n, &o, qs);
+        if (grad) forces(q, grad + (size_t)b * 3 * p->n, qs);
+        HQ_CUDA(cudaStreamSynchronize(qs));
+      } catch (const Error &e) {
+        status[b] = e.status;
+        msg[b] = e.msg;
+      } catch (const std::exception &e) {
+        status[b] = HQCGB_CUDA_ERROR;
+        msg[b] = e.what();
+      }
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nthreads; ++t) pool.emplace_back(work, t);
+  work(0);
+  for (auto &th : pool) th.join();
+  int worst = HQCGB_OK;
+  for (int b = 0; b < n_cfg; ++b) {
+    if (status[b] > HQCGB_NOT_CONVERGED) {
+      throw Error{status[b], "configuration " + std::to_string(b) + ": " + msg[b]};
+    }
+    worst = std::max(worst, status[b]);
+  }
+  return worst;
+}
+
+// ---------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------
 #define HQ_GUARD(...)                                     \
@@ -747,22 +861,23 @@ int hqcgb_scf(hqcgb_plan *plan, const double *xp, const hqcgb_scf_out *out, void
 
 int hqcgb_scf_batch(hqcgb_plan *plan, int n_cfg, const double *xp, const hqcgb_scf_out *out,
                     void *stream) {
+  return hqcgb_pes_batch(plan, n_cfg, xp, out, nullptr, stream);
+}
+
+int hqcgb_plan_set_concurrency(hqcgb_plan *plan, int workers) {
+  HQ_GUARD({
+    HQ_REQUIRE(plan && workers >= 1 && workers <= 64, "workers must be in [1, 64]");
+    plan->concurrency = workers;
+    return HQCGB_OK;
+  });
+}
+
+int hqcgb_pes_batch(hqcgb_plan *plan, int n_cfg, const double *xp, const hqcgb_scf_out *out,
+                    double *grad, void *stream) {
   HQ_GUARD({
     HQ_REQUIRE(plan && xp && out && n_cfg >= 0, "null argument");
-    int worst = HQCGB_OK;
-    size_t nn = (size_t)plan->nao * plan->nao;
-    for (int b = 0; b < n_cfg; ++b) {
-      hqcgb_scf_out o = *out;
-      if (o.mo_coeff) o.mo_coeff += b * nn;
-      if (o.dm) o.dm += b * nn;
-      if (o.bands) o.bands += (size_t)b * plan->nao;
-      if (o.energies) o.energies += 5 * b;
-      if (o.converged) o.converged += b;
-      if (o.iterations) o.iterations += b;
-      int s = scf_one(plan, xp + (size_t)b * 3 * plan->n, &o, (cudaStream_t)stream);
-      if (s > worst) worst = s;
-    }
-    return worst;
+    HQ_REQUIRE(!grad || plan->P.want_forces, "plan was created without want_forces");
+    return run_batch(plan, n_cfg, xp, out, grad, (cudaStream_t)stream);
   });
 }
 

@@ -6,7 +6,9 @@
 Rydberg per rs unit from the engine's adjoint (absent from the reference;
 under Fermi smearing the electronic part is the gradient of E - sigma*Se).
 """
-from .solver import make_solver
+import torch
+
+from .solver import make_solver, RY
 from .potential import potential_energy_pp_and_grad
 
 
@@ -15,7 +17,7 @@ def make_pes(n, L, rs, basis, rcut=24, tol=1e-7, max_cycle=100, grid_length=0.12
              xc='lda,vwn', smearing=False, smearing_method='fermi', smearing_sigma=0.,
              search_method='bisect', search_cycle=100, search_tol=1e-7, gamma=True, Gmax=15,
              kappa=10, mode='default', precision='fp64', forces=False, n_grid=None,
-             exx_occ_threshold=0.0):
+             exx_occ_threshold=0.0, concurrency=1):
     if mode not in ("default", "dev"):
         raise ValueError(f"Invalid mode: {mode}.")
     solver = make_solver(n, L, rs, basis, rcut=rcut, tol=tol, max_cycle=max_cycle,
@@ -25,18 +27,30 @@ def make_pes(n, L, rs, basis, rcut=24, tol=1e-7, max_cycle=100, grid_length=0.12
                          smearing_sigma=smearing_sigma, search_method=search_method,
                          search_cycle=search_cycle, search_tol=search_tol, gamma=gamma,
                          precision=precision, forces=forces, n_grid=n_grid,
-                         exx_occ_threshold=exx_occ_threshold)
+                         exx_occ_threshold=exx_occ_threshold, concurrency=concurrency)
+
+    def _vpp(xp):
+        """Ewald energy and gradient of one configuration or a batch."""
+        if getattr(xp, "ndim", 2) == 3:
+            pairs = [potential_energy_pp_and_grad(x, L, rs, kappa=kappa, Gmax=Gmax) for x in xp]
+            return torch.stack([e for e, _ in pairs]), torch.stack([g for _, g in pairs])
+        return potential_energy_pp_and_grad(xp, L, rs, kappa=kappa, Gmax=Gmax)
 
     def pes(xp):
         _, _, _, E, Ki, Vep, Vee, Se, conv = solver(xp)
-        Vpp, _ = potential_energy_pp_and_grad(xp, L, rs, kappa=kappa, Gmax=Gmax)
+        Vpp, _ = _vpp(xp)
         if mode == "dev":
             return E + Vpp, Ki, Vep, Vee, Vpp, Se, conv
         return E + Vpp
 
     def value_and_grad(xp):
+        """(E + Vpp, d/dxp); a batch (B, n, 3) gives (B,) and (B, n, 3)."""
+        if getattr(xp, "ndim", 2) == 3:
+            out = solver.batch(xp, forces=True, full=False)
+            Vpp, gpp = _vpp(xp)
+            return out["energies"][:, 0] * RY + Vpp, out["grad"] * (RY * rs) + gpp
         out = solver(xp)
-        Vpp, gpp = potential_energy_pp_and_grad(xp, L, rs, kappa=kappa, Gmax=Gmax)
+        Vpp, gpp = _vpp(xp)
         return out[3] + Vpp, solver.grad() + gpp
 
     pes.solver = solver

@@ -140,6 +140,35 @@ class Plan:
         _lib.check(st, allow=(0, 1))
         return out
 
+    def set_concurrency(self, workers):
+        """Configurations a batch call runs at once (each extra one clones the
+        workspace; see hqcgb_plan_set_concurrency)."""
+        _lib.check(_lib.load().hqcgb_plan_set_concurrency(self.handle, int(workers)))
+
+    def scf_batch(self, xps_bohr, forces=False, full=True):
+        """SCF (and forces) of every configuration of xps_bohr (B, n, 3) on the
+        device; full=False skips the per-configuration matrices."""
+        lib = _lib.load()
+        nao, dev = self.nao, self.device
+        B = xps_bohr.shape[0]
+        out = dict(bands=torch.empty(B, nao, dtype=torch.float64, device=dev),
+                   energies=torch.empty(B, 5, dtype=torch.float64, device=dev),
+                   converged=torch.zeros(B, dtype=torch.int32, device=dev),
+                   iterations=torch.zeros(B, dtype=torch.int32, device=dev))
+        if full:
+            out["mo_coeff"] = torch.empty(B, nao, nao, dtype=torch.float64, device=dev)
+            out["dm"] = torch.empty(B, nao, nao, dtype=torch.float64, device=dev)
+        ptr = lambda k: ctypes.c_void_p(out[k].data_ptr()) if k in out else ctypes.c_void_p(0)
+        o = _lib.ScfOut(*[ptr(k) for k in ("mo_coeff", "dm", "bands", "energies", "converged",
+                                            "iterations")])
+        g = torch.empty(B, self.n, 3, dtype=torch.float64, device=dev) if forces else None
+        xps_bohr = xps_bohr.contiguous()
+        st = lib.hqcgb_pes_batch(self.handle, B, ctypes.c_void_p(xps_bohr.data_ptr()), ctypes.byref(o),
+                                 ctypes.c_void_p(g.data_ptr() if g is not None else 0), self.stream())
+        _lib.check(st, allow=(0, 1))
+        out["grad"] = g
+        return out
+
     def forces(self):
         """dE/dR (Hartree/Bohr) of the last SCF, (n, 3) on the device."""
         lib = _lib.load()
@@ -186,11 +215,15 @@ def make_solver(n: int, L: float, rs: float, basis: str,
                 precision: str = 'fp64',
                 forces: bool = False,
                 n_grid=None,
-                exx_occ_threshold: float = 0.0):
+                exx_occ_threshold: float = 0.0,
+                concurrency: int = 1):
     """PBC solver factory (hqc/pbc/solver.py:14-32).
 
     ``solver(xp)`` -> (mo_coeff, dm, bands, E, Ki, Vep, Vee, Se, converged):
     bands and energies in Rydberg, E excludes Vpp (solver.py:705-767).
+    A batch xp of shape (B, n, 3) returns the same tuple with a leading batch
+    axis -- what ``jax.vmap(solver)`` returns for the reference
+    (test/test.py:157); ``concurrency`` configurations of a batch run at once.
     ``use_jit`` is accepted for signature compatibility (the engine is always
     compiled).  Only the Gamma point is implemented (``gamma=True``).
     """
@@ -202,8 +235,23 @@ def make_solver(n: int, L: float, rs: float, basis: str,
                 search_method, search_cycle, search_tol, precision=precision, forces=forces,
                 n_grid=n_grid, exx_occ_threshold=exx_occ_threshold)
 
+    if concurrency > 1:
+        plan.set_concurrency(concurrency)
+
+    def batch(xps, forces=False, full=True):
+        xp_t = _as_device(xps, plan.device)
+        assert xp_t.dim() == 3 and xp_t.shape[1] == n
+        out = plan.scf_batch(xp_t * rs, forces=forces, full=full)
+        solver.iterations = out["iterations"].tolist()
+        return out
+
     def solver(xp):
         xp_t = _as_device(xp, plan.device)
+        if xp_t.dim() == 3:
+            out = batch(xp_t)
+            e = out["energies"]
+            return (out["mo_coeff"], out["dm"], out["bands"] * RY, e[:, 0] * RY, e[:, 1] * RY,
+                    e[:, 2] * RY, e[:, 3] * RY, e[:, 4], out["converged"] != 0)
         assert xp_t.shape[0] == n
         out = plan.scf(xp_t * rs)
         e = out["energies"]
@@ -217,5 +265,6 @@ def make_solver(n: int, L: float, rs: float, basis: str,
 
     solver.plan = plan
     solver.grad = grad
+    solver.batch = batch
     solver.n_grid = plan.ng
     return solver

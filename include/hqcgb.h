@@ -105,6 +105,22 @@ int hqcgb_scf(hqcgb_plan *plan, const double *xp, const hqcgb_scf_out *out, void
 int hqcgb_scf_batch(hqcgb_plan *plan, int n_cfg, const double *xp, const hqcgb_scf_out *out,
                     void *stream);
 
+/* Number of configurations a batch call runs concurrently (default 1:
+ * sequentially on this plan).  With k > 1 the plan creates k - 1 clones of
+ * its workspace (same parameters, own CUDA streams) on the first batch call;
+ * each configuration of a batch runs on one of them, driven by its own host
+ * thread.  Memory grows k-fold; results are identical to the sequential run. */
+int hqcgb_plan_set_concurrency(hqcgb_plan *plan, int workers);
+
+/* hqcgb_scf_batch plus, when grad is not NULL, the nuclear gradient of every
+ * configuration into grad [n_cfg][n_atoms][3] (Hartree/Bohr, device) -- the
+ * energy-and-force evaluation of a batch of configurations (the reference's
+ * jax.vmap of make_pes with jax.grad, test/test.py:157, pes.py:78-115).
+ * Returns the worst status over the batch; an error in any configuration is
+ * reported with its index. */
+int hqcgb_pes_batch(hqcgb_plan *plan, int n_cfg, const double *xp, const hqcgb_scf_out *out,
+                    double *grad, void *stream);
+
 /* Nuclear gradient dE/dR [n_atoms][3] (Hartree/Bohr, device) of the last SCF.
  * No counterpart in the reference (forces are absent there,
  * doc/solver_algorithm.md:1210); with Fermi smearing it is the gradient of
