@@ -3,12 +3,14 @@
 Workload (the metric's configuration): H54 as a bcc 3x3x3 lattice at rs 1.31
 with N(0, 0.1 Bohr) displacements (seed 7, a new seed per step), gth-dzvp,
 GGA-PBE, 81^3 grid (the reference's odd grid for the requested 80^3), Gamma
-point; one step = SCF + adjoint forces + Ewald of one configuration through
-the engine.  Inputs (positions) are resident in HBM before the timed region;
-every step touches > 1 GB of grid data (AO values), more than the 129 MB L2,
-so no flush is needed between steps.
+point; one step = SCF + adjoint forces + Ewald of one batch of B
+configurations (default 8, run concurrently by as many engine workers)
+through the public batched API.  Inputs (positions) are resident in HBM
+before the timed region; every configuration streams > 2 GB of grid data (AO
+values and gradients), far more than the 129 MB L2, so no flush is needed.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|mixed]
+                  [--batch B] [--concurrency C]
   python bench.py --impl reference ...   (the CPU oracle, all host threads)
 
 Prints one JSON line (rank 0).
@@ -37,6 +39,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"])
+    ap.add_argument("--batch", type=int, default=8, help="configurations per step")
+    ap.add_argument("--concurrency", type=int, default=0, help="configurations at once (0: batch)")
+    ap.add_argument("--no-fp64-plain", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     return ap.parse_args()
@@ -106,21 +111,47 @@ def peaks():
     return 6800.0, 1900.0, "fallback"
 
 
-# algorithmic work of the dominant stages, per launch, for the roofline
-def stage_work(stage, n, nao, N, precision):
-    """(bound, algorithmic bytes or flops per launch) of a stage."""
-    esize = 8 if precision == "fp64" else 4
-    if stage == "density":
-        # reads the AO grid once, writes rho (+ grad rho for GGA)
-        return "hbm", nao * N * esize + 4 * N * 8
-    if stage == "quadrature":
-        return "hbm", 2 * nao * N * esize
-    if stage == "fft":
-        # 3 axis passes, complex read + write per pass
-        return "hbm", 3 * 2 * 16 * N
-    if stage in ("tc_density", "tc_quadrature"):
-        return "tensor", 2.0 * N * nao * nao
-    return None, None
+CONFIG = {"workload": "H54 bcc rs=1.31 gth-dzvp PBE 81^3 Gamma, SCF tol 1e-7 Ry + forces",
+          "n_atoms": 54, "n_ao": 270, "grid": 531441}
+
+
+def psi_density_roofline(hbm_gbs, src, reps=5):
+    """The orbital-density kernel (the dominant grid kernel: tcgen05 3xTF32,
+    HBM-bound) timed alone with CUDA events on its own stream at the H54
+    shapes: algorithmic bytes = the grid-major AO values and gradients it
+    streams once (4 x N x 288 fp32) + Y^T + rho and grad rho (4 x N fp64)."""
+    import torch
+    from hqc_gb300 import _lib
+    nao, N, nocc, ldk = 270, 531441, 27, 288
+    ld = (N + 63) // 64 * 64
+    g = torch.Generator(device="cuda").manual_seed(1)
+    phi = torch.zeros(nao, ld, dtype=torch.float32, device="cuda")
+    phi[:, :N] = torch.randn(nao, N, generator=g, device="cuda")
+    dphi = torch.zeros(3 * nao, ld, dtype=torch.float32, device="cuda")
+    dphi[:, :N] = torch.randn(3 * nao, N, generator=g, device="cuda")
+    C = torch.randn(nao, nao, dtype=torch.float64, device="cuda") / nao ** 0.5
+    occ = torch.zeros(nao, dtype=torch.float64, device="cuda")
+    occ[:nocc] = 2.0
+    _lib.tc_orbital_density(phi, C, occ, N, nocc, dphi)  # warm
+    torch.cuda.synchronize()
+    _lib.profile(1)
+    for _ in range(reps):
+        _lib.tc_orbital_density(phi, C, occ, N, nocc, dphi)
+    torch.cuda.synchronize()
+    cnt, tot = _lib.stage_stats()["psi_density"]
+    _lib.profile(0)
+    avg_s = tot / cnt / 1000.0
+    algo = 4 * N * ldk * 4 + 2 * 32 * ldk * 4 + 4 * N * 8
+    achieved = algo / avg_s / 1e9
+    del phi, dphi
+    torch.cuda.empty_cache()
+    return {"bound": "hbm", "achieved": achieved, "peak": hbm_gbs, "unit": "GB/s",
+            "frac": achieved / hbm_gbs, "traffic": 2449194000 + 26072576,
+            "kernel": "k_tc_psi_density<32> (orbital-form density + gradient, H54 shapes)",
+            "algorithmic_bytes": algo, "avg_ms": avg_s * 1e3, "launches": cnt,
+            "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs, burst)" if src == "measured" else src,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch "
+                              "(profiles/psi_density_h54.md)"}
 
 
 def run_ours(args):
@@ -133,29 +164,32 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     precision = "mixed" if args.precision == "auto" else args.precision
+    B = args.batch
+    conc = args.concurrency or B
     w0 = workload(7)
     n, L, rs = w0["n"], w0["L"], w0["rs"]
     kw = dict(dft=True, xc=w0["xc"], grid_length=w0["grid_length"], tol=1e-7, max_cycle=100,
-              precision=precision, forces=True)
-    pes = make_pes(n, L, rs, w0["basis"], **kw)
+              forces=True)
+    pes = make_pes(n, L, rs, w0["basis"], precision=precision, concurrency=conc, **kw)
     nao = pes.solver.plan.nao
     N = pes.solver.plan.ng ** 3
-    # per-step configurations (different noise seeds), resident on the device
+    # per-step batches of B configurations (new noise seeds), resident on the device
     total = args.warmup + args.steps
-    xps = [torch.as_tensor(workload(1000 * rank + 7 + s)["xp"], device="cuda") for s in range(total)]
+    seeds = [[100000 * rank + 1000 * s + b for b in range(B)] for s in range(total)]
+    batches = [torch.as_tensor(np.stack([workload(x)["xp"] for x in ss]), device="cuda")
+               for ss in seeds]
     iters = []
 
-    def step(xp):
-        E, g = pes.value_and_grad(xp)
-        iters.append(pes.solver.iterations)
+    def step(xb):
+        E, g = pes.value_and_grad(xb)
+        iters.extend(pes.solver.iterations)
         return E, g
 
     for s in range(args.warmup):
-        step(xps[s])
+        step(batches[s])
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
-    _lib.profile(1)
     _lib.load().hqcgb_launch_count(1)
     start = torch.cuda.Event(enable_timing=True)
     stop = torch.cuda.Event(enable_timing=True)
@@ -163,63 +197,75 @@ def run_ours(args):
         torch.cuda.synchronize()
         start.record()
         for s in range(args.steps):
-            E, g = step(xps[args.warmup + s])
+            E, g = step(batches[args.warmup + s])
         stop.record()
         torch.cuda.synchronize()
     ms = start.elapsed_time(stop)
     launches = int(_lib.load().hqcgb_launch_count(0))
+    E_last, g_last = E.cpu().numpy(), g.cpu().numpy()
+    # stage timing (CUDA events around every stage) in one untimed batch run
+    # one configuration at a time, so that the per-stage device times add up
+    _lib.profile(1)
+    pes.solver.plan.set_concurrency(1)
+    step(batches[0])
+    torch.cuda.synchronize()
     stats = _lib.stage_stats()
     _lib.profile(0)
+    pes.solver.plan.set_concurrency(conc)
     if world > 1:
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
-    value = world * args.steps / (ms / 1000.0)
+    value = world * B * args.steps / (ms / 1000.0)
+    # device time per evaluation by stage, configurations run one at a time
+    stage_ms = {k: round(v[1] / B, 3) for k, v in stats.items() if v[0]}
 
-    # roofline of the dominant stage
     hbm, bf16, src = peaks()
-    dom = max((k for k in stats if stage_work(k, n, nao, N, precision)[0]), key=lambda k: stats[k][1])
-    bound, work = stage_work(dom, n, nao, N, precision)
-    cnt, tot_ms = stats[dom]
-    avg_s = tot_ms / max(cnt, 1) / 1000.0
-    if bound == "hbm":
-        achieved = work / avg_s / 1e9
-        roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": achieved / hbm, "traffic": None, "kernel": dom,
-                "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs)" if src == "measured" else src,
-                "launches": cnt, "avg_ms": tot_ms / max(cnt, 1)}
-    else:
-        achieved = work / avg_s / 1e12
-        roof = {"bound": "tensor", "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
-                "frac": achieved / bf16, "traffic": None, "kernel": dom, "launches": cnt,
-                "avg_ms": tot_ms / max(cnt, 1)}
-    stage_ms = {k: round(v[1] / args.steps, 3) for k, v in stats.items() if v[0]}
+    roof = psi_density_roofline(hbm, src)
+
+    # the plain FP64 single-configuration path on the last timed batch's first
+    # configuration: its speed, and the mixed path's error against it
+    fp64 = None
+    if not args.no_fp64_plain:
+        ref = make_pes(n, L, rs, w0["basis"], precision="fp64", **kw)
+        x0 = batches[-1][0]
+        ref.value_and_grad(batches[0][0])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        Er, gr = ref.value_and_grad(x0)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        dE = abs(float(E_last[0]) - float(Er)) / 2 / n               # Ry -> Ha, per atom
+        dF = float(np.abs(g_last[0] - gr.cpu().numpy()).max()) / 2 / rs  # Ry/rs -> Ha/Bohr
+        fp64 = {"value": 1.0 / dt, "unit": UNIT, "steps": 1, "batch": 1,
+                "mixed_dE_Ha_per_atom": dE, "mixed_max_force_err_Ha_per_Bohr": dF}
+        del ref
 
     # end to end through the public API: host positions in, host E and forces out
     e2e = None
     if not args.no_e2e:
-        xh = [np.ascontiguousarray(workload(1000 * rank + 500 + s)["xp"]) for s in range(args.steps)]
+        xh = [np.stack([workload(900000 + 1000 * s + b)["xp"] for b in range(B)])
+              for s in range(args.steps + 1)]
         pes.value_and_grad(xh[0])
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for s in range(args.steps):
-            E, g = pes.value_and_grad(xh[s])
-            _ = float(E), g.cpu().numpy()
+            E, g = pes.value_and_grad(xh[s + 1])
+            _ = E.cpu().numpy(), g.cpu().numpy()
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
-        e2e = {"value": args.steps / dt, "unit": UNIT, "h2d_bytes_per_step": n * 3 * 8,
-               "d2h_bytes_per_step": 8 + n * 3 * 8}
+        e2e = {"value": B * args.steps / dt, "unit": UNIT, "h2d_bytes_per_step": B * n * 3 * 8,
+               "d2h_bytes_per_step": B * (8 + n * 3 * 8)}
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if precision == "fp64" else "tf32x3+f64",
-            "data": "synthetic (bcc H54 + seeded N(0,0.1 Bohr) noise, new seed per step)",
-            "config": {"workload": "H54 bcc rs=1.31 gth-dzvp PBE 81^3 Gamma, SCF tol 1e-7 Ry + forces",
-                       "precision_path": precision, "batch": 1, "n_ao": nao, "grid": N,
-                       "scf_iterations_mean": float(np.mean(iters[args.warmup:])),
-                       "l2": "inputs > L2 (1.15 GB AO grid per step), no flush",
-                       "parallelism": f"replicas x{world}"},
-            "roofline": roof, "stage_ms_per_step": stage_ms, "e2e": e2e,
+            "data": "synthetic (bcc H54 + seeded N(0,0.1 Bohr) noise, a new seed per configuration)",
+            "config": dict(CONFIG, precision_path=precision, batch=B, concurrency=conc,
+                           scf_iterations_mean=float(np.mean(iters[B * args.warmup:])),
+                           l2="inputs > L2 (every configuration streams > 2 GB of AO grids), no flush",
+                           parallelism=f"replicas x{world}"),
+            "roofline": roof, "fp64_plain": fp64, "gpu_ms_per_eval_by_stage": stage_ms, "e2e": e2e,
             "gpu_launches": launches, "clocks": clk.summary()}
     if rank == 0 and not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(iters_per_eval=float(np.mean(iters)))
@@ -272,7 +318,7 @@ def run_reference(args):
     return {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
-            "data": "synthetic", "config": {"workload": "H54 bcc rs=1.31 gth-dzvp PBE 81^3 Gamma"},
+            "data": "synthetic", "config": dict(CONFIG, batch=1, concurrency=1),
             "cpu_baseline": cb,
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "reference is JAX (not installable here, no network); timed its NumPy FP64 "

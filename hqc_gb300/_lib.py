@@ -47,7 +47,7 @@ EXPORTS = ("hqcgb_plan_create", "hqcgb_plan_destroy", "hqcgb_scf", "hqcgb_scf_ba
            "hqcgb_launch_count", "hqcgb_profile", "hqcgb_stage_stats", "hqcgb_eigh",
            "hqcgb_eigh_noalloc", "hqcgb_eigh_mixed", "hqcgb_tc_quadrature", "hqcgb_tc_density",
            "hqcgb_tc_orbital_density", "hqcgb_plan_set_concurrency", "hqcgb_pes_batch")
-N_STAGES = 13
+N_STAGES = 14
 
 _lib = None
 

@@ -948,7 +948,7 @@ void launch_psi_operand(const double *C, const double *occ, int nao, int nmo, in
 // rho (and grad rho) from the grid-major AO values and the pre-split Y^T.
 void launch_tc_psi_density(const float *phiT, const float *dphiT, const float *Yhl, int npsi, int ldk,
                            long long N, double *rho, double *grho, int *err, cudaStream_t st) {
-  HQ_STAGE(ST_DENSITY, st);
+  HQ_STAGE(ST_PSI, st);
   HQ_REQUIRE(npsi >= 16 && npsi <= tc::kPsiMaxN && npsi % 16 == 0, "orbital count out of range");
   HQ_REQUIRE(tc::psi_ring(npsi, grho ? 4 : 1) > 0, "orbital count too large for the TMEM layout");
   HQ_REQUIRE(ldk % tc::kStageK == 0, "AO stride must be a multiple of 32");
