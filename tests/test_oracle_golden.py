@@ -91,3 +91,28 @@ def test_vpp_matches_reference_and_madelung():
     # known answers: simple-cubic and bcc Madelung energies
     assert abs(z["vpp_n1"] - (-2.8372974794806 / box(1))) < 1e-9
     assert abs(z["vpp_bcc16"] - (-16 * 1.791858520 / 1.31)) < 1e-6
+
+
+@pytest.mark.parametrize("kw", [dict(dft=False), dict(dft=True, xc="pbe")])
+def test_oracle_gradient_matches_finite_differences(kw):
+    """The oracle's analytic electronic gradient (the checker of the GPU
+    forces, which have no reference implementation) against central finite
+    differences of its own SCF energy, H2 szv on a 21^3 grid."""
+    from oracle.gpw import Solver
+    from oracle.forces import electronic_gradient
+    n, rs = 2, 1.5
+    L = (4 / 3 * np.pi * n) ** (1 / 3)
+    xp = np.array([[0.3, 0.5, 0.4], [1.1, 0.9, 1.3]])
+    common = dict(n_grid=21, tol=1e-12, max_cycle=200, **kw)
+    s = Solver(n, L, rs, "gth-szv", **common)
+    s.solve(xp)
+    g = electronic_gradient(s)  # Ha/Bohr
+    h = 1e-4  # rs units
+    for a, d in ((0, 0), (1, 2)):
+        e = []
+        for sgn in (1, -1):
+            x = xp.copy()
+            x[a, d] += sgn * h
+            e.append(Solver(n, L, rs, "gth-szv", **common).solve(x)[3])
+        fd = (e[0] - e[1]) / (2 * h * rs) / 2  # Ry per rs unit -> Ha/Bohr
+        assert abs(fd - g[a, d]) < 2e-6, (a, d, fd, g[a, d])
