@@ -128,7 +128,17 @@ int tc_psi_width(int nuse);
 void launch_psi_operand(const double *C, const double *occ, int nao, int nmo, int nuse, int ldk,
                         float *Yhl, cudaStream_t st);
 void launch_tc_psi_density(const float *phiT, const float *dphiT, const float *Yhl, int npsi, int ldk,
-                           long long N, double *rho, double *grho, int *err, cudaStream_t st);
+                           long long N, double *rho, double *grho, int *err, cudaStream_t st,
+                           float *psi_out = nullptr);
+// forces_mixed.cu
+int force_orb_blocks(long long N);
+void launch_force_operand(const double *C, const double *occ, int nao, int nuse, int npsi,
+                          float *Y32, cudaStream_t st);
+void launch_to_float(long long n, const double *a, float *b, cudaStream_t st);
+void launch_force_grid_orb(const float *F32, const double *coef, const int *ao_l, const int *ao_cart,
+                           int n_atoms, int nb, int nprim, int ng, const double *veff,
+                           const double *u, const float *psi, const float *Y32, int npsi, double dV,
+                           double *part, double *grad, cudaStream_t st);
 void launch_tc_density(const float *phi, const float *phiT, const float *dphi, const float *D32,
                        int nao, long long N, long long ld, double *part, double *rho, double *grho,
                        int *err, cudaStream_t st, int nsplit = 2, int drain = 3);

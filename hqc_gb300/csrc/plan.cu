@@ -118,6 +118,10 @@ struct hqcgb_plan {
   float *dphiT32 = nullptr, *Yhl = nullptr;  // grid-major AO gradients; split Y^T
   double *c1_prev = nullptr;                 // eigenvectors of the previous F'
   bool have_prev = false;
+  // mixed Kohn-Sham forces from the occupied orbitals on the grid
+  bool orb_forces = false, keep_psi = false;
+  float *psi32 = nullptr, *F1d32 = nullptr, *Y32 = nullptr;  // [4][64][N], F1d, [nao][64]
+  int npsi_kept = 0, nuse_kept = 0;
   std::vector<double> hocc;                   // host copy of the occupations
   float *phi32 = nullptr, *dphi32 = nullptr, *phiT32 = nullptr, *D32 = nullptr, *w32 = nullptr,
         *u32 = nullptr, *z32 = nullptr;
@@ -244,7 +248,9 @@ static void create(const hqcgb_params *in, hqcgb_plan *p) {
   p->F1d = p->alloc<double>((size_t)n * 3 * p->ng * P.n_prim * 6);
   // the FP64 AO grid is kept by the FP64 path, and by the mixed path for the
   // parts it runs in FP64 (exact exchange, forces)
-  bool fp64_grid = !p->mixed || p->hf || P.want_forces;
+  p->orb_forces = p->mixed && !p->hf && P.want_forces && !P.smearing;
+  const bool fp64_forces = P.want_forces && !p->orb_forces;
+  bool fp64_grid = !p->mixed || p->hf || fp64_forces;
   if (fp64_grid) {
     p->phi = p->alloc<double>((size_t)nao * N);
     if (p->need_dphi) p->dphi = p->alloc<double>((size_t)3 * nao * N);
@@ -279,6 +285,11 @@ static void create(const hqcgb_params *in, hqcgb_plan *p) {
     p->mew.wbuf = p->alloc<double>(2 * nn);
     p->mew.iwork = p->alloc<int>(5 * (size_t)nao + 1);
     p->c1_prev = p->alloc<double>(nn);
+    if (p->orb_forces) {
+      p->psi32 = p->alloc<float>((size_t)(p->gga ? 4 : 1) * tc_psi_max(false) * N);
+      p->F1d32 = p->alloc<float>((size_t)n * 3 * p->ng * P.n_prim * 6);
+      p->Y32 = p->alloc<float>((size_t)nao * tc_psi_max(false));
+    }
   }
   p->ph = p->alloc<double2>((size_t)n * 3 * p->ng);
   for (double **m : {&p->S, &p->T, &p->V, &p->H, &p->St, &p->vorth, &p->F, &p->F2e, &p->K, &p->Fp,
@@ -304,20 +315,21 @@ static void create(const hqcgb_params *in, hqcgb_plan *p) {
   if (p->gga) {
     p->grho = p->alloc<double>(3 * N);
     p->u = p->alloc<double>(3 * N);
-    p->Z = p->alloc<double>((size_t)nao * N);
+    if (!p->mixed || fp64_forces) p->Z = p->alloc<double>((size_t)nao * N);
   }
-  if (P.want_forces || p->hf) {
+  if (fp64_forces || p->hf) {
     p->X = p->alloc<double>((size_t)nao * N);
     if (!p->Z) p->Z = p->alloc<double>((size_t)nao * N);
   }
-  if (P.want_forces && p->gga) p->DPsi = p->alloc<double>((size_t)nao * N);
+  if (fp64_forces && p->gga) p->DPsi = p->alloc<double>((size_t)nao * N);
   p->cbuf_batch = p->hf ? nao : 1;
   if (p->hf) p->W = p->alloc<double>((size_t)nao * N);
   p->cbuf = p->alloc<double2>((size_t)p->cbuf_batch * N);
-  p->qpart = p->alloc<double>((size_t)quad_chunks(N) * nn);
+  if (!p->mixed || p->hf) p->qpart = p->alloc<double>((size_t)quad_chunks(N) * nn);
   p->xpart = p->alloc<double>((size_t)2 * xc_blocks(N));
   if (P.want_forces) {
-    p->fpart = p->alloc<double>((size_t)nao * force_grid_blocks(N) * 3);
+    p->fpart = p->alloc<double>(std::max((size_t)nao * force_grid_blocks(N) * 3,
+                                         (size_t)force_orb_blocks(N) * n * 3));
     p->gpart = p->alloc<double>((size_t)n * n * p->nb * p->nb * 3);
     p->vpart = p->alloc<double>((size_t)vloc_force_blocks(N) * n * 3);
   }
@@ -457,8 +469,14 @@ static double fock(Ctx &c) {
       // rho = sum_k |psi_k|^2 from Y = C_occ sqrt(f) (n_use / n_ao of the work)
       launch_psi_operand(p->C, p->occ, n, n, nuse, tc_ldk(n), p->Yhl, c.st);
       launch_tc_psi_density(p->phiT32, p->dphiT32, p->Yhl, tc_psi_width(nuse), tc_ldk(n), N, p->rho,
-                            p->gga ? p->grho : nullptr, p->tc_err, c.st);
+                            p->gga ? p->grho : nullptr, p->tc_err, c.st,
+                            p->keep_psi ? p->psi32 : nullptr);
+      if (p->keep_psi) {
+        p->npsi_kept = tc_psi_width(nuse);
+        p->nuse_kept = nuse;
+      }
     } else {
+      if (p->keep_psi) p->npsi_kept = 0;
       launch_to_f32(p->D, n, n, n, 1.0, p->D32, tc_ldk(n), c.st);
       launch_tc_density(p->phi32, p->phiT32, p->dphi32, p->D32, n, N, p->ld, p->tcd_part, p->rho,
                         p->gga ? p->grho : nullptr, p->tc_err, c.st);
@@ -545,8 +563,9 @@ static void geometry(Ctx &c, const double *xp_dev) {
   launch_complex_real(p->cbuf, N, 1.0, p->vloc, c.st);
   if (p->mixed) {
     launch_to_f32(p->vloc, N, N, 1, p->dV, p->w32, p->ld, c.st);
+    // one-off per geometry: drained every stage for the most accurate V
     launch_tc_quadrature(p->phi32, nullptr, p->w32, nullptr, (float)p->dV, n, N, p->ld, false, 1.0,
-                         p->tcq_part, p->V, p->tc_err, c.st);
+                         p->tcq_part, p->V, p->tc_err, c.st, 2, 1);
   } else {
     launch_quadrature(p->phi, p->phi, p->vloc, n, N, true, p->dV, false, p->qpart, p->V, c.st);
   }
@@ -634,9 +653,12 @@ static int scf_one(hqcgb_plan *p, const double *xp_dev, const hqcgb_scf_out *out
     }
   }
   int converged = (loop != P.max_cycle) ? 1 : 0;
-  // post-processing (solver.py:758-767 / 890-899)
+  // post-processing (solver.py:758-767 / 890-899); the mixed force path keeps
+  // the orbitals on the grid from this last density pass
   density_matrix(c);
+  p->keep_psi = p->orb_forces;
   fock(c);
+  p->keep_psi = false;
   dot((long long)nn, p->T, p->D, 1.0, p->scal + S_KI, false, st);
   dot((long long)nn, p->V, p->D, 1.0, p->scal + S_VEP, false, st);
   entropy(n, p->occ, p->scal + S_SE, st);
@@ -658,6 +680,35 @@ static int scf_one(hqcgb_plan *p, const double *xp_dev, const hqcgb_scf_out *out
   return converged ? HQCGB_OK : HQCGB_NOT_CONVERGED;
 }
 
+// Mixed Kohn-Sham forces: the S/T terms as in the FP64 path (done by the
+// caller), the structure-factor term and the effective potential from the
+// final SCF density, and the grid term from the orbitals kept by the last
+// density pass (forces_mixed.cu).
+static void orbital_forces(Ctx &c, double *grad) {
+  hqcgb_plan *p = c.p;
+  const hqcgb_params &P = p->P;
+  cudaStream_t st = c.st;
+  long long N = p->N;
+  if (p->npsi_kept == 0)
+    throw Error{HQCGB_BAD_ARG, "mixed forces need at most 32 (GGA) / 64 occupied orbitals"};
+  launch_real_to_complex(p->rho, nullptr, N, 1, p->cbuf, st);
+  launch_fft3d(p->cbuf, p->ng, 1, p->tw, false, st);
+  launch_vloc_force(p->ph, p->cbuf, p->n, p->ng, p->L, p->vpart, st);
+  launch_sum_partials(p->vpart, vloc_force_blocks(N), 3 * p->n, 3 * p->n, 1.0, grad, true, st);
+  launch_scale_complex(p->cbuf, p->coul, N, 1, st);
+  launch_fft3d(p->cbuf, p->ng, 1, p->tw, true, st);
+  launch_complex_real(p->cbuf, N, 1.0, p->vh, st);
+  launch_xc_pointwise(P.xc, p->rho, p->gga ? p->grho : nullptr, p->vh, N, p->dV, p->wq, p->vxc,
+                      p->gga ? p->u : nullptr, p->xpart, st);
+  launch_add3(N, p->vloc, p->vh, p->vxc, p->veff, st);
+  launch_to_float((long long)p->n * 3 * p->ng * P.n_prim * 6, p->F1d, p->F1d32, st);
+  launch_force_operand(p->C, p->occ, p->nao, p->nuse_kept, p->npsi_kept, p->Y32, st);
+  launch_force_grid_orb(p->F1d32, p->coef, p->ao_l, p->ao_cart, p->n, p->nb, p->nprim, p->ng,
+                        p->veff, p->gga ? p->u : nullptr, p->psi32, p->Y32, p->npsi_kept, p->dV,
+                        p->fpart, grad, st);
+  HQ_CUDA(cudaStreamSynchronize(st));
+}
+
 static void forces(hqcgb_plan *p, double *grad, cudaStream_t st) {
   Ctx c{p, st};
   const hqcgb_params &P = p->P;
@@ -672,6 +723,10 @@ static void forces(hqcgb_plan *p, double *grad, cudaStream_t st) {
   gemm(false, true, n, n, n, 1.0, p->C, n, p->C, n, p->psi, 0.0, p->t2, n, st);
   launch_overlap_kinetic(p->xp, p->n, p->nb, p->nprim, p->alpha, p->coef, p->ao_l, p->ao_cart,
                          p->lattice, P.n_lattice, nullptr, nullptr, p->D, p->t2, p->gpart, grad, st);
+  if (p->orb_forces) {
+    orbital_forces(c, grad);
+    return;
+  }
   // density, X = D phi, Hartree, structure-factor term
   launch_density(p->phi, p->gga ? p->dphi : nullptr, p->D, n, N, p->rho, p->gga ? p->grho : nullptr,
                  p->X, st);

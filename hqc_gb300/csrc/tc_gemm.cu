@@ -688,6 +688,7 @@ struct PsiArgs {
   long long N;
   int ldk, npsi, ncomp;
   double *rho, *grho;  // [N], [3][N]
+  float *psi_out;      // [ncomp][npsi][N] psi_k and grad psi_k (fp32), or null
   int *err;
 };
 
@@ -859,6 +860,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_psi_density(PsiArgs a) {
               psi[c0 + i] = v[i];
               rho += v[i] * v[i];
             }
+            if (a.psi_out && g < a.N)
+#pragma unroll
+              for (int i = 0; i < 16; ++i) a.psi_out[(long long)(c0 + i) * a.N + g] = (float)v[i];
           }
           double gr[3] = {0, 0, 0};
           for (int comp2 = 1; comp2 < a.ncomp; ++comp2) {
@@ -869,9 +873,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_psi_density(PsiArgs a) {
               tmem_ld16_nowait(tbase + colC + (uint32_t)(comp2 * NPSI + c0), cs);
               tmem_wait_ld();
 #pragma unroll
-              for (int i = 0; i < 16; ++i)
-                gr[comp2 - 1] +=
-                    psi[c0 + i] * ((double)__uint_as_float(ss[i]) + (double)__uint_as_float(cs[i]));
+              for (int i = 0; i < 16; ++i) {
+                const double dv = (double)__uint_as_float(ss[i]) + (double)__uint_as_float(cs[i]);
+                gr[comp2 - 1] += psi[c0 + i] * dv;
+                if (a.psi_out && g < a.N)
+                  a.psi_out[(long long)(comp2 * NPSI + c0 + i) * a.N + g] = (float)dv;
+              }
             }
           }
           if (g < a.N) {
@@ -947,7 +954,8 @@ void launch_psi_operand(const double *C, const double *occ, int nao, int nmo, in
 
 // rho (and grad rho) from the grid-major AO values and the pre-split Y^T.
 void launch_tc_psi_density(const float *phiT, const float *dphiT, const float *Yhl, int npsi, int ldk,
-                           long long N, double *rho, double *grho, int *err, cudaStream_t st) {
+                           long long N, double *rho, double *grho, int *err, cudaStream_t st,
+                           float *psi_out) {
   HQ_STAGE(ST_PSI, st);
   HQ_REQUIRE(npsi >= 16 && npsi <= tc::kPsiMaxN && npsi % 16 == 0, "orbital count out of range");
   HQ_REQUIRE(tc::psi_ring(npsi, grho ? 4 : 1) > 0, "orbital count too large for the TMEM layout");
@@ -969,6 +977,7 @@ void launch_tc_psi_density(const float *phiT, const float *dphiT, const float *Y
   tc::PsiArgs a;
   a.phiT = phiT; a.dphiT = grho ? dphiT : nullptr; a.Yhl = Yhl; a.N = N; a.ldk = ldk;
   a.npsi = npsi; a.ncomp = grho ? 4 : 1; a.rho = rho; a.grho = grho; a.err = err;
+  a.psi_out = psi_out;
   HQ_REQUIRE(!grho || dphiT, "GGA density needs the gradient operand");
   long long ntiles = ceil_div(N, tc::kM);
   int grid = (int)std::min<long long>(ntiles, nsm);
