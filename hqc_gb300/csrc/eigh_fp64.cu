@@ -12,18 +12,16 @@
 // GB300's FP64 rate makes every O(n^3) stage FP64-bound on one SM; a batch
 // of matrices runs one block per SM.
 #include "common.cuh"
+#include "eigh_tridiag.cuh"
 #include "kernels.h"
 
 namespace hqcgb {
 
 constexpr int kEigThreads = 1024;
 
-__device__ inline double e_sqrt(double x) { return sqrt(x); }
-__device__ inline float e_sqrt(float x) { return sqrtf(x); }
+
 __device__ inline double e_hypot(double a, double b) { return hypot(a, b); }
 __device__ inline float e_hypot(float a, float b) { return hypotf(a, b); }
-__device__ inline double e_copysign(double a, double b) { return copysign(a, b); }
-__device__ inline float e_copysign(float a, float b) { return copysignf(a, b); }
 template <typename T> struct EigEps;
 template <> struct EigEps<double> { static constexpr double v = 1e-16; };
 template <> struct EigEps<float> { static constexpr float v = 6e-8f; };
@@ -53,69 +51,7 @@ __global__ void __launch_bounds__(kEigThreads)
   int fail = 0;
 
   // ---------------- 1. tridiagonalisation ----------------
-  for (int k = 0; k < n - 2; ++k) {
-    int m = n - k - 1;
-    const T *col = A + (long long)(k + 1) * n + k;  // A[k+1+i][k] = col[i*n]
-    T s2 = 0;
-    for (int i = 1 + tid; i < m; i += nt) {
-      T x = col[(long long)i * n];
-      s2 += x * x;
-    }
-    s2 = block_sum(s2, red);
-    if (tid == 0) {
-      T x0 = col[0];
-      if (s2 == T(0)) {
-        tau[k] = T(0);
-        e[k] = x0;
-        s_dbl[0] = T(0);
-      } else {
-        T beta = -e_copysign(e_sqrt(x0 * x0 + s2), x0);
-        tau[k] = (beta - x0) / beta;
-        e[k] = beta;
-        s_dbl[0] = T(1) / (x0 - beta);
-      }
-    }
-    __syncthreads();
-    T tk = tau[k];
-    if (tk == T(0)) {
-      for (int i = tid; i < m; i += nt) v[i] = (i == 0) ? T(1) : T(0);
-      __syncthreads();
-      continue;
-    }
-    T sc = s_dbl[0];
-    for (int i = tid; i < m; i += nt) v[i] = (i == 0) ? T(1) : col[(long long)i * n] * sc;
-    __syncthreads();
-    // p = tau * A22 v  (one warp per row, coalesced over columns)
-    T *A22 = A + (long long)(k + 1) * n + (k + 1);
-    for (int i = warp; i < m; i += nw) {
-      const T *row = A22 + (long long)i * n;
-      T s = 0;
-      for (int j = lane; j < m; j += 32) s += row[j] * v[j];
-      s = warp_sum(s);
-      if (lane == 0) p[i] = tk * s;
-    }
-    __syncthreads();
-    T pv = 0;
-    for (int i = tid; i < m; i += nt) pv += p[i] * v[i];
-    pv = block_sum(pv, red);
-    T alpha = T(-0.5) * tk * pv;
-    for (int i = tid; i < m; i += nt) p[i] += alpha * v[i];  // p becomes w
-    __syncthreads();
-    for (long long idx = tid; idx < (long long)m * m; idx += nt) {
-      int i = (int)(idx / m), j = (int)(idx % m);
-      A22[(long long)i * n + j] -= v[i] * p[j] + p[i] * v[j];
-    }
-    // keep v below the subdiagonal of column k
-    for (int i = 1 + tid; i < m; i += nt) A[(long long)(k + 1 + i) * n + k] = v[i];
-    __syncthreads();
-  }
-  for (int i = tid; i < n; i += nt) d[i] = A[(long long)i * n + i];
-  if (tid == 0) {
-    if (n >= 2) e[n - 2] = A[(long long)(n - 1) * n + (n - 2)];
-    e[n - 1] = T(0);
-    if (n >= 2) tau[n - 2] = T(0);
-    tau[n - 1] = T(0);
-  }
+  householder_tridiag<T>(n, A, d, e, tau, v, p, red, s_dbl, nullptr);
   // Zt = I
   for (long long idx = tid; idx < (long long)n * n; idx += nt)
     Zt[idx] = ((int)(idx / n) == (int)(idx % n)) ? T(1) : T(0);

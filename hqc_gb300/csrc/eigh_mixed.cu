@@ -1,8 +1,8 @@
 // Mixed-precision symmetric eigensolver of the mixed SCF path.
 //
-// Stage 1 (FP32, one thread block): Householder tridiagonalisation, implicit
-// QL and back-transformation -- the FP64 algorithm of eigh_fp64.cu run in
-// FP32, 30-60x cheaper per operation on GB300.
+// Stage 1 (FP32, eigh_f32.cu): Householder tridiagonalisation, bisection and
+// inverse iteration on the tridiagonal, back-transformation -- single
+// precision is 30-60x cheaper per operation than FP64 on GB300.
 // Stage 2 (FP64): Ogita-Aishima refinement
 // (T. Ogita, K. Aishima, "Iterative refinement for symmetric eigenvalue
 // decomposition", Japan J. Indust. Appl. Math. 35 (2018) 1007-1035):
@@ -355,22 +355,30 @@ static double oa_iteration(int n, const double *A, double *X, double *w, MixedEi
   return em[1];
 }
 
-// Full solve: FP32 stage, then refinement until the relative off-diagonal
-// norm measured before a step is at rounding level (1e-12).  Returns false
-// when the refinement does not get there within 8 steps (the caller then
-// uses the FP64 solver) or the FP32 stage failed.
-bool eigh_mixed(int n, const double *A, double *V, double *w, MixedEigWork &ws, cudaStream_t st) {
+// Full solve: FP32 stage (eigh_f32.cu; the QL solver of eigh_fp64.cu when
+// `wide`), then refinement until the relative
+// off-diagonal norm measured before a step is at rounding level (1e-12).
+// Returns false when the refinement does not get there within 8 steps (the
+// caller then uses the FP64 solver).
+bool eigh_mixed(int n, const double *A, double *V, double *w, MixedEigWork &ws, cudaStream_t st,
+                bool wide) {
   HQ_STAGE(ST_JACOBI, st);
   long long nn = (long long)n * n;
   k_f64_to_f32<<<ceil_div(nn, 256), 256, 0, st>>>(nn, A, ws.A32);
   HQ_LAUNCH_CHECK();
-  eigh_tql_f32(n, 1, ws.A32, ws.V32, ws.w32, ws.work32, ws.status, st);
+  if (wide) {
+    // spectra spanning many orders of magnitude with dense near-degenerate
+    // groups (the overlap matrix): the QL sweep's vectors refine reliably
+    eigh_tql_f32(n, 1, ws.A32, ws.V32, ws.w32, ws.work32, ws.status, st);
+    int hs = 0;
+    HQ_CUDA(cudaMemcpyAsync(&hs, ws.status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    HQ_CUDA(cudaStreamSynchronize(st));
+    if (hs < 0) return false;
+  } else {
+    eigh_f32(n, ws.A32, ws.V32, ws.w32, ws.f32scr, st);
+  }
   k_f32_to_f64<<<ceil_div(nn, 256), 256, 0, st>>>(nn, ws.V32, V);
   HQ_LAUNCH_CHECK();
-  int hs = 0;
-  HQ_CUDA(cudaMemcpyAsync(&hs, ws.status, sizeof(int), cudaMemcpyDeviceToHost, st));
-  HQ_CUDA(cudaStreamSynchronize(st));
-  if (hs < 0) return false;
   for (int it = 0; it < 8; ++it) {
     double off = oa_iteration(n, A, V, w, ws, st);
     if (off < 1e-12) {
@@ -415,13 +423,15 @@ extern "C" int hqcgb_eigh_mixed(int n, const double *A, double *w, double *V, vo
     size_t nn = (size_t)n * n;
     MixedEigWork ws{};
     void *blk = nullptr;
-    size_t f32 = 3 * nn + 2 * (size_t)n + 64, f64 = 6 * nn + 64, i32 = 5 * (size_t)n + 64;  // emax: 64
+    size_t f32 = 3 * nn + 2 * (size_t)n + 64 + eigh_f32_scratch_floats(n), f64 = 6 * nn + 64,
+           i32 = 5 * (size_t)n + 64;  // emax: 64
     HQ_CUDA(cudaMallocAsync(&blk, f64 * sizeof(double) + f32 * sizeof(float) + i32 * sizeof(int), st));
     double *d = reinterpret_cast<double *>(blk);
     ws.T1 = d; ws.S = d + nn; ws.G = d + 2 * nn; ws.E = d + 3 * nn; ws.wbuf = d + 4 * nn;
     ws.emax = d + 6 * nn;
     float *f = reinterpret_cast<float *>(d + f64);
     ws.A32 = f; ws.V32 = f + nn; ws.work32 = f + 2 * nn; ws.w32 = f + 3 * nn;
+    ws.f32scr = f + 3 * nn + 2 * n + 64;
     ws.status = reinterpret_cast<int *>(f + f32);
     ws.iwork = ws.status + 64;
     HQ_CUDA(cudaMemsetAsync(ws.status, 0, sizeof(int), st));

@@ -87,14 +87,17 @@ void launch_add3(long long N, const double *a, const double *b, const double *c,
 // eigh_fp64.cu / eigh_mixed.cu
 void eigh_tql_f32(int n, int batch, float *A, float *V, float *w, float *work, int *status,
                   cudaStream_t st);
+size_t eigh_f32_scratch_floats(int n);
+void eigh_f32(int n, float *A, float *V, float *w, float *scr, cudaStream_t st);
 struct MixedEigWork {
-  float *A32, *V32, *w32, *work32;
+  float *A32, *V32, *w32, *work32, *f32scr;
   double *T1, *S, *G, *E, *emax, *wbuf;  // wbuf: 2 n^2 (cluster blocks); emax: 16
   int *status, *iwork;                    // iwork: 5 n + 1
 };
 bool eigh_mixed_warm(int n, const double *A, const double *X0, double *V, double *w,
                      MixedEigWork &ws, cudaStream_t st);
-bool eigh_mixed(int n, const double *A, double *V, double *w, MixedEigWork &ws, cudaStream_t st);
+bool eigh_mixed(int n, const double *A, double *V, double *w, MixedEigWork &ws, cudaStream_t st,
+                bool wide = false);
 
 // fft (FP32 transforms)
 void launch_fft3d_f32(float2 *c, int ng, int batch, const double2 *tw, bool inverse,

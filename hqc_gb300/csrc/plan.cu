@@ -276,6 +276,7 @@ static void create(const hqcgb_params *in, hqcgb_plan *p) {
     p->mew.V32 = p->alloc<float>(nn);
     p->mew.w32 = p->alloc<float>(nao);
     p->mew.work32 = p->alloc<float>(nn);
+    p->mew.f32scr = p->alloc<float>(eigh_f32_scratch_floats(nao));
     p->mew.T1 = p->alloc<double>(nn);
     p->mew.S = p->alloc<double>(nn);
     p->mew.G = p->alloc<double>(nn);
@@ -352,12 +353,12 @@ static void sync_scalars(Ctx &c) {
 
 // Symmetric eigensolver: Householder + QL (eigh_fp64.cu); the Jacobi solver
 // is kept as the fallback when a QL sweep limit is hit.
-static void eigh(Ctx &c, const double *A, double *vecs, double *vals) {
+static void eigh(Ctx &c, const double *A, double *vecs, double *vals, bool wide = false) {
   hqcgb_plan *p = c.p;
   int n = p->nao;
   if (p->mixed) {
-    // FP32 Householder + QL, then FP64 Ogita-Aishima refinement
-    if (eigh_mixed(n, A, vecs, vals, p->mew, c.st)) {
+    // FP32 solve, then FP64 Ogita-Aishima refinement
+    if (eigh_mixed(n, A, vecs, vals, p->mew, c.st, wide)) {
       HQ_CUDA(cudaMemsetAsync(p->jstat, 0, sizeof(int), c.st));
       return;
     }
@@ -573,7 +574,7 @@ static void geometry(Ctx &c, const double *xp_dev) {
   if (p->hf) launch_quadrature(p->phi, p->phi, nullptr, n, N, true, p->dV, false, p->qpart, p->St, c.st);
   // S^{-1/2} as U w^{-1/2} (solver.py:729-730)
   HQ_CUDA(cudaMemsetAsync(p->ibad, 0, sizeof(int), c.st));
-  eigh(c, p->S, p->c1, p->ws);
+  eigh(c, p->S, p->c1, p->ws, true);
   inv_sqrt_cols(n, p->c1, p->ws, p->vorth, p->ibad, c.st);
   int bad = 0;
   HQ_CUDA(cudaMemcpyAsync(&bad, p->ibad, sizeof(int), cudaMemcpyDeviceToHost, c.st));
