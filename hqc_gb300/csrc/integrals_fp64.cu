@@ -25,33 +25,96 @@ struct AOInfo {
   int l, cart;
 };
 
-// One thread per (i, j, p, q): S, T of that element and, if grad,
-// the contribution D_pq dT/dR_i - W_pq dS/dR_i (R = R_i - R_j; the
-// derivative with respect to R_j is its negative).
-__global__ void k_overlap_kinetic(const double *__restrict__ xp, int n, int nb, int nprim,
-                                  const double *__restrict__ alpha, const double *__restrict__ coef,
-                                  const int *__restrict__ ao_l, const int *__restrict__ ao_cart,
-                                  const double *__restrict__ lattice, int nlat,
-                                  double *__restrict__ S, double *__restrict__ T,
-                                  const double *__restrict__ D, const double *__restrict__ W,
-                                  double *__restrict__ gpart) {
-  long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  long long total = (long long)n * n * nb * nb;
-  if (idx >= total) return;
-  int q = idx % nb;
-  int p = (idx / nb) % nb;
-  int j = (idx / ((long long)nb * nb)) % n;
-  int i = (int)(idx / ((long long)nb * nb * n));
-  int nao = n * nb;
-  bool grad = gpart != nullptr;
-  int lp = ao_l[p], lq = ao_l[q];
-  int mbase[3] = {0, 0, 0};
-  if (lp) mbase[ao_cart[p]] += 1;
-  if (lq) mbase[ao_cart[q]] += 1;
+// Two passes.  (1) One thread per (atom pair i, j; primitive pair a, b)
+// accumulates over the lattice sphere the Hermite products
+//   QS[m] = K_ab sum_t e_t h_m0(u_x) h_m1(u_y) h_m2(u_z),
+//   QT[m] = K_ab sum_t e_t sum_d h_{m + 2 e_d}(u),   e_t = exp(-mu |R + t|^2),
+// for every multi-index m an s/p pair needs: |m| <= 2 for S and T, |m| <= 3
+// for their first derivatives (K_ab = (pi / (a + b))^(3/2)).  The exponential
+// and the Hermite factors of a lattice term are computed once for all AO
+// pairs.  (2) One thread per (i, j, p, q) contracts them with the
+// coefficients: S_pq = sum_ab c'_pa c'_qb QS[m(p,q)], T = -1/2 (same with QT),
+// and, with forces, the contribution D_pq dT/dR_i - W_pq dS/dR_i
+// (R = R_i - R_j; the derivative with respect to R_j is its negative).
+__constant__ int kMidx[20][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {2, 0, 0},
+                                 {0, 2, 0}, {0, 0, 2}, {1, 1, 0}, {1, 0, 1}, {0, 1, 1},
+                                 {3, 0, 0}, {0, 3, 0}, {0, 0, 3}, {2, 1, 0}, {2, 0, 1},
+                                 {1, 2, 0}, {0, 2, 1}, {1, 0, 2}, {0, 1, 2}, {1, 1, 1}};
+constexpr int kNq = 20;  // slots per (i, j, a, b): QS[20], QT[20]
+
+__device__ inline int midx_of(int m0, int m1, int m2) {
+  for (int k = 0; k < kNq; ++k)
+    if (kMidx[k][0] == m0 && kMidx[k][1] == m1 && kMidx[k][2] == m2) return k;
+  return 0;
+}
+
+template <int NQ>
+__global__ void k_ovl_lattice(const double *__restrict__ xp, int n, int nprim,
+                              const double *__restrict__ alpha, const double *__restrict__ lattice,
+                              int nlat, double *__restrict__ Q) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int np2 = nprim * nprim;
+  if (idx >= (long long)n * n * np2) return;
+  const int ab = (int)(idx % np2), a = ab / nprim, b = ab % nprim;
+  const int j = (int)((idx / np2) % n), i = (int)(idx / ((long long)np2 * n));
   double R[3];
   for (int d = 0; d < 3; ++d) R[d] = xp[i * 3 + d] - xp[j * 3 + d];
-  double sS = 0, sT = 0;
-  double gS[3] = {0, 0, 0}, gT[3] = {0, 0, 0};
+  const double asum = alpha[a] + alpha[b];
+  const double mu = alpha[a] * alpha[b] / asum;
+  const double K = pow(M_PI / asum, 1.5);
+  double qs[NQ], qt[NQ];
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) qs[k] = qt[k] = 0.0;
+  for (int t = 0; t < nlat; ++t) {
+    double u[3], u2 = 0;
+    for (int d = 0; d < 3; ++d) {
+      u[d] = R[d] + lattice[t * 3 + d];
+      u2 += u[d] * u[d];
+    }
+    double e = mu * u2;
+    if (e > 700.0) continue;
+    e = K * exp(-e);
+    double hx[6], hy[6], hz[6];
+    hermite6(mu, u[0], hx);
+    hermite6(mu, u[1], hy);
+    hermite6(mu, u[2], hz);
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) {
+      const int m0 = kMidx[k][0], m1 = kMidx[k][1], m2 = kMidx[k][2];
+      qs[k] += e * hx[m0] * hy[m1] * hz[m2];
+      qt[k] += e * (hx[m0 + 2] * hy[m1] * hz[m2] + hx[m0] * hy[m1 + 2] * hz[m2] +
+                    hx[m0] * hy[m1] * hz[m2 + 2]);
+    }
+  }
+  double *out = Q + idx * (2 * kNq);
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) {
+    out[k] = qs[k];
+    out[kNq + k] = qt[k];
+  }
+}
+
+__global__ void k_ovl_contract(int n, int nb, int nprim, const double *__restrict__ alpha,
+                               const double *__restrict__ coef, const int *__restrict__ ao_l,
+                               const int *__restrict__ ao_cart, const double *__restrict__ Q,
+                               double *__restrict__ S, double *__restrict__ T,
+                               const double *__restrict__ D, const double *__restrict__ W,
+                               double *__restrict__ gpart) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)n * n * nb * nb) return;
+  const int q = (int)(idx % nb), p = (int)((idx / nb) % nb);
+  const int j = (int)((idx / ((long long)nb * nb)) % n), i = (int)(idx / ((long long)nb * nb * n));
+  const int nao = n * nb, np2 = nprim * nprim;
+  const int lp = ao_l[p], lq = ao_l[q];
+  int mb[3] = {0, 0, 0};
+  if (lp) mb[ao_cart[p]] += 1;
+  if (lq) mb[ao_cart[q]] += 1;
+  const bool grad = gpart != nullptr;
+  const int ks = midx_of(mb[0], mb[1], mb[2]);
+  int kc[3];
+  for (int c = 0; c < 3; ++c) kc[c] = midx_of(mb[0] + (c == 0), mb[1] + (c == 1), mb[2] + (c == 2));
+  double sS = 0, sT = 0, gS[3] = {0, 0, 0}, gT[3] = {0, 0, 0};
+  const double *Qij = Q + ((long long)i * n + j) * np2 * (2 * kNq);
   for (int a = 0; a < nprim; ++a) {
     double ca = coef[p * nprim + a];
     if (ca == 0.0) continue;
@@ -60,42 +123,28 @@ __global__ void k_overlap_kinetic(const double *__restrict__ xp, int n, int nb, 
       double cb = coef[q * nprim + b];
       if (cb == 0.0) continue;
       if (lq) cb *= -0.5 / alpha[b];
-      double asum = alpha[a] + alpha[b];
-      double mu = alpha[a] * alpha[b] / asum;
-      double K = ca * cb * pow(M_PI / asum, 1.5);
-      for (int t = 0; t < nlat; ++t) {
-        double u[3], u2 = 0;
-        for (int d = 0; d < 3; ++d) {
-          u[d] = R[d] + lattice[t * 3 + d];
-          u2 += u[d] * u[d];
+      const double cc = ca * cb;
+      const double *qv = Qij + (long long)(a * nprim + b) * (2 * kNq);
+      sS += cc * qv[ks];
+      sT += cc * qv[kNq + ks];
+      if (grad)
+        for (int c = 0; c < 3; ++c) {
+          gS[c] += cc * qv[kc[c]];
+          gT[c] += cc * qv[kNq + kc[c]];
         }
-        double e = mu * u2;
-        if (e > 700.0) continue;
-        e = K * exp(-e);
-        double h[3][6];
-        for (int d = 0; d < 3; ++d) hermite6(mu, u[d], h[d]);
-        int m0 = mbase[0], m1 = mbase[1], m2 = mbase[2];
-        sS += e * h[0][m0] * h[1][m1] * h[2][m2];
-        sT += -0.5 * e * (h[0][m0 + 2] * h[1][m1] * h[2][m2] + h[0][m0] * h[1][m1 + 2] * h[2][m2] +
-                          h[0][m0] * h[1][m1] * h[2][m2 + 2]);
-        if (grad) {
-          for (int c = 0; c < 3; ++c) {
-            int n0 = m0 + (c == 0), n1 = m1 + (c == 1), n2 = m2 + (c == 2);
-            gS[c] += e * h[0][n0] * h[1][n1] * h[2][n2];
-            gT[c] += -0.5 * e * (h[0][n0 + 2] * h[1][n1] * h[2][n2] + h[0][n0] * h[1][n1 + 2] * h[2][n2] +
-                                 h[0][n0] * h[1][n1] * h[2][n2 + 2]);
-          }
-        }
-      }
     }
   }
-  long long pq = (long long)(i * nb + p) * nao + (j * nb + q);
+  const long long pq = (long long)(i * nb + p) * nao + (j * nb + q);
   if (S) S[pq] = sS;
-  if (T) T[pq] = sT;
+  if (T) T[pq] = -0.5 * sT;
   if (grad) {
-    double dd = D[pq], ww = W[pq];
-    for (int c = 0; c < 3; ++c) gpart[idx * 3 + c] = (i == j) ? 0.0 : dd * gT[c] - ww * gS[c];
+    const double dd = D[pq], ww = W[pq];
+    for (int c = 0; c < 3; ++c) gpart[idx * 3 + c] = (i == j) ? 0.0 : dd * (-0.5 * gT[c]) - ww * gS[c];
   }
+}
+
+size_t ovl_scratch_doubles(int n, int nprim) {
+  return (size_t)n * n * nprim * nprim * 2 * kNq;
 }
 
 // grad[A][c] += sum_{j,p,q} gpart(A,j,p,q) - sum_{i,p,q} gpart(i,A,p,q)
@@ -121,11 +170,18 @@ __global__ void k_reduce_pair_grad(const double *__restrict__ gpart, int n, int 
 void launch_overlap_kinetic(const double *xp, int n, int nb, int nprim, const double *alpha,
                             const double *coef, const int *ao_l, const int *ao_cart,
                             const double *lattice, int nlat, double *S, double *T, const double *D,
-                            const double *W, double *gpart, double *grad, cudaStream_t st) {
+                            const double *W, double *gpart, double *grad, double *Q,
+                            cudaStream_t st) {
   HQ_STAGE(ST_OVERLAP, st);
-  long long total = (long long)n * n * nb * nb;
-  k_overlap_kinetic<<<ceil_div(total, 128), 128, 0, st>>>(xp, n, nb, nprim, alpha, coef, ao_l,
-                                                          ao_cart, lattice, nlat, S, T, D, W, gpart);
+  const long long terms = (long long)n * n * nprim * nprim;
+  if (gpart)
+    k_ovl_lattice<20><<<ceil_div(terms, 128), 128, 0, st>>>(xp, n, nprim, alpha, lattice, nlat, Q);
+  else
+    k_ovl_lattice<10><<<ceil_div(terms, 128), 128, 0, st>>>(xp, n, nprim, alpha, lattice, nlat, Q);
+  HQ_LAUNCH_CHECK();
+  const long long total = (long long)n * n * nb * nb;
+  k_ovl_contract<<<ceil_div(total, 128), 128, 0, st>>>(n, nb, nprim, alpha, coef, ao_l, ao_cart, Q, S,
+                                                      T, D, W, gpart);
   HQ_LAUNCH_CHECK();
   if (gpart) {
     k_reduce_pair_grad<<<n, 256, 0, st>>>(gpart, n, nb, grad);

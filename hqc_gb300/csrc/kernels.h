@@ -60,10 +60,12 @@ void inv_sqrt_cols(int n, const double *U, const double *w, double *v, int *bad,
 void antisym(int n, const double *X, double *e, cudaStream_t st);
 
 // integrals_fp64.cu
+size_t ovl_scratch_doubles(int n, int nprim);
 void launch_overlap_kinetic(const double *xp, int n, int nb, int nprim, const double *alpha,
                             const double *coef, const int *ao_l, const int *ao_cart,
                             const double *lattice, int nlat, double *S, double *T, const double *D,
-                            const double *W, double *gpart, double *grad, cudaStream_t st);
+                            const double *W, double *gpart, double *grad, double *Q,
+                            cudaStream_t st);
 void launch_ewald(const double *xp, int n, double L, double rs, double kappa, int gmax,
                   double *pair_e, double *pair_g, double *energy, double *grad, cudaStream_t st);
 

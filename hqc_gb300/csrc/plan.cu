@@ -116,6 +116,8 @@ struct hqcgb_plan {
   bool mixed = false;
   long long ld = 0;
   float *dphiT32 = nullptr, *Yhl = nullptr;  // grid-major AO gradients; split Y^T
+  double *ovq = nullptr;                     // lattice sums of the S/T Hermite products
+  bool allow_warm = false;                   // warm eigen-refinement after the DIIS warm-up
   double *c1_prev = nullptr;                 // eigenvectors of the previous F'
   bool have_prev = false;
   // mixed Kohn-Sham forces from the occupied orbitals on the grid
@@ -293,6 +295,7 @@ static void create(const hqcgb_params *in, hqcgb_plan *p) {
     }
   }
   p->ph = p->alloc<double2>((size_t)n * 3 * p->ng);
+  p->ovq = p->alloc<double>(ovl_scratch_doubles(n, P.n_prim));
   for (double **m : {&p->S, &p->T, &p->V, &p->H, &p->St, &p->vorth, &p->F, &p->F2e, &p->K, &p->Fp,
                      &p->C, &p->c1, &p->D, &p->t1, &p->t2, &p->err, &p->jtmp, &p->jA})
     *m = p->alloc<double>(nn);
@@ -386,7 +389,7 @@ static void diagonalize(Ctx &c, const double *Fm) {
     HQ_CUDA(cudaMemcpyAsync(p->Fp, p->t1, sizeof(double) * n * n, cudaMemcpyDeviceToDevice, c.st));
   }
   // mixed: refine the previous iteration's eigenvectors when they are close
-  bool done = p->mixed && p->have_prev &&
+  bool done = p->mixed && p->have_prev && p->allow_warm &&
               eigh_mixed_warm(n, p->Fp, p->c1_prev, p->c1, p->w, p->mew, c.st);
   if (!done) eigh(c, p->Fp, p->c1, p->w);
   if (p->mixed) {
@@ -558,7 +561,7 @@ static void geometry(Ctx &c, const double *xp_dev) {
   }
   launch_overlap_kinetic(p->xp, p->n, p->nb, p->nprim, p->alpha, p->coef, p->ao_l, p->ao_cart,
                          p->lattice, P.n_lattice, p->S, p->T, nullptr, nullptr, nullptr, nullptr,
-                         c.st);
+                         p->ovq, c.st);
   launch_vloc_G(p->xp, p->n, p->ng, p->L, p->ph, p->cbuf, c.st);
   launch_fft3d(p->cbuf, p->ng, 1, p->tw, true, c.st);
   launch_complex_real(p->cbuf, N, 1.0, p->vloc, c.st);
@@ -590,6 +593,7 @@ static int scf_one(hqcgb_plan *p, const double *xp_dev, const hqcgb_scf_out *out
   size_t nn = (size_t)n * n;
   p->have_state = false;
   p->have_prev = false;
+  p->allow_warm = false;
   geometry(c, xp_dev);
   // Hcore guess (solver.py:739-745)
   diagonalize(c, p->H);
@@ -618,7 +622,11 @@ static int scf_one(hqcgb_plan *p, const double *xp_dev, const hqcgb_scf_out *out
       ++loop;
       if (trace_on()) fprintf(stderr, "scf %3d E=%.12f dE=%.3e err=%.3e\n", loop, E1, E1 - E0, enorm);
     };
+    // the Fock matrix still moves a lot in the plain warm-up iterations:
+    // eigenvectors of the previous one are too far for the warm refinement
+    p->allow_warm = false;
     while (loop < P.diis_start_cycle + sp) step(p->Fk + head * nn);
+    p->allow_warm = true;
     E0 = E1 - 1.0;
     // The mixed path's Fock build carries noise (3xTF32, FP32 accumulation):
     // its stopping tests are floored at that noise (|dE| 1e-6 Ha, commutator
@@ -634,6 +642,7 @@ static int scf_one(hqcgb_plan *p, const double *xp_dev, const hqcgb_scf_out *out
   } else {
     const double etol = p->mixed ? std::max(P.tol, 2e-6) : P.tol;
     while (std::fabs(E1 - E0) > etol && loop < P.max_cycle) {
+      p->allow_warm = loop >= 3;
       double En = fock(c);
       diagonalize(c, p->F);
       density_matrix(c);
@@ -723,7 +732,8 @@ static void forces(hqcgb_plan *p, double *grad, cudaStream_t st) {
   launch_axpy_grid(n, n, 1.0, p->occ, p->w, p->psi, st);   // psi = f * eps
   gemm(false, true, n, n, n, 1.0, p->C, n, p->C, n, p->psi, 0.0, p->t2, n, st);
   launch_overlap_kinetic(p->xp, p->n, p->nb, p->nprim, p->alpha, p->coef, p->ao_l, p->ao_cart,
-                         p->lattice, P.n_lattice, nullptr, nullptr, p->D, p->t2, p->gpart, grad, st);
+                         p->lattice, P.n_lattice, nullptr, nullptr, p->D, p->t2, p->gpart, grad,
+                         p->ovq, st);
   if (p->orb_forces) {
     orbital_forces(c, grad);
     return;
