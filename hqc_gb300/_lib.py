@@ -96,7 +96,7 @@ def load():
                                      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                      ctypes.c_void_p, ctypes.c_void_p]
     lib.hqcgb_tc_orbital_density.argtypes = [ctypes.c_int, ctypes.c_longlong, ctypes.c_longlong] + \
-        [ctypes.c_void_p] * 4 + [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 3
+        [ctypes.c_void_p] * 4 + [ctypes.c_int, ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 3
     lib.hqcgb_eigh_mixed.argtypes = [ctypes.c_int] + [ctypes.c_void_p] * 4
     lib.hqcgb_eigh_noalloc.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                        ctypes.c_void_p, ctypes.c_void_p]
@@ -217,7 +217,7 @@ def tc_density(phi32, D32, N=None, nsplit=2, drain=1):
     return rho
 
 
-def tc_orbital_density(phi32, C, occ, N=None, nuse=None, dphi32=None):
+def tc_orbital_density(phi32, C, occ, N=None, nuse=None, dphi32=None, drain=1):
     """rho = sum_k occ_k (sum_p C[p,k] phi_p)^2 (and grad rho with dphi32) on
     the tensor cores; phi32 (nao, ld) fp32, C (nao, nmo) and occ (nmo,) fp64."""
     import torch
@@ -235,6 +235,6 @@ def tc_orbital_density(phi32, C, occ, N=None, nuse=None, dphi32=None):
     check(lib.hqcgb_tc_orbital_density(
         nao, N, ld, ctypes.c_void_p(phi32.data_ptr()),
         ctypes.c_void_p(dphi32.data_ptr() if dphi32 is not None else 0),
-        ctypes.c_void_p(C.data_ptr()), ctypes.c_void_p(occ.data_ptr()), nmo, nuse,
+        ctypes.c_void_p(C.data_ptr()), ctypes.c_void_p(occ.data_ptr()), nmo, nuse, drain,
         ctypes.c_void_p(rho.data_ptr()), ctypes.c_void_p(grho.data_ptr() if grho is not None else 0), st))
     return rho if grho is None else (rho, grho)

@@ -10,7 +10,7 @@
 //     matrix by the method of bisection", Numer. Math. 9 (1967) 386-393), all
 //     in parallel; then the eigenvectors of T by inverse iteration with a
 //     partial-pivoting LU of T - lambda I (J. H. Wilkinson, "The Algebraic
-//     Eigenvalue Problem", 1965, ch. 5), eigenvalues closer than 1e-3 ||T||
+//     Eigenvalue Problem", 1965, ch. 5), eigenvalues closer than 1e-4 ||T||
 //     treated as a cluster whose vectors one thread computes in turn,
 //     orthogonalising each against the earlier ones (modified Gram-Schmidt).
 //  3. k_backtransform_f32 (a block per 32 columns): V = Q Z, the reflectors
@@ -105,7 +105,10 @@ __global__ void __launch_bounds__(kTriThreads)
 
   // --- eigenvectors by inverse iteration; the first member of each cluster
   // computes the cluster's vectors in order
-  const float sep = 1e-3f * tnorm;
+  // clusters: eigenvalues within 1e-4 ||T||; vectors of eigenvalues further
+  // apart are orthogonal to FP32 eps ||T|| / gap <= 1e-3, which the FP64
+  // refinement removes
+  const float sep = 1e-4f * tnorm;
   const float tiny = FLT_EPSILON * tnorm + pivmin;
   for (int i0 = tid; i0 < n; i0 += nt) {
     if (i0 > 0 && lam[i0] - lam[i0 - 1] <= sep) continue;

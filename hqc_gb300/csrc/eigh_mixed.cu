@@ -46,8 +46,11 @@ __global__ void k_f32_to_f64(long long n, const float *__restrict__ a, double *_
 // kMaxCluster are left unrotated and flagged in emax[2].
 // emax[0] = max |E|, emax[1] = ||S - diag(l)||_F / ||A||_F before the
 // update, emax[2] = 1 when a cluster was too large, emax[3] = cluster count.
-constexpr int kMaxCluster = 48;
+constexpr int kMaxCluster = 48;      // largest cluster rotated (wide spectra)
+constexpr int kMaxClusterFock = 12;  // ... for Fock matrices (keeps the pass short)
+constexpr int kShCluster = 12;       // clusters up to this size rotate in shared memory
 constexpr int kOaThreads = 256;
+constexpr int kOaJacobiThreads = 16;  // clusters rotated with their blocks in shared memory
 
 // non-negative doubles compare like their bit patterns
 __device__ inline void atomic_max_nonneg(double *a, double v) {
@@ -109,7 +112,7 @@ __global__ void __launch_bounds__(1024) k_oa_clusters(int n, const double *__res
                                                       double *__restrict__ lam,
                                                       double *__restrict__ emax,
                                                       int *__restrict__ iwork,
-                                                      double *__restrict__ wbuf) {
+                                                      double *__restrict__ wbuf, int max_cluster) {
   __shared__ int s_nclus;
   const int tid = threadIdx.x, nt = blockDim.x;
   int *order = iwork, *cid = iwork + n, *cstart = iwork + 2 * n, *csize = iwork + 3 * n,
@@ -142,7 +145,7 @@ __global__ void __launch_bounds__(1024) k_oa_clusters(int n, const double *__res
       int j = i;
       while (j + 1 < n && lam[order[j + 1]] - lam[order[j]] <= delta) ++j;
       int k = j - i + 1;
-      if (k >= 2 && k <= kMaxCluster) {
+      if (k >= 2 && k <= max_cluster) {
         cstart[nclus] = i;
         csize[nclus] = k;
         coff[nclus] = off;
@@ -150,7 +153,7 @@ __global__ void __launch_bounds__(1024) k_oa_clusters(int n, const double *__res
         for (int m = i; m <= j; ++m) cid[order[m]] = nclus;
         ++nclus;
       } else {
-        if (k > kMaxCluster) bad = 1;
+        if (k > max_cluster) bad = 1;
         for (int m = i; m <= j; ++m) cid[order[m]] = -1;
       }
       i = j + 1;
@@ -164,10 +167,14 @@ __global__ void __launch_bounds__(1024) k_oa_clusters(int n, const double *__res
   }
   __syncthreads();
   const int nclus = s_nclus;
-  // cyclic Jacobi on each cluster block B = S_CC; W accumulates the rotations
+  // cyclic Jacobi on each cluster block B = S_CC (in shared memory); W
+  // accumulates the rotations and goes to wbuf for the rotation passes
+  __shared__ double jb[kOaJacobiThreads][2 * kShCluster * kShCluster];
   for (int c = tid; c < nclus; c += nt) {
     const int k = csize[c], s0 = cstart[c];
-    double *B = wbuf + coff[c], *W = B + k * k;
+    const bool in_sh = tid < kOaJacobiThreads && k <= kShCluster;
+    double *B = in_sh ? jb[tid] : wbuf + coff[c];
+    double *W = B + k * k;
     for (int a = 0; a < k; ++a)
       for (int b = 0; b < k; ++b) {
         long long ia = order[s0 + a], ib = order[s0 + b];
@@ -204,6 +211,8 @@ __global__ void __launch_bounds__(1024) k_oa_clusters(int n, const double *__res
           }
         }
     }
+    if (in_sh)
+      for (int m = 0; m < k * k; ++m) wbuf[coff[c] + k * k + m] = W[m];
   }
 }
 
@@ -325,7 +334,7 @@ static void sort_eigpairs(int n, double *w, double *X, MixedEigWork &ws, cudaStr
 
 // One refinement step; returns ||X^T A X - diag|| / ||A|| before the update.
 static double oa_iteration(int n, const double *A, double *X, double *w, MixedEigWork &ws,
-                           cudaStream_t st) {
+                           cudaStream_t st, int max_cluster = kMaxClusterFock) {
   const long long nn = (long long)n * n;
   const int grid = (int)std::min<long long>(ceil_div(nn, kOaThreads), 148);
   double *red = ws.emax + 8;  // [0..4] grid reductions
@@ -335,7 +344,7 @@ static double oa_iteration(int n, const double *A, double *X, double *w, MixedEi
   HQ_CUDA(cudaMemsetAsync(red, 0, 5 * sizeof(double), st));
   k_oa_stats<<<grid, kOaThreads, 0, st>>>(n, A, ws.S, ws.G, red);
   HQ_LAUNCH_CHECK();
-  k_oa_clusters<<<1, 1024, 0, st>>>(n, ws.S, ws.G, red, w, ws.emax, ws.iwork, ws.wbuf);
+  k_oa_clusters<<<1, 1024, 0, st>>>(n, ws.S, ws.G, red, w, ws.emax, ws.iwork, ws.wbuf, max_cluster);
   HQ_LAUNCH_CHECK();
   k_oa_rotate_cols<<<grid, kOaThreads, 0, st>>>(n, X, ws.S, ws.G, ws.iwork, ws.wbuf);
   HQ_LAUNCH_CHECK();
@@ -380,7 +389,7 @@ bool eigh_mixed(int n, const double *A, double *V, double *w, MixedEigWork &ws, 
   k_f32_to_f64<<<ceil_div(nn, 256), 256, 0, st>>>(nn, ws.V32, V);
   HQ_LAUNCH_CHECK();
   for (int it = 0; it < 8; ++it) {
-    double off = oa_iteration(n, A, V, w, ws, st);
+    double off = oa_iteration(n, A, V, w, ws, st, wide ? kMaxCluster : kMaxClusterFock);
     if (off < 1e-12) {
       sort_eigpairs(n, w, V, ws, st);
       return true;

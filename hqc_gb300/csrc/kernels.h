@@ -134,7 +134,7 @@ void launch_psi_operand(const double *C, const double *occ, int nao, int nmo, in
                         float *Yhl, cudaStream_t st);
 void launch_tc_psi_density(const float *phiT, const float *dphiT, const float *Yhl, int npsi, int ldk,
                            long long N, double *rho, double *grho, int *err, cudaStream_t st,
-                           float *psi_out = nullptr);
+                           float *psi_out = nullptr, int psi_drain = 1);
 // forces_mixed.cu
 int force_orb_blocks(long long N);
 void launch_force_operand(const double *C, const double *occ, int nao, int nuse, int npsi,

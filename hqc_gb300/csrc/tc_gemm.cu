@@ -689,6 +689,7 @@ struct PsiArgs {
   int ldk, npsi, ncomp;
   double *rho, *grho;  // [N], [3][N]
   float *psi_out;      // [ncomp][npsi][N] psi_k and grad psi_k (fp32), or null
+  int drain;           // K blocks per drained accumulation (1 = every 32 AOs)
   int *err;
 };
 
@@ -716,6 +717,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_psi_density(PsiArgs a) {
   const int per_tile = a.ncomp * nkb;
   const long long S = my_tiles * per_tile;
   const int RA = psi_ring(NPSI, a.ncomp);
+  const int DR = a.drain;  // K blocks of 32 accumulated per TMEM slot before a drain
   const uint32_t colS = (uint32_t)(RA * 2 * NPSI), colC = colS + (uint32_t)(a.ncomp * NPSI);
   const int ncols = (int)colC + a.ncomp * NPSI;
   int tcols = 32;
@@ -796,53 +798,57 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_psi_density(PsiArgs a) {
     }
     cp_async_wait<0>();
   } else if (warp < 8) {
-    // drains and epilogue: thread = grid point (TMEM lane)
+    // drains and epilogue: thread = grid point (TMEM lane).  Group G of this
+    // CTA is (tile, component, K blocks [g0, g0 + DR)) and lives in slot G % RA.
     const int row = (warp & 3) * 32 + lane;
     const uint32_t tbase = P.tmem_base + ((uint32_t)((warp & 3) * 32) << 16);
-    for (long long st = 0; st < S; ++st) {
-      const int b = (int)(st % RA);
-      const long long use = st / RA;
-      bool got = ok && mbar_wait(&P.acc_full[b], (unsigned)(use & 1), a.err, 23);
-      if (!got) ok = false;
-      tc_fence_after();
-      const int r = (int)(st % per_tile), comp = r / nkb, kb = r % nkb;
-      if (got) {
-        const uint32_t slot = tbase + (uint32_t)(b * 2 * NPSI);
-        const uint32_t sc = tbase + colS + (uint32_t)(comp * NPSI);
-        const uint32_t cc = tbase + colC + (uint32_t)(comp * NPSI);
+    long long G = 0;
+    for (long long t = 0; t < my_tiles; ++t) {
+      for (int comp = 0; comp < a.ncomp; ++comp) {
+        for (int g0 = 0; g0 < nkb; g0 += DR, ++G) {
+          const int b = (int)(G % RA);
+          const long long use = G / RA;
+          bool got = ok && mbar_wait(&P.acc_full[b], (unsigned)(use & 1), a.err, 23);
+          if (!got) ok = false;
+          tc_fence_after();
+          if (got) {
+            const uint32_t slot = tbase + (uint32_t)(b * 2 * NPSI);
+            const uint32_t sc = tbase + colS + (uint32_t)(comp * NPSI);
+            const uint32_t cc = tbase + colC + (uint32_t)(comp * NPSI);
 #pragma unroll
-        for (int c0 = 0; c0 < NPSI; c0 += 16) {
-          uint32_t vb[16], vs[16], ss[16], cs[16];
-          tmem_ld16_nowait(slot + c0, vb);
-          tmem_ld16_nowait(slot + NPSI + c0, vs);
-          if (kb > 0) {
-            tmem_ld16_nowait(sc + c0, ss);
-            tmem_ld16_nowait(cc + c0, cs);
-          }
-          tmem_wait_ld();
-          float so[16], co[16];
+            for (int c0 = 0; c0 < NPSI; c0 += 16) {
+              uint32_t vb[16], vs[16], ss[16], cs[16];
+              tmem_ld16_nowait(slot + c0, vb);
+              tmem_ld16_nowait(slot + NPSI + c0, vs);
+              if (g0 > 0) {
+                tmem_ld16_nowait(sc + c0, ss);
+                tmem_ld16_nowait(cc + c0, cs);
+              }
+              tmem_wait_ld();
+              float so[16], co[16];
 #pragma unroll
-          for (int i = 0; i < 16; ++i) {
-            float big = __uint_as_float(vb[i]), small = __uint_as_float(vs[i]);
-            if (kb == 0) {
-              so[i] = big;
-              co[i] = small;
-            } else {
-              so[i] = __uint_as_float(ss[i]);
-              co[i] = __uint_as_float(cs[i]);
-              two_sum_add(so[i], co[i], big);
-              co[i] += small;
+              for (int i = 0; i < 16; ++i) {
+                float big = __uint_as_float(vb[i]), small = __uint_as_float(vs[i]);
+                if (g0 == 0) {
+                  so[i] = big;
+                  co[i] = small;
+                } else {
+                  so[i] = __uint_as_float(ss[i]);
+                  co[i] = __uint_as_float(cs[i]);
+                  two_sum_add(so[i], co[i], big);
+                  co[i] += small;
+                }
+              }
+              tmem_st16(sc + c0, so);
+              tmem_st16(cc + c0, co);
             }
+            tmem_wait_st();
           }
-          tmem_st16(sc + c0, so);
-          tmem_st16(cc + c0, co);
+          tc_fence_before();
+          mbar_arrive(&P.acc_empty[b]);
         }
-        tmem_wait_st();
       }
-      tc_fence_before();
-      mbar_arrive(&P.acc_empty[b]);
-      if (r == per_tile - 1) {  // tile complete: psi = S + C for every component
-        const long long t = st / per_tile;
+      {  // tile complete: psi = S + C for every component
         const long long g = (blockIdx.x + t * gridDim.x) * (long long)kM + row;
         if (ok) {
           double psi[NPSI];
@@ -891,29 +897,39 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_psi_density(PsiArgs a) {
     }
   } else if (lane == 0) {
     const uint32_t idesc = idesc_tf32(kM, NPSI);
-    for (long long st = 0; st < S; ++st) {
-      const int slot = (int)(st % kPsiRing);
-      const int b = (int)(st % RA);
-      const long long ause = st / RA;
-      if (ok && ause > 0 && !mbar_wait(&P.acc_empty[b], (unsigned)((ause - 1) & 1), a.err, 24))
-        ok = false;
-      if (ok && !mbar_wait(&P.full[slot], (unsigned)((st / kPsiRing) & 1), a.err, 22)) ok = false;
-      tc_fence_after();
-      if (ok) {
-        const uint32_t dbig = P.tmem_base + (uint32_t)(b * 2 * NPSI), dsmall = dbig + NPSI;
-        const uint32_t base = smem_u32(sm + slot * kPsiStageBytes);
-        const uint32_t Ah = base, Al = base + kTile;
-        const uint32_t Bh = base + (uint32_t)kPsiAPieces, Bl = Bh + (uint32_t)kPsiBPiece;
+    long long st = 0, G = 0;
+    for (long long t = 0; t < my_tiles; ++t) {
+      for (int comp = 0; comp < a.ncomp; ++comp) {
+        for (int g0 = 0; g0 < nkb; g0 += DR, ++G) {
+          const int b = (int)(G % RA);
+          const long long ause = G / RA;
+          if (ok && ause > 0 && !mbar_wait(&P.acc_empty[b], (unsigned)((ause - 1) & 1), a.err, 24))
+            ok = false;
+          tc_fence_after();
+          const uint32_t dbig = P.tmem_base + (uint32_t)(b * 2 * NPSI), dsmall = dbig + NPSI;
+          const int g1 = min(g0 + DR, nkb);
+          for (int kb = g0; kb < g1; ++kb, ++st) {
+            const int slot = (int)(st % kPsiRing);
+            if (ok && !mbar_wait(&P.full[slot], (unsigned)((st / kPsiRing) & 1), a.err, 22)) ok = false;
+            tc_fence_after();
+            if (ok) {
+              const uint32_t base = smem_u32(sm + slot * kPsiStageBytes);
+              const uint32_t Ah = base, Al = base + kTile;
+              const uint32_t Bh = base + (uint32_t)kPsiAPieces, Bl = Bh + (uint32_t)kPsiBPiece;
 #pragma unroll
-        for (int ks = 0; ks < kStageK / 8; ++ks) {
-          uint32_t off = ks * 32;
-          mma_tf32(dsmall, sdesc(Al + off), sdesc(Bh + off), idesc, ks == 0 ? 0 : 1);
-          mma_tf32(dsmall, sdesc(Ah + off), sdesc(Bl + off), idesc, 1);
-          mma_tf32(dbig, sdesc(Ah + off), sdesc(Bh + off), idesc, ks == 0 ? 0 : 1);
+              for (int ks = 0; ks < kStageK / 8; ++ks) {
+                const uint32_t off = ks * 32;
+                const int acc = (kb > g0 || ks > 0) ? 1 : 0;
+                mma_tf32(dsmall, sdesc(Al + off), sdesc(Bh + off), idesc, acc);
+                mma_tf32(dsmall, sdesc(Ah + off), sdesc(Bl + off), idesc, 1);
+                mma_tf32(dbig, sdesc(Ah + off), sdesc(Bh + off), idesc, acc);
+              }
+            }
+            mma_commit(&P.empty[slot]);
+          }
+          mma_commit(&P.acc_full[b]);
         }
       }
-      mma_commit(&P.empty[slot]);
-      mma_commit(&P.acc_full[b]);
     }
   }
   tc_fence_before();
@@ -955,7 +971,8 @@ void launch_psi_operand(const double *C, const double *occ, int nao, int nmo, in
 // rho (and grad rho) from the grid-major AO values and the pre-split Y^T.
 void launch_tc_psi_density(const float *phiT, const float *dphiT, const float *Yhl, int npsi, int ldk,
                            long long N, double *rho, double *grho, int *err, cudaStream_t st,
-                           float *psi_out) {
+                           float *psi_out, int psi_drain) {
+  HQ_REQUIRE(psi_drain >= 1, "drain interval must be >= 1");
   HQ_STAGE(ST_PSI, st);
   HQ_REQUIRE(npsi >= 16 && npsi <= tc::kPsiMaxN && npsi % 16 == 0, "orbital count out of range");
   HQ_REQUIRE(tc::psi_ring(npsi, grho ? 4 : 1) > 0, "orbital count too large for the TMEM layout");
@@ -978,6 +995,7 @@ void launch_tc_psi_density(const float *phiT, const float *dphiT, const float *Y
   a.phiT = phiT; a.dphiT = grho ? dphiT : nullptr; a.Yhl = Yhl; a.N = N; a.ldk = ldk;
   a.npsi = npsi; a.ncomp = grho ? 4 : 1; a.rho = rho; a.grho = grho; a.err = err;
   a.psi_out = psi_out;
+  a.drain = psi_drain;
   HQ_REQUIRE(!grho || dphiT, "GGA density needs the gradient operand");
   long long ntiles = ceil_div(N, tc::kM);
   int grid = (int)std::min<long long>(ntiles, nsm);
@@ -1172,7 +1190,8 @@ extern "C" int hqcgb_tc_density(int nao, long long N, long long ld, const float 
 // dphi are AO-major fp32 with row stride ld.
 extern "C" int hqcgb_tc_orbital_density(int nao, long long N, long long ld, const float *phi,
                                         const float *dphi, const double *C, const double *occ,
-                                        int nmo, int nuse, double *rho, double *grho, void *stream) {
+                                        int nmo, int nuse, int drain, double *rho, double *grho,
+                                        void *stream) {
   using namespace hqcgb;
   cudaStream_t st = (cudaStream_t)stream;
   try {
@@ -1195,7 +1214,7 @@ extern "C" int hqcgb_tc_orbital_density(int nao, long long N, long long ld, cons
                              st);
     launch_psi_operand(C, occ, nao, nmo, nuse, ldk, Yhl, st);
     launch_tc_psi_density(phiT, dphi ? phiT + (size_t)N * ldk : nullptr, Yhl, tc_psi_width(nuse), ldk,
-                          N, rho, grho, err, st);
+                          N, rho, grho, err, st, nullptr, drain);
     int h = 0;
     HQ_CUDA(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, st));
     HQ_CUDA(cudaFreeAsync(phiT, st));

@@ -168,10 +168,11 @@ int hqcgb_tc_density(int nao, long long N, long long ld, const float *phi, const
  * psi_k = sum_p C[p][k] phi_p over the first nuse (<= 64) orbitals, and
  * with dphi (3 x [nao][ld]) also grad rho (3 x N) -- the density of
  * D = C diag(occ) C^T (hqc/pbc/solver.py:566-577,690) at nuse/nao of the
- * work.  C is [nao][nmo] row-major FP64; phi/dphi fp32 as above. */
+ * work.  C is [nao][nmo] row-major FP64; phi/dphi fp32 as above; drain =
+ * K blocks of 32 AOs accumulated in TMEM between compensated drains. */
 int hqcgb_tc_orbital_density(int nao, long long N, long long ld, const float *phi,
                              const float *dphi, const double *C, const double *occ, int nmo,
-                             int nuse, double *rho, double *grho, void *stream);
+                             int nuse, int drain, double *rho, double *grho, void *stream);
 
 /* Largest n accepted by hqcgb_eigh_noalloc. */
 #define HQCGB_EIGH_NOALLOC_MAX_N 320
