@@ -61,7 +61,7 @@ def build(force=False, verbose=False, jobs=None):
             if verbose and msg:
                 print(msg)
     if force or todo or not os.path.exists(LIB):
-        cmd = [cc, *ARCH, "-shared", "-o", LIB, *objs]
+        cmd = [cc, *ARCH, "-shared", "-o", LIB, *objs, "-lcublas"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stderr}")

@@ -2,8 +2,10 @@
 // n x n matrix to single precision, for the FP64 refinement in
 // eigh_mixed.cu.  Three kernels:
 //
-//  1. k_tridiag_f32 (one block): Householder reduction to tridiagonal
-//     T = Q^T A Q (eigh_tridiag.cuh), reflectors stored contiguously.
+//  1. k_tridiag_f32_smem (one block): Householder reduction to tridiagonal
+//     T = Q^T A Q with the matrix in shared memory (k_tridiag_f32, the
+//     global-memory form of eigh_tridiag.cuh, above 310 AOs), reflectors
+//     stored contiguously.
 //  2. k_tri_eig_f32 (one block, a thread per eigenvalue): the eigenvalues of
 //     T by bisection on Sturm counts (W. Barth, R. S. Martin, J. H.
 //     Wilkinson, "Calculation of the eigenvalues of a symmetric tridiagonal
@@ -21,6 +23,8 @@
 // over eigenvalues; the FP64 refinement then fixes what single precision
 // leaves (inaccurate vectors within clusters included).
 #include <cfloat>
+#include <cstdio>
+#include <cstdlib>
 
 #include "common.cuh"
 #include "eigh_tridiag.cuh"
@@ -45,6 +49,95 @@ __global__ void __launch_bounds__(kTriThreads)
   }
 }
 
+// The same reduction with the matrix held in shared memory as a packed lower
+// triangle (element (i, j), i >= j, at i (i + 1) / 2 + j): the symmetric
+// matrix-vector product and the rank-2 update of each step touch only shared
+// memory.  For n with n (n + 1) / 2 + 5 n floats within the shared-memory
+// budget (n <= 310).
+__device__ inline int tri_ix(int i, int j) { return i * (i + 1) / 2 + j; }
+
+__global__ void __launch_bounds__(kTriThreads)
+    k_tridiag_f32_smem(int n, const float *__restrict__ A, float *__restrict__ dg,
+                       float *__restrict__ eg, float *__restrict__ taug, float *__restrict__ hv) {
+  extern __shared__ __align__(16) float tsh[];
+  float *L = tsh, *d = L + n * (n + 1) / 2, *e = d + n, *tau = e + n, *v = tau + n, *p = v + n;
+  __shared__ float red[32];
+  __shared__ float s_beta[2];
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+  for (int idx = tid; idx < n * (n + 1) / 2; idx += nt) {
+    // row i of the packed triangle: the largest i with i (i + 1) / 2 <= idx
+    int i = (int)((sqrtf(8.f * (float)idx + 1.f) - 1.f) * 0.5f);
+    while (i * (i + 1) / 2 > idx) --i;
+    while ((i + 1) * (i + 2) / 2 <= idx) ++i;
+    L[idx] = A[(long long)i * n + (idx - i * (i + 1) / 2)];
+  }
+  __syncthreads();
+  for (int k = 0; k < n - 2; ++k) {
+    const int m = n - k - 1;  // trailing rows k+1 .. n-1
+    float s2 = 0.f;
+    for (int i = 1 + tid; i < m; i += nt) {
+      float x = L[tri_ix(k + 1 + i, k)];
+      s2 += x * x;
+    }
+    s2 = block_sum(s2, red);
+    if (tid == 0) {
+      const float x0 = L[tri_ix(k + 1, k)];
+      if (s2 == 0.f) {
+        tau[k] = 0.f;
+        e[k] = x0;
+        s_beta[0] = 0.f;
+      } else {
+        const float beta = -copysignf(sqrtf(x0 * x0 + s2), x0);
+        tau[k] = (beta - x0) / beta;
+        e[k] = beta;
+        s_beta[0] = 1.f / (x0 - beta);
+      }
+    }
+    __syncthreads();
+    const float tk = tau[k], sc = s_beta[0];
+    for (int i = tid; i < m; i += nt) {
+      v[i] = (i == 0) ? 1.f : (tk == 0.f ? 0.f : L[tri_ix(k + 1 + i, k)] * sc);
+      hv[(long long)k * n + i] = v[i];
+    }
+    __syncthreads();
+    if (tk == 0.f) continue;
+    // p = tau A22 v, one warp per row i: sum over j <= i of L[i][j] v_j and
+    // over j > i of L[j][i] v_j (trailing block indices)
+    for (int i = warp; i < m; i += nw) {
+      const int gi = k + 1 + i;
+      float sum = 0.f;
+      for (int j = lane; j < m; j += 32) {
+        const int gj = k + 1 + j;
+        sum += (j <= i ? L[tri_ix(gi, gj)] : L[tri_ix(gj, gi)]) * v[j];
+      }
+      sum = warp_sum(sum);
+      if (lane == 0) p[i] = tk * sum;
+    }
+    __syncthreads();
+    float pv = 0.f;
+    for (int i = tid; i < m; i += nt) pv += p[i] * v[i];
+    pv = block_sum(pv, red);
+    const float alpha = -0.5f * tk * pv;
+    for (int i = tid; i < m; i += nt) p[i] += alpha * v[i];  // p becomes w
+    __syncthreads();
+    // rank-2 update of the trailing lower triangle
+    const int tri = m * (m + 1) / 2;
+    for (int idx = tid; idx < tri; idx += nt) {
+      int i = (int)((sqrtf(8.f * (float)idx + 1.f) - 1.f) * 0.5f);
+      while (i * (i + 1) / 2 > idx) --i;
+      while ((i + 1) * (i + 2) / 2 <= idx) ++i;
+      const int j = idx - i * (i + 1) / 2;
+      L[tri_ix(k + 1 + i, k + 1 + j)] -= v[i] * p[j] + p[i] * v[j];
+    }
+    __syncthreads();
+  }
+  for (int i = tid; i < n; i += nt) {
+    dg[i] = L[tri_ix(i, i)];
+    eg[i] = i < n - 2 ? e[i] : (i == n - 2 ? L[tri_ix(n - 1, n - 2)] : 0.f);
+    taug[i] = i < n - 2 ? tau[i] : 0.f;
+  }
+}
+
 // number of eigenvalues of the tridiagonal (d, e2 = e^2) below x
 __device__ inline int sturm_count(int n, const float *__restrict__ d, const float *__restrict__ e2,
                                   float x, float pivmin) {
@@ -60,7 +153,8 @@ __device__ inline int sturm_count(int n, const float *__restrict__ d, const floa
 }
 
 // Eigenpairs of the tridiagonal (d, e): w ascending, Z[r][c] column c the
-// eigenvector of w[c].  scr: 6 n floats per cluster leader (LU and vector).
+// eigenvector of w[c].  scr: 6 n x n floats (LU factors and the vector of
+// each cluster leader, interleaved by leader).
 __global__ void __launch_bounds__(kTriThreads)
     k_tri_eig_f32(int n, const float *__restrict__ dg, const float *__restrict__ eg,
                   float *__restrict__ w, float *__restrict__ Z, float *__restrict__ scr) {
@@ -114,8 +208,17 @@ __global__ void __launch_bounds__(kTriThreads)
     if (i0 > 0 && lam[i0] - lam[i0 - 1] <= sep) continue;
     int i1 = i0;
     while (i1 + 1 < n && lam[i1 + 1] - lam[i1] <= sep) ++i1;
-    float *u1 = scr + (long long)i0 * 6 * n, *u2 = u1 + n, *u3 = u2 + n, *lm = u3 + n,
-          *pv = lm + n, *x = pv + n;
+    // per-leader arrays interleaved by leader (element k of leader i0 at
+    // k * n + i0): the leaders step through k together, so a warp's accesses
+    // are one coalesced line instead of 32 scattered ones
+    float *u1 = scr + i0, *u2 = u1 + (long long)n * n, *u3 = u2 + (long long)n * n,
+          *lm = u3 + (long long)n * n, *pv = lm + (long long)n * n, *x = pv + (long long)n * n;
+#define U1(k) u1[(long long)(k) * n]
+#define U2(k) u2[(long long)(k) * n]
+#define U3(k) u3[(long long)(k) * n]
+#define LM(k) lm[(long long)(k) * n]
+#define PV(k) pv[(long long)(k) * n]
+#define XX(k) x[(long long)(k) * n]
     float shift_prev = 0.f;
     for (int j = i0; j <= i1; ++j) {
       // equal eigenvalues in a cluster are separated a little so that the
@@ -131,49 +234,55 @@ __global__ void __launch_bounds__(kTriThreads)
         if (fabsf(b) >= fabsf(a)) {
           if (b == 0.f) b = tiny;
           const float l = a / b;
-          u1[k] = b; u2[k] = c; u3[k] = 0.f; lm[k] = l; pv[k] = 0.f;
+          U1(k) = b; U2(k) = c; U3(k) = 0.f; LM(k) = l; PV(k) = 0.f;
           b = bn - l * c;
           c = cn;
         } else {
           const float l = b / a;
-          u1[k] = a; u2[k] = bn; u3[k] = cn; lm[k] = l; pv[k] = 1.f;
+          U1(k) = a; U2(k) = bn; U3(k) = cn; LM(k) = l; PV(k) = 1.f;
           b = c - l * bn;
           c = -l * cn;
         }
       }
-      u1[n - 1] = fabsf(b) < tiny ? (b < 0.f ? -tiny : tiny) : b;
+      U1(n - 1) = fabsf(b) < tiny ? (b < 0.f ? -tiny : tiny) : b;
       for (int k = 0; k < n - 1; ++k)
-        if (fabsf(u1[k]) < tiny) u1[k] = u1[k] < 0.f ? -tiny : tiny;
+        if (fabsf(U1(k)) < tiny) U1(k) = U1(k) < 0.f ? -tiny : tiny;
       // start vector: deterministic, not orthogonal to any eigenvector in practice
-      for (int k = 0; k < n; ++k) x[k] = 1.f + 0.37f * __sinf(0.7f * (float)k + 1.3f * (float)j);
+      for (int k = 0; k < n; ++k) XX(k) = 1.f + 0.37f * __sinf(0.7f * (float)k + 1.3f * (float)j);
       for (int it = 0; it < 3; ++it) {
         // L y = P x
         for (int k = 0; k < n - 1; ++k) {
-          if (pv[k] != 0.f) {
-            float t = x[k];
-            x[k] = x[k + 1];
-            x[k + 1] = t;
+          if (PV(k) != 0.f) {
+            float t = XX(k);
+            XX(k) = XX(k + 1);
+            XX(k + 1) = t;
           }
-          x[k + 1] -= lm[k] * x[k];
+          XX(k + 1) -= LM(k) * XX(k);
         }
         // U z = y
-        x[n - 1] /= u1[n - 1];
-        if (n > 1) x[n - 2] = (x[n - 2] - u2[n - 2] * x[n - 1]) / u1[n - 2];
+        XX(n - 1) /= U1(n - 1);
+        if (n > 1) XX(n - 2) = (XX(n - 2) - U2(n - 2) * XX(n - 1)) / U1(n - 2);
         for (int k = n - 3; k >= 0; --k)
-          x[k] = (x[k] - u2[k] * x[k + 1] - u3[k] * x[k + 2]) / u1[k];
+          XX(k) = (XX(k) - U2(k) * XX(k + 1) - U3(k) * XX(k + 2)) / U1(k);
         // orthogonalise against the cluster's earlier vectors, normalise
         for (int q = i0; q < j; ++q) {
           float s = 0.f;
-          for (int k = 0; k < n; ++k) s += Z[(long long)k * n + q] * x[k];
-          for (int k = 0; k < n; ++k) x[k] -= s * Z[(long long)k * n + q];
+          for (int k = 0; k < n; ++k) s += Z[(long long)k * n + q] * XX(k);
+          for (int k = 0; k < n; ++k) XX(k) -= s * Z[(long long)k * n + q];
         }
         float nrm = 0.f;
-        for (int k = 0; k < n; ++k) nrm += x[k] * x[k];
+        for (int k = 0; k < n; ++k) nrm += XX(k) * XX(k);
         nrm = nrm > 0.f ? rsqrtf(nrm) : 0.f;
-        for (int k = 0; k < n; ++k) x[k] *= nrm;
+        for (int k = 0; k < n; ++k) XX(k) *= nrm;
       }
-      for (int k = 0; k < n; ++k) Z[(long long)k * n + j] = x[k];
+      for (int k = 0; k < n; ++k) Z[(long long)k * n + j] = XX(k);
     }
+#undef U1
+#undef U2
+#undef U3
+#undef LM
+#undef PV
+#undef XX
   }
 }
 
@@ -229,13 +338,40 @@ void eigh_f32(int n, float *A, float *V, float *w, float *scr, cudaStream_t st) 
                                  (int)sm3));
     attr3 = sm3;
   }
-  k_tridiag_f32<<<1, kTriThreads, sm1, st>>>(n, A, dg, eg, taug, hv);
+  const bool tr = std::getenv("HQCGB_TRACE") != nullptr;
+  cudaEvent_t ev[4];
+  if (tr)
+    for (auto &x : ev) cudaEventCreate(&x);
+  if (tr) cudaEventRecord(ev[0], st);
+  const size_t smt = ((size_t)n * (n + 1) / 2 + 5 * (size_t)n) * sizeof(float);
+  if (smt <= 200 * 1024) {
+    static size_t attr1 = 0;
+    if (smt > attr1) {
+      HQ_CUDA(cudaFuncSetAttribute(k_tridiag_f32_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smt));
+      attr1 = smt;
+    }
+    k_tridiag_f32_smem<<<1, kTriThreads, smt, st>>>(n, A, dg, eg, taug, hv);
+  } else {
+    k_tridiag_f32<<<1, kTriThreads, sm1, st>>>(n, A, dg, eg, taug, hv);
+  }
   HQ_LAUNCH_CHECK();
+  if (tr) cudaEventRecord(ev[1], st);
   // Z (tridiagonal eigenvectors) goes to V, then V = Q Z in place per tile
   k_tri_eig_f32<<<1, kTriThreads, sm2, st>>>(n, dg, eg, w, V, lu);
   HQ_LAUNCH_CHECK();
+  if (tr) cudaEventRecord(ev[2], st);
   k_backtransform_f32<<<ceil_div(n, 32), 256, sm3, st>>>(n, hv, taug, V, V);
   HQ_LAUNCH_CHECK();
+  if (tr) {
+    cudaEventRecord(ev[3], st);
+    cudaEventSynchronize(ev[3]);
+    float t[3];
+    for (int k = 0; k < 3; ++k) cudaEventElapsedTime(&t[k], ev[k], ev[k + 1]);
+    fprintf(stderr, "  fp32 tridiag %.3f ms, bisection+inverse iteration %.3f ms, back %.3f ms\n", t[0],
+            t[1], t[2]);
+    for (auto &x : ev) cudaEventDestroy(x);
+  }
 }
 
 }  // namespace hqcgb

@@ -16,6 +16,7 @@
 // or three; all of it is FP64 GEMM work spread over many SMs.  The result
 // stands in for jnp.linalg.eigh (hqc/pbc/scf.py:69,138,198).
 #include <algorithm>
+#include <chrono>
 #include <cstdlib>
 
 #include "common.cuh"
@@ -358,9 +359,14 @@ static double oa_iteration(int n, const double *A, double *X, double *w, MixedEi
   double em[13];
   HQ_CUDA(cudaMemcpyAsync(em, ws.emax, 13 * sizeof(double), cudaMemcpyDeviceToHost, st));
   HQ_CUDA(cudaStreamSynchronize(st));
-  if (std::getenv("HQCGB_TRACE"))
-    fprintf(stderr, "  oa off=%.3e max|E|=%.3e clusters=%g%s\n", em[1], em[8 + 4], em[3],
-            em[2] != 0 ? " (cluster too large)" : "");
+  if (std::getenv("HQCGB_TRACE")) {
+    static auto t_last = std::chrono::steady_clock::now();
+    auto now = std::chrono::steady_clock::now();
+    fprintf(stderr, "  oa off=%.3e max|E|=%.3e clusters=%g%s (%.3f ms since last)\n", em[1], em[8 + 4],
+            em[3], em[2] != 0 ? " (cluster too large)" : "",
+            std::chrono::duration<double, std::milli>(now - t_last).count());
+    t_last = now;
+  }
   return em[1];
 }
 
@@ -384,7 +390,23 @@ bool eigh_mixed(int n, const double *A, double *V, double *w, MixedEigWork &ws, 
     HQ_CUDA(cudaStreamSynchronize(st));
     if (hs < 0) return false;
   } else {
+    const bool tr = std::getenv("HQCGB_TRACE") != nullptr;
+    cudaEvent_t e0, e1;
+    if (tr) {
+      cudaEventCreate(&e0);
+      cudaEventCreate(&e1);
+      cudaEventRecord(e0, st);
+    }
     eigh_f32(n, ws.A32, ws.V32, ws.w32, ws.f32scr, st);
+    if (tr) {
+      cudaEventRecord(e1, st);
+      cudaEventSynchronize(e1);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      fprintf(stderr, "  fp32 stage %.3f ms\n", ms);
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+    }
   }
   k_f32_to_f64<<<ceil_div(nn, 256), 256, 0, st>>>(nn, ws.V32, V);
   HQ_LAUNCH_CHECK();

@@ -108,7 +108,7 @@ void launch_poisson_f32(const double *src, double *dst, float2 *cbuf, const doub
                         const double2 *tw, cudaStream_t st);
 
 // grid_mixed.cu
-void launch_phi32(const double *F, const double *coef, const int *ao_l, const int *ao_cart,
+void launch_phi32(const float *F32, const double *coef, const int *ao_l, const int *ao_cart,
                   int nao_atom, int nprim, int nao, int ng, long long ld, float *phi, float *dphi,
                   cudaStream_t st);
 void launch_to_f32(const double *in, long long ldi, long long N, int rows, double scale, float *out,

@@ -1,7 +1,7 @@
 // Small dense FP64 linear algebra of the SCF loop (n_ao <= 1024).
 //
 //  * gemm: C = alpha op(A) diag(d) op(B) + beta C   (hqc/pbc/scf.py:68,137,197;
-//    solver.py:575-577, 700)
+//    solver.py:575-577, 700); cuBLAS DGEMM without the diagonal
 //  * jacobi_eigh: symmetric eigensolver, parallel cyclic Jacobi with
 //    round-robin pair ordering, one block per matrix, ascending eigenvalues
 //    (stands in for jnp.linalg.eigh; eigenvectors differ only by gauge)
@@ -9,6 +9,8 @@
 //    (hqc/pbc/scf.py:174-194)
 //  * occupations: Fermi / Gauss smearing with the reference's bisection and
 //    Newton chemical-potential searches, quirks kept (hqc/tools/smearing.py)
+#include <cublas_v2.h>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -54,10 +56,30 @@ __global__ void k_gemm(int ta, int tb, int M, int N, int K, double alpha,
   }
 }
 
+// Plain FP64 GEMMs (no diagonal) go to cuBLAS: row-major C = op(A) op(B) is
+// column-major C^T = op(B)^T op(A)^T.  One handle per host thread (batch
+// workers run their own threads and streams).
+static cublasHandle_t blas_handle() {
+  static thread_local cublasHandle_t h = nullptr;
+  if (!h) {
+    if (cublasCreate(&h) != CUBLAS_STATUS_SUCCESS)
+      throw Error{HQCGB_CUDA_ERROR, "cublasCreate failed"};
+  }
+  return h;
+}
+
 void gemm(bool ta, bool tb, int M, int N, int K, double alpha, const double *A, int lda,
           const double *B, int ldb, const double *d, double beta, double *C, int ldc,
           cudaStream_t st) {
   HQ_STAGE(ST_GEMM_SMALL, st);
+  if (!d) {
+    cublasHandle_t h = blas_handle();
+    cublasSetStream(h, st);
+    cublasStatus_t r = cublasDgemm(h, tb ? CUBLAS_OP_T : CUBLAS_OP_N, ta ? CUBLAS_OP_T : CUBLAS_OP_N,
+                                   N, M, K, &alpha, B, ldb, A, lda, &beta, C, ldc);
+    if (r != CUBLAS_STATUS_SUCCESS) throw Error{HQCGB_CUDA_ERROR, "cublasDgemm failed"};
+    return;
+  }
   dim3 grid(ceil_div(N, 32), ceil_div(M, 32));
   k_gemm<<<grid, 256, 0, st>>>(ta, tb, M, N, K, alpha, A, lda, B, ldb, d, beta, C, ldc);
   HQ_LAUNCH_CHECK();

@@ -292,9 +292,9 @@ static void create(const hqcgb_params *in, hqcgb_plan *p) {
     p->mew.wbuf = p->alloc<double>(2 * nn);
     p->mew.iwork = p->alloc<int>(5 * (size_t)nao + 1);
     p->c1_prev = p->alloc<double>(nn);
+    p->F1d32 = p->alloc<float>((size_t)n * 3 * p->ng * P.n_prim * 6);
     if (p->orb_forces) {
       p->psi32 = p->alloc<float>((size_t)(p->gga ? 4 : 1) * tc_psi_max(false) * N);
-      p->F1d32 = p->alloc<float>((size_t)n * 3 * p->ng * P.n_prim * 6);
       p->Y32 = p->alloc<float>((size_t)nao * tc_psi_max(false));
     }
   }
@@ -555,7 +555,8 @@ static void geometry(Ctx &c, const double *xp_dev) {
     launch_phi(p->F1d, p->coef, p->ao_l, p->ao_cart, p->nb, p->nprim, n, p->ng, p->phi, p->dphi,
                c.st);
   if (p->mixed) {
-    launch_phi32(p->F1d, p->coef, p->ao_l, p->ao_cart, p->nb, p->nprim, n, p->ng, p->ld, p->phi32,
+    launch_to_float((long long)p->n * 3 * p->ng * P.n_prim * 6, p->F1d, p->F1d32, c.st);
+    launch_phi32(p->F1d32, p->coef, p->ao_l, p->ao_cart, p->nb, p->nprim, n, p->ng, p->ld, p->phi32,
                  p->dphi32, c.st);
     launch_transpose_phi(p->phi32, n, N, p->ld, p->phiT32, c.st);
     if (p->gga)
@@ -715,7 +716,6 @@ static void orbital_forces(Ctx &c, double *grad) {
   launch_xc_pointwise(P.xc, p->rho, p->gga ? p->grho : nullptr, p->vh, N, p->dV, p->wq, p->vxc,
                       p->gga ? p->u : nullptr, p->xpart, st);
   launch_add3(N, p->vloc, p->vh, p->vxc, p->veff, st);
-  launch_to_float((long long)p->n * 3 * p->ng * P.n_prim * 6, p->F1d, p->F1d32, st);
   launch_force_operand(p->C, p->occ, p->nao, p->nuse_kept, p->npsi_kept, p->Y32, st);
   launch_force_grid_orb(p->F1d32, p->coef, p->ao_l, p->ao_cart, p->n, p->nb, p->nprim, p->ng,
                         p->veff, p->gga ? p->u : nullptr, p->psi32, p->Y32, p->npsi_kept, p->dV,
