@@ -188,7 +188,8 @@ __global__ void __launch_bounds__(1024) k_oa_clusters(int n, const double *__res
         diag += B[a * k + a] * B[a * k + a];
         for (int b = a + 1; b < k; ++b) offd += B[a * k + b] * B[a * k + b];
       }
-      if (offd <= 1e-34 * diag || offd == 0.0) break;
+      // rounding level: off-diagonal entries ~1e-15 of the diagonal
+      if (offd <= 1e-30 * diag || offd == 0.0) break;
       for (int a = 0; a < k - 1; ++a)
         for (int b = a + 1; b < k; ++b) {
           double bab = B[a * k + b];
