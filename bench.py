@@ -52,6 +52,29 @@ def workload(seed):
     return h54_bcc_pbe(noise_seed=seed)
 
 
+def shard_seeds(rank, steps, batch):
+    """Noise seeds of this rank's configurations, step by step: ranks never
+    share a configuration (weak scaling: each rank runs its own batches)."""
+    return [[100000 * rank + 1000 * s + b for b in range(batch)] for s in range(steps)]
+
+
+def max_over_ranks(ms, device):
+    """The slowest rank's time (every rank gets it)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return ms
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(world, batch, steps, ms):
+    """Whole-job evaluations per second: every rank's configurations over the
+    slowest rank's time."""
+    return world * batch * steps / (ms / 1000.0)
+
+
 def dist_info():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -175,7 +198,7 @@ def run_ours(args):
     N = pes.solver.plan.ng ** 3
     # per-step batches of B configurations (new noise seeds), resident on the device
     total = args.warmup + args.steps
-    seeds = [[100000 * rank + 1000 * s + b for b in range(B)] for s in range(total)]
+    seeds = shard_seeds(rank, total, B)
     batches = [torch.as_tensor(np.stack([workload(x)["xp"] for x in ss]), device="cuda")
                for ss in seeds]
     iters = []
@@ -212,11 +235,8 @@ def run_ours(args):
     stats = _lib.stage_stats()
     _lib.profile(0)
     pes.solver.plan.set_concurrency(conc)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * B * args.steps / (ms / 1000.0)
+    ms = max_over_ranks(ms, "cuda")
+    value = job_throughput(world, B, args.steps, ms)
     # device time per evaluation by stage, configurations run one at a time
     stage_ms = {k: round(v[1] / B, 3) for k, v in stats.items() if v[0]}
 

@@ -675,6 +675,11 @@ __global__ void k_transpose_phi(const float *__restrict__ phi, int nao, long lon
 // (ncomp npsi columns each).
 // ---------------------------------------------------------------------------
 constexpr int kPsiMaxN = 64;
+constexpr int kPsiPW = 4;                       // producer warps (copies + TF32 split)
+constexpr int kPsiProducers = kPsiPW * 32;
+constexpr int kPsiRowsPerThread = kM * 8 / kPsiProducers;  // A rows per producer thread
+constexpr int kPsiMmaWarp = kPsiPW + 4;         // after the 4 drain warps
+constexpr int kPsiThreads = kPsiProducers + kDrainers + 32;
 constexpr int kPsiRing = 4;
 constexpr size_t kPsiAPieces = 2 * kTile;                       // A hi, A lo
 constexpr size_t kPsiBPiece = (size_t)kPsiMaxN * 128;           // one B piece
@@ -706,7 +711,7 @@ struct PsiPipe {
 };
 
 template <int NPSI>
-__global__ void __launch_bounds__(kThreads, 1) k_tc_psi_density(PsiArgs a) {
+__global__ void __launch_bounds__(kPsiThreads, 1) k_tc_psi_density(PsiArgs a) {
   extern __shared__ __align__(1024) char smraw[];
   char *sm = (char *)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
   __shared__ PsiPipe P;
@@ -725,7 +730,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_psi_density(PsiArgs a) {
 
   if (tid == 0) {
     for (int b = 0; b < kPsiRing; ++b) {
-      mbar_init(&P.full[b], kProducers);
+      mbar_init(&P.full[b], kPsiProducers);
       mbar_init(&P.empty[b], 1);
     }
     for (int b = 0; b < 4; ++b) {
@@ -734,14 +739,14 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_psi_density(PsiArgs a) {
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 8) tmem_alloc(&P.tmem_base, tcols);
+  if (warp == kPsiMmaWarp) tmem_alloc(&P.tmem_base, tcols);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
 
   bool ok = true;
-  if (warp < 4) {
-    // producer: A chunks (row (tid>>3) + 16 j, 16-byte chunk tid & 7), then
+  if (warp < kPsiPW) {
+    // producer: A chunks (row (tid>>3) + 32 j, 16-byte chunk tid & 7), then
     // this thread's share of the B piece chunks (rows of Y^T)
     const int cch = tid & 7;
     const int bchunks = NPSI * 8;  // per piece
@@ -754,15 +759,15 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_psi_density(PsiArgs a) {
       const long long g0 = (blockIdx.x + t * gridDim.x) * (long long)kM;
       const float *src = comp == 0 ? a.phiT : a.dphiT + (long long)(comp - 1) * a.N * a.ldk;
 #pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        int row = (tid >> 3) + 16 * j;
+      for (int j = 0; j < kPsiRowsPerThread; ++j) {
+        int row = (tid >> 3) + (kPsiProducers / 8) * j;
         long long g = g0 + row;
         uint32_t off = swz(row, cch);
         const float *gp = src + (g < a.N ? g : 0) * (long long)a.ldk + kb * kStageK + cch * 4;
         if (g < a.N) cp_async16(base + off, gp);
         else cp_async_zero16(base + off, src);
       }
-      for (int c = tid; c < 2 * bchunks; c += kProducers) {
+      for (int c = tid; c < 2 * bchunks; c += kPsiProducers) {
         int piece = c / bchunks, cc = c % bchunks, row = cc >> 3, ch = cc & 7;
         const float *gp = a.Yhl + ((long long)piece * NPSI + row) * a.ldk + kb * kStageK + ch * 4;
         cp_async16(base + (uint32_t)(kPsiAPieces + piece * kPsiBPiece) + swz(row, ch), gp);
@@ -778,8 +783,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_psi_density(PsiArgs a) {
       if (ok) {
         char *base = sm + (st % kPsiRing) * kPsiStageBytes;
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          int row = (tid >> 3) + 16 * j;
+        for (int j = 0; j < kPsiRowsPerThread; ++j) {
+          int row = (tid >> 3) + (kPsiProducers / 8) * j;
           uint32_t off = swz(row, cch);
           float4 v = *reinterpret_cast<float4 *>(base + off);
           store_split4(base, row, cch, v);
@@ -797,7 +802,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_psi_density(PsiArgs a) {
       cp_async_commit();
     }
     cp_async_wait<0>();
-  } else if (warp < 8) {
+  } else if (warp < kPsiPW + 4) {
     // drains and epilogue: thread = grid point (TMEM lane).  Group G of this
     // CTA is (tile, component, K blocks [g0, g0 + DR)) and lives in slot G % RA.
     const int row = (warp & 3) * 32 + lane;
@@ -934,7 +939,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc_psi_density(PsiArgs a) {
   }
   tc_fence_before();
   __syncthreads();
-  if (warp == 8) {
+  if (warp == kPsiMmaWarp) {
     tc_fence_after();
     tmem_dealloc(P.tmem_base, tcols);
   }
@@ -1000,10 +1005,10 @@ void launch_tc_psi_density(const float *phiT, const float *dphiT, const float *Y
   long long ntiles = ceil_div(N, tc::kM);
   int grid = (int)std::min<long long>(ntiles, nsm);
   switch (npsi) {
-    case 16: tc::k_tc_psi_density<16><<<grid, tc::kThreads, tc::kPsiSmem, st>>>(a); break;
-    case 32: tc::k_tc_psi_density<32><<<grid, tc::kThreads, tc::kPsiSmem, st>>>(a); break;
-    case 48: tc::k_tc_psi_density<48><<<grid, tc::kThreads, tc::kPsiSmem, st>>>(a); break;
-    default: tc::k_tc_psi_density<64><<<grid, tc::kThreads, tc::kPsiSmem, st>>>(a); break;
+    case 16: tc::k_tc_psi_density<16><<<grid, tc::kPsiThreads, tc::kPsiSmem, st>>>(a); break;
+    case 32: tc::k_tc_psi_density<32><<<grid, tc::kPsiThreads, tc::kPsiSmem, st>>>(a); break;
+    case 48: tc::k_tc_psi_density<48><<<grid, tc::kPsiThreads, tc::kPsiSmem, st>>>(a); break;
+    default: tc::k_tc_psi_density<64><<<grid, tc::kPsiThreads, tc::kPsiSmem, st>>>(a); break;
   }
   HQ_LAUNCH_CHECK();
 }

@@ -197,3 +197,24 @@ def test_h16_dzvp_pbe_forces_match_oracle():
     assert abs(float(out[3]) - ro[3]) < 1e-8
     np.testing.assert_allclose(_np(out[2]), ro[2], atol=1e-6)
     np.testing.assert_allclose(g, electronic_gradient(ref), atol=1e-7)
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("mixed", 2e-6)])
+def test_energy_periodic_in_lattice_translations(precision, tol):
+    """Shifting every proton by a lattice vector is the same crystal: the
+    energy and the forces are unchanged (the reference checks the
+    periodicity of its GTO values, test/test_pbc_gto.py:116-127)."""
+    from hqc_gb300 import make_solver
+    n, rs = 8, 1.5
+    L = (4 / 3 * np.pi * n) ** (1 / 3)
+    xp = np.random.default_rng(21).uniform(0, L, (n, 3))
+    s = make_solver(n, L, rs, "gth-dzv", grid_length=L * rs / 30, dft=True, xc="pbe", tol=1e-9,
+                    precision=precision, forces=True)
+    e0 = float(s(xp)[3])
+    g0 = _np(s.plan.forces())
+    shifted = xp + np.array([L, 0.0, -2 * L])
+    shifted[3] -= np.array([0.0, L, 0.0])
+    e1 = float(s(shifted)[3])
+    g1 = _np(s.plan.forces())
+    assert abs(e1 - e0) < tol
+    np.testing.assert_allclose(g1, g0, atol=max(tol, 1e-9))
