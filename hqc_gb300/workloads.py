@@ -58,3 +58,18 @@ def h32_dzv_lda(seed=1):
     return dict(n=n, L=L, rs=rs, basis="gth-dzv", dft=True, xc="lda,vwn",
                 grid_length=L * rs / 64.0, smearing=True, smearing_method="gauss",
                 smearing_sigma=sigma, xp=uniform(n, seed))
+
+
+def hf_fermi(n=16, rs=1.4, seed=3, count=3, grid=None):
+    """Configuration family 4 at one density: H16 (or H32) dzv Hartree-Fock
+    with Fermi smearing at 5000 K (sigma = 0.5 * 5000 / 157888.09 Ha), 49^3
+    grid for H16 (65^3 for H32) unless `grid` points per side are given;
+    `count` configurations of the family, seeded uniformly in the box."""
+    L = box(n)
+    sigma = 0.5 * 5000 / 157888.09
+    if grid is None:
+        grid = 48.0 if n == 16 else 64.0
+    rng = np.random.default_rng(seed)
+    return dict(n=n, L=L, rs=rs, basis="gth-dzv", dft=False, grid_length=L * rs / grid,
+                smearing=True, smearing_method="fermi", smearing_sigma=sigma,
+                xps=rng.uniform(0.0, L, (count, n, 3)))

@@ -199,11 +199,15 @@ def test_h16_dzvp_pbe_forces_match_oracle():
     np.testing.assert_allclose(g, electronic_gradient(ref), atol=1e-7)
 
 
-@pytest.mark.parametrize("precision,tol", [("fp64", 1e-10), ("mixed", 2e-6)])
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-7), ("mixed", 2e-6)])
 def test_energy_periodic_in_lattice_translations(precision, tol):
-    """Shifting every proton by a lattice vector is the same crystal: the
-    energy and the forces are unchanged (the reference checks the
-    periodicity of its GTO values, test/test_pbc_gto.py:116-127)."""
+    """Shifting protons by lattice vectors is the same crystal: energy and
+    forces agree (the reference checks the periodicity of its GTO values,
+    test/test_pbc_gto.py:116-127).  Not to rounding: like the reference, the
+    engine does not wrap positions into the box (hqc/pbc/solver.py:722) and
+    sums S and T over a fixed sphere of lattice vectors of radius 24 Bohr
+    (solver.py:162-176), so a shift changes which far images of the most
+    diffuse primitives are included, by about exp(-mu (24 - |R|)^2) ~ 1e-8."""
     from hqc_gb300 import make_solver
     n, rs = 8, 1.5
     L = (4 / 3 * np.pi * n) ** (1 / 3)
@@ -217,4 +221,4 @@ def test_energy_periodic_in_lattice_translations(precision, tol):
     e1 = float(s(shifted)[3])
     g1 = _np(s.plan.forces())
     assert abs(e1 - e0) < tol
-    np.testing.assert_allclose(g1, g0, atol=max(tol, 1e-9))
+    np.testing.assert_allclose(g1, g0, atol=1e-6)
