@@ -46,7 +46,8 @@ EXPORTS = ("hqcgb_plan_create", "hqcgb_plan_destroy", "hqcgb_scf", "hqcgb_scf_ba
            "hqcgb_forces", "hqcgb_ewald", "hqcgb_plan_query", "hqcgb_last_error",
            "hqcgb_launch_count", "hqcgb_profile", "hqcgb_stage_stats", "hqcgb_eigh",
            "hqcgb_eigh_noalloc", "hqcgb_eigh_mixed", "hqcgb_tc_quadrature", "hqcgb_tc_density",
-           "hqcgb_tc_orbital_density", "hqcgb_plan_set_concurrency", "hqcgb_pes_batch")
+           "hqcgb_tc_orbital_density", "hqcgb_plan_set_concurrency", "hqcgb_pes_batch",
+           "hqcgb_ao_points", "hqcgb_slater")
 N_STAGES = 14
 
 _lib = None
@@ -75,6 +76,14 @@ def load():
                                     ctypes.POINTER(ScfOut), ctypes.c_void_p]
     lib.hqcgb_forces.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
     lib.hqcgb_plan_set_concurrency.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.hqcgb_ao_points.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, c_double_p, c_double_p,
+                                    c_int_p, c_int_p, ctypes.c_int, c_double_p, ctypes.c_void_p,
+                                    ctypes.c_longlong, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                    ctypes.c_void_p]
+    lib.hqcgb_slater.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, c_double_p, c_double_p,
+                                 c_int_p, c_int_p, ctypes.c_int, c_double_p, ctypes.c_int, ctypes.c_int,
+                                 ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                 c_int_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
     lib.hqcgb_pes_batch.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                     ctypes.POINTER(ScfOut), ctypes.c_void_p, ctypes.c_void_p]
     lib.hqcgb_ewald.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_double,

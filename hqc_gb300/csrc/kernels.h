@@ -86,6 +86,10 @@ void launch_gga_psi(const double *dphi, const double *u, int nao, long long N, d
 void launch_add3(long long N, const double *a, const double *b, const double *c, double *out,
                  cudaStream_t st);
 
+void gemm_batched_rowmajor(int M, int N, int K, const double *A, int lda, long long sa,
+                           const double *B, int ldb, long long sb, double *C, int ldc, long long sc,
+                           int batch, cudaStream_t st);
+
 // eigh_fp64.cu / eigh_mixed.cu
 void eigh_tql_f32(int n, int batch, float *A, float *V, float *w, float *work, int *status,
                   cudaStream_t st);

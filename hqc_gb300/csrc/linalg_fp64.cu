@@ -85,6 +85,20 @@ void gemm(bool ta, bool tb, int M, int N, int K, double alpha, const double *A, 
   HQ_LAUNCH_CHECK();
 }
 
+// C[b] = A[b] B[b] for row-major M x K and K x N blocks (strides in elements;
+// stride 0 shares a block): cuBLAS strided-batched DGEMM, column-major view.
+void gemm_batched_rowmajor(int M, int N, int K, const double *A, int lda, long long sa,
+                           const double *B, int ldb, long long sb, double *C, int ldc, long long sc,
+                           int batch, cudaStream_t st) {
+  HQ_STAGE(ST_GEMM_SMALL, st);
+  cublasHandle_t h = blas_handle();
+  cublasSetStream(h, st);
+  const double one = 1.0, zero = 0.0;
+  cublasStatus_t r = cublasDgemmStridedBatched(h, CUBLAS_OP_N, CUBLAS_OP_N, N, M, K, &one, B, ldb, sb,
+                                               A, lda, sa, &zero, C, ldc, sc, batch);
+  if (r != CUBLAS_STATUS_SUCCESS) throw Error{HQCGB_CUDA_ERROR, "cublasDgemmStridedBatched failed"};
+}
+
 // out = a*X + b*Y (+ c*Z^T): generic elementwise combos on n x n matrices.
 __global__ void k_axpby(int n, double a, const double *__restrict__ X, double b,
                         const double *__restrict__ Y, int transY, double *__restrict__ out) {

@@ -121,6 +121,27 @@ int hqcgb_plan_set_concurrency(hqcgb_plan *plan, int workers);
 int hqcgb_pes_batch(hqcgb_plan *plan, int n_cfg, const double *xp, const hqcgb_scf_out *out,
                     double *grad, void *stream);
 
+/* AO values of n_atoms protons at npts points (electron positions), Gamma
+ * point: the reference's eval_pbc_ao (hqc/pbc/gto.py:326-369) with the 1D
+ * lattice lat1d of make_pbc_gto (tmax = rcut // L).  Basis tables as in the
+ * plan parameters, host pointers; xp [ngroups][n_atoms][3], xe [npts][3] (device,
+ * Bohr), pts_per_group consecutive points per proton set; out
+ * [npts][n_atoms * nao_atom] (device). */
+int hqcgb_ao_points(int n_atoms, int nao_atom, int n_prim, const double *alpha,
+                    const double *coef, const int *ao_l, const int *ao_cart, int n_lat1d,
+                    const double *lat1d, const double *xp, long long npts, int pts_per_group,
+                    const double *xe, double *out, void *stream);
+
+/* Slater matrices of W walkers (make_slater, hqc/pbc/slater.py:42-104,
+ * Gamma): up[w] = AO(xe[w][0:n/2]) mo[:, state_idx[0:n/2]] and dn[w] the
+ * same for electrons n/2..n-1 and state_idx[n/2:n].  xp [xp_groups][n][3]
+ * (xp_groups 1 or W), xe [W][n][3] (device, Bohr); mo [nao][nmo] row-major
+ * (device); state_idx [n] (host); up, dn [W][n/2][n/2] (device). */
+int hqcgb_slater(int n, int nao_atom, int n_prim, const double *alpha, const double *coef,
+                 const int *ao_l, const int *ao_cart, int n_lat1d, const double *lat1d, int W,
+                 int xp_groups, const double *xp, const double *xe, const double *mo, int nmo,
+                 const int *state_idx, double *up, double *dn, void *stream);
+
 /* Nuclear gradient dE/dR [n_atoms][3] (Hartree/Bohr, device) of the last SCF.
  * No counterpart in the reference (forces are absent there,
  * doc/solver_algorithm.md:1210); with Fermi smearing it is the gradient of
