@@ -24,6 +24,9 @@
 // of 128 columns.  Every mbarrier wait has an iteration limit: on expiry the
 // kernel records an error code in *err, stops issuing work, waits (bounded)
 // for its MMAs, frees TMEM and returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <algorithm>
 
 #include "common.cuh"
@@ -666,20 +669,22 @@ __global__ void k_transpose_phi(const float *__restrict__ phi, int nao, long lon
 // stage s of a CTA is (tile, component, K block).
 //
 // Accuracy.  The tensor core's FP32 accumulation truncates, so sums of many
-// MMAs drift low (about half an ulp per instruction).  Every stage therefore
-// accumulates in its own TMEM slot -- the large hi*hi products and the
-// 2^-11 smaller cross products in separate accumulators -- and the epilogue
-// warps drain each stage into compensated (TwoSum) FP32 sums S + C kept in
-// TMEM per component; psi = S + C is formed in FP64 at the end of a tile.
-// TMEM: a ring of RA stage slots of 2 npsi columns, then S and C
-// (ncomp npsi columns each).
+// MMAs drift low (about half an ulp per instruction).  Every group of DR
+// K blocks therefore accumulates in its own TMEM slot -- the large hi*hi
+// products and the 2^-11 smaller cross products in separate accumulators --
+// and the epilogue warps drain each group into compensated (TwoSum) FP32
+// sums held in registers for the current component; psi = S + C is rounded
+// to FP32 once (unbiased) and rho, grad rho are summed in FP64.
+// Loads: bulk tensor copies (TMA) issued by one thread into a 4-stage ring.
+// TMEM: a ring of up to 8 accumulator slots of 2 npsi columns.
 // ---------------------------------------------------------------------------
 constexpr int kPsiMaxN = 64;
-constexpr int kPsiPW = 4;                       // producer warps (copies + TF32 split)
+constexpr int kPsiPW = 4;                       // splitter warps (in-place TF32 split)
 constexpr int kPsiProducers = kPsiPW * 32;
-constexpr int kPsiRowsPerThread = kM * 8 / kPsiProducers;  // A rows per producer thread
+constexpr int kPsiRowsPerThread = kM * 8 / kPsiProducers;  // A rows per splitter thread
 constexpr int kPsiMmaWarp = kPsiPW + 4;         // after the 4 drain warps
-constexpr int kPsiThreads = kPsiProducers + kDrainers + 32;
+constexpr int kPsiTmaWarp = kPsiMmaWarp + 1;    // one thread issues the bulk tensor loads
+constexpr int kPsiThreads = kPsiProducers + kDrainers + 64;
 constexpr int kPsiRing = 4;
 constexpr size_t kPsiAPieces = 2 * kTile;                       // A hi, A lo
 constexpr size_t kPsiBPiece = (size_t)kPsiMaxN * 128;           // one B piece
@@ -698,20 +703,37 @@ struct PsiArgs {
   int *err;
 };
 
-// TMEM stage-slot ring depth for (npsi, ncomp); 0 when it does not fit.
+// TMEM accumulator-slot ring depth for npsi (2 npsi columns per slot).
 __host__ __device__ inline int psi_ring(int npsi, int ncomp) {
-  for (int ra = 4; ra >= 2; ra -= 2)
-    if (ra * 2 * npsi + 2 * ncomp * npsi <= 512) return ra;
-  return 0;
+  (void)ncomp;
+  int ra = 512 / (2 * npsi);
+  return ra > 8 ? 8 : ra;
 }
 
 struct PsiPipe {
-  uint64_t full[kPsiRing], empty[kPsiRing], acc_full[4], acc_empty[4];
+  uint64_t loaded[kPsiRing], full[kPsiRing], empty[kPsiRing], acc_full[8], acc_empty[8];
   uint32_t tmem_base;
 };
 
+// TMA: bulk tensor copy of one box of a 2D tensor map into shared memory,
+// completion counted in bytes on an mbarrier.
+__device__ inline void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ inline void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
 template <int NPSI>
-__global__ void __launch_bounds__(kPsiThreads, 1) k_tc_psi_density(PsiArgs a) {
+__global__ void __launch_bounds__(kPsiThreads, 1)
+    k_tc_psi_density(PsiArgs a, const __grid_constant__ CUtensorMap tmA,
+                     const __grid_constant__ CUtensorMap tmD, const __grid_constant__ CUtensorMap tmY) {
   extern __shared__ __align__(1024) char smraw[];
   char *sm = (char *)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
   __shared__ PsiPipe P;
@@ -723,17 +745,17 @@ __global__ void __launch_bounds__(kPsiThreads, 1) k_tc_psi_density(PsiArgs a) {
   const long long S = my_tiles * per_tile;
   const int RA = psi_ring(NPSI, a.ncomp);
   const int DR = a.drain;  // K blocks of 32 accumulated per TMEM slot before a drain
-  const uint32_t colS = (uint32_t)(RA * 2 * NPSI), colC = colS + (uint32_t)(a.ncomp * NPSI);
-  const int ncols = (int)colC + a.ncomp * NPSI;
+  const int ncols = RA * 2 * NPSI;
   int tcols = 32;
   while (tcols < ncols) tcols <<= 1;
 
   if (tid == 0) {
     for (int b = 0; b < kPsiRing; ++b) {
+      mbar_init(&P.loaded[b], 1);
       mbar_init(&P.full[b], kPsiProducers);
       mbar_init(&P.empty[b], 1);
     }
-    for (int b = 0; b < 4; ++b) {
+    for (int b = 0; b < 8; ++b) {
       mbar_init(&P.acc_full[b], 1);
       mbar_init(&P.acc_empty[b], kDrainers);
     }
@@ -745,43 +767,39 @@ __global__ void __launch_bounds__(kPsiThreads, 1) k_tc_psi_density(PsiArgs a) {
   tc_fence_after();
 
   bool ok = true;
-  if (warp < kPsiPW) {
-    // producer: A chunks (row (tid>>3) + 32 j, 16-byte chunk tid & 7), then
-    // this thread's share of the B piece chunks (rows of Y^T)
-    const int cch = tid & 7;
-    const int bchunks = NPSI * 8;  // per piece
-    const uint32_t sbase = smem_u32(sm);
-    auto issue = [&](long long st) {
-      const int slot = (int)(st % kPsiRing);
-      const uint32_t base = sbase + slot * (uint32_t)kPsiStageBytes;
-      const long long t = st / per_tile;
-      const int r = (int)(st % per_tile), comp = r / nkb, kb = r % nkb;
-      const long long g0 = (blockIdx.x + t * gridDim.x) * (long long)kM;
-      const float *src = comp == 0 ? a.phiT : a.dphiT + (long long)(comp - 1) * a.N * a.ldk;
-#pragma unroll
-      for (int j = 0; j < kPsiRowsPerThread; ++j) {
-        int row = (tid >> 3) + (kPsiProducers / 8) * j;
-        long long g = g0 + row;
-        uint32_t off = swz(row, cch);
-        const float *gp = src + (g < a.N ? g : 0) * (long long)a.ldk + kb * kStageK + cch * 4;
-        if (g < a.N) cp_async16(base + off, gp);
-        else cp_async_zero16(base + off, src);
+  if (warp == kPsiTmaWarp) {
+    // loads: stage s of this CTA is (tile, component, K block); the A box
+    // (128 grid points x 32 AOs, raw fp32) lands in the stage's high-piece
+    // slot in the 128-byte-swizzled K-major layout, the two pieces of Y^T in
+    // the B slots.  Rows past the grid read as zero (OOB fill).
+    if (lane == 0) {
+      const uint32_t bytes = (uint32_t)kTile + 2u * NPSI * 128u;
+      for (long long st = 0; st < S; ++st) {
+        const int slot = (int)(st % kPsiRing);
+        const long long use = st / kPsiRing;
+        if (ok && use > 0 && !mbar_wait(&P.empty[slot], (unsigned)((use - 1) & 1), a.err, 25))
+          ok = false;
+        if (!ok) break;
+        const long long t = st / per_tile;
+        const int r = (int)(st % per_tile), comp = r / nkb, kb = r % nkb;
+        const int g0 = (int)((blockIdx.x + t * gridDim.x) * (long long)kM);
+        const uint32_t base = smem_u32(sm + slot * kPsiStageBytes);
+        mbar_expect_tx(&P.loaded[slot], bytes);
+        if (comp == 0) tma_load_2d(base, &tmA, kb * kStageK, g0, &P.loaded[slot]);
+        else tma_load_2d(base, &tmD, kb * kStageK, (int)((comp - 1) * a.N) + g0, &P.loaded[slot]);
+        tma_load_2d(base + (uint32_t)kPsiAPieces, &tmY, kb * kStageK, 0, &P.loaded[slot]);
+        tma_load_2d(base + (uint32_t)(kPsiAPieces + kPsiBPiece), &tmY, kb * kStageK, NPSI,
+                    &P.loaded[slot]);
       }
-      for (int c = tid; c < 2 * bchunks; c += kPsiProducers) {
-        int piece = c / bchunks, cc = c % bchunks, row = cc >> 3, ch = cc & 7;
-        const float *gp = a.Yhl + ((long long)piece * NPSI + row) * a.ldk + kb * kStageK + ch * 4;
-        cp_async16(base + (uint32_t)(kPsiAPieces + piece * kPsiBPiece) + swz(row, ch), gp);
-      }
-    };
-    constexpr int L = kPsiRing - 1;  // copies in flight ahead of the split
-    for (int st = 0; st < L; ++st) {
-      if (st < S) issue(st);
-      cp_async_commit();
     }
+  } else if (warp < kPsiPW) {
+    // splitters: raw fp32 -> TF32 hi (in place) and lo pieces of the A box
+    const int cch = tid & 7;
     for (long long st = 0; st < S; ++st) {
-      cp_async_wait<L - 1>();
+      const int slot = (int)(st % kPsiRing);
+      if (ok && !mbar_wait(&P.loaded[slot], (unsigned)((st / kPsiRing) & 1), a.err, 21)) ok = false;
       if (ok) {
-        char *base = sm + (st % kPsiRing) * kPsiStageBytes;
+        char *base = sm + slot * kPsiStageBytes;
 #pragma unroll
         for (int j = 0; j < kPsiRowsPerThread; ++j) {
           int row = (tid >> 3) + (kPsiProducers / 8) * j;
@@ -791,25 +809,22 @@ __global__ void __launch_bounds__(kPsiThreads, 1) k_tc_psi_density(PsiArgs a) {
         }
       }
       fence_proxy_async();
-      mbar_arrive(&P.full[st % kPsiRing]);
-      long long nx = st + L;
-      if (nx < S) {
-        long long use = nx / kPsiRing;
-        if (ok && use > 0 && !mbar_wait(&P.empty[nx % kPsiRing], (unsigned)((use - 1) & 1), a.err, 21))
-          ok = false;
-        issue(nx);
-      }
-      cp_async_commit();
+      mbar_arrive(&P.full[slot]);
     }
-    cp_async_wait<0>();
   } else if (warp < kPsiPW + 4) {
     // drains and epilogue: thread = grid point (TMEM lane).  Group G of this
-    // CTA is (tile, component, K blocks [g0, g0 + DR)) and lives in slot G % RA.
+    // CTA is (tile, component, K blocks [g0, g0 + DR)) and lives in slot
+    // G % RA.  The compensated sums of the current component stay in
+    // registers; psi (the value component) is kept for the gradient products.
     const int row = (warp & 3) * 32 + lane;
     const uint32_t tbase = P.tmem_base + ((uint32_t)((warp & 3) * 32) << 16);
     long long G = 0;
     for (long long t = 0; t < my_tiles; ++t) {
+      const long long g = (blockIdx.x + t * gridDim.x) * (long long)kM + row;
+      float p0[NPSI];
+      double rho = 0, gr[3] = {0, 0, 0};
       for (int comp = 0; comp < a.ncomp; ++comp) {
+        float sv[NPSI], cv[NPSI];
         for (int g0 = 0; g0 < nkb; g0 += DR, ++G) {
           const int b = (int)(G % RA);
           const long long use = G / RA;
@@ -818,86 +833,47 @@ __global__ void __launch_bounds__(kPsiThreads, 1) k_tc_psi_density(PsiArgs a) {
           tc_fence_after();
           if (got) {
             const uint32_t slot = tbase + (uint32_t)(b * 2 * NPSI);
-            const uint32_t sc = tbase + colS + (uint32_t)(comp * NPSI);
-            const uint32_t cc = tbase + colC + (uint32_t)(comp * NPSI);
 #pragma unroll
             for (int c0 = 0; c0 < NPSI; c0 += 16) {
-              uint32_t vb[16], vs[16], ss[16], cs[16];
+              uint32_t vb[16], vs[16];
               tmem_ld16_nowait(slot + c0, vb);
               tmem_ld16_nowait(slot + NPSI + c0, vs);
-              if (g0 > 0) {
-                tmem_ld16_nowait(sc + c0, ss);
-                tmem_ld16_nowait(cc + c0, cs);
-              }
               tmem_wait_ld();
-              float so[16], co[16];
 #pragma unroll
               for (int i = 0; i < 16; ++i) {
-                float big = __uint_as_float(vb[i]), small = __uint_as_float(vs[i]);
+                const float big = __uint_as_float(vb[i]), small = __uint_as_float(vs[i]);
                 if (g0 == 0) {
-                  so[i] = big;
-                  co[i] = small;
+                  sv[c0 + i] = big;
+                  cv[c0 + i] = small;
                 } else {
-                  so[i] = __uint_as_float(ss[i]);
-                  co[i] = __uint_as_float(cs[i]);
-                  two_sum_add(so[i], co[i], big);
-                  co[i] += small;
+                  two_sum_add(sv[c0 + i], cv[c0 + i], big);
+                  cv[c0 + i] += small;
                 }
               }
-              tmem_st16(sc + c0, so);
-              tmem_st16(cc + c0, co);
             }
-            tmem_wait_st();
           }
           tc_fence_before();
           mbar_arrive(&P.acc_empty[b]);
         }
-      }
-      {  // tile complete: psi = S + C for every component
-        const long long g = (blockIdx.x + t * gridDim.x) * (long long)kM + row;
+        // component complete: value = S + C (FP32, rounded once)
         if (ok) {
-          double psi[NPSI];
-          double rho = 0;
 #pragma unroll
-          for (int c0 = 0; c0 < NPSI; c0 += 16) {
-            double v[16];
-            uint32_t ss[16], cs[16];
-            tmem_ld16_nowait(tbase + colS + c0, ss);
-            tmem_ld16_nowait(tbase + colC + c0, cs);
-            tmem_wait_ld();
-#pragma unroll
-            for (int i = 0; i < 16; ++i) {
-              v[i] = (double)__uint_as_float(ss[i]) + (double)__uint_as_float(cs[i]);
-              psi[c0 + i] = v[i];
-              rho += v[i] * v[i];
+          for (int k = 0; k < NPSI; ++k) {
+            const float v = sv[k] + cv[k];
+            if (comp == 0) {
+              p0[k] = v;
+              rho += (double)v * (double)v;
+            } else {
+              gr[comp - 1] += (double)p0[k] * (double)v;
             }
-            if (a.psi_out && g < a.N)
-#pragma unroll
-              for (int i = 0; i < 16; ++i) a.psi_out[(long long)(c0 + i) * a.N + g] = (float)v[i];
-          }
-          double gr[3] = {0, 0, 0};
-          for (int comp2 = 1; comp2 < a.ncomp; ++comp2) {
-#pragma unroll
-            for (int c0 = 0; c0 < NPSI; c0 += 16) {
-              uint32_t ss[16], cs[16];
-              tmem_ld16_nowait(tbase + colS + (uint32_t)(comp2 * NPSI + c0), ss);
-              tmem_ld16_nowait(tbase + colC + (uint32_t)(comp2 * NPSI + c0), cs);
-              tmem_wait_ld();
-#pragma unroll
-              for (int i = 0; i < 16; ++i) {
-                const double dv = (double)__uint_as_float(ss[i]) + (double)__uint_as_float(cs[i]);
-                gr[comp2 - 1] += psi[c0 + i] * dv;
-                if (a.psi_out && g < a.N)
-                  a.psi_out[(long long)(comp2 * NPSI + c0 + i) * a.N + g] = (float)dv;
-              }
-            }
-          }
-          if (g < a.N) {
-            a.rho[g] = rho;
-            if (a.ncomp > 1)
-              for (int c = 0; c < 3; ++c) a.grho[(long long)c * a.N + g] = 2.0 * gr[c];
+            if (a.psi_out && g < a.N) a.psi_out[(long long)(comp * NPSI + k) * a.N + g] = v;
           }
         }
+      }
+      if (ok && g < a.N) {
+        a.rho[g] = rho;
+        if (a.ncomp > 1)
+          for (int c = 0; c < 3; ++c) a.grho[(long long)c * a.N + g] = 2.0 * gr[c];
       }
     }
   } else if (lane == 0) {
@@ -962,6 +938,35 @@ __global__ void k_psi_operand(const double *__restrict__ C, const double *__rest
 
 }  // namespace tc
 
+namespace tc {
+// 2D row-major fp32 tensor [rows][ld] as a TMA map with boxes of 32 x box_rows
+// and 128-byte swizzle (the UMMA K-major canonical layout of a 32-element
+// K block); out-of-range rows read as zero.  The driver's encoder is looked
+// up at run time (no link-time dependency on the driver library).
+CUtensorMap tensor_map_2d(const float *base, long long ld, long long rows, int box_rows) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  if (!encode) {
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    HQ_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
+    HQ_REQUIRE(fn && q == cudaDriverEntryPointSuccess, "cuTensorMapEncodeTiled unavailable");
+    encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }
+  HQ_REQUIRE(((uintptr_t)base & 15) == 0, "TMA base must be 16-byte aligned");
+  HQ_REQUIRE(ld % 32 == 0, "TMA row stride must be a multiple of 32 floats");
+  CUtensorMap m;
+  cuuint64_t dims[2] = {(cuuint64_t)ld, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)ld * sizeof(float)};
+  cuuint32_t box[2] = {(cuuint32_t)kStageK, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = encode(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(base), dims, strides,
+                      box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) throw Error{HQCGB_CUDA_ERROR, "cuTensorMapEncodeTiled failed"};
+  return m;
+}
+}  // namespace tc
+
 // ---------------------------------------------------------------------------
 int tc_psi_max(bool gga) { return gga ? 32 : tc::kPsiMaxN; }
 int tc_psi_width(int nuse) { return ceil_div(nuse, 16) * 16; }
@@ -1002,13 +1007,18 @@ void launch_tc_psi_density(const float *phiT, const float *dphiT, const float *Y
   a.psi_out = psi_out;
   a.drain = psi_drain;
   HQ_REQUIRE(!grho || dphiT, "GGA density needs the gradient operand");
+  HQ_REQUIRE(N <= (1LL << 29), "grid too large for 32-bit TMA row coordinates");
+  // boxes of 32 fp32 (128 B, the swizzle span) x rows; row strides ldk * 4 B
+  CUtensorMap tmA = tc::tensor_map_2d(phiT, ldk, N, tc::kM);
+  CUtensorMap tmD = tc::tensor_map_2d(grho ? dphiT : phiT, ldk, grho ? 3 * N : N, tc::kM);
+  CUtensorMap tmY = tc::tensor_map_2d(Yhl, ldk, 2LL * npsi, npsi);
   long long ntiles = ceil_div(N, tc::kM);
   int grid = (int)std::min<long long>(ntiles, nsm);
   switch (npsi) {
-    case 16: tc::k_tc_psi_density<16><<<grid, tc::kPsiThreads, tc::kPsiSmem, st>>>(a); break;
-    case 32: tc::k_tc_psi_density<32><<<grid, tc::kPsiThreads, tc::kPsiSmem, st>>>(a); break;
-    case 48: tc::k_tc_psi_density<48><<<grid, tc::kPsiThreads, tc::kPsiSmem, st>>>(a); break;
-    default: tc::k_tc_psi_density<64><<<grid, tc::kPsiThreads, tc::kPsiSmem, st>>>(a); break;
+    case 16: tc::k_tc_psi_density<16><<<grid, tc::kPsiThreads, tc::kPsiSmem, st>>>(a, tmA, tmD, tmY); break;
+    case 32: tc::k_tc_psi_density<32><<<grid, tc::kPsiThreads, tc::kPsiSmem, st>>>(a, tmA, tmD, tmY); break;
+    case 48: tc::k_tc_psi_density<48><<<grid, tc::kPsiThreads, tc::kPsiSmem, st>>>(a, tmA, tmD, tmY); break;
+    default: tc::k_tc_psi_density<64><<<grid, tc::kPsiThreads, tc::kPsiSmem, st>>>(a, tmA, tmD, tmY); break;
   }
   HQ_LAUNCH_CHECK();
 }
