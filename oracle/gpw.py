@@ -52,26 +52,33 @@ class Setup:
         self.coul = self.VG * self.Omega  # 4 pi / G^2 with G=0 -> 0
 
     # ------------------------------------------------------------------
-    def gto1d(self, xp, lextra=0):
+    def gto1d(self, xp, lextra=0, kpt=None):
         """Lattice-summed 1D factors ``hqc/pbc/gto.py:326-339``.
 
         Returns g[A, d, i, a, l] = sum_t u^l exp(-alpha_a u^2), u = x_i - R_Ad - t,
-        for l = 0 .. lmax + lextra.
+        for l = 0 .. lmax + lextra.  With a k-point each term also carries the
+        Bloch phase exp(i k_d t) (``eval_pbc_gaussian_power_x_kpt``,
+        gto.py:371-388) and the result is complex.
         """
         lm = self.basis.lmax + lextra
         u = self.x1d[None, None, :, None] - xp[:, :, None, None] - self.lat1d[None, None, None, :]
         e = np.exp(-self.basis.alpha[None, None, None, :, None] * (u ** 2)[..., None, :])
+        if kpt is not None:
+            ph = np.exp(1j * np.asarray(kpt, dtype=float)[:, None] * self.lat1d[None, :])  # (d,t)
+            e = e * ph[None, :, None, None, :]
         pw = np.stack([u ** l for l in range(lm + 1)], axis=-1)  # (A,d,i,t,l)
         return np.einsum("Aditl,Adiat->Adial", pw, e)
 
-    def ao_grid(self, xp, deriv=0, atoms=None):
+    def ao_grid(self, xp, deriv=0, atoms=None, kpt=None):
         """AO values on the grid, ``hqc/pbc/gto.py:341-369`` on Rmesh.
 
         deriv=0: Phi (nao, ng, ng, ng); deriv=1 also grad (3, nao, ...);
         deriv=2 also the hessian (6, nao, ...) ordered xx, yy, zz, xy, xz, yz.
+        With a k-point the Bloch sums of gto.py:390-427 (complex).
         """
         b = self.basis
-        g = self.gto1d(xp, lextra=deriv)  # (A,3,n,a,l)
+        g = self.gto1d(xp, lextra=deriv, kpt=kpt)  # (A,3,n,a,l)
+        dt = complex if kpt is not None else float
         alpha = b.alpha
 
         def d1(gd, l):
@@ -89,9 +96,9 @@ class Setup:
 
         atoms = list(range(self.n)) if atoms is None else list(atoms)
         nao, ng = len(atoms) * b.nao, self.ng
-        phi = np.zeros((nao, ng, ng, ng))
-        grad = np.zeros((3, nao, ng, ng, ng)) if deriv >= 1 else None
-        hess = np.zeros((6, nao, ng, ng, ng)) if deriv >= 2 else None
+        phi = np.zeros((nao, ng, ng, ng), dtype=dt)
+        grad = np.zeros((3, nao, ng, ng, ng), dtype=dt) if deriv >= 1 else None
+        hess = np.zeros((6, nao, ng, ng, ng), dtype=dt) if deriv >= 2 else None
         pairs = [(0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2)]
         for ia, A in enumerate(atoms):
             for k in range(b.nao):
@@ -118,7 +125,7 @@ class Setup:
         return phi, grad, hess
 
     # ------------------------------------------------------------------
-    def overlap_kinetic(self, xp, deriv=False):
+    def overlap_kinetic(self, xp, deriv=False, kpt=None):
         """Analytic lattice-summed S and T, ``hqc/pbc/solver.py:240-389``.
 
         The reference obtains p-type integrals by ``jacfwd`` of the s-type
@@ -126,6 +133,9 @@ class Setup:
         derivatives are taken in closed form (Hermite derivatives of
         exp(-mu |R+t|^2)).  With deriv=True also returns dS, dT of shape
         (n_atoms, 3, nao, nao): derivative with respect to atom A's position.
+        With a k-point every lattice term carries exp(-i k.t)
+        (``_eval_intermediate_integral_kpt``, solver.py:257-274) and S, T are
+        complex Hermitian.
         """
         b = self.basis
         a = b.alpha
@@ -133,15 +143,17 @@ class Setup:
         mu = a[:, None] * a[None, :] / asum
         K = np.pi ** 1.5 / asum ** 1.5
         nb = b.nao
-        S = np.zeros((self.nao, self.nao))
-        T = np.zeros((self.nao, self.nao))
-        dS = np.zeros((self.n, 3, self.nao, self.nao)) if deriv else None
-        dT = np.zeros((self.n, 3, self.nao, self.nao)) if deriv else None
+        dt = complex if kpt is not None else float
+        phase = None if kpt is None else np.exp(-1j * self.lattice @ np.asarray(kpt, dtype=float))
+        S = np.zeros((self.nao, self.nao), dtype=dt)
+        T = np.zeros((self.nao, self.nao), dtype=dt)
+        dS = np.zeros((self.n, 3, self.nao, self.nao), dtype=dt) if deriv else None
+        dT = np.zeros((self.n, 3, self.nao, self.nao), dtype=dt) if deriv else None
         order = 3 if deriv else 2
         for i in range(self.n):
             for j in range(self.n):
                 R = xp[i] - xp[j]
-                fs, fk = _hermite_lattice(R, self.lattice, mu, K, order)
+                fs, fk = _hermite_lattice(R, self.lattice, mu, K, order, phase)
                 Sb, Tb = _sp_block(b, fs, fk, 0)
                 S[i * nb:(i + 1) * nb, j * nb:(j + 1) * nb] = Sb
                 T[i * nb:(i + 1) * nb, j * nb:(j + 1) * nb] = Tb
@@ -178,16 +190,20 @@ class Setup:
         return (np.fft.ifftn(vG) * self.N).real
 
 
-def _hermite_lattice(R, lattice, mu, K, order):
+def _hermite_lattice(R, lattice, mu, K, order, phase=None):
     """Derivatives up to ``order`` of f(R) = sum_t K e^{-mu|R+t|^2} (overlap)
     and g(R) = sum_t K mu (3 - 2 mu |R+t|^2) e^{-mu|R+t|^2} (kinetic).
 
     Returns lists fs, fk where index k holds the k-th derivative tensor with
     the primitive-pair axes last: shapes (), (3,), (3,3), (3,3,3) + mu.shape.
+    ``phase`` (complex, one per lattice vector) weights each term; the
+    derivatives act on the Gaussian only, as the phase does not depend on R.
     """
     u = R[None, :] + lattice  # (t,3)
     u2 = (u ** 2).sum(1)
     E = K[None] * np.exp(-mu[None] * u2[:, None, None])  # (t,a,b)
+    if phase is not None:
+        E = E * phase[:, None, None]
     I = np.eye(3)
     m = mu[None]
     fs = [E.sum(0)]
@@ -236,7 +252,7 @@ def _sp_block(b, fs, fk, extra, c=None):
     ia = 1.0 / b.alpha
     out = []
     for f in (fs, fk):
-        M = np.zeros((nb, nb))
+        M = np.zeros((nb, nb), dtype=np.result_type(f[0], float))
         for p in range(nb):
             for q in range(nb):
                 lp, lq = b.l[p], b.l[q]
@@ -353,8 +369,17 @@ def entropy(occ, eps=1e-15):
 # ----------------------------------------------------------------------
 # The solver
 # ----------------------------------------------------------------------
+def _tr(A, D):
+    """Re tr(A D) (the reference's ``einsum('pq,qp', A, dm).real``)."""
+    if np.iscomplexobj(A) or np.iscomplexobj(D):
+        return float(np.real(np.sum(A * D.T)))
+    return np.sum(A * D)
+
+
 class Solver:
-    """``make_solver`` (solver.py:14-978), Gamma point, streamed form."""
+    """``make_solver`` (solver.py:14-978), streamed form: the Gamma point
+    (``hf_gamma`` / ``dft_gamma``) and, when ``solve`` is given a k-point,
+    ``hf_kpt`` / ``dft_kpt`` (solver.py:769-962) with complex AOs."""
 
     def __init__(self, n, L, rs, basis, rcut=24, tol=1e-7, max_cycle=100, grid_length=0.12,
                  diis=True, diis_space=8, diis_start_cycle=1, diis_damp=0.0, dft=False,
@@ -374,39 +399,42 @@ class Solver:
 
     # grid pieces --------------------------------------------------------
     def density(self, D, phi, grad=None):
-        """rho = sum_pq D_pq phi_p phi_q (solver.py:690), as X = D phi (BLAS)."""
+        """rho = Re sum_pq D_pq phi_p phi_q^* (solver.py:690), as X = D phi^*
+        (BLAS); grad rho = 2 Re sum_pq D_pq grad phi_p phi_q^*."""
         shp = phi.shape
         P = phi.reshape(shp[0], -1)
-        X = (D @ P)
-        rho = np.einsum("pg,pg->g", P, X).reshape(shp[1:])
+        X = (D @ P.conj())
+        rho = np.einsum("pg,pg->g", P, X).real.reshape(shp[1:])
         X = X.reshape(shp)
         if grad is None:
             return rho, None, X
         grho = 2 * np.einsum("dpg,pg->dg", grad.reshape(3, shp[0], -1),
-                             X.reshape(shp[0], -1)).reshape((3,) + shp[1:])
+                             X.reshape(shp[0], -1)).real.reshape((3,) + shp[1:])
         return rho, grho, X
 
     def quadrature(self, w, phi):
-        """V_pq = dV sum_r phi_p w phi_q (solver.py:693)."""
+        """V_pq = dV sum_r phi_p^* w phi_q (solver.py:693)."""
         P = phi.reshape(phi.shape[0], -1)
-        return self.st.dV * ((P * w.reshape(1, -1)) @ P.T)
+        return self.st.dV * ((P.conj() * w.reshape(1, -1)) @ P.T)
 
     def hartree(self, rho, phi):
         vh = self.st.poisson(rho)
         return self.quadrature(vh, phi), vh
 
     def exchange(self, D, C, occ, phi, Stilde):
-        """K_pq = sum_i f_i dV sum_r (phi_p psi_i) W_qi + Madelung K0
-        (equals ``exchange(eris + eris0, dm)``, solver.py:430-431, 604-614)."""
+        """K_pq = sum_i f_i dV sum_r (phi_p^* psi_i) W_qi^* + Madelung K0 with
+        W_qi = v_H[phi_q^* psi_i] (equals ``exchange(eris + eris0, dm)``,
+        solver.py:430-431, 509-524, 604-614; the Gamma point drops the
+        conjugations)."""
         st = self.st
         K = np.zeros_like(D)
         for i in range(C.shape[1]):
             if occ[i] <= self.exx_thr:
                 continue
             psi = np.einsum("p,pijk->ijk", C[:, i], phi)
-            pair = phi * psi[None]
+            pair = phi.conj() * psi[None]
             W = st.poisson(pair)
-            K += occ[i] * st.dV * (pair.reshape(pair.shape[0], -1) @ W.reshape(W.shape[0], -1).T)
+            K += occ[i] * st.dV * (pair.reshape(pair.shape[0], -1) @ W.reshape(W.shape[0], -1).conj().T)
         K0 = 4 * np.pi / st.L * MADELUNG_SC * (Stilde @ D @ Stilde)
         return K + K0
 
@@ -418,33 +446,35 @@ class Solver:
         if self.xc.gga:
             u = 2 * vsig[None] * grho  # 2 v_sigma grad rho
             Y = np.einsum("dg,dpg->pg", u.reshape(3, -1), grad.reshape(3, grad.shape[1], -1))
-            M = self.st.dV * (Y @ phi.reshape(phi.shape[0], -1).T)
-            V = V + M + M.T
+            M = self.st.dV * (Y.conj() @ phi.reshape(phi.shape[0], -1).T)
+            V = V + M + M.conj().T
         return Exc, V
 
     # solve --------------------------------------------------------------
-    def setup_geometry(self, xp_rs):
+    def setup_geometry(self, xp_rs, kpt=None):
         st = self.st
         xp = np.asarray(xp_rs, dtype=float) * st.rs
-        S, T, _, _ = st.overlap_kinetic(xp)
+        S, T, _, _ = st.overlap_kinetic(xp, kpt=kpt)
         need_grad = self.dft and self.xc.gga
-        phi, grad, _ = st.ao_grid(xp, deriv=1 if need_grad else 0)
+        phi, grad, _ = st.ao_grid(xp, deriv=1 if need_grad else 0, kpt=kpt)
         vloc = st.vloc_grid(xp)
         V = self.quadrature(vloc, phi)
         P = phi.reshape(phi.shape[0], -1)
         return dict(xp=xp, S=S, T=T, phi=phi, grad=grad, vloc=vloc, V=V,
-                    Stilde=st.dV * (P @ P.T))
+                    Stilde=st.dV * (P.conj() @ P.T))
 
-    def solve(self, xp_rs):
-        g = self.setup_geometry(xp_rs)
+    def solve(self, xp_rs, kpt=None):
+        """One SCF; ``kpt`` (3,) in 1/Bohr selects the k-point solver."""
+        g = self.setup_geometry(xp_rs, kpt)
         S, T, V, phi, grad = g["S"], g["T"], g["V"], g["phi"], g["grad"]
+        cplx = np.iscomplexobj(S)
         w, u = np.linalg.eigh(S)
         v = u @ np.diag(w ** -0.5)
         H = T + V
         occf = self.occ
 
         def dmat(C, e):
-            return C @ np.diag(occf(e)) @ C.T
+            return C @ np.diag(occf(e)) @ C.conj().T
 
         def veff(D, C, e):
             rho = self.density(D, phi)[0]
@@ -454,11 +484,15 @@ class Solver:
             else:
                 K = self.exchange(D, C, occf(e), phi, g["Stilde"])
                 Vxc = -0.5 * K
-                Exc = 0.5 * np.sum(Vxc * D)
+                Exc = 0.5 * _tr(Vxc, D)
             return J, Exc, Vxc
 
         def diag(F):
-            e, c = np.linalg.eigh(v.T @ F @ v)
+            F1 = v.conj().T @ F @ v
+            if cplx:
+                # jnp.linalg.eigh symmetrises its input: (F1 + F1^H) / 2
+                F1 = 0.5 * (F1 + F1.conj().T)
+            e, c = np.linalg.eigh(F1)
             return v @ c, e
 
         C, e = diag(H)
@@ -469,9 +503,9 @@ class Solver:
             C, e, E, conv = self._fixed_point(H, D, C, e, diag, dmat, veff)
         D = dmat(C, e)
         J, Exc, _ = veff(D, C, e)
-        Ki = np.sum(T * D)
-        Vep = np.sum(V * D)
-        Vee = 0.5 * np.sum(J * D) + Exc
+        Ki = _tr(T, D)
+        Vep = _tr(V, D)
+        Vee = 0.5 * _tr(J, D) + Exc
         Se = entropy(occf(e))
         self.last = dict(g=g, C=C, e=e, D=D, occ=occf(e), E=E, v=v)
         return C, D, e * RY, E * RY, Ki * RY, Vep * RY, Vee * RY, Se, conv
@@ -481,7 +515,7 @@ class Solver:
         E0, E1, loop = 0.0, 1.0, 0
         while abs(E1 - E0) > self.tol and loop < self.max_cycle:
             J, Exc, Vxc = veff(D, C, e)
-            Enew = 0.5 * np.sum((2 * H + J) * D) + Exc
+            Enew = 0.5 * _tr(2 * H + J, D) + Exc
             C, e = diag(H + J + Vxc)
             D = dmat(C, e)
             E0, E1, loop = E1, Enew, loop + 1
@@ -501,7 +535,7 @@ class Solver:
             C, e = diag(Fk[-1])
             D = dmat(C, e)
             J, Exc, Vxc = veff(D, C, e)
-            Enew = 0.5 * np.sum((2 * H + J) * D) + Exc
+            Enew = 0.5 * _tr(2 * H + J, D) + Exc
             F = H + J + Vxc
             err = S @ D @ F - F @ D @ S
             Fk = Fk[1:] + [F]
@@ -510,14 +544,15 @@ class Solver:
         E0 = E1 - 1.0
         while ((abs(E1 - E0) > self.tol) or (np.linalg.norm(ek[-1]) > 10 * self.tol)) \
                 and loop < self.max_cycle:
+            # no conjugation: complex-symmetric B for complex error vectors
             B = np.einsum("imn,jmn->ij", np.array(ek), np.array(ek))
             eta = 1e-12 * (np.trace(B) / sp + 1.0)
             B = B + eta * np.eye(sp)
-            h = np.zeros((sp + 1, sp + 1))
+            h = np.zeros((sp + 1, sp + 1), dtype=B.dtype)
             h[:sp, :sp] = B
             h[:sp, sp] = -1
             h[sp, :sp] = -1
-            gvec = np.zeros(sp + 1)
+            gvec = np.zeros(sp + 1, dtype=B.dtype)
             gvec[sp] = -1
             c = np.linalg.solve(h, gvec)[:sp]
             Fx = np.einsum("k,kab->ab", c, np.array(Fk))
@@ -525,7 +560,7 @@ class Solver:
             C, e = diag(Fx)
             D = dmat(C, e)
             J, Exc, Vxc = veff(D, C, e)
-            Enew = 0.5 * np.sum((2 * H + J) * D) + Exc
+            Enew = 0.5 * _tr(2 * H + J, D) + Exc
             F = H + J + Vxc
             err = S @ D @ F - F @ D @ S
             Fk = Fk[1:] + [F]

@@ -39,6 +39,41 @@ def test_solver_matches_reference(name):
             assert abs(out[i] - z[k]) < 1e-8, k
 
 
+@pytest.mark.parametrize("name", ["hf_kpt_dzv", "dft_kpt_dzv"])
+def test_kpoint_solver_matches_reference(name):
+    """``hf_kpt`` / ``dft_kpt`` (solver.py:769-962): complex Bloch AOs, complex
+    DIIS with the reference's unconjugated B matrix; the density matrix is
+    gauge invariant, mo_coeff only up to a phase per column."""
+    meta, z = load_golden(name)
+    kw = dict(meta["kwargs"])
+    assert kw.pop("gamma") is False
+    s = Solver(meta["n"], float(z["L"]), meta["rs"], meta["basis"], **kw)
+    out = s.solve(z["xp"], z["kpt"])
+    assert bool(out[8]) == bool(z["converged"])
+    assert abs(out[3] - z["E"]) < 1e-9
+    np.testing.assert_allclose(out[2], z["bands"], atol=1e-7)
+    np.testing.assert_allclose(out[1], z["dm"], atol=1e-7)
+    for k, i in (("Ki", 4), ("Vep", 5), ("Vee", 6), ("Se", 7)):
+        assert abs(out[i] - z[k]) < 1e-8, k
+    # columns equal up to a phase: |c_ref^H S c| = 1 (non-degenerate bands)
+    S = s.last["g"]["S"]
+    ov = np.abs(np.sum(z["mo_coeff"].conj() * (S @ out[0]), axis=0))
+    np.testing.assert_allclose(ov, 1.0, atol=1e-7)
+
+
+def test_kpoint_gamma_limit():
+    """k = 0 through the complex path equals the Gamma solver."""
+    meta, z = load_golden("hf_dzv_diis")
+    kw = dict(meta["kwargs"])
+    s = Solver(meta["n"], float(z["L"]), meta["rs"], meta["basis"], **kw)
+    g = s.solve(z["xp"])
+    k = s.solve(z["xp"], np.zeros(3))
+    assert abs(g[3] - k[3]) < 1e-10
+    np.testing.assert_allclose(g[2], k[2], atol=1e-9)
+    np.testing.assert_allclose(g[1], k[1].real, atol=1e-9)
+    assert np.abs(k[1].imag).max() < 1e-12
+
+
 @pytest.mark.parametrize("name", ["hf_dzv_gauss_bisect", "hf_h8_dzv_gauss_bisect"])
 def test_gauss_smearing_quirk_not_converged(name):
     """Gaussian occupations are capped at 1 in the reference (smearing.py:52);
