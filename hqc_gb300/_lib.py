@@ -47,7 +47,8 @@ EXPORTS = ("hqcgb_plan_create", "hqcgb_plan_destroy", "hqcgb_scf", "hqcgb_scf_ba
            "hqcgb_launch_count", "hqcgb_profile", "hqcgb_stage_stats", "hqcgb_eigh",
            "hqcgb_eigh_noalloc", "hqcgb_eigh_mixed", "hqcgb_tc_quadrature", "hqcgb_tc_density",
            "hqcgb_tc_orbital_density", "hqcgb_plan_set_concurrency", "hqcgb_pes_batch",
-           "hqcgb_ao_points", "hqcgb_slater")
+           "hqcgb_ao_points", "hqcgb_slater", "hqcgb_kplan_create", "hqcgb_kplan_destroy",
+           "hqcgb_scf_kpt", "hqcgb_scf_kpt_batch", "hqcgb_kplan_query", "hqcgb_eigh_herm")
 N_STAGES = 14
 
 _lib = None
@@ -92,6 +93,17 @@ def load():
     lib.hqcgb_plan_query.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p,
                                      ctypes.c_size_t, ctypes.c_void_p]
     lib.hqcgb_plan_query.restype = ctypes.c_longlong
+    lib.hqcgb_kplan_create.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(ctypes.c_void_p)]
+    lib.hqcgb_kplan_destroy.argtypes = [ctypes.c_void_p]
+    lib.hqcgb_scf_kpt.argtypes = [ctypes.c_void_p, ctypes.c_void_p, c_double_p,
+                                  ctypes.POINTER(ScfOut), ctypes.c_void_p]
+    lib.hqcgb_scf_kpt_batch.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, c_double_p,
+                                        ctypes.POINTER(ScfOut), ctypes.c_void_p]
+    lib.hqcgb_kplan_query.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p,
+                                      ctypes.c_size_t, ctypes.c_void_p]
+    lib.hqcgb_kplan_query.restype = ctypes.c_longlong
+    lib.hqcgb_eigh_herm.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                    ctypes.c_void_p, ctypes.c_void_p]
     lib.hqcgb_last_error.restype = ctypes.c_char_p
     lib.hqcgb_launch_count.argtypes = [ctypes.c_int]
     lib.hqcgb_launch_count.restype = ctypes.c_longlong
@@ -157,6 +169,26 @@ def eigh(A):
     st = ctypes.c_void_p(torch.cuda.current_stream(A.device).cuda_stream)
     check(lib.hqcgb_eigh(n, b, ctypes.c_void_p(A3.data_ptr()), ctypes.c_void_p(w.data_ptr()),
                          ctypes.c_void_p(V.data_ptr()), st))
+    return (w[0], V[0]) if single else (w, V)
+
+
+def eigh_herm(A):
+    """FP64 complex Hermitian eigendecomposition on the GPU: (w ascending,
+    V columns).  ``A`` is a complex128 CUDA tensor (n, n) or (batch, n, n);
+    both triangles are read, so it must be Hermitian."""
+    import torch
+    lib = load()
+    A = A.contiguous()
+    if A.dtype != torch.complex128:
+        raise TypeError("eigh_herm expects a complex128 tensor")
+    single = A.dim() == 2
+    A3 = A.unsqueeze(0) if single else A
+    b, n, _ = A3.shape
+    w = torch.empty(b, n, dtype=torch.float64, device=A.device)
+    V = torch.empty(b, n, n, dtype=torch.complex128, device=A.device)
+    st = ctypes.c_void_p(torch.cuda.current_stream(A.device).cuda_stream)
+    check(lib.hqcgb_eigh_herm(n, b, ctypes.c_void_p(A3.data_ptr()), ctypes.c_void_p(w.data_ptr()),
+                              ctypes.c_void_p(V.data_ptr()), st))
     return (w[0], V[0]) if single else (w, V)
 
 

@@ -20,12 +20,6 @@ namespace hqcgb {
 constexpr int kEigThreads = 1024;
 
 
-__device__ inline double e_hypot(double a, double b) { return hypot(a, b); }
-__device__ inline float e_hypot(float a, float b) { return hypotf(a, b); }
-template <typename T> struct EigEps;
-template <> struct EigEps<double> { static constexpr double v = 1e-16; };
-template <> struct EigEps<float> { static constexpr float v = 6e-8f; };
-
 // T = double: the FP64 solver; T = float: the first stage of the mixed solver.
 template <typename T>
 __global__ void __launch_bounds__(kEigThreads)
@@ -58,95 +52,7 @@ __global__ void __launch_bounds__(kEigThreads)
   __syncthreads();
 
   // ---------------- 2. implicit QL ----------------
-  for (int l = 0; l < n; ++l) {
-    int iter = 0;
-    while (true) {
-      if (tid == 0) {
-        int m;
-        for (m = l; m < n - 1; ++m) {
-          T dd = fabs(d[m]) + fabs(d[m + 1]);
-          if (fabs(e[m]) <= EigEps<T>::v * dd) break;
-        }
-        int nrot = 0, lo = l;
-        if (m != l) {
-          if (iter++ >= 60) {
-            fail = 1;
-            m = l;
-          } else {
-            T g = (d[l + 1] - d[l]) / (T(2) * e[l]);
-            T r = e_hypot(g, T(1));
-            g = d[m] - d[l] + e[l] / (g + e_copysign(r, g));
-            T s = T(1), c = T(1), pp = T(0);
-            int i;
-            bool early = false;
-            for (i = m - 1; i >= l; --i) {
-              T f = s * e[i], b = c * e[i];
-              r = e_hypot(f, g);
-              e[i + 1] = r;
-              if (r == T(0)) {
-                d[i + 1] -= pp;
-                e[m] = T(0);
-                early = true;
-                break;
-              }
-              s = f / r;
-              c = g / r;
-              g = d[i + 1] - pp;
-              r = (d[i] - g) * s + T(2) * c * b;
-              pp = s * r;
-              d[i + 1] = g + pp;
-              g = c * r - b;
-              rc[nrot] = c;
-              rs[nrot] = s;
-              ++nrot;
-            }
-            lo = early ? i + 1 : l;
-            if (!early) {
-              d[l] -= pp;
-              e[l] = g;
-              e[m] = T(0);
-            }
-          }
-        }
-        s_int[0] = m;
-        s_int[1] = nrot;
-        s_int[2] = lo;
-        s_int[3] = fail;
-      }
-      __syncthreads();
-      int m = s_int[0], nrot = s_int[1];
-      fail = s_int[3];
-      // apply the rotations of this sweep: rotation t acts on columns
-      // (i, i+1) with i = m-1-t; thread k owns row k of Z
-      if (nrot > 0) {
-        // batches of RB rotations: the RB loads of a batch are independent
-        // and issued together; the carried element stays in a register
-        constexpr int RB = sizeof(T) == 8 ? 16 : 32;
-        for (int k = tid; k < n; k += nt) {
-          T cur = Zt[(long long)m * n + k];
-          for (int t0 = 0; t0 < nrot; t0 += RB) {
-            T z[RB];
-#pragma unroll
-            for (int u = 0; u < RB; ++u)
-              if (t0 + u < nrot) z[u] = Zt[(long long)(m - 1 - t0 - u) * n + k];
-#pragma unroll
-            for (int u = 0; u < RB; ++u) {
-              if (t0 + u < nrot) {
-                int i = m - 1 - t0 - u;
-                T c = rc[t0 + u], s = rs[t0 + u];
-                Zt[(long long)(i + 1) * n + k] = s * z[u] + c * cur;
-                cur = c * z[u] - s * cur;
-              }
-            }
-          }
-          Zt[(long long)(m - nrot) * n + k] = cur;
-        }
-      }
-      __syncthreads();
-      if (m == l || fail) break;
-    }
-    if (fail) break;
-  }
+  fail = tridiag_ql<T, T>(n, d, e, Zt, rc, rs, s_int);
 
   // ---------------- 3. back-transformation ----------------
   // Z <- H_k Z for k = n-3 .. 0 on rows k+1..n-1; Zt[c][r] layout.

@@ -1,5 +1,7 @@
 // Householder reduction of a symmetric matrix to tridiagonal form (lower
-// variant), shared by the FP64 solver and the FP32 stage of the mixed solver.
+// variant), shared by the FP64 solver and the FP32 stage of the mixed solver,
+// and the implicit QL iteration on the tridiagonal, shared with the complex
+// Hermitian solver (whose tridiagonal is real).
 // One thread block; A (n x n, row-major, global) is overwritten: the
 // trailing matrix receives rank-2 updates and column k keeps the Householder
 // vector v_k below the subdiagonal (v_k[0] = 1 implied).  On return d, e,
@@ -91,6 +93,121 @@ __device__ void householder_tridiag(int n, T *__restrict__ A, T *__restrict__ d,
     tau[n - 1] = T(0);
   }
   __syncthreads();
+}
+
+__device__ inline double e_hypot(double a, double b) { return hypot(a, b); }
+__device__ inline float e_hypot(float a, float b) { return hypotf(a, b); }
+template <typename T> struct EigEps;
+template <> struct EigEps<double> { static constexpr double v = 1e-16; };
+template <> struct EigEps<float> { static constexpr float v = 6e-8f; };
+
+// a x + b y for a real scalar pair and a real or complex element
+__device__ inline double lin2(double a, double x, double b, double y) { return a * x + b * y; }
+__device__ inline float lin2(float a, float x, float b, float y) { return a * x + b * y; }
+__device__ inline double2 lin2(double a, double2 x, double b, double2 y) {
+  return make_double2(a * x.x + b * y.x, a * x.y + b * y.y);
+}
+
+// Implicit QL with Wilkinson-type shifts on the tridiagonal (d, e), one
+// block.  Each sweep's Givens rotations are computed by thread 0 (rc, rs:
+// shared, n each) and applied by all threads to the transposed eigenvector
+// matrix Zt[c][r] (E = T, or double2 for complex eigenvectors with a real
+// tridiagonal).  Returns nonzero when a sweep limit was hit.
+template <typename T, typename E>
+__device__ int tridiag_ql(int n, T *__restrict__ d, T *__restrict__ e, E *__restrict__ Zt,
+                          T *__restrict__ rc, T *__restrict__ rs, int *s_int) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  int fail = 0;
+  for (int l = 0; l < n; ++l) {
+    int iter = 0;
+    while (true) {
+      if (tid == 0) {
+        int m;
+        for (m = l; m < n - 1; ++m) {
+          T dd = fabs(d[m]) + fabs(d[m + 1]);
+          if (fabs(e[m]) <= EigEps<T>::v * dd) break;
+        }
+        int nrot = 0, lo = l;
+        if (m != l) {
+          if (iter++ >= 60) {
+            fail = 1;
+            m = l;
+          } else {
+            T g = (d[l + 1] - d[l]) / (T(2) * e[l]);
+            T r = e_hypot(g, T(1));
+            g = d[m] - d[l] + e[l] / (g + e_copysign(r, g));
+            T s = T(1), c = T(1), pp = T(0);
+            int i;
+            bool early = false;
+            for (i = m - 1; i >= l; --i) {
+              T f = s * e[i], b = c * e[i];
+              r = e_hypot(f, g);
+              e[i + 1] = r;
+              if (r == T(0)) {
+                d[i + 1] -= pp;
+                e[m] = T(0);
+                early = true;
+                break;
+              }
+              s = f / r;
+              c = g / r;
+              g = d[i + 1] - pp;
+              r = (d[i] - g) * s + T(2) * c * b;
+              pp = s * r;
+              d[i + 1] = g + pp;
+              g = c * r - b;
+              rc[nrot] = c;
+              rs[nrot] = s;
+              ++nrot;
+            }
+            lo = early ? i + 1 : l;
+            if (!early) {
+              d[l] -= pp;
+              e[l] = g;
+              e[m] = T(0);
+            }
+          }
+        }
+        s_int[0] = m;
+        s_int[1] = nrot;
+        s_int[2] = lo;
+        s_int[3] = fail;
+      }
+      __syncthreads();
+      int m = s_int[0], nrot = s_int[1];
+      fail = s_int[3];
+      // apply the rotations of this sweep: rotation t acts on columns
+      // (i, i+1) with i = m-1-t; thread k owns row k of Z
+      if (nrot > 0) {
+        // batches of RB rotations: the RB loads of a batch are independent
+        // and issued together; the carried element stays in a register
+        constexpr int RB = sizeof(E) == 4 ? 32 : 16;
+        for (int k = tid; k < n; k += nt) {
+          E cur = Zt[(long long)m * n + k];
+          for (int t0 = 0; t0 < nrot; t0 += RB) {
+            E z[RB];
+#pragma unroll
+            for (int u = 0; u < RB; ++u)
+              if (t0 + u < nrot) z[u] = Zt[(long long)(m - 1 - t0 - u) * n + k];
+#pragma unroll
+            for (int u = 0; u < RB; ++u) {
+              if (t0 + u < nrot) {
+                int i = m - 1 - t0 - u;
+                T c = rc[t0 + u], s = rs[t0 + u];
+                Zt[(long long)(i + 1) * n + k] = lin2(s, z[u], c, cur);
+                cur = lin2(c, z[u], -s, cur);
+              }
+            }
+          }
+          Zt[(long long)(m - nrot) * n + k] = cur;
+        }
+      }
+      __syncthreads();
+      if (m == l || fail) break;
+    }
+    if (fail) break;
+  }
+  return fail;
 }
 
 }  // namespace hqcgb

@@ -48,10 +48,13 @@ __device__ inline int midx_of(int m0, int m1, int m2) {
   return 0;
 }
 
-template <int NQ>
+// KPT: each lattice term also carries exp(-i k.t) (hqc/pbc/solver.py:257-274);
+// the real and imaginary sums are stored side by side, Q[(i,j,a,b)][4][kNq] =
+// {QS re, QT re, QS im, QT im}.
+template <int NQ, bool KPT>
 __global__ void k_ovl_lattice(const double *__restrict__ xp, int n, int nprim,
                               const double *__restrict__ alpha, const double *__restrict__ lattice,
-                              int nlat, double *__restrict__ Q) {
+                              int nlat, const double *__restrict__ kpt, double *__restrict__ Q) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int np2 = nprim * nprim;
   if (idx >= (long long)n * n * np2) return;
@@ -62,9 +65,12 @@ __global__ void k_ovl_lattice(const double *__restrict__ xp, int n, int nprim,
   const double asum = alpha[a] + alpha[b];
   const double mu = alpha[a] * alpha[b] / asum;
   const double K = pow(M_PI / asum, 1.5);
-  double qs[NQ], qt[NQ];
+  double qs[NQ], qt[NQ], qsi[KPT ? NQ : 1], qti[KPT ? NQ : 1];
 #pragma unroll
   for (int k = 0; k < NQ; ++k) qs[k] = qt[k] = 0.0;
+  if (KPT)
+#pragma unroll
+    for (int k = 0; k < NQ; ++k) qsi[k] = qti[k] = 0.0;
   for (int t = 0; t < nlat; ++t) {
     double u[3], u2 = 0;
     for (int d = 0; d < 3; ++d) {
@@ -74,6 +80,14 @@ __global__ void k_ovl_lattice(const double *__restrict__ xp, int n, int nprim,
     double e = mu * u2;
     if (e > 700.0) continue;
     e = K * exp(-e);
+    double ei = 0.0;
+    if (KPT) {
+      double sn, cs;
+      sincos(-(kpt[0] * lattice[t * 3] + kpt[1] * lattice[t * 3 + 1] + kpt[2] * lattice[t * 3 + 2]),
+             &sn, &cs);
+      ei = e * sn;
+      e *= cs;
+    }
     double hx[6], hy[6], hz[6];
     hermite6(mu, u[0], hx);
     hermite6(mu, u[1], hy);
@@ -81,16 +95,26 @@ __global__ void k_ovl_lattice(const double *__restrict__ xp, int n, int nprim,
 #pragma unroll
     for (int k = 0; k < NQ; ++k) {
       const int m0 = kMidx[k][0], m1 = kMidx[k][1], m2 = kMidx[k][2];
-      qs[k] += e * hx[m0] * hy[m1] * hz[m2];
-      qt[k] += e * (hx[m0 + 2] * hy[m1] * hz[m2] + hx[m0] * hy[m1 + 2] * hz[m2] +
-                    hx[m0] * hy[m1] * hz[m2 + 2]);
+      const double hs = hx[m0] * hy[m1] * hz[m2];
+      const double ht = hx[m0 + 2] * hy[m1] * hz[m2] + hx[m0] * hy[m1 + 2] * hz[m2] +
+                        hx[m0] * hy[m1] * hz[m2 + 2];
+      qs[k] += e * hs;
+      qt[k] += e * ht;
+      if (KPT) {
+        qsi[k] += ei * hs;
+        qti[k] += ei * ht;
+      }
     }
   }
-  double *out = Q + idx * (2 * kNq);
+  double *out = Q + idx * ((KPT ? 4 : 2) * kNq);
 #pragma unroll
   for (int k = 0; k < NQ; ++k) {
     out[k] = qs[k];
     out[kNq + k] = qt[k];
+    if (KPT) {
+      out[2 * kNq + k] = qsi[k];
+      out[3 * kNq + k] = qti[k];
+    }
   }
 }
 
@@ -143,8 +167,49 @@ __global__ void k_ovl_contract(int n, int nb, int nprim, const double *__restric
   }
 }
 
+// k-point contraction: complex S, T (interleaved) from the phase-weighted sums.
+__global__ void k_ovl_contract_kpt(int n, int nb, int nprim, const double *__restrict__ alpha,
+                                   const double *__restrict__ coef, const int *__restrict__ ao_l,
+                                   const int *__restrict__ ao_cart, const double *__restrict__ Q,
+                                   double2 *__restrict__ S, double2 *__restrict__ T) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)n * n * nb * nb) return;
+  const int q = (int)(idx % nb), p = (int)((idx / nb) % nb);
+  const int j = (int)((idx / ((long long)nb * nb)) % n), i = (int)(idx / ((long long)nb * nb * n));
+  const int nao = n * nb, np2 = nprim * nprim;
+  const int lp = ao_l[p], lq = ao_l[q];
+  int mb[3] = {0, 0, 0};
+  if (lp) mb[ao_cart[p]] += 1;
+  if (lq) mb[ao_cart[q]] += 1;
+  const int ks = midx_of(mb[0], mb[1], mb[2]);
+  double sS = 0, sT = 0, sSi = 0, sTi = 0;
+  const double *Qij = Q + ((long long)i * n + j) * np2 * (4 * kNq);
+  for (int a = 0; a < nprim; ++a) {
+    double ca = coef[p * nprim + a];
+    if (ca == 0.0) continue;
+    if (lp) ca *= 0.5 / alpha[a];
+    for (int b = 0; b < nprim; ++b) {
+      double cb = coef[q * nprim + b];
+      if (cb == 0.0) continue;
+      if (lq) cb *= -0.5 / alpha[b];
+      const double cc = ca * cb;
+      const double *qv = Qij + (long long)(a * nprim + b) * (4 * kNq);
+      sS += cc * qv[ks];
+      sT += cc * qv[kNq + ks];
+      sSi += cc * qv[2 * kNq + ks];
+      sTi += cc * qv[3 * kNq + ks];
+    }
+  }
+  const long long pq = (long long)(i * nb + p) * nao + (j * nb + q);
+  S[pq] = make_double2(sS, sSi);
+  T[pq] = make_double2(-0.5 * sT, -0.5 * sTi);
+}
+
 size_t ovl_scratch_doubles(int n, int nprim) {
   return (size_t)n * n * nprim * nprim * 2 * kNq;
+}
+size_t ovl_scratch_doubles_kpt(int n, int nprim) {
+  return (size_t)n * n * nprim * nprim * 4 * kNq;
 }
 
 // grad[A][c] += sum_{j,p,q} gpart(A,j,p,q) - sum_{i,p,q} gpart(i,A,p,q)
@@ -175,9 +240,11 @@ void launch_overlap_kinetic(const double *xp, int n, int nb, int nprim, const do
   HQ_STAGE(ST_OVERLAP, st);
   const long long terms = (long long)n * n * nprim * nprim;
   if (gpart)
-    k_ovl_lattice<20><<<ceil_div(terms, 128), 128, 0, st>>>(xp, n, nprim, alpha, lattice, nlat, Q);
+    k_ovl_lattice<20, false><<<ceil_div(terms, 128), 128, 0, st>>>(xp, n, nprim, alpha, lattice, nlat,
+                                                                   nullptr, Q);
   else
-    k_ovl_lattice<10><<<ceil_div(terms, 128), 128, 0, st>>>(xp, n, nprim, alpha, lattice, nlat, Q);
+    k_ovl_lattice<10, false><<<ceil_div(terms, 128), 128, 0, st>>>(xp, n, nprim, alpha, lattice, nlat,
+                                                                   nullptr, Q);
   HQ_LAUNCH_CHECK();
   const long long total = (long long)n * n * nb * nb;
   k_ovl_contract<<<ceil_div(total, 128), 128, 0, st>>>(n, nb, nprim, alpha, coef, ao_l, ao_cart, Q, S,
@@ -187,6 +254,22 @@ void launch_overlap_kinetic(const double *xp, int n, int nb, int nprim, const do
     k_reduce_pair_grad<<<n, 256, 0, st>>>(gpart, n, nb, grad);
     HQ_LAUNCH_CHECK();
   }
+}
+
+// S^k, T^k at k-point kpt (device, 1/Bohr): complex Hermitian, interleaved.
+void launch_overlap_kinetic_kpt(const double *xp, int n, int nb, int nprim, const double *alpha,
+                                const double *coef, const int *ao_l, const int *ao_cart,
+                                const double *lattice, int nlat, const double *kpt, double2 *S,
+                                double2 *T, double *Q, cudaStream_t st) {
+  HQ_STAGE(ST_OVERLAP, st);
+  const long long terms = (long long)n * n * nprim * nprim;
+  k_ovl_lattice<10, true><<<ceil_div(terms, 128), 128, 0, st>>>(xp, n, nprim, alpha, lattice, nlat,
+                                                                kpt, Q);
+  HQ_LAUNCH_CHECK();
+  const long long total = (long long)n * n * nb * nb;
+  k_ovl_contract_kpt<<<ceil_div(total, 128), 128, 0, st>>>(n, nb, nprim, alpha, coef, ao_l, ao_cart,
+                                                          Q, S, T);
+  HQ_LAUNCH_CHECK();
 }
 
 // ---------------------------------------------------------------------------

@@ -86,6 +86,17 @@ void launch_gga_psi(const double *dphi, const double *u, int nao, long long N, d
 void launch_add3(long long N, const double *a, const double *b, const double *c, double *out,
                  cudaStream_t st);
 
+void zgemm(char opa, char opb, int M, int N, int K, double2 alpha, const double2 *A, int lda,
+           const double2 *B, int ldb, double2 beta, double2 *C, int ldc, cudaStream_t st);
+size_t ovl_scratch_doubles_kpt(int n, int nprim);
+void launch_overlap_kinetic_kpt(const double *xp, int n, int nb, int nprim, const double *alpha,
+                                const double *coef, const int *ao_l, const int *ao_cart,
+                                const double *lattice, int nlat, const double *kpt, double2 *S,
+                                double2 *T, double *Q, cudaStream_t st);
+// eigh_herm.cu
+void eigh_herm(int n, int batch, double2 *A, double2 *V, double *w, double2 *work, int *status,
+               cudaStream_t st);
+
 void gemm_batched_rowmajor(int M, int N, int K, const double *A, int lda, long long sa,
                            const double *B, int ldb, long long sb, double *C, int ldc, long long sc,
                            int batch, cudaStream_t st);

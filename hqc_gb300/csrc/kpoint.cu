@@ -1,0 +1,875 @@
+// Single k-point SCF (FP64, complex): hf_kpt / dft_kpt of
+// hqc/pbc/solver.py:769-962 with the drivers of hqc/pbc/scf.py.
+//
+// Representation.  The plan keeps the CONJUGATED Bloch AOs on the grid,
+//   phibar_p(r) = conj(phi^k_p(r)),  phi^k_p(r) = sum_t phi_p(r - R_p - t) e^{i k.t}
+// (hqc/pbc/gto.py:371-427 on Rmesh), AO-major [p][g], so that every grid
+// contraction is one complex GEMM with plain / conjugate-transposed operands:
+//   quadrature  M_pq = dV sum_r conj(phi_p) w phi_q      = (Z Phibar^H)_pq, Z = dV w Phibar
+//   orbitals    psibar_i = conj(psi_i) = (C^H Phibar)_i,  rho = sum_i f_i |psibar_i|^2
+//   exchange    K_pq = sum_i f_i dV sum_r P_pi conj(W_qi) = f_i dV (P W^H)_pq,
+//               P_pi = conj(phi_p) psi_i = phibar_p conj(psibar_i),  W = v_H[P]
+//   Madelung    K0 = c S~ D S~,  S~ = dV Phibar Phibar^H     (solver.py:509-524)
+// These equal the reference's G-space forms (rhoG, eris, eris0) by Parseval
+// on the same odd grid.  S and T are the phase-weighted lattice sums of
+// integrals_fp64.cu (solver.py:257-274); the complex Hermitian eigensolver is
+// eigh_herm.cu.  DIIS keeps the reference's B = einsum('imn,jmn->ij', e, e)
+// WITHOUT conjugation (scf.py:178), solved in complex arithmetic, and the
+// Fock matrices handed to the eigensolver are symmetrised, (F + F^H) / 2, as
+// jnp.linalg.eigh does with its input.
+#include <algorithm>
+#include <complex>
+#include <vector>
+
+#include "common.cuh"
+#include "zmath.cuh"
+#include "kernels.h"
+
+namespace hqcgb {
+
+static constexpr double kMadelungK = 0.22578495;  // solver.py:404, 510
+
+// Factor table F[A][d][i][a][s] (complex): s = 3 l + k, k = value, first and
+// second derivative of u^l exp(-alpha u^2), each lattice term times the
+// conjugate Bloch phase exp(-i k_d t).
+__global__ void k_gto1d_kpt(const double *__restrict__ xp, int n_atoms, int ng, double L,
+                            const double *__restrict__ alpha, int nprim,
+                            const double *__restrict__ lat1d, int nlat, const double *__restrict__ kpt,
+                            double2 *__restrict__ F) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long total = (long long)n_atoms * 3 * ng * nprim;
+  if (idx >= total) return;
+  const int a = (int)(idx % nprim);
+  long long r = idx / nprim;
+  const int i = (int)(r % ng);
+  r /= ng;
+  const int d = (int)(r % 3);
+  const int A = (int)(r / 3);
+  const double x = i * L / ng - xp[A * 3 + d];
+  const double al = alpha[a], kd = kpt[d];
+  double sr[6] = {0, 0, 0, 0, 0, 0}, si[6] = {0, 0, 0, 0, 0, 0};
+  for (int t = 0; t < nlat; ++t) {
+    const double u = x - lat1d[t];
+    const double e = exp(-al * u * u);
+    double sn, cs;
+    sincos(-kd * lat1d[t], &sn, &cs);
+    const double v[6] = {e,
+                         -2.0 * al * u * e,
+                         (4.0 * al * al * u * u - 2.0 * al) * e,
+                         u * e,
+                         (1.0 - 2.0 * al * u * u) * e,
+                         (4.0 * al * al * u * u * u - 6.0 * al * u) * e};
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      sr[k] += v[k] * cs;
+      si[k] += v[k] * sn;
+    }
+  }
+  double2 *out = F + idx * 6;
+#pragma unroll
+  for (int k = 0; k < 6; ++k) out[k] = make_double2(sr[k], si[k]);
+}
+
+// AO value (c1 < 0) or its derivative along c1.
+__device__ inline double2 ao_eval_kpt(const double2 *__restrict__ F, const double *__restrict__ coef,
+                                      int nprim, int ng, int A, int l, int cart, int ix, int iy,
+                                      int iz, int c1) {
+  int pw[3] = {0, 0, 0};
+  if (l == 1) pw[cart] = 1;
+  int kd[3] = {0, 0, 0};
+  if (c1 >= 0) kd[c1] = 1;
+  const double2 *fx = F + ((((long long)A * 3 + 0) * ng + ix) * nprim) * 6 + 3 * pw[0] + kd[0];
+  const double2 *fy = F + ((((long long)A * 3 + 1) * ng + iy) * nprim) * 6 + 3 * pw[1] + kd[1];
+  const double2 *fz = F + ((((long long)A * 3 + 2) * ng + iz) * nprim) * 6 + 3 * pw[2] + kd[2];
+  double2 v = make_double2(0.0, 0.0);
+  for (int a = 0; a < nprim; ++a) {
+    const double2 t = zmul(zmul(fx[a * 6], fy[a * 6]), fz[a * 6]);
+    v.x += coef[a] * t.x;
+    v.y += coef[a] * t.y;
+  }
+  return v;
+}
+
+__global__ void k_phi_kpt(const double2 *__restrict__ F, const double *__restrict__ coef,
+                          const int *__restrict__ ao_l, const int *__restrict__ ao_cart, int nao_atom,
+                          int nprim, int nao, int ng, double2 *__restrict__ phi,
+                          double2 *__restrict__ dphi) {
+  const long long N = (long long)ng * ng * ng;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)nao * N) return;
+  const int p = (int)(idx / N);
+  const long long g = idx - (long long)p * N;
+  const int iz = (int)(g % ng), iy = (int)((g / ng) % ng), ix = (int)(g / ((long long)ng * ng));
+  const int A = p / nao_atom, k = p % nao_atom;
+  const double *c = coef + k * nprim;
+  phi[idx] = ao_eval_kpt(F, c, nprim, ng, A, ao_l[k], ao_cart[k], ix, iy, iz, -1);
+  if (dphi)
+    for (int d = 0; d < 3; ++d)
+      dphi[(long long)d * nao * N + idx] = ao_eval_kpt(F, c, nprim, ng, A, ao_l[k], ao_cart[k], ix, iy, iz, d);
+}
+
+// rho(g) = sum_i f_i |psibar_i(g)|^2 and, with dPsi [3][nuse][N],
+// grad rho = 2 sum_i f_i Re(psibar_i conj(grad psibar_i)).
+__global__ void k_rho_orb(const double2 *__restrict__ Psi, const double2 *__restrict__ dPsi,
+                          const double *__restrict__ occ, int nuse, long long N,
+                          double *__restrict__ rho, double *__restrict__ grho) {
+  const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= N) return;
+  double r = 0, gx = 0, gy = 0, gz = 0;
+  for (int i = 0; i < nuse; ++i) {
+    const double f = occ[i];
+    const double2 ps = Psi[(long long)i * N + g];
+    r += f * zabs2(ps);
+    if (dPsi) {
+      const double2 dx = dPsi[(long long)i * N + g], dy = dPsi[(long long)(nuse + i) * N + g],
+                    dz = dPsi[(long long)(2 * nuse + i) * N + g];
+      gx += f * (ps.x * dx.x + ps.y * dx.y);
+      gy += f * (ps.x * dy.x + ps.y * dy.y);
+      gz += f * (ps.x * dz.x + ps.y * dz.y);
+    }
+  }
+  rho[g] = r;
+  if (grho) {
+    grho[g] = 2.0 * gx;
+    grho[N + g] = 2.0 * gy;
+    grho[2 * N + g] = 2.0 * gz;
+  }
+}
+
+// Z_p(g) = a w(g) phibar_p(g) + b u(g) . grad phibar_p(g)   (u, dphi optional)
+__global__ void k_zoperand(const double2 *__restrict__ phi, const double2 *__restrict__ dphi,
+                           const double *__restrict__ w, const double *__restrict__ u, int nao,
+                           long long N, double a, double b, double2 *__restrict__ Z) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)nao * N) return;
+  const long long g = idx % N, NN = (long long)nao * N;
+  double2 z = zscale(a * w[g], phi[idx]);
+  if (u) {
+    const double2 d0 = dphi[idx], d1 = dphi[NN + idx], d2 = dphi[2 * NN + idx];
+    const double u0 = b * u[g], u1 = b * u[N + g], u2 = b * u[2 * N + g];
+    z.x += u0 * d0.x + u1 * d1.x + u2 * d2.x;
+    z.y += u0 * d0.y + u1 * d1.y + u2 * d2.y;
+  }
+  Z[idx] = z;
+}
+
+// Exchange pair densities of orbital i: P_p = phibar_p conj(psibar_i), into P
+// and W (W is then transformed in place by the Poisson solve).
+__global__ void k_pair_kpt(const double2 *__restrict__ phi, const double2 *__restrict__ psi, int nao,
+                           long long N, double2 *__restrict__ P, double2 *__restrict__ W) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)nao * N) return;
+  const double2 v = zmul(phi[idx], zconj(psi[idx % N]));
+  P[idx] = v;
+  W[idx] = v;
+}
+
+// out = a X + b op(Y), op(Y) = Y or Y^H (herm); out must not alias Y when herm.
+__global__ void k_zcomb(int n, double a, const double2 *__restrict__ X, double b,
+                        const double2 *__restrict__ Y, int herm, double2 *__restrict__ out) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n * n) return;
+  const int i = idx / n, j = idx % n;
+  const double2 y = Y ? (herm ? zconj(Y[j * n + i]) : Y[idx]) : make_double2(0.0, 0.0);
+  const double2 x = X ? X[idx] : make_double2(0.0, 0.0);
+  out[idx] = make_double2(a * x.x + b * y.x, a * x.y + b * y.y);
+}
+
+// e = X - X^H  (the DIIS commutator S D F - F D S with X = S D F)
+__global__ void k_zantiherm(int n, const double2 *__restrict__ X, double2 *__restrict__ e) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n * n) return;
+  const int i = idx / n, j = idx % n;
+  e[idx] = zsub(X[idx], zconj(X[j * n + i]));
+}
+
+// out[p][k] = C[p][k] f[k]
+__global__ void k_zscale_cols(int n, const double2 *__restrict__ C, const double *__restrict__ f,
+                              double2 *__restrict__ out) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n * n) return;
+  out[idx] = zscale(f[idx % n], C[idx]);
+}
+
+// v[p][k] = U[p][k] / sqrt(w[k]); bad = 1 when some w[k] <= 0 (solver.py:795-796)
+__global__ void k_zinv_sqrt_cols(int n, const double2 *__restrict__ U, const double *__restrict__ w,
+                                 double2 *__restrict__ v, int *__restrict__ bad) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n * n) return;
+  const double wk = w[idx % n];
+  if (!(wk > 0.0)) {
+    *bad = 1;
+    v[idx] = make_double2(0.0, 0.0);
+    return;
+  }
+  v[idx] = zscale(1.0 / sqrt(wk), U[idx]);
+}
+
+// B[i][j] = sum_mn e_i[mn] e_j[mn] (no conjugation, scf.py:178); one block per (i, j)
+__global__ void k_zdiis_B(int sp, long long nn, const double2 *__restrict__ ek, double2 *__restrict__ B) {
+  __shared__ double sh[32];
+  const int i = blockIdx.x / sp, j = blockIdx.x % sp;
+  const double2 *a = ek + (long long)i * nn, *b = ek + (long long)j * nn;
+  double sr = 0, si = 0;
+  for (long long k = threadIdx.x; k < nn; k += blockDim.x) {
+    const double2 t = zmul(a[k], b[k]);
+    sr += t.x;
+    si += t.y;
+  }
+  sr = block_sum(sr, sh);
+  si = block_sum(si, sh);
+  if (threadIdx.x == 0) B[blockIdx.x] = make_double2(sr, si);
+}
+
+// out = (1 - damp) sum_k c_k F_k + damp F_last
+__global__ void k_zdiis_combine(int sp, long long nn, const double2 *__restrict__ Fk,
+                                const double2 *__restrict__ c, int last, double damp,
+                                double2 *__restrict__ out) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= nn) return;
+  double2 s = make_double2(0.0, 0.0);
+  for (int k = 0; k < sp; ++k) s = zadd(s, zmul(c[k], Fk[(long long)k * nn + idx]));
+  const double2 fl = Fk[(long long)last * nn + idx];
+  out[idx] = make_double2((1.0 - damp) * s.x + damp * fl.x, (1.0 - damp) * s.y + damp * fl.y);
+}
+
+static void zcomb(int n, double a, const double2 *X, double b, const double2 *Y, bool herm,
+                  double2 *out, cudaStream_t st) {
+  k_zcomb<<<ceil_div((long long)n * n, 256), 256, 0, st>>>(n, a, X, b, Y, herm ? 1 : 0, out);
+  HQ_LAUNCH_CHECK();
+}
+
+// Solve the complex (sp + 1) DIIS system of scf.py:177-188 on the host
+// (LU with partial pivoting, as jnp.linalg.solve).
+static std::vector<std::complex<double>> diis_coefficients(const std::vector<double2> &Bh, int sp) {
+  using cd = std::complex<double>;
+  const int m = sp + 1;
+  std::vector<cd> h((size_t)m * m, cd(0.0)), g(m, cd(0.0));
+  cd tr(0.0);
+  for (int i = 0; i < sp; ++i) tr += cd(Bh[i * sp + i].x, Bh[i * sp + i].y);
+  const cd eta = 1e-12 * (tr / (double)sp + 1.0);
+  for (int i = 0; i < sp; ++i) {
+    for (int j = 0; j < sp; ++j) h[i * m + j] = cd(Bh[i * sp + j].x, Bh[i * sp + j].y);
+    h[i * m + i] += eta;
+    h[i * m + sp] = -1.0;
+    h[sp * m + i] = -1.0;
+  }
+  g[sp] = -1.0;
+  for (int k = 0; k < m; ++k) {
+    int piv = k;
+    for (int r = k + 1; r < m; ++r)
+      if (std::abs(h[r * m + k]) > std::abs(h[piv * m + k])) piv = r;
+    if (piv != k) {
+      for (int c = 0; c < m; ++c) std::swap(h[k * m + c], h[piv * m + c]);
+      std::swap(g[k], g[piv]);
+    }
+    const cd dkk = h[k * m + k];
+    if (dkk == cd(0.0)) throw Error{HQCGB_NAN, "singular DIIS system"};
+    for (int r = k + 1; r < m; ++r) {
+      const cd l = h[r * m + k] / dkk;
+      if (l == cd(0.0)) continue;
+      for (int c = k; c < m; ++c) h[r * m + c] -= l * h[k * m + c];
+      g[r] -= l * g[k];
+    }
+  }
+  std::vector<cd> x(m);
+  for (int k = m - 1; k >= 0; --k) {
+    cd s = g[k];
+    for (int c = k + 1; c < m; ++c) s -= h[k * m + c] * x[c];
+    x[k] = s / h[k * m + k];
+  }
+  x.resize(sp);
+  return x;
+}
+
+}  // namespace hqcgb
+
+using namespace hqcgb;
+
+struct hqcgb_kplan {
+  hqcgb_params P{};
+  int n = 0, nb = 0, nao = 0, ng = 0, nprim = 0;
+  long long N = 0;
+  double L = 0, Omega = 0, dV = 0;
+  bool gga = false, hf = false;
+  std::vector<void *> allocs;
+  // constant tables
+  double *alpha = nullptr, *coef = nullptr, *lat1d = nullptr, *lattice = nullptr, *coul = nullptr;
+  int *ao_l = nullptr, *ao_cart = nullptr;
+  double2 *tw = nullptr;
+  // geometry
+  double *xp = nullptr, *kpt = nullptr;
+  double2 *F1d = nullptr, *phi = nullptr, *dphi = nullptr, *ph = nullptr;
+  // grid work: operand / pair densities, their potentials, conjugated orbitals
+  double2 *Z = nullptr, *W = nullptr, *Psi = nullptr, *dPsi = nullptr, *cbuf = nullptr;
+  // matrices (complex, row-major nao x nao)
+  double2 *S = nullptr, *T = nullptr, *V = nullptr, *H = nullptr, *St = nullptr, *vorth = nullptr,
+          *F = nullptr, *F2e = nullptr, *K = nullptr, *Fp = nullptr, *C = nullptr, *c1 = nullptr,
+          *D = nullptr, *t1 = nullptr, *t2 = nullptr, *err = nullptr, *Fk = nullptr, *ek = nullptr,
+          *jA = nullptr, *jwork = nullptr, *Bm = nullptr, *dc = nullptr;
+  double *w = nullptr, *ws = nullptr, *occ = nullptr, *mu = nullptr, *ovq = nullptr;
+  double *rho = nullptr, *grho = nullptr, *vh = nullptr, *wq = nullptr, *vxc = nullptr, *u = nullptr,
+         *vloc = nullptr, *xpart = nullptr, *scal = nullptr, *hscal = nullptr;
+  int *jstat = nullptr, *ibad = nullptr;
+  std::vector<double> h_occ;
+  int nuse = 0;
+  bool have_state = false;
+
+  template <class X>
+  X *alloc(size_t count) {
+    void *q = nullptr;
+    if (count == 0) count = 1;
+    HQ_CUDA(cudaMalloc(&q, count * sizeof(X)));
+    allocs.push_back(q);
+    return (X *)q;
+  }
+  ~hqcgb_kplan() {
+    for (void *q : allocs) cudaFree(q);
+    if (hscal) cudaFreeHost(hscal);
+  }
+};
+
+namespace hqcgb {
+
+enum { K_TRHD = 0, K_EXC = 1, K_VHRHO = 2, K_TRKD = 3, K_ERR2 = 4, K_SE = 5, K_KI = 6, K_VEP = 7,
+       K_NSLOT = 16 };
+
+static void kupload(void *dst, const void *src, size_t bytes) {
+  HQ_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
+}
+
+static double kocc_shift(const hqcgb_params &P, int nmo) {
+  if (!P.smearing) return 0.0;
+  const double n = P.n_atoms;
+  if (P.smearing_method == HQCGB_SMEAR_FERMI) return -P.smearing_sigma * std::log(2 * nmo / n - 1);
+  // erfinv(1 - n / nmo) by Newton on erf
+  const double y = 1.0 - n / nmo;
+  double x = 0.0;
+  for (int it = 0; it < 200; ++it) {
+    const double dx = (std::erf(x) - y) / (2.0 / std::sqrt(M_PI) * std::exp(-x * x));
+    x -= dx;
+    if (std::fabs(dx) < 1e-16 * (1 + std::fabs(x))) break;
+  }
+  return -P.smearing_sigma * x;
+}
+
+static void kcreate(const hqcgb_params &P, hqcgb_kplan *p) {
+  HQ_REQUIRE(P.n_atoms >= 1, "n_atoms must be >= 1");
+  HQ_REQUIRE(P.n_grid >= 3 && P.n_grid <= kMaxGrid, "n_grid out of range");
+  HQ_REQUIRE(P.nao_atom >= 1 && P.n_prim >= 1, "empty basis");
+  HQ_REQUIRE(P.L > 0, "L must be positive");
+  HQ_REQUIRE(P.n_atoms * P.nao_atom <= kMaxNao, "too many AOs");
+  HQ_REQUIRE(P.diis_space >= 1 && P.diis_space <= 32, "diis_space must be in [1, 32]");
+  HQ_REQUIRE(P.max_cycle >= 0, "max_cycle must be >= 0");
+  HQ_REQUIRE(!P.smearing || P.smearing_sigma > 0, "smearing_sigma must be > 0 with smearing");
+  HQ_REQUIRE(P.precision == HQCGB_PREC_FP64, "the k-point solver runs in FP64 only");
+  HQ_REQUIRE(!P.want_forces, "the k-point solver has no forces");
+  for (int k = 0; k < P.nao_atom; ++k) {
+    HQ_REQUIRE(P.ao_l[k] == 0 || P.ao_l[k] == 1, "only s and p AOs are supported");
+    HQ_REQUIRE(P.ao_cart[k] >= 0 && P.ao_cart[k] < 3, "bad cartesian index");
+  }
+  p->P = P;
+  p->P.alpha = nullptr;  // host tables are not kept
+  p->P.coef = nullptr;
+  p->P.ao_l = p->P.ao_cart = nullptr;
+  p->P.lat1d = p->P.lattice = nullptr;
+  p->n = P.n_atoms;
+  p->nb = P.nao_atom;
+  p->nao = p->n * p->nb;
+  p->ng = P.n_grid;
+  p->nprim = P.n_prim;
+  p->N = (long long)p->ng * p->ng * p->ng;
+  p->L = P.L;
+  p->Omega = P.L * P.L * P.L;
+  p->dV = p->Omega / (double)p->N;
+  p->hf = !P.dft;
+  p->gga = P.dft && P.xc == HQCGB_XC_PBE;
+  const int n = p->n, nao = p->nao;
+  const long long N = p->N;
+  const size_t nn = (size_t)nao * nao;
+
+  p->alpha = p->alloc<double>(P.n_prim);
+  kupload(p->alpha, P.alpha, sizeof(double) * P.n_prim);
+  p->coef = p->alloc<double>((size_t)P.nao_atom * P.n_prim);
+  kupload(p->coef, P.coef, sizeof(double) * P.nao_atom * P.n_prim);
+  p->ao_l = p->alloc<int>(P.nao_atom);
+  kupload(p->ao_l, P.ao_l, sizeof(int) * P.nao_atom);
+  p->ao_cart = p->alloc<int>(P.nao_atom);
+  kupload(p->ao_cart, P.ao_cart, sizeof(int) * P.nao_atom);
+  p->lat1d = p->alloc<double>(P.n_lat1d);
+  kupload(p->lat1d, P.lat1d, sizeof(double) * P.n_lat1d);
+  p->lattice = p->alloc<double>(3 * (size_t)P.n_lattice);
+  kupload(p->lattice, P.lattice, sizeof(double) * 3 * P.n_lattice);
+  std::vector<double2> tw(p->ng);
+  for (int k = 0; k < p->ng; ++k) {
+    const double a = -2.0 * M_PI * k / p->ng;
+    tw[k] = make_double2(std::cos(a), std::sin(a));
+  }
+  p->tw = p->alloc<double2>(p->ng);
+  kupload(p->tw, tw.data(), sizeof(double2) * p->ng);
+  p->coul = p->alloc<double>(N);
+  launch_coulomb_table(p->ng, p->L, p->coul, 0);
+
+  p->xp = p->alloc<double>(3 * (size_t)n);
+  p->kpt = p->alloc<double>(3);
+  p->F1d = p->alloc<double2>((size_t)n * 3 * p->ng * P.n_prim * 6);
+  p->phi = p->alloc<double2>((size_t)nao * N);
+  if (p->gga) p->dphi = p->alloc<double2>((size_t)3 * nao * N);
+  p->ph = p->alloc<double2>((size_t)n * 3 * p->ng);
+  p->Z = p->alloc<double2>((size_t)nao * N);
+  if (p->hf) p->W = p->alloc<double2>((size_t)nao * N);
+  p->Psi = p->alloc<double2>((size_t)nao * N);
+  if (p->gga) p->dPsi = p->alloc<double2>((size_t)3 * nao * N);
+  p->cbuf = p->alloc<double2>(N);
+  for (double2 **m : {&p->S, &p->T, &p->V, &p->H, &p->St, &p->vorth, &p->F, &p->F2e, &p->K, &p->Fp,
+                      &p->C, &p->c1, &p->D, &p->t1, &p->t2, &p->err, &p->jA, &p->jwork})
+    *m = p->alloc<double2>(nn);
+  p->Fk = p->alloc<double2>((size_t)P.diis_space * nn);
+  p->ek = p->alloc<double2>((size_t)P.diis_space * nn);
+  p->Bm = p->alloc<double2>((size_t)P.diis_space * P.diis_space);
+  p->dc = p->alloc<double2>(P.diis_space);
+  p->w = p->alloc<double>(nao);
+  p->ws = p->alloc<double>(nao);
+  p->occ = p->alloc<double>(nao);
+  p->mu = p->alloc<double>(1);
+  p->ovq = p->alloc<double>(ovl_scratch_doubles_kpt(n, P.n_prim));
+  p->rho = p->alloc<double>(N);
+  p->vh = p->alloc<double>(N);
+  p->wq = p->alloc<double>(N);
+  p->vxc = p->alloc<double>(N);
+  p->vloc = p->alloc<double>(N);
+  if (p->gga) {
+    p->grho = p->alloc<double>(3 * N);
+    p->u = p->alloc<double>(3 * N);
+  }
+  p->xpart = p->alloc<double>((size_t)2 * xc_blocks(N));
+  p->jstat = p->alloc<int>(1);
+  p->ibad = p->alloc<int>(1);
+  p->scal = p->alloc<double>(K_NSLOT);
+  HQ_CUDA(cudaMallocHost(&p->hscal, K_NSLOT * sizeof(double)));
+  p->h_occ.resize(nao);
+  HQ_CUDA(cudaDeviceSynchronize());
+}
+
+struct KCtx {
+  hqcgb_kplan *p;
+  cudaStream_t st;
+};
+
+static void ksync(KCtx &c) {
+  HQ_CUDA(cudaMemcpyAsync(c.p->hscal, c.p->scal, K_NSLOT * sizeof(double), cudaMemcpyDeviceToHost,
+                          c.st));
+  HQ_CUDA(cudaStreamSynchronize(c.st));
+}
+
+// Re tr(X D) for Hermitian D: the real dot product of the interleaved arrays
+static void kdot(KCtx &c, const double2 *X, const double2 *D, int slot) {
+  dot(2LL * c.p->nao * c.p->nao, reinterpret_cast<const double *>(X),
+      reinterpret_cast<const double *>(D), 1.0, c.p->scal + slot, false, c.st);
+}
+
+// Eigen-decomposition of (A + A^H) / 2 (jnp.linalg.eigh's symmetrised input)
+static void keigh(KCtx &c, const double2 *A, double2 *vecs, double *vals) {
+  hqcgb_kplan *p = c.p;
+  const int n = p->nao;
+  zcomb(n, 0.5, A, 0.5, A, true, p->jA, c.st);
+  eigh_herm(n, 1, p->jA, vecs, vals, p->jwork, p->jstat, c.st);
+}
+
+static void kcheck_eig(KCtx &c) {
+  int s = 0;
+  HQ_CUDA(cudaMemcpyAsync(&s, c.p->jstat, sizeof(int), cudaMemcpyDeviceToHost, c.st));
+  HQ_CUDA(cudaStreamSynchronize(c.st));
+  if (s < 0) throw Error{HQCGB_EIG_FAIL, "Hermitian eigensolver did not converge"};
+}
+
+static const double2 kOne = {1.0, 0.0}, kZero = {0.0, 0.0};
+
+// C, w from a Fock matrix: F' = v^H F v, eigh, C = v c' (scf.py:68-72)
+static void kdiagonalize(KCtx &c, const double2 *Fm) {
+  hqcgb_kplan *p = c.p;
+  const int n = p->nao;
+  zgemm('N', 'N', n, n, n, kOne, Fm, n, p->vorth, n, kZero, p->t1, n, c.st);
+  zgemm('C', 'N', n, n, n, kOne, p->vorth, n, p->t1, n, kZero, p->Fp, n, c.st);
+  keigh(c, p->Fp, p->c1, p->w);
+  zgemm('N', 'N', n, n, n, kOne, p->vorth, n, p->c1, n, kZero, p->C, n, c.st);
+}
+
+// occupations and D = C diag(f) C^H (solver.py:567-577)
+static void kdensity_matrix(KCtx &c) {
+  hqcgb_kplan *p = c.p;
+  const hqcgb_params &P = p->P;
+  const int n = p->nao;
+  occupations(P.n_atoms, n, P.smearing, P.smearing_method, P.smearing_sigma, P.search_method,
+              P.search_cycle, P.search_tol, kocc_shift(P, n), p->w, p->occ, p->mu, c.st);
+  k_zscale_cols<<<ceil_div((long long)n * n, 256), 256, 0, c.st>>>(n, p->C, p->occ, p->t1);
+  HQ_LAUNCH_CHECK();
+  zgemm('N', 'C', n, n, n, kOne, p->t1, n, p->C, n, kZero, p->D, n, c.st);
+}
+
+static void kpoisson_real(KCtx &c, const double *src, double *dst) {
+  hqcgb_kplan *p = c.p;
+  launch_real_to_complex(src, nullptr, p->N, 1, p->cbuf, c.st);
+  launch_fft3d(p->cbuf, p->ng, 1, p->tw, false, c.st);
+  launch_scale_complex(p->cbuf, p->coul, p->N, 1, c.st);
+  launch_fft3d(p->cbuf, p->ng, 1, p->tw, true, c.st);
+  launch_complex_real(p->cbuf, p->N, 1.0, dst, c.st);
+}
+
+// F2e = Z Phibar^H (+ its Hermitian conjugate with GGA), Z from w (and u)
+static void kquadrature(KCtx &c, const double *w, const double *u, double2 *out) {
+  hqcgb_kplan *p = c.p;
+  const int n = p->nao;
+  const long long N = p->N;
+  HQ_STAGE(ST_QUAD, c.st);
+  k_zoperand<<<ceil_div((long long)n * N, 256), 256, 0, c.st>>>(p->phi, p->dphi, w, u, n, N,
+                                                                  u ? 0.5 : 1.0, p->dV, p->Z);
+  HQ_LAUNCH_CHECK();
+  if (u) {
+    zgemm('N', 'C', n, n, (int)N, kOne, p->Z, (int)N, p->phi, (int)N, kZero, p->t1, n, c.st);
+    zcomb(n, 1.0, p->t1, 1.0, p->t1, true, out, c.st);
+  } else {
+    zgemm('N', 'C', n, n, (int)N, kOne, p->Z, (int)N, p->phi, (int)N, kZero, out, n, c.st);
+  }
+}
+
+// Exact exchange with the Madelung term (solver.py:509-524, 604-614, 819-822)
+static void kexchange(KCtx &c) {
+  hqcgb_kplan *p = c.p;
+  const int n = p->nao;
+  const long long N = p->N;
+  HQ_STAGE(ST_EXCHANGE, c.st);
+  HQ_CUDA(cudaMemsetAsync(p->K, 0, sizeof(double2) * n * n, c.st));
+  for (int i = 0; i < p->nuse; ++i) {
+    const double f = p->h_occ[i];
+    if (!(f > p->P.exx_occ_threshold)) continue;
+    k_pair_kpt<<<ceil_div((long long)n * N, 256), 256, 0, c.st>>>(p->phi, p->Psi + (long long)i * N, n,
+                                                                    N, p->Z, p->W);
+    HQ_LAUNCH_CHECK();
+    launch_fft3d(p->W, p->ng, n, p->tw, false, c.st);
+    launch_scale_complex(p->W, p->coul, N, n, c.st);
+    launch_fft3d(p->W, p->ng, n, p->tw, true, c.st);
+    zgemm('N', 'C', n, n, (int)N, make_double2(f * p->dV, 0.0), p->Z, (int)N, p->W, (int)N, kOne, p->K,
+          n, c.st);
+  }
+  zcomb(n, 0.5, p->K, 0.5, p->K, true, p->t1, c.st);
+  const double cM = 4.0 * M_PI / p->L * kMadelungK;
+  zgemm('N', 'N', n, n, n, kOne, p->St, n, p->D, n, kZero, p->t2, n, c.st);
+  zgemm('N', 'N', n, n, n, kOne, p->t2, n, p->St, n, kZero, p->K, n, c.st);
+  zcomb(n, 1.0, p->t1, cM, p->K, false, p->K, c.st);
+}
+
+// Two-electron Fock part and energy for the current C, occ, D; F = H + F2e.
+static double kfock(KCtx &c) {
+  hqcgb_kplan *p = c.p;
+  const hqcgb_params &P = p->P;
+  const int n = p->nao;
+  const long long N = p->N;
+  HQ_CUDA(cudaMemcpyAsync(p->h_occ.data(), p->occ, sizeof(double) * n, cudaMemcpyDeviceToHost, c.st));
+  HQ_CUDA(cudaStreamSynchronize(c.st));
+  int nuse = 0;
+  for (int k = 0; k < n; ++k)
+    if (p->h_occ[k] > 0.0) nuse = k + 1;
+  p->nuse = nuse;
+  {
+    HQ_STAGE(ST_DENSITY, c.st);
+    if (nuse > 0) {
+      zgemm('C', 'N', nuse, (int)N, n, kOne, p->C, n, p->phi, (int)N, kZero, p->Psi, (int)N, c.st);
+      if (p->gga)
+        for (int d = 0; d < 3; ++d)
+          zgemm('C', 'N', nuse, (int)N, n, kOne, p->C, n, p->dphi + (long long)d * n * N, (int)N, kZero,
+                p->dPsi + (long long)d * nuse * N, (int)N, c.st);
+    }
+    k_rho_orb<<<ceil_div(N, 256), 256, 0, c.st>>>(p->Psi, p->gga ? p->dPsi : nullptr, p->occ, nuse, N,
+                                                    p->rho, p->gga ? p->grho : nullptr);
+    HQ_LAUNCH_CHECK();
+  }
+  kpoisson_real(c, p->rho, p->vh);
+  const int kind = P.dft ? P.xc : -1;
+  launch_xc_pointwise(kind, p->rho, p->gga ? p->grho : nullptr, p->vh, N, p->dV, p->wq, p->vxc,
+                      p->gga ? p->u : nullptr, p->xpart, c.st);
+  launch_sum_partials(p->xpart, xc_blocks(N), 2, 2, 1.0, p->scal + K_EXC, false, c.st);
+  kquadrature(c, p->wq, p->gga ? p->u : nullptr, p->F2e);
+  if (p->hf) {
+    kexchange(c);
+    kdot(c, p->K, p->D, K_TRKD);
+    zcomb(n, 1.0, p->F2e, -0.5, p->K, false, p->F2e, c.st);
+  }
+  zcomb(n, 1.0, p->H, 1.0, p->F2e, false, p->F, c.st);
+  kdot(c, p->H, p->D, K_TRHD);
+  ksync(c);
+  const double *s = p->hscal;
+  double E = s[K_TRHD] + 0.5 * p->dV * s[K_VHRHO];
+  E += P.dft ? p->dV * s[K_EXC] : -0.25 * s[K_TRKD];
+  return E;
+}
+
+// e = S D F - F D S and its Frobenius norm (scf.py, get_diis_errvec_sdf)
+static double kerr_vector(KCtx &c, double2 *e) {
+  hqcgb_kplan *p = c.p;
+  const int n = p->nao;
+  zgemm('N', 'N', n, n, n, kOne, p->S, n, p->D, n, kZero, p->t1, n, c.st);
+  zgemm('N', 'N', n, n, n, kOne, p->t1, n, p->F, n, kZero, p->t2, n, c.st);
+  k_zantiherm<<<ceil_div((long long)n * n, 256), 256, 0, c.st>>>(n, p->t2, e);
+  HQ_LAUNCH_CHECK();
+  kdot(c, e, e, K_ERR2);
+  ksync(c);
+  return std::sqrt(p->hscal[K_ERR2]);
+}
+
+static void kgeometry(KCtx &c, const double *xp_dev, const double *kpt_host) {
+  hqcgb_kplan *p = c.p;
+  const hqcgb_params &P = p->P;
+  const int n = p->nao;
+  const long long N = p->N;
+  HQ_CUDA(cudaMemcpyAsync(p->xp, xp_dev, sizeof(double) * 3 * p->n, cudaMemcpyDeviceToDevice, c.st));
+  HQ_CUDA(cudaMemcpyAsync(p->kpt, kpt_host, sizeof(double) * 3, cudaMemcpyHostToDevice, c.st));
+  {
+    HQ_STAGE(ST_GTO, c.st);
+    const long long total = (long long)p->n * 3 * p->ng * p->nprim;
+    k_gto1d_kpt<<<ceil_div(total, 256), 256, 0, c.st>>>(p->xp, p->n, p->ng, p->L, p->alpha, p->nprim,
+                                                         p->lat1d, P.n_lat1d, p->kpt, p->F1d);
+    HQ_LAUNCH_CHECK();
+  }
+  {
+    HQ_STAGE(ST_PHI, c.st);
+    k_phi_kpt<<<ceil_div((long long)n * N, 256), 256, 0, c.st>>>(p->F1d, p->coef, p->ao_l, p->ao_cart,
+                                                                   p->nb, p->nprim, n, p->ng, p->phi,
+                                                                   p->dphi);
+    HQ_LAUNCH_CHECK();
+  }
+  launch_overlap_kinetic_kpt(p->xp, p->n, p->nb, p->nprim, p->alpha, p->coef, p->ao_l, p->ao_cart,
+                             p->lattice, P.n_lattice, p->kpt, p->S, p->T, p->ovq, c.st);
+  launch_vloc_G(p->xp, p->n, p->ng, p->L, p->ph, p->cbuf, c.st);
+  launch_fft3d(p->cbuf, p->ng, 1, p->tw, true, c.st);
+  launch_complex_real(p->cbuf, N, 1.0, p->vloc, c.st);
+  {
+    HQ_STAGE(ST_QUAD, c.st);
+    k_zoperand<<<ceil_div((long long)n * N, 256), 256, 0, c.st>>>(p->phi, nullptr, p->vloc, nullptr, n,
+                                                                    N, p->dV, 0.0, p->Z);
+    HQ_LAUNCH_CHECK();
+    zgemm('N', 'C', n, n, (int)N, kOne, p->Z, (int)N, p->phi, (int)N, kZero, p->V, n, c.st);
+  }
+  zcomb(n, 1.0, p->T, 1.0, p->V, false, p->H, c.st);
+  if (p->hf)
+    zgemm('N', 'C', n, n, (int)N, make_double2(p->dV, 0.0), p->phi, (int)N, p->phi, (int)N, kZero, p->St,
+          n, c.st);
+  // S^{-1/2} as U w^{-1/2} (solver.py:795-796)
+  HQ_CUDA(cudaMemsetAsync(p->ibad, 0, sizeof(int), c.st));
+  keigh(c, p->S, p->c1, p->ws);
+  k_zinv_sqrt_cols<<<ceil_div((long long)n * n, 256), 256, 0, c.st>>>(n, p->c1, p->ws, p->vorth, p->ibad);
+  HQ_LAUNCH_CHECK();
+  int bad = 0;
+  HQ_CUDA(cudaMemcpyAsync(&bad, p->ibad, sizeof(int), cudaMemcpyDeviceToHost, c.st));
+  HQ_CUDA(cudaStreamSynchronize(c.st));
+  kcheck_eig(c);
+  if (bad) throw Error{HQCGB_NAN, "overlap matrix is not positive definite (coincident atoms?)"};
+}
+
+// DIIS extrapolation: complex coefficients from the unconjugated B (scf.py:177-194)
+static void kdiis_extrapolate(KCtx &c, int head, double2 *out) {
+  hqcgb_kplan *p = c.p;
+  const int sp = p->P.diis_space;
+  const long long nn = (long long)p->nao * p->nao;
+  k_zdiis_B<<<sp * sp, 256, 0, c.st>>>(sp, nn, p->ek, p->Bm);
+  HQ_LAUNCH_CHECK();
+  std::vector<double2> Bh((size_t)sp * sp);
+  HQ_CUDA(cudaMemcpyAsync(Bh.data(), p->Bm, sizeof(double2) * sp * sp, cudaMemcpyDeviceToHost, c.st));
+  HQ_CUDA(cudaStreamSynchronize(c.st));
+  std::vector<std::complex<double>> x = diis_coefficients(Bh, sp);
+  std::vector<double2> ch(sp);
+  for (int k = 0; k < sp; ++k) ch[k] = make_double2(x[k].real(), x[k].imag());
+  HQ_CUDA(cudaMemcpyAsync(p->dc, ch.data(), sizeof(double2) * sp, cudaMemcpyHostToDevice, c.st));
+  k_zdiis_combine<<<ceil_div(nn, 256), 256, 0, c.st>>>(sp, nn, p->Fk, p->dc, head, p->P.diis_damp, out);
+  HQ_LAUNCH_CHECK();
+  HQ_CUDA(cudaStreamSynchronize(c.st));  // ch lives on this frame
+}
+
+}  // namespace hqcgb
+
+namespace hqcgb {
+
+static int kscf_one(hqcgb_kplan *p, const double *xp_dev, const double *kpt_host,
+                    const hqcgb_scf_out *out, cudaStream_t st) {
+  KCtx c{p, st};
+  const hqcgb_params &P = p->P;
+  const int n = p->nao;
+  const size_t nn = (size_t)n * n, zb = nn * sizeof(double2);
+  p->have_state = false;
+  kgeometry(c, xp_dev, kpt_host);
+  // Hcore guess (solver.py:805-817)
+  kdiagonalize(c, p->H);
+  kdensity_matrix(c);
+  double E0 = 0.0, E1 = 1.0;
+  int loop = 0;
+  if (P.diis) {
+    const int sp = P.diis_space;
+    kfock(c);
+    kerr_vector(c, p->err);
+    for (int k = 0; k < sp; ++k) {
+      HQ_CUDA(cudaMemcpyAsync(p->Fk + k * nn, p->F, zb, cudaMemcpyDeviceToDevice, st));
+      HQ_CUDA(cudaMemcpyAsync(p->ek + k * nn, p->err, zb, cudaMemcpyDeviceToDevice, st));
+    }
+    int head = sp - 1;
+    double enorm = 0.0;
+    auto step = [&](const double2 *Fin) {
+      kdiagonalize(c, Fin);
+      kdensity_matrix(c);
+      const double En = kfock(c);
+      head = (head + 1) % sp;
+      HQ_CUDA(cudaMemcpyAsync(p->Fk + head * nn, p->F, zb, cudaMemcpyDeviceToDevice, st));
+      enorm = kerr_vector(c, p->ek + head * nn);
+      E0 = E1;
+      E1 = En;
+      ++loop;
+    };
+    // plain iterations filling the DIIS history (scf.py:124-169)
+    while (loop < P.diis_start_cycle + sp) step(p->Fk + head * nn);
+    E0 = E1 - 1.0;
+    while ((std::fabs(E1 - E0) > P.tol || enorm > 10.0 * P.tol) && loop < P.max_cycle) {
+      kdiis_extrapolate(c, head, p->t2);  // t2 is free until the exchange step
+      step(p->t2);
+      if (!std::isfinite(E1)) throw Error{HQCGB_NAN, "non-finite energy in the SCF"};
+    }
+  } else {
+    // fixed_point_scf (scf.py:21-88)
+    while (std::fabs(E1 - E0) > P.tol && loop < P.max_cycle) {
+      const double En = kfock(c);
+      kdiagonalize(c, p->F);
+      kdensity_matrix(c);
+      E0 = E1;
+      E1 = En;
+      ++loop;
+      if (!std::isfinite(E1)) throw Error{HQCGB_NAN, "non-finite energy in the SCF"};
+    }
+  }
+  kcheck_eig(c);
+  const int converged = (loop != P.max_cycle) ? 1 : 0;
+  // post-processing (solver.py:824-837 / 950-962)
+  kdensity_matrix(c);
+  kfock(c);
+  kdot(c, p->T, p->D, K_KI);
+  kdot(c, p->V, p->D, K_VEP);
+  entropy(n, p->occ, p->scal + K_SE, st);
+  ksync(c);
+  const double *s = p->hscal;
+  const double Exc = P.dft ? p->dV * s[K_EXC] : -0.25 * s[K_TRKD];
+  const double Vee = 0.5 * p->dV * s[K_VHRHO] + Exc;
+  const double en[5] = {E1, s[K_KI], s[K_VEP], Vee, s[K_SE]};
+  if (out) {
+    if (out->mo_coeff) HQ_CUDA(cudaMemcpyAsync(out->mo_coeff, p->C, zb, cudaMemcpyDeviceToDevice, st));
+    if (out->dm) HQ_CUDA(cudaMemcpyAsync(out->dm, p->D, zb, cudaMemcpyDeviceToDevice, st));
+    if (out->bands) HQ_CUDA(cudaMemcpyAsync(out->bands, p->w, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    if (out->energies) HQ_CUDA(cudaMemcpyAsync(out->energies, en, sizeof(en), cudaMemcpyHostToDevice, st));
+    if (out->converged)
+      HQ_CUDA(cudaMemcpyAsync(out->converged, &converged, sizeof(int), cudaMemcpyHostToDevice, st));
+    if (out->iterations)
+      HQ_CUDA(cudaMemcpyAsync(out->iterations, &loop, sizeof(int), cudaMemcpyHostToDevice, st));
+    HQ_CUDA(cudaStreamSynchronize(st));
+  }
+  p->have_state = true;
+  return converged ? HQCGB_OK : HQCGB_NOT_CONVERGED;
+}
+
+static int kfail(const Error &e) {
+  set_error(e.msg);
+  return e.status;
+}
+
+}  // namespace hqcgb
+
+extern "C" {
+
+int hqcgb_kplan_create(const hqcgb_params *params, hqcgb_kplan **plan) {
+  if (!params || !plan) {
+    set_error("null argument");
+    return HQCGB_BAD_ARG;
+  }
+  hqcgb_kplan *p = new hqcgb_kplan();
+  try {
+    kcreate(*params, p);
+  } catch (const Error &e) {
+    delete p;
+    return kfail(e);
+  }
+  *plan = p;
+  return HQCGB_OK;
+}
+
+int hqcgb_kplan_destroy(hqcgb_kplan *plan) {
+  delete plan;
+  return HQCGB_OK;
+}
+
+int hqcgb_scf_kpt(hqcgb_kplan *plan, const double *xp, const double *kpt, const hqcgb_scf_out *out,
+                  void *stream) {
+  try {
+    HQ_REQUIRE(plan && xp && kpt, "null argument");
+    return kscf_one(plan, xp, kpt, out, (cudaStream_t)stream);
+  } catch (const Error &e) {
+    return kfail(e);
+  }
+}
+
+int hqcgb_scf_kpt_batch(hqcgb_kplan *plan, int n_cfg, const double *xp, const double *kpts,
+                        const hqcgb_scf_out *out, void *stream) {
+  try {
+    HQ_REQUIRE(plan && xp && kpts && out && n_cfg >= 0, "null argument");
+    const int nao = plan->nao;
+    int worst = HQCGB_OK;
+    for (int b = 0; b < n_cfg; ++b) {
+      hqcgb_scf_out o = *out;
+      const size_t zz = 2 * (size_t)nao * nao;
+      if (o.mo_coeff) o.mo_coeff += b * zz;
+      if (o.dm) o.dm += b * zz;
+      if (o.bands) o.bands += (size_t)b * nao;
+      if (o.energies) o.energies += (size_t)b * 5;
+      if (o.converged) o.converged += b;
+      if (o.iterations) o.iterations += b;
+      int s;
+      try {
+        s = kscf_one(plan, xp + (size_t)b * 3 * plan->n, kpts + (size_t)b * 3, &o, (cudaStream_t)stream);
+      } catch (const Error &e) {
+        throw Error{e.status, "configuration " + std::to_string(b) + ": " + e.msg};
+      }
+      worst = std::max(worst, s);
+    }
+    return worst;
+  } catch (const Error &e) {
+    return kfail(e);
+  }
+}
+
+long long hqcgb_kplan_query(hqcgb_kplan *p, const char *name, void *dst, size_t bytes, void *stream) {
+  try {
+    HQ_REQUIRE(p && name, "null argument");
+    const std::string s(name);
+    const size_t zn = sizeof(double2) * p->nao * p->nao;
+    const void *src = nullptr;
+    size_t sz = 0;
+    if (s == "S") src = p->S, sz = zn;
+    else if (s == "T") src = p->T, sz = zn;
+    else if (s == "V") src = p->V, sz = zn;
+    else if (s == "H") src = p->H, sz = zn;
+    else if (s == "D") src = p->D, sz = zn;
+    else if (s == "F") src = p->F, sz = zn;
+    else if (s == "K") src = p->K, sz = zn;
+    else if (s == "St") src = p->St, sz = zn;
+    else if (s == "phi") src = p->phi, sz = sizeof(double2) * p->nao * p->N;
+    else if (s == "rho") src = p->rho, sz = sizeof(double) * p->N;
+    else if (s == "vh") src = p->vh, sz = sizeof(double) * p->N;
+    else if (s == "vloc") src = p->vloc, sz = sizeof(double) * p->N;
+    else throw Error{HQCGB_BAD_ARG, "unknown buffer " + s};
+    if (!dst) return (long long)sz;
+    HQ_REQUIRE(bytes >= sz, "destination too small");
+    if (!src) return 0;
+    HQ_CUDA(cudaMemcpyAsync(dst, src, sz, cudaMemcpyDeviceToDevice, (cudaStream_t)stream));
+    HQ_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    return (long long)sz;
+  } catch (const Error &e) {
+    set_error(e.msg);
+    return -(long long)e.status;
+  }
+}
+
+}  // extern "C"

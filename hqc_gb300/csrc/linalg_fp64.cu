@@ -85,6 +85,19 @@ void gemm(bool ta, bool tb, int M, int N, int K, double alpha, const double *A, 
   HQ_LAUNCH_CHECK();
 }
 
+// Row-major complex C = alpha op(A) op(B) + beta C, op 'N' (as is), 'T'
+// (transpose) or 'C' (conjugate transpose): cuBLAS ZGEMM on the column-major
+// view, where a row-major X reads as X^T and op carries over unchanged.
+void zgemm(char opa, char opb, int M, int N, int K, double2 alpha, const double2 *A, int lda,
+           const double2 *B, int ldb, double2 beta, double2 *C, int ldc, cudaStream_t st) {
+  HQ_STAGE(ST_GEMM_SMALL, st);
+  auto op = [](char c) { return c == 'T' ? CUBLAS_OP_T : (c == 'C' ? CUBLAS_OP_C : CUBLAS_OP_N); };
+  cublasHandle_t h = blas_handle();
+  cublasSetStream(h, st);
+  cublasStatus_t r = cublasZgemm(h, op(opb), op(opa), N, M, K, &alpha, B, ldb, A, lda, &beta, C, ldc);
+  if (r != CUBLAS_STATUS_SUCCESS) throw Error{HQCGB_CUDA_ERROR, "cublasZgemm failed"};
+}
+
 // C[b] = A[b] B[b] for row-major M x K and K x N blocks (strides in elements;
 // stride 0 shares a block): cuBLAS strided-batched DGEMM, column-major view.
 void gemm_batched_rowmajor(int M, int N, int K, const double *A, int lda, long long sa,

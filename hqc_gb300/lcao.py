@@ -1,7 +1,8 @@
 """``make_lcao`` (hqc/pbc/lcao.py:11-103): ``lcao(xp)`` -> (mo_coeff, bands, E).
 
 Same as ``make_solver`` except the default chemical-potential search is
-Newton (lcao.py:26) and only three outputs are returned.
+Newton (lcao.py:26) and only three outputs are returned; ``gamma=False``
+gives ``lcao(xp, kpt)`` (lcao_kpt, lcao.py:80-94).
 """
 from .solver import make_solver
 
@@ -20,9 +21,14 @@ def make_lcao(n, L, rs, basis, rcut=24, tol=1e-7, max_cycle=100, grid_length=0.1
                          precision=precision, forces=forces, n_grid=n_grid,
                          exx_occ_threshold=exx_occ_threshold)
 
-    def lcao(xp):
-        mo_coeff, _, bands, E, _, _, _, _, _ = solver(xp)
-        return mo_coeff, bands, E
+    if gamma:
+        def lcao(xp):
+            mo_coeff, _, bands, E, _, _, _, _, _ = solver(xp)
+            return mo_coeff, bands, E
+    else:
+        def lcao(xp, kpt):
+            mo_coeff, _, bands, E, _, _, _, _, _ = solver(xp, kpt)
+            return mo_coeff, bands, E
 
     lcao.solver = solver
     return lcao

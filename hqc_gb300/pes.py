@@ -5,6 +5,8 @@
 ``forces=True``, ``pes.value_and_grad(xp)`` returns (E + Vpp, d/dxp) in
 Rydberg per rs unit from the engine's adjoint (absent from the reference;
 under Fermi smearing the electronic part is the gradient of E - sigma*Se).
+``gamma=False`` gives ``pes(xp, kpt)`` (pes_kpt / pes_dev_kpt,
+pes.py:88-137), without forces.
 """
 import torch
 
@@ -36,8 +38,10 @@ def make_pes(n, L, rs, basis, rcut=24, tol=1e-7, max_cycle=100, grid_length=0.12
             return torch.stack([e for e, _ in pairs]), torch.stack([g for _, g in pairs])
         return potential_energy_pp_and_grad(xp, L, rs, kappa=kappa, Gmax=Gmax)
 
-    def pes(xp):
-        _, _, _, E, Ki, Vep, Vee, Se, conv = solver(xp)
+    def pes(xp, *kpt):
+        if gamma == bool(kpt):
+            raise TypeError("pes(xp) at the Gamma point, pes(xp, kpt) with gamma=False")
+        _, _, _, E, Ki, Vep, Vee, Se, conv = solver(xp, *kpt)
         Vpp, _ = _vpp(xp)
         if mode == "dev":
             return E + Vpp, Ki, Vep, Vee, Vpp, Se, conv

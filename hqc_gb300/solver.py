@@ -62,7 +62,7 @@ class Plan:
     def __init__(self, n, L_bohr, basis, rcut, tol, max_cycle, grid_length, diis, diis_space,
                  diis_start_cycle, diis_damp, dft, xc, smearing, smearing_method, smearing_sigma,
                  search_method, search_cycle, search_tol, precision="fp64", forces=False,
-                 n_grid=None, exx_occ_threshold=0.0):
+                 n_grid=None, exx_occ_threshold=0.0, kpoint=False):
         lib = _lib.load()
         if not torch.cuda.is_available():
             raise RuntimeError("hqc_gb300 needs a CUDA GPU (no CPU fallback)")
@@ -114,9 +114,14 @@ class Plan:
         self.params = P
         self.device = torch.device("cuda", torch.cuda.current_device())
         h = ctypes.c_void_p()
-        _lib.check(lib.hqcgb_plan_create(ctypes.byref(P), ctypes.byref(h)))
+        self.kpoint = bool(kpoint)
+        if self.kpoint:
+            _lib.check(lib.hqcgb_kplan_create(ctypes.byref(P), ctypes.byref(h)))
+            self._finalizer = weakref.finalize(self, lib.hqcgb_kplan_destroy, h)
+        else:
+            _lib.check(lib.hqcgb_plan_create(ctypes.byref(P), ctypes.byref(h)))
+            self._finalizer = weakref.finalize(self, lib.hqcgb_plan_destroy, h)
         self.handle = h
-        self._finalizer = weakref.finalize(self, lib.hqcgb_plan_destroy, h)
 
     def stream(self):
         return ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
@@ -137,6 +142,27 @@ class Plan:
         xp_bohr = xp_bohr.contiguous()
         st = lib.hqcgb_scf(self.handle, ctypes.c_void_p(xp_bohr.data_ptr()), ctypes.byref(o),
                            self.stream())
+        _lib.check(st, allow=(0, 1))
+        return out
+
+    def scf_kpt(self, xps_bohr, kpts):
+        """k-point SCFs: xps_bohr (B, n, 3) on the device, kpts (B, 3) in
+        1/Bohr (host array); mo_coeff and dm come back complex128."""
+        lib = _lib.load()
+        nao, dev = self.nao, self.device
+        B = xps_bohr.shape[0]
+        out = dict(mo_coeff=torch.empty(B, nao, nao, dtype=torch.complex128, device=dev),
+                   dm=torch.empty(B, nao, nao, dtype=torch.complex128, device=dev),
+                   bands=torch.empty(B, nao, dtype=torch.float64, device=dev),
+                   energies=torch.empty(B, 5, dtype=torch.float64, device=dev),
+                   converged=torch.zeros(B, dtype=torch.int32, device=dev),
+                   iterations=torch.zeros(B, dtype=torch.int32, device=dev))
+        o = _lib.ScfOut(*[ctypes.c_void_p(out[k].data_ptr()) for k in
+                          ("mo_coeff", "dm", "bands", "energies", "converged", "iterations")])
+        xps_bohr = xps_bohr.contiguous()
+        k = np.ascontiguousarray(kpts, dtype=np.float64).reshape(B, 3)
+        st = lib.hqcgb_scf_kpt_batch(self.handle, B, ctypes.c_void_p(xps_bohr.data_ptr()),
+                                     k.ctypes.data_as(_lib.c_double_p), ctypes.byref(o), self.stream())
         _lib.check(st, allow=(0, 1))
         return out
 
@@ -177,13 +203,16 @@ class Plan:
         return g
 
     def query(self, name):
+        """An internal buffer as a flat float64 tensor (complex k-point
+        matrices as interleaved pairs: ``torch.view_as_complex`` after a
+        reshape to (..., 2))."""
         lib = _lib.load()
-        nbytes = lib.hqcgb_plan_query(self.handle, name.encode(), None, 0, self.stream())
+        q = lib.hqcgb_kplan_query if self.kpoint else lib.hqcgb_plan_query
+        nbytes = q(self.handle, name.encode(), None, 0, self.stream())
         if nbytes < 0:
             raise KeyError(name)
         t = torch.empty(nbytes // 8, dtype=torch.float64, device=self.device)
-        lib.hqcgb_plan_query(self.handle, name.encode(), ctypes.c_void_p(t.data_ptr()), nbytes,
-                             self.stream())
+        q(self.handle, name.encode(), ctypes.c_void_p(t.data_ptr()), nbytes, self.stream())
         return t
 
 
@@ -225,11 +254,24 @@ def make_solver(n: int, L: float, rs: float, basis: str,
     axis -- what ``jax.vmap(solver)`` returns for the reference
     (test/test.py:157); ``concurrency`` configurations of a batch run at once.
     ``use_jit`` is accepted for signature compatibility (the engine is always
-    compiled).  Only the Gamma point is implemented (``gamma=True``).
+    compiled).
+
+    ``gamma=False`` returns ``solver(xp, kpt)`` for one k-point (kpt (3,) in
+    1/Bohr, first Brillouin zone (-pi/(L rs), pi/(L rs)); solver.py:769-962):
+    the same tuple with complex128 mo_coeff and dm.  It runs in FP64 without
+    forces; a batch of xp (B, n, 3) and/or kpt (B, 3) broadcasts like
+    ``jax.vmap``.
     """
-    if not gamma:
-        raise NotImplementedError("single k-point solver (gamma=False) is not implemented")
     L_bohr = float(L) * float(rs)
+    if not gamma:
+        if precision != "fp64":
+            raise NotImplementedError("the k-point solver runs in FP64 only (precision='fp64')")
+        if forces:
+            raise NotImplementedError("the k-point solver has no forces")
+        return _make_kpoint_solver(n, L_bohr, rs, basis, rcut, tol, max_cycle, grid_length, diis,
+                                   diis_space, diis_start_cycle, diis_damp, dft, xc, smearing,
+                                   smearing_method, smearing_sigma, search_method, search_cycle,
+                                   search_tol, n_grid, exx_occ_threshold)
     plan = Plan(n, L_bohr, basis, rcut, tol, max_cycle, grid_length, diis, diis_space,
                 diis_start_cycle, diis_damp, dft, xc, smearing, smearing_method, smearing_sigma,
                 search_method, search_cycle, search_tol, precision=precision, forces=forces,
@@ -266,5 +308,36 @@ def make_solver(n: int, L: float, rs: float, basis: str,
     solver.plan = plan
     solver.grad = grad
     solver.batch = batch
+    solver.n_grid = plan.ng
+    return solver
+
+
+def _make_kpoint_solver(n, L_bohr, rs, basis, rcut, tol, max_cycle, grid_length, diis, diis_space,
+                        diis_start_cycle, diis_damp, dft, xc, smearing, smearing_method,
+                        smearing_sigma, search_method, search_cycle, search_tol, n_grid,
+                        exx_occ_threshold):
+    plan = Plan(n, L_bohr, basis, rcut, tol, max_cycle, grid_length, diis, diis_space,
+                diis_start_cycle, diis_damp, dft, xc, smearing, smearing_method, smearing_sigma,
+                search_method, search_cycle, search_tol, precision="fp64", forces=False,
+                n_grid=n_grid, exx_occ_threshold=exx_occ_threshold, kpoint=True)
+
+    def solver(xp, kpt):
+        xp_t = _as_device(xp, plan.device)
+        k = np.asarray(kpt.detach().cpu() if isinstance(kpt, torch.Tensor) else kpt, dtype=np.float64)
+        batched = xp_t.dim() == 3 or k.ndim == 2
+        B = max(xp_t.shape[0] if xp_t.dim() == 3 else 1, k.shape[0] if k.ndim == 2 else 1)
+        xps = xp_t.expand(B, n, 3) if xp_t.dim() == 3 else xp_t.reshape(1, n, 3).expand(B, n, 3)
+        ks = np.broadcast_to(k.reshape(-1, 3), (B, 3))
+        out = plan.scf_kpt(xps.contiguous() * rs, ks)
+        solver.iterations = out["iterations"].tolist()
+        e = out["energies"]
+        res = (out["mo_coeff"], out["dm"], out["bands"] * RY, e[:, 0] * RY, e[:, 1] * RY,
+               e[:, 2] * RY, e[:, 3] * RY, e[:, 4], out["converged"] != 0)
+        if not batched:
+            res = tuple(r[0] for r in res)
+            solver.iterations = solver.iterations[0]
+        return res
+
+    solver.plan = plan
     solver.n_grid = plan.ng
     return solver

@@ -208,6 +208,44 @@ int hqcgb_tc_orbital_density(int nao, long long N, long long ld, const float *ph
  * No counterpart in the reference. */
 int hqcgb_eigh_noalloc(int n, const double *A, double *w, double *V, void *stream);
 
+/* ---- single k-point solver (make_solver with gamma=False) ---------------- */
+
+typedef struct hqcgb_kplan hqcgb_kplan;
+
+/* Factory of the k-point solver: the same parameters as hqcgb_plan_create
+ * (precision must be HQCGB_PREC_FP64, want_forces 0).  Replaces the
+ * table-building part of make_solver(gamma=False) (hqc/pbc/solver.py:209-231,
+ * 378-389). */
+int hqcgb_kplan_create(const hqcgb_params *params, hqcgb_kplan **plan);
+int hqcgb_kplan_destroy(hqcgb_kplan *plan);
+
+/* One SCF at proton positions xp [n_atoms][3] (Bohr, device) and k-point
+ * kpt [3] (1/Bohr, HOST).  Replaces hf_kpt / dft_kpt (hqc/pbc/solver.py:
+ * 769-837, 901-962).  mo_coeff and dm are complex, interleaved (re, im):
+ * 2 * nao * nao doubles each; the other outputs as in hqcgb_scf. */
+int hqcgb_scf_kpt(hqcgb_kplan *plan, const double *xp, const double *kpt,
+                  const hqcgb_scf_out *out, void *stream);
+
+/* n_cfg k-point SCFs in sequence: xp [n_cfg][n_atoms][3] (device), kpts
+ * [n_cfg][3] (host); outputs strided by their per-configuration sizes (the
+ * reference's jax.vmap(solver) over (xp, kpt)).  Returns the worst status. */
+int hqcgb_scf_kpt_batch(hqcgb_kplan *plan, int n_cfg, const double *xp, const double *kpts,
+                        const hqcgb_scf_out *out, void *stream);
+
+/* Copy an internal buffer of the last k-point SCF into dst (device): "S",
+ * "T", "V", "H", "D", "F", "K", "St" (complex nao x nao), "phi" (conjugated
+ * Bloch AOs, complex nao x N), "rho", "vh", "vloc" (real N).  Bytes copied
+ * (or needed when dst is NULL), < 0 on error. */
+long long hqcgb_kplan_query(hqcgb_kplan *plan, const char *name, void *dst, size_t bytes,
+                            void *stream);
+
+/* Complex Hermitian FP64 eigensolver on `batch` row-major n x n matrices A
+ * (complex, interleaved; device, not modified; both triangles are read, so A
+ * must be Hermitian): ascending eigenvalues w [batch][n] and eigenvectors as
+ * the columns of V [batch][n][n] (complex).  The k-point solver's
+ * jnp.linalg.eigh (hqc/pbc/solver.py:795, 812; hqc/pbc/scf.py:69,138,198). */
+int hqcgb_eigh_herm(int n, int batch, const double *A, double *w, double *V, void *stream);
+
 /* Human-readable description of the last error on this host thread. */
 const char *hqcgb_last_error(void);
 
