@@ -88,6 +88,9 @@ void launch_add3(long long N, const double *a, const double *b, const double *c,
 
 void zgemm(char opa, char opb, int M, int N, int K, double2 alpha, const double2 *A, int lda,
            const double2 *B, int ldb, double2 beta, double2 *C, int ldc, cudaStream_t st);
+void zgemm_batched_rowmajor(int M, int N, int K, const double2 *A, int lda, long long sa,
+                            const double2 *B, int ldb, long long sb, double2 *C, int ldc,
+                            long long sc, int batch, cudaStream_t st);
 size_t ovl_scratch_doubles_kpt(int n, int nprim);
 void launch_overlap_kinetic_kpt(const double *xp, int n, int nb, int nprim, const double *alpha,
                                 const double *coef, const int *ao_l, const int *ao_cart,

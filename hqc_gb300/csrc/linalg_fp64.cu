@@ -112,6 +112,20 @@ void gemm_batched_rowmajor(int M, int N, int K, const double *A, int lda, long l
   if (r != CUBLAS_STATUS_SUCCESS) throw Error{HQCGB_CUDA_ERROR, "cublasDgemmStridedBatched failed"};
 }
 
+// Complex C[b] = A[b] B[b] (row-major, strides in elements; stride 0 shares a
+// block): cuBLAS strided-batched ZGEMM on the column-major view.
+void zgemm_batched_rowmajor(int M, int N, int K, const double2 *A, int lda, long long sa,
+                            const double2 *B, int ldb, long long sb, double2 *C, int ldc,
+                            long long sc, int batch, cudaStream_t st) {
+  HQ_STAGE(ST_GEMM_SMALL, st);
+  cublasHandle_t h = blas_handle();
+  cublasSetStream(h, st);
+  const double2 one = make_double2(1.0, 0.0), zero = make_double2(0.0, 0.0);
+  cublasStatus_t r = cublasZgemmStridedBatched(h, CUBLAS_OP_N, CUBLAS_OP_N, N, M, K, &one, B, ldb, sb,
+                                               A, lda, sa, &zero, C, ldc, sc, batch);
+  if (r != CUBLAS_STATUS_SUCCESS) throw Error{HQCGB_CUDA_ERROR, "cublasZgemmStridedBatched failed"};
+}
+
 // out = a*X + b*Y (+ c*Z^T): generic elementwise combos on n x n matrices.
 __global__ void k_axpby(int n, double a, const double *__restrict__ X, double b,
                         const double *__restrict__ Y, int transY, double *__restrict__ out) {

@@ -142,6 +142,20 @@ int hqcgb_slater(int n, int nao_atom, int n_prim, const double *alpha, const dou
                  int xp_groups, const double *xp, const double *xe, const double *mo, int nmo,
                  const int *state_idx, double *up, double *dn, void *stream);
 
+/* k-point variants (make_pbc_gto with gamma=False, eval_pbc_ao_kpt,
+ * hqc/pbc/gto.py:371-427; make_slater's slater_kpt, hqc/pbc/slater.py:72-93):
+ * every lattice term carries exp(i k.t), kpt [3] in 1/Bohr (HOST).  out,
+ * mo, up and dn are complex, interleaved (re, im); other arguments as above. */
+int hqcgb_ao_points_kpt(int n_atoms, int nao_atom, int n_prim, const double *alpha,
+                        const double *coef, const int *ao_l, const int *ao_cart, int n_lat1d,
+                        const double *lat1d, const double *kpt, const double *xp, long long npts,
+                        int pts_per_group, const double *xe, double *out, void *stream);
+int hqcgb_slater_kpt(int n, int nao_atom, int n_prim, const double *alpha, const double *coef,
+                     const int *ao_l, const int *ao_cart, int n_lat1d, const double *lat1d,
+                     const double *kpt, int W, int xp_groups, const double *xp, const double *xe,
+                     const double *mo, int nmo, const int *state_idx, double *up, double *dn,
+                     void *stream);
+
 /* Nuclear gradient dE/dR [n_atoms][3] (Hartree/Bohr, device) of the last SCF.
  * No counterpart in the reference (forces are absent there,
  * doc/solver_algorithm.md:1210); with Fermi smearing it is the gradient of

@@ -156,6 +156,23 @@ def run_gto_case():
     return rec, dict(n=n, rs=rs, seeds=43)
 
 
+def run_gto_kpt_case():
+    """eval_pbc_ao_kpt values (``hqc/pbc/gto.py:371-427``): Bloch AOs at a
+    random k-point of the first Brillouin zone, random electrons."""
+    n, rs = 8, 1.5
+    L = box(n) * rs
+    rng = np.random.default_rng(44)
+    xp = rng.uniform(0.0, L, (n, 3))
+    xe = rng.uniform(0.0, L, (16, 3))
+    kpt = rng.uniform(-np.pi / L, np.pi / L, 3)
+    rec = dict(xp=xp, xe=xe, L=L, kpt=kpt)
+    for basis in ("gth-szv", "gth-dzv", "gth-dzvp"):
+        f = make_pbc_gto(basis, L, gamma=False)
+        vals = np.stack([np.asarray(f(jnp.array(xp), jnp.array(e), jnp.array(kpt))) for e in xe])
+        rec["ao_" + basis.replace("-", "_")] = vals
+    return rec, dict(n=n, rs=rs, seeds=44)
+
+
 def run_vpp_case():
     """potential_energy_pp (``hqc/pbc/potential.py:103-130``)."""
     rec = {}
@@ -178,13 +195,15 @@ def run_vpp_case():
 def main(selected):
     manifest_path = os.path.join(HERE, "manifest.json")
     manifest = json.load(open(manifest_path)) if os.path.exists(manifest_path) else {}
-    jobs = list(SOLVER_CASES) + ["gto_values", "vpp"]
+    jobs = list(SOLVER_CASES) + ["gto_values", "gto_values_kpt", "vpp"]
     if selected:
         jobs = [j for j in jobs if j in selected]
     for name in jobs:
         t0 = time.time()
         if name == "gto_values":
             rec, meta = run_gto_case()
+        elif name == "gto_values_kpt":
+            rec, meta = run_gto_kpt_case()
         elif name == "vpp":
             rec, meta = run_vpp_case()
         else:

@@ -45,3 +45,46 @@ def test_slater_matrices_and_walker_batches():
     ao = ex.ao_values(xps[2], xe[2]).cpu().numpy()
     np.testing.assert_allclose(up2[2].cpu().numpy(), ao[:4] @ mo[:, idx[:4]], atol=1e-12)
     np.testing.assert_allclose(dn2[2].cpu().numpy(), ao[4:] @ mo[:, idx[4:]], atol=1e-12)
+
+
+@pytest.mark.parametrize("basis", ["gth-szv", "gth-dzv", "gth-dzvp"])
+def test_ao_values_kpt_match_reference_golden(basis):
+    """Bloch AOs against the reference's eval_pbc_ao_kpt (gto.py:371-427)."""
+    from hqc_gb300 import make_slater
+    meta, z = load_golden("gto_values_kpt")
+    n, rs = meta["n"], meta["rs"]
+    L = float(z["L"]) / rs
+    sl = make_slater(n, L, rs, basis, gamma=False)
+    ao = sl.ao_values(z["xp"] / rs, z["xe"] / rs, z["kpt"]).cpu().numpy()
+    np.testing.assert_allclose(ao, z["ao_" + basis.replace("-", "_")], atol=1e-12)
+
+
+def test_slater_kpt_matrices_and_walker_batches():
+    """slater_kpt (hqc/pbc/slater.py:72-93): complex AO values times complex
+    MOs; the k-point SCF's own mo_coeff as the orbitals."""
+    from hqc_gb300 import make_slater, make_solver
+    n, rs, basis = 8, 1.5, "gth-dzv"
+    L = (4 / 3 * np.pi * n) ** (1 / 3)
+    rng = np.random.default_rng(6)
+    xp = rng.uniform(0, L, (n, 3))
+    xe = rng.uniform(0, L, (3, n, 3))
+    kpt = rng.uniform(-np.pi / L / rs, np.pi / L / rs, 3)
+    mo = make_solver(n, L, rs, basis, grid_length=0.2, gamma=False)(xp, kpt)[0].cpu().numpy()
+    sl = make_slater(n, L, rs, basis, gamma=False)
+    up, dn = sl(xp, xe, mo, kpt)
+    assert up.dtype.is_complex
+    for w in range(3):
+        ao = sl.ao_values(xp, xe[w], kpt).cpu().numpy()
+        np.testing.assert_allclose(up[w].cpu().numpy(), ao[:n // 2] @ mo[:, :n // 2], atol=1e-12)
+        np.testing.assert_allclose(dn[w].cpu().numpy(), ao[n // 2:] @ mo[:, :n // 2], atol=1e-12)
+    ex = make_slater(n, L, rs, basis, groundstate=False, gamma=False)
+    idx = np.array([0, 1, 2, 5, 0, 1, 3, 4])
+    up2, dn2 = ex(xp, xe[1], mo, kpt, idx)
+    ao = ex.ao_values(xp, xe[1], kpt).cpu().numpy()
+    np.testing.assert_allclose(up2.cpu().numpy(), ao[:4] @ mo[:, idx[:4]], atol=1e-12)
+    np.testing.assert_allclose(dn2.cpu().numpy(), ao[4:] @ mo[:, idx[4:]], atol=1e-12)
+    # k = 0 reduces to the Gamma AO values
+    g = make_slater(n, L, rs, basis).ao_values(xp, xe[0]).cpu().numpy()
+    k0 = sl.ao_values(xp, xe[0], np.zeros(3)).cpu().numpy()
+    np.testing.assert_allclose(k0.real, g, atol=1e-13)
+    assert np.abs(k0.imag).max() == 0.0

@@ -100,20 +100,37 @@ def test_gto_values_match_reference():
     for basis in ("gth-szv", "gth-dzv", "gth-dzvp"):
         st = Setup(meta["n"], L / meta["rs"], meta["rs"], basis, n_grid=5)
         ref = z["ao_" + basis.replace("-", "_")]
-        b = st.basis
-        xp, xe = z["xp"], z["xe"]
-        # evaluate the lattice-summed AOs at arbitrary points
-        out = np.zeros_like(ref)
-        for e, r in enumerate(xe):
-            for A in range(xp.shape[0]):
-                u = r[:, None] - xp[A][:, None] - st.lat1d[None, :]  # (3, t)
-                g = np.exp(-b.alpha[None, :, None] * u[:, None, :] ** 2)  # (3,a,t)
-                g0 = g.sum(-1)
-                g1 = (g * u[:, None, :]).sum(-1)
-                for k in range(b.nao):
-                    f = [g0[d] if not (b.l[k] == 1 and b.cart[k] == d) else g1[d] for d in range(3)]
-                    out[e, A * b.nao + k] = np.sum(b.coef[k] * f[0] * f[1] * f[2])
+        out = _ao_at_points(st, z["xp"], z["xe"])
         np.testing.assert_allclose(out, ref, atol=1e-12, rtol=1e-10)
+
+
+def _ao_at_points(st, xp, xe, kpt=None):
+    """Lattice-summed AOs at arbitrary points (Bloch sums with exp(i k.t)
+    when a k-point is given), from the oracle's basis tables."""
+    b = st.basis
+    out = np.zeros((xe.shape[0], xp.shape[0] * b.nao), dtype=float if kpt is None else complex)
+    for e, r in enumerate(xe):
+        for A in range(xp.shape[0]):
+            u = r[:, None] - xp[A][:, None] - st.lat1d[None, :]  # (3, t)
+            g = np.exp(-b.alpha[None, :, None] * u[:, None, :] ** 2)  # (3,a,t)
+            if kpt is not None:
+                g = g * np.exp(1j * np.asarray(kpt)[:, None] * st.lat1d[None, :])[:, None, :]
+            g0 = g.sum(-1)
+            g1 = (g * u[:, None, :]).sum(-1)
+            for k in range(b.nao):
+                f = [g0[d] if not (b.l[k] == 1 and b.cart[k] == d) else g1[d] for d in range(3)]
+                out[e, A * b.nao + k] = np.sum(b.coef[k] * f[0] * f[1] * f[2])
+    return out
+
+
+def test_gto_values_kpt_match_reference():
+    """Bloch AOs of eval_pbc_ao_kpt (gto.py:371-427) at random points."""
+    meta, z = load_golden("gto_values_kpt")
+    L = float(z["L"])
+    for basis in ("gth-szv", "gth-dzv", "gth-dzvp"):
+        st = Setup(meta["n"], L / meta["rs"], meta["rs"], basis, n_grid=5)
+        out = _ao_at_points(st, z["xp"], z["xe"], z["kpt"])
+        np.testing.assert_allclose(out, z["ao_" + basis.replace("-", "_")], atol=1e-12, rtol=1e-10)
 
 
 def test_vpp_matches_reference_and_madelung():
