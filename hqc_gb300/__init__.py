@@ -1,14 +1,17 @@
 """GB300-native (sm_103a) periodic GPW SCF engine with hqc's Python API.
 
-Drop-in factories: ``make_solver``, ``make_lcao``, ``make_pes``,
-``make_slater`` and ``potential_energy_pp`` (reference: ZihangL/hqc
+Drop-in factories: ``make_solver``, ``make_lcao``, ``make_pes`` (Gamma
+and single k-point), ``make_slater``, ``make_overlap``, and the Ewald sums
+``potential_energy_pp`` / ``potential_energy`` (reference: ZihangL/hqc
 ``hqc/pbc``).  The compute
 runs in ``libhqcgb.so`` (``include/hqcgb.h``); there is no CPU fallback.
 """
 from .solver import make_solver  # noqa: F401
 from .lcao import make_lcao  # noqa: F401
 from .pes import make_pes  # noqa: F401
-from .potential import potential_energy_pp, potential_energy_pp_and_grad  # noqa: F401
+from .potential import (potential_energy_pp, potential_energy_pp_and_grad,  # noqa: F401
+                        potential_energy, kpoints, Madelung)
+from .overlap import make_overlap  # noqa: F401
 from .slater import make_slater  # noqa: F401
 from . import basis  # noqa: F401
 

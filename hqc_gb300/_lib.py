@@ -49,7 +49,7 @@ EXPORTS = ("hqcgb_plan_create", "hqcgb_plan_destroy", "hqcgb_scf", "hqcgb_scf_ba
            "hqcgb_tc_orbital_density", "hqcgb_plan_set_concurrency", "hqcgb_pes_batch",
            "hqcgb_ao_points", "hqcgb_slater", "hqcgb_kplan_create", "hqcgb_kplan_destroy",
            "hqcgb_scf_kpt", "hqcgb_scf_kpt_batch", "hqcgb_kplan_query", "hqcgb_eigh_herm",
-           "hqcgb_ao_points_kpt", "hqcgb_slater_kpt")
+           "hqcgb_ao_points_kpt", "hqcgb_slater_kpt", "hqcgb_overlap", "hqcgb_coulomb_energy")
 N_STAGES = 14
 
 _lib = None
@@ -95,6 +95,13 @@ def load():
                                      ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                      ctypes.c_void_p, ctypes.c_int, c_int_p, ctypes.c_void_p,
                                      ctypes.c_void_p, ctypes.c_void_p]
+    lib.hqcgb_overlap.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, c_double_p, c_double_p,
+                                  c_int_p, c_int_p, ctypes.c_int, c_double_p, ctypes.c_int,
+                                  ctypes.c_void_p, c_double_p, ctypes.c_void_p, ctypes.c_void_p,
+                                  ctypes.c_void_p]
+    lib.hqcgb_coulomb_energy.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                         ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                         c_int_p, ctypes.c_void_p, ctypes.c_void_p]
     lib.hqcgb_pes_batch.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                     ctypes.POINTER(ScfOut), ctypes.c_void_p, ctypes.c_void_p]
     lib.hqcgb_ewald.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_double,

@@ -156,6 +156,25 @@ int hqcgb_slater_kpt(int n, int nao_atom, int n_prim, const double *alpha, const
                      const double *mo, int nmo, const int *state_idx, double *up, double *dn,
                      void *stream);
 
+/* Overlap matrices without a plan: make_overlap (hqc/pbc/overlap.py:11-319)
+ * for n_cfg configurations xp [n_cfg][n_atoms][3] (device, Bohr) over the
+ * lattice sphere `lattice` [n_lattice][3] (host, Bohr; |t| <= rcut).  kpts
+ * NULL: real S [n_cfg][nao][nao]; kpts [n_cfg][3] (host, 1/Bohr): complex
+ * Hermitian S^k (interleaved).  T (kinetic, same layout) may be NULL. */
+int hqcgb_overlap(int n_atoms, int nao_atom, int n_prim, const double *alpha, const double *coef,
+                  const int *ao_l, const int *ao_cart, int n_lattice, const double *lattice,
+                  int n_cfg, const double *xp, const double *kpts, double *S, double *T,
+                  void *stream);
+
+/* Ewald energies of proton + electron configurations, batched over walkers:
+ * potential_energy (hqc/pbc/potential.py:69-101).  x [B][n][dim] (device, rs
+ * units; the first n/2 particles are protons), L the box side (rs units),
+ * G [nG][dim] the integer reciprocal vectors (host; kpoints(dim, Gmax));
+ * out [B][3] = (vpp, vep, vee) (device), 2 rs / L times the pair sums as in
+ * the reference (the Madelung constant is not included). */
+int hqcgb_coulomb_energy(int B, int n, int dim, const double *x, double L, double rs, double kappa,
+                         int nG, const int *G, double *out, void *stream);
+
 /* Nuclear gradient dE/dR [n_atoms][3] (Hartree/Bohr, device) of the last SCF.
  * No counterpart in the reference (forces are absent there,
  * doc/solver_algorithm.md:1210); with Fermi smearing it is the gradient of

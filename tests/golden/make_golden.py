@@ -35,7 +35,8 @@ from hqc.pbc.solver import make_solver  # noqa: E402
 from hqc.pbc.lcao import make_lcao  # noqa: E402
 from hqc.pbc.pes import make_pes  # noqa: E402
 from hqc.pbc.gto import make_pbc_gto  # noqa: E402
-from hqc.pbc.potential import potential_energy_pp  # noqa: E402
+from hqc.pbc.overlap import make_overlap  # noqa: E402
+from hqc.pbc.potential import potential_energy_pp, potential_energy, kpoints, Madelung  # noqa: E402
 
 
 def box(n):
@@ -173,6 +174,44 @@ def run_gto_kpt_case():
     return rec, dict(n=n, rs=rs, seeds=44)
 
 
+def run_coulomb_case():
+    """potential_energy (``hqc/pbc/potential.py:69-101``) of proton + electron
+    walker batches, with kpoints / Madelung (6-33), as in
+    ``test/tools/observables.py:8-25``: 3D (Gmax 15, kappa 10) and a 2D case."""
+    rec, meta = {}, {}
+    rng = np.random.default_rng(45)
+    for tag, n, rs, dim, gmax in (("h8", 8, 1.31, 3, 15), ("h16", 16, 1.5, 3, 15), ("d2", 6, 1.2, 2, 10)):
+        L = box(n) if dim == 3 else np.sqrt(np.pi * n)
+        x = rng.uniform(-0.5 * L, 1.5 * L, (3, 2 * n, dim))  # protons then electrons, some outside the box
+        G = np.asarray(kpoints(dim, gmax))
+        vpp, vep, vee = potential_energy(jnp.array(x.copy()), 10.0, G, L, rs)
+        rec["x_" + tag] = x
+        rec["vpp_" + tag], rec["vep_" + tag], rec["vee_" + tag] = (np.asarray(v) for v in (vpp, vep, vee))
+        rec["madelung_" + tag] = np.asarray(Madelung(dim, 10.0, G))
+        rec["L_" + tag] = np.asarray(L)
+        meta[tag] = dict(n=n, rs=rs, dim=dim, Gmax=gmax, kappa=10.0)
+    return rec, meta
+
+
+def run_overlap_case():
+    """make_overlap (``hqc/pbc/overlap.py:11-319``) at Gamma and at a k-point,
+    rcut 18 and 24, the three bases."""
+    n, rs = 4, 1.5
+    L = box(n)
+    rng = np.random.default_rng(46)
+    xp = rng.uniform(0.0, L, (n, 3))
+    kpt = rng.uniform(-np.pi / L / rs, np.pi / L / rs, 3)
+    rec = dict(xp=xp, kpt=kpt, L=np.asarray(L))
+    for basis in ("gth-szv", "gth-dzv", "gth-dzvp"):
+        tag = basis.replace("-", "_")
+        for rcut in (18, 24):
+            f = make_overlap(n, L, rs, basis, rcut=rcut, gamma=True, use_jit=False)
+            rec[f"S_{tag}_{rcut}"] = np.asarray(f(jnp.array(xp.copy())))
+        fk = make_overlap(n, L, rs, basis, rcut=24, gamma=False, use_jit=False)
+        rec[f"Sk_{tag}"] = np.asarray(fk(jnp.array(xp.copy()), jnp.array(kpt)))
+    return rec, dict(n=n, rs=rs, seeds=46)
+
+
 def run_vpp_case():
     """potential_energy_pp (``hqc/pbc/potential.py:103-130``)."""
     rec = {}
@@ -195,7 +234,7 @@ def run_vpp_case():
 def main(selected):
     manifest_path = os.path.join(HERE, "manifest.json")
     manifest = json.load(open(manifest_path)) if os.path.exists(manifest_path) else {}
-    jobs = list(SOLVER_CASES) + ["gto_values", "gto_values_kpt", "vpp"]
+    jobs = list(SOLVER_CASES) + ["gto_values", "gto_values_kpt", "vpp", "coulomb_pe", "overlap"]
     if selected:
         jobs = [j for j in jobs if j in selected]
     for name in jobs:
@@ -204,6 +243,10 @@ def main(selected):
             rec, meta = run_gto_case()
         elif name == "gto_values_kpt":
             rec, meta = run_gto_kpt_case()
+        elif name == "coulomb_pe":
+            rec, meta = run_coulomb_case()
+        elif name == "overlap":
+            rec, meta = run_overlap_case()
         elif name == "vpp":
             rec, meta = run_vpp_case()
         else:

@@ -168,3 +168,31 @@ def test_oracle_gradient_matches_finite_differences(kw):
             e.append(Solver(n, L, rs, "gth-szv", **common).solve(x)[3])
         fd = (e[0] - e[1]) / (2 * h * rs) / 2  # Ry per rs unit -> Ha/Bohr
         assert abs(fd - g[a, d]) < 2e-6, (a, d, fd, g[a, d])
+
+
+def test_potential_energy_matches_reference():
+    """Proton + electron Ewald sums of walker batches (potential.py:69-101),
+    3D and 2D, with the reference's kpoints / Madelung."""
+    from oracle.ewald import potential_energy, kpoints, madelung_dim
+    meta, z = load_golden("coulomb_pe")
+    for tag, m in meta.items():
+        G = kpoints(m["dim"], m["Gmax"])
+        out = potential_energy(z["x_" + tag], m["kappa"], G, float(z["L_" + tag]), m["rs"])
+        for v, k in zip(out, ("vpp", "vep", "vee")):
+            np.testing.assert_allclose(v, z[k + "_" + tag], atol=1e-12, err_msg=tag + k)
+        assert abs(madelung_dim(m["dim"], m["kappa"], G) - z["madelung_" + tag]) < 1e-13
+
+
+def test_overlap_matches_reference():
+    """Standalone make_overlap (overlap.py:11-319): Gamma at rcut 18 and 24,
+    and a k-point (complex Hermitian S^k)."""
+    meta, z = load_golden("overlap")
+    n, rs, L = meta["n"], meta["rs"], float(z["L"])
+    xp = z["xp"] * rs
+    for basis in ("gth-szv", "gth-dzv", "gth-dzvp"):
+        tag = basis.replace("-", "_")
+        for rcut in (18, 24):
+            st = Setup(n, L, rs, basis, rcut=rcut, n_grid=5)
+            np.testing.assert_allclose(st.overlap_kinetic(xp)[0], z[f"S_{tag}_{rcut}"], atol=1e-13)
+        st = Setup(n, L, rs, basis, rcut=24, n_grid=5)
+        np.testing.assert_allclose(st.overlap_kinetic(xp, kpt=z["kpt"])[0], z[f"Sk_{tag}"], atol=1e-13)
