@@ -58,8 +58,10 @@ __global__ void k_ovl_lattice(const double *__restrict__ xp, int n, int nprim,
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int np2 = nprim * nprim;
   if (idx >= (long long)n * n * np2) return;
-  const int ab = (int)(idx % np2), a = ab / nprim, b = ab % nprim;
-  const int j = (int)((idx / np2) % n), i = (int)(idx / ((long long)np2 * n));
+  // atom pairs fastest: a warp shares one primitive pair (one mu), so its
+  // lanes skip the same far lattice terms
+  const int ab = (int)(idx / ((long long)n * n)), a = ab / nprim, b = ab % nprim;
+  const int ij = (int)(idx % ((long long)n * n)), i = ij / n, j = ij % n;
   double R[3];
   for (int d = 0; d < 3; ++d) R[d] = xp[i * 3 + d] - xp[j * 3 + d];
   const double asum = alpha[a] + alpha[b];
@@ -78,7 +80,9 @@ __global__ void k_ovl_lattice(const double *__restrict__ xp, int n, int nprim,
       u2 += u[d] * u[d];
     }
     double e = mu * u2;
-    if (e > 700.0) continue;
+    // exp(-60) times the largest Hermite factor (degree <= 5) is below 1e-18
+    // of every matrix element: far images add nothing in FP64
+    if (e > 60.0) continue;
     e = K * exp(-e);
     double ei = 0.0;
     if (KPT) {
@@ -106,7 +110,7 @@ __global__ void k_ovl_lattice(const double *__restrict__ xp, int n, int nprim,
       }
     }
   }
-  double *out = Q + idx * ((KPT ? 4 : 2) * kNq);
+  double *out = Q + (((long long)i * n + j) * np2 + ab) * ((KPT ? 4 : 2) * kNq);
 #pragma unroll
   for (int k = 0; k < NQ; ++k) {
     out[k] = qs[k];
@@ -273,83 +277,146 @@ void launch_overlap_kinetic_kpt(const double *xp, int n, int nb, int nprim, cons
 }
 
 // ---------------------------------------------------------------------------
-// Ewald (potential.py:103-130).  xp in rs units, L in rs units.  One block per
-// pair (i<j) accumulates psi and its gradient over G; the self term is added
-// by block 0.  energy in Ry; grad in Ry per rs unit.
+// Ewald (potential.py:103-130).  xp in rs units, L in rs units; energy in Ry,
+// grad in Ry per rs unit.  psi(r) = erfc(kappa |r|)/|r| (nearest image) +
+// sum_G g(G) cos(2 pi G.r) + g0 over 0 < |G|^2 <= Gmax^2 (L = 1 units).  The
+// reciprocal part of sum_{i<j} psi(r_ij) is taken from the structure factor
+// S(G) = sum_i exp(2 pi i G.x_i / L):  sum_{i<j} cos(2 pi G.r_ij) =
+// (|S|^2 - n) / 2, and its derivative with respect to atom a is
+// -2 pi G Im(conj(S) exp(2 pi i G.x_a / L)) -- n N_G phases instead of the
+// pairwise n^2 N_G / 2.
 // ---------------------------------------------------------------------------
-__global__ void k_ewald_pairs(const double *__restrict__ xp, int n, double L, double kappa,
-                              int gmax, double *__restrict__ pair_e, double *__restrict__ pair_g) {
+constexpr int kEwThreads = 256;
+
+__device__ inline bool ewald_g(long long k, int gmax, int &gx, int &gy, int &gz, int &G2) {
+  const int side = 2 * gmax + 1;
+  gx = (int)(k / ((long long)side * side)) - gmax;
+  gy = (int)((k / side) % side) - gmax;
+  gz = (int)(k % side) - gmax;
+  G2 = gx * gx + gy * gy + gz * gz;
+  return G2 != 0 && G2 <= gmax * gmax;
+}
+
+__device__ inline double ewald_gk(int G2, double kappa) {
+  return exp(-M_PI * M_PI * G2 / (kappa * kappa)) / (M_PI * G2);
+}
+
+// S(G) per cube point (0 outside the sphere) and the reciprocal energy per block
+__global__ void __launch_bounds__(kEwThreads)
+    k_ewald_sf(const double *__restrict__ xp, int n, double L, double kappa, int gmax,
+               double2 *__restrict__ S, double *__restrict__ part_e) {
   __shared__ double sh[32];
-  int pidx = blockIdx.x;
-  // decode pair index -> (i, j), i < j (row-major over the upper triangle)
-  int i = 0, rem = pidx;
-  while (rem >= n - 1 - i) { rem -= n - 1 - i; ++i; }
-  int j = i + 1 + rem;
-  double r[3];
-  for (int d = 0; d < 3; ++d) {
-    double a = xp[i * 3 + d] - L * floor(xp[i * 3 + d] / L);
-    double b = xp[j * 3 + d] - L * floor(xp[j * 3 + d] / L);
-    double x = (a - b) / L;
-    r[d] = x - rint(x);
+  const int side = 2 * gmax + 1;
+  const long long nG = (long long)side * side * side;
+  const long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double e = 0;
+  if (k < nG) {
+    int gx, gy, gz, G2;
+    double sr = 0, si = 0;
+    if (ewald_g(k, gmax, gx, gy, gz, G2)) {
+      for (int i = 0; i < n; ++i) {
+        const double ph = (gx * xp[i * 3] + gy * xp[i * 3 + 1] + gz * xp[i * 3 + 2]) / L;
+        double sn, cs;
+        sincospi(2.0 * ph, &sn, &cs);
+        sr += cs;
+        si += sn;
+      }
+      e = ewald_gk(G2, kappa) * 0.5 * (sr * sr + si * si - n);
+    }
+    S[k] = make_double2(sr, si);
   }
-  int side = 2 * gmax + 1;
-  long long nG = (long long)side * side * side;
-  double v = 0, g[3] = {0, 0, 0};
+  e = block_sum(e, sh);
+  if (threadIdx.x == 0) part_e[blockIdx.x] = e;
+}
+
+// reciprocal derivative of sum_{i<j} psi with respect to r_a (L = 1 units); one block per atom
+__global__ void __launch_bounds__(kEwThreads)
+    k_ewald_recip_grad(const double *__restrict__ xp, int n, double L, double kappa, int gmax,
+                       const double2 *__restrict__ S, double *__restrict__ gr) {
+  __shared__ double sh[32];
+  const int a = blockIdx.x;
+  const int side = 2 * gmax + 1;
+  const long long nG = (long long)side * side * side;
+  double g0 = 0, g1 = 0, g2 = 0;
   for (long long k = threadIdx.x; k < nG; k += blockDim.x) {
-    int gx = (int)(k / (side * side)) - gmax, gy = (int)((k / side) % side) - gmax,
-        gz = (int)(k % side) - gmax;
-    int G2 = gx * gx + gy * gy + gz * gz;
-    if (G2 == 0 || G2 > gmax * gmax) continue;
-    double gk = exp(-M_PI * M_PI * G2 / (kappa * kappa)) / (M_PI * G2);
-    double ph = 2.0 * M_PI * (gx * r[0] + gy * r[1] + gz * r[2]);
-    double s, c;
-    sincos(ph, &s, &c);
-    v += gk * c;
-    double f = -gk * s * 2.0 * M_PI;
-    g[0] += f * gx; g[1] += f * gy; g[2] += f * gz;
+    int gx, gy, gz, G2;
+    if (!ewald_g(k, gmax, gx, gy, gz, G2)) continue;
+    const double ph = (gx * xp[a * 3] + gy * xp[a * 3 + 1] + gz * xp[a * 3 + 2]) / L;
+    double sn, cs;
+    sincospi(2.0 * ph, &sn, &cs);
+    const double2 sk = S[k];
+    const double f = -2.0 * M_PI * ewald_gk(G2, kappa) * (sk.x * sn - sk.y * cs);
+    g0 += f * gx;
+    g1 += f * gy;
+    g2 += f * gz;
   }
-  v = block_sum(v, sh);
-  for (int d = 0; d < 3; ++d) g[d] = block_sum(g[d], sh);
+  g0 = block_sum(g0, sh);
+  g1 = block_sum(g1, sh);
+  g2 = block_sum(g2, sh);
   if (threadIdx.x == 0) {
-    double dd = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
-    double sr = erfc(kappa * dd) / dd;
-    double dsr = -2.0 * kappa / sqrt(M_PI) * exp(-kappa * kappa * dd * dd) / dd - sr / dd;
-    pair_e[pidx] = sr + v - M_PI / (kappa * kappa);
-    for (int d = 0; d < 3; ++d) pair_g[pidx * 3 + d] = dsr * r[d] / dd + g[d];
+    gr[a * 3] = g0;
+    gr[a * 3 + 1] = g1;
+    gr[a * 3 + 2] = g2;
   }
 }
 
+// nearest-image real-space term and its derivative, one thread per pair (i < j)
+__global__ void k_ewald_real(const double *__restrict__ xp, int n, double L, double kappa,
+                             double *__restrict__ pair_e, double *__restrict__ pair_g) {
+  const int npair = n * (n - 1) / 2;
+  const int pidx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pidx >= npair) return;
+  int i = 0, rem = pidx;
+  while (rem >= n - 1 - i) {
+    rem -= n - 1 - i;
+    ++i;
+  }
+  const int j = i + 1 + rem;
+  double r[3];
+  for (int d = 0; d < 3; ++d) {
+    const double a = xp[i * 3 + d] - L * floor(xp[i * 3 + d] / L);
+    const double b = xp[j * 3 + d] - L * floor(xp[j * 3 + d] / L);
+    const double x = (a - b) / L;
+    r[d] = x - rint(x);
+  }
+  const double dd = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+  const double sr = erfc(kappa * dd) / dd;
+  const double dsr = -2.0 * kappa / sqrt(M_PI) * exp(-kappa * kappa * dd * dd) / dd - sr / dd;
+  pair_e[pidx] = sr;
+  for (int d = 0; d < 3; ++d) pair_g[pidx * 3 + d] = dsr * r[d] / dd;
+}
+
 __global__ void k_ewald_finish(const double *__restrict__ pair_e, const double *__restrict__ pair_g,
+                               const double *__restrict__ part_e, int nblk, const double *__restrict__ gr,
                                int n, double L, double rs, double kappa, int gmax,
                                double *__restrict__ energy, double *__restrict__ grad) {
   __shared__ double sh[32];
-  int npair = n * (n - 1) / 2;
+  const int npair = n * (n - 1) / 2;
   double s = 0;
   for (int k = threadIdx.x; k < npair; k += blockDim.x) s += pair_e[k];
+  for (int k = threadIdx.x; k < nblk; k += blockDim.x) s += part_e[k];
   s = block_sum(s, sh);
   // Madelung constant of the unit simple-cubic lattice with this kappa / Gmax
   double m = 0;
-  int side = 2 * gmax + 1;
-  long long nG = (long long)side * side * side;
+  const int side = 2 * gmax + 1;
+  const long long nG = (long long)side * side * side;
   for (long long k = threadIdx.x; k < nG; k += blockDim.x) {
-    int gx = (int)(k / (side * side)) - gmax, gy = (int)((k / side) % side) - gmax,
-        gz = (int)(k % side) - gmax;
-    int G2 = gx * gx + gy * gy + gz * gz;
-    if (G2 == 0 || G2 > gmax * gmax) continue;
-    m += exp(-M_PI * M_PI * G2 / (kappa * kappa)) / (M_PI * G2);
+    int gx, gy, gz, G2;
+    if (ewald_g(k, gmax, gx, gy, gz, G2)) m += ewald_gk(G2, kappa);
   }
   m = block_sum(m, sh);
   if (threadIdx.x == 0) {
-    double mad = m - M_PI / (kappa * kappa) - 2.0 * kappa / sqrt(M_PI);
-    *energy = 2.0 * s / L / rs + n * mad / L / rs;
+    const double g0 = -M_PI / (kappa * kappa);
+    const double mad = m + g0 - 2.0 * kappa / sqrt(M_PI);
+    *energy = 2.0 * (s + npair * g0) / L / rs + n * mad / L / rs;
   }
   if (grad) {
     for (int a = threadIdx.x; a < n; a += blockDim.x) {
-      double acc[3] = {0, 0, 0};
+      double acc[3] = {gr[a * 3], gr[a * 3 + 1], gr[a * 3 + 2]};
       int k = 0;
       for (int i = 0; i < n; ++i)
         for (int j = i + 1; j < n; ++j, ++k) {
-          double sgn = (i == a) ? 1.0 : ((j == a) ? -1.0 : 0.0);
+          const double sgn = (i == a) ? 1.0 : ((j == a) ? -1.0 : 0.0);
           if (sgn != 0.0)
             for (int d = 0; d < 3; ++d) acc[d] += sgn * pair_g[k * 3 + d];
         }
@@ -358,15 +425,32 @@ __global__ void k_ewald_finish(const double *__restrict__ pair_e, const double *
   }
 }
 
-void launch_ewald(const double *xp, int n, double L, double rs, double kappa, int gmax,
-                  double *pair_e, double *pair_g, double *energy, double *grad, cudaStream_t st) {
+size_t ewald_work_doubles(int n, int gmax) {
+  const long long side = 2LL * gmax + 1, nG = side * side * side;
+  const size_t npair = (size_t)n * (n - 1) / 2;
+  return 4 * (npair + 1) + 2 * (size_t)nG + (size_t)ceil_div(nG, kEwThreads) + 3 * (size_t)n;
+}
+
+void launch_ewald(const double *xp, int n, double L, double rs, double kappa, int gmax, double *work,
+                  double *energy, double *grad, cudaStream_t st) {
   HQ_STAGE(ST_EWALD, st);
-  int npair = n * (n - 1) / 2;
-  if (npair > 0) {
-    k_ewald_pairs<<<npair, 256, 0, st>>>(xp, n, L, kappa, gmax, pair_e, pair_g);
+  const int npair = n * (n - 1) / 2;
+  const long long side = 2LL * gmax + 1, nG = side * side * side;
+  const int nblk = ceil_div(nG, kEwThreads);
+  double *pe = work, *pg = pe + (npair + 1), *Sd = pg + 3 * ((size_t)npair + 1);
+  double *part = Sd + 2 * nG, *gr = part + nblk;
+  double2 *S = reinterpret_cast<double2 *>(Sd);  // 16-byte aligned: 4 (npair + 1) doubles before it
+  k_ewald_sf<<<nblk, kEwThreads, 0, st>>>(xp, n, L, kappa, gmax, S, part);
+  HQ_LAUNCH_CHECK();
+  if (grad) {
+    k_ewald_recip_grad<<<n, kEwThreads, 0, st>>>(xp, n, L, kappa, gmax, S, gr);
     HQ_LAUNCH_CHECK();
   }
-  k_ewald_finish<<<1, 256, 0, st>>>(pair_e, pair_g, n, L, rs, kappa, gmax, energy, grad);
+  if (npair > 0) {
+    k_ewald_real<<<ceil_div(npair, 128), 128, 0, st>>>(xp, n, L, kappa, pe, pg);
+    HQ_LAUNCH_CHECK();
+  }
+  k_ewald_finish<<<1, 256, 0, st>>>(pe, pg, part, nblk, gr, n, L, rs, kappa, gmax, energy, grad);
   HQ_LAUNCH_CHECK();
 }
 

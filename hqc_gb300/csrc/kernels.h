@@ -66,8 +66,9 @@ void launch_overlap_kinetic(const double *xp, int n, int nb, int nprim, const do
                             const double *lattice, int nlat, double *S, double *T, const double *D,
                             const double *W, double *gpart, double *grad, double *Q,
                             cudaStream_t st);
-void launch_ewald(const double *xp, int n, double L, double rs, double kappa, int gmax,
-                  double *pair_e, double *pair_g, double *energy, double *grad, cudaStream_t st);
+size_t ewald_work_doubles(int n, int gmax);
+void launch_ewald(const double *xp, int n, double L, double rs, double kappa, int gmax, double *work,
+                  double *energy, double *grad, cudaStream_t st);
 
 // forces_fp64.cu / exchange
 void launch_psi(const double *C, int nao, int col, const double *phi, long long N, double *psi,

@@ -964,13 +964,11 @@ int hqcgb_ewald(const double *xp, int n, double L, double rs, double kappa, int 
   HQ_GUARD({
     HQ_REQUIRE(xp && energy && n >= 1 && L > 0 && rs > 0 && kappa > 0 && gmax >= 1, "bad argument");
     cudaStream_t st = (cudaStream_t)stream;
-    int npair = n * (n - 1) / 2;
-    double *pe = nullptr, *pg = nullptr;
-    HQ_CUDA(cudaMallocAsync(&pe, sizeof(double) * (npair + 1), st));
-    HQ_CUDA(cudaMallocAsync(&pg, sizeof(double) * 3 * (npair + 1), st));
-    launch_ewald(xp, n, L, rs, kappa, gmax, pe, pg, energy, grad, st);
-    HQ_CUDA(cudaFreeAsync(pe, st));
-    HQ_CUDA(cudaFreeAsync(pg, st));
+    HQ_REQUIRE(gmax <= 200, "Gmax too large");
+    double *work = nullptr;
+    HQ_CUDA(cudaMallocAsync(&work, sizeof(double) * ewald_work_doubles(n, gmax), st));
+    launch_ewald(xp, n, L, rs, kappa, gmax, work, energy, grad, st);
+    HQ_CUDA(cudaFreeAsync(work, st));
     return HQCGB_OK;
   });
 }
