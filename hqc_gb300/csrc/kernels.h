@@ -136,13 +136,16 @@ void launch_to_f32(const double *in, long long ldi, long long N, int rows, doubl
 // tc_gemm.cu (tcgen05, 3xTF32)
 int tc_quad_chunk();
 size_t tc_quad_partial_doubles(int nao, long long N);
-void launch_tc_gemm_nt(const float *A, const float *B, const float *w, int nao, long long N,
-                       long long ld, bool sym, bool add_transpose, double scale, double *partial,
-                       double *M, int *err, cudaStream_t st, int nsplit = 2, int drain = 4);
-void launch_tc_quadrature(const float *phi, const float *dphi, const float *w, const float *u,
-                          float dV, int nao, long long N, long long ld, bool gga, double scale,
-                          double *partial, double *M, int *err, cudaStream_t st, int nsplit = 2,
-                          int drain = 4, float *zbuf = nullptr);
+void launch_tc_quad_split(const float *Ahl, const float *Bhl, int nao, long long N, long long ld,
+                          bool sym, bool add_transpose, double scale, double *partial, double *M,
+                          int *err, cudaStream_t st, int drain);
+void launch_split_operand(const float *phi, const float *dphi, const float *w, const float *u, int nao,
+                          long long N, long long ldi, long long ldo, float a, float b, float *out,
+                          cudaStream_t st);
+void launch_tc_quadrature(const float *phi, const float *dphi, const float *phihl, const float *w,
+                          const float *u, float dV, int nao, long long N, long long ld, bool gga,
+                          double scale, double *partial, double *M, int *err, cudaStream_t st, int drain,
+                          float *zhl);
 size_t tc_density_partial_doubles(int nao, long long ld, bool gga);
 int tc_ldk(int nao);
 void launch_transpose_phi(const float *phi, int nao, long long N, long long ld, float *phiT,

@@ -130,7 +130,8 @@ struct hqcgb_plan {
   int npsi_kept = 0, nuse_kept = 0;
   std::vector<double> hocc;                   // host copy of the occupations
   float *phi32 = nullptr, *dphi32 = nullptr, *phiT32 = nullptr, *D32 = nullptr, *w32 = nullptr,
-        *u32 = nullptr, *z32 = nullptr;
+        *u32 = nullptr;
+  float *phihl = nullptr, *zhl = nullptr;  // TF32 hi/lo pieces of phi and of the quadrature operand
   double *tcq_part = nullptr, *tcd_part = nullptr;
   float2 *cbuf32 = nullptr;
   int *tc_err = nullptr;
@@ -270,7 +271,8 @@ static void create(const hqcgb_params *in, hqcgb_plan *p) {
     p->hocc.resize(nao);
     p->D32 = p->alloc<float>((size_t)nao * tc_ldk(nao));
     HQ_CUDA(cudaMemset(p->D32, 0, sizeof(float) * nao * tc_ldk(nao)));
-    if (p->gga) p->z32 = p->alloc<float>((size_t)nao * p->ld);
+    p->phihl = p->alloc<float>((size_t)2 * nao * p->ld);
+    p->zhl = p->alloc<float>((size_t)2 * nao * p->ld);
     p->w32 = p->alloc<float>(p->ld);
     p->u32 = p->alloc<float>(3 * p->ld);
     p->tcq_part = p->alloc<double>(tc_quad_partial_doubles(nao, N));
@@ -495,8 +497,8 @@ static double fock(Ctx &c) {
     launch_sum_partials(p->xpart, xc_blocks(N), 2, 2, 1.0, p->scal + S_EXC, false, c.st);
     launch_to_f32(p->wq, N, N, 1, 1.0, p->w32, p->ld, c.st);
     if (p->gga) launch_to_f32(p->u, N, N, 3, 1.0, p->u32, p->ld, c.st);
-    launch_tc_quadrature(p->phi32, p->dphi32, p->w32, p->u32, (float)p->dV, n, N, p->ld, p->gga, 1.0,
-                         p->tcq_part, p->F2e, p->tc_err, c.st, 2, 4, p->z32);
+    launch_tc_quadrature(p->phi32, p->dphi32, p->phihl, p->w32, p->u32, (float)p->dV, n, N, p->ld,
+                         p->gga, 1.0, p->tcq_part, p->F2e, p->tc_err, c.st, 4, p->zhl);
   } else {
   launch_density(p->phi, p->gga ? p->dphi : nullptr, p->D, n, N, p->rho, p->gga ? p->grho : nullptr,
                  nullptr, c.st);
@@ -558,6 +560,8 @@ static void geometry(Ctx &c, const double *xp_dev) {
     launch_to_float((long long)p->n * 3 * p->ng * P.n_prim * 6, p->F1d, p->F1d32, c.st);
     launch_phi32(p->F1d32, p->coef, p->ao_l, p->ao_cart, p->nb, p->nprim, n, p->ng, p->ld, p->phi32,
                  p->dphi32, c.st);
+    // phi split once per geometry into the TF32 pieces the quadrature reads
+    launch_split_operand(p->phi32, nullptr, nullptr, nullptr, n, N, p->ld, p->ld, 1.f, 0.f, p->phihl, c.st);
     launch_transpose_phi(p->phi32, n, N, p->ld, p->phiT32, c.st);
     if (p->gga)
       for (int d = 0; d < 3; ++d)
@@ -573,8 +577,8 @@ static void geometry(Ctx &c, const double *xp_dev) {
   if (p->mixed) {
     launch_to_f32(p->vloc, N, N, 1, p->dV, p->w32, p->ld, c.st);
     // one-off per geometry: drained every stage for the most accurate V
-    launch_tc_quadrature(p->phi32, nullptr, p->w32, nullptr, (float)p->dV, n, N, p->ld, false, 1.0,
-                         p->tcq_part, p->V, p->tc_err, c.st, 2, 1);
+    launch_tc_quadrature(p->phi32, nullptr, p->phihl, p->w32, nullptr, (float)p->dV, n, N, p->ld, false,
+                         1.0, p->tcq_part, p->V, p->tc_err, c.st, 1, p->zhl);
   } else {
     launch_quadrature(p->phi, p->phi, p->vloc, n, N, true, p->dV, false, p->qpart, p->V, c.st);
   }

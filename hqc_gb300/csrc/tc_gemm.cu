@@ -463,52 +463,8 @@ __device__ inline void pipe_finish(Pipe &P) {
   }
 }
 
-// ---------------------------------------------------------------------------
-// Quadrature: grid (m_tiles, n_tiles, k_chunks); tile 128 x 128; FP64
-// partial tiles P[chunk][tile_m][tile_n][128][128] of sum_g A_p(g) w(g) B_q(g).
-// ---------------------------------------------------------------------------
-struct QuadArgs {
-  Operand A, B;
-  const float *w;
-  int nao, sym, drain, ns;
-  long long N;
-  int kchunk;
-  double *partial;
-  int *err;
-};
-
+// FP64 partial tiles of the quadrature: P[chunk][tile_m][tile_n][128][128].
 constexpr size_t kWslotBytes = kStages * kProducers * sizeof(float4);
-constexpr size_t kQuadSmem = kStages * kStageBytes + kWslotBytes + 1024;
-
-__global__ void __launch_bounds__(kThreads, 1) k_tc_quadrature(QuadArgs a) {
-  extern __shared__ __align__(1024) char smraw[];
-  char *sm = (char *)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
-  __shared__ Pipe P;
-  const int mt = blockIdx.x, nt = blockIdx.y, chunk = blockIdx.z;
-  if (a.sym && nt < mt) return;  // whole CTA exits before any barrier use
-  pipe_init(P);
-  const long long k0 = (long long)chunk * a.kchunk;
-  const long long k1 = min(k0 + (long long)a.kchunk, a.N);
-  const int nstages = (int)((k1 - k0 + kStageK - 1) / kStageK);
-  const int tid = threadIdx.x;
-  float4 *wslot = reinterpret_cast<float4 *>(sm + kStages * kStageBytes);
-  bool ok = run_pipe(P, sm, wslot, a.A, mt * kM, a.B, nt * kN, a.w, k0, k1, nstages, a.drain, a.ns,
-                     a.err, 0);
-  const int warp = tid >> 5;
-  if (warp >= 4 && warp < 8) {
-    int row = (warp & 3) * 32 + (tid & 31);
-    double *out = a.partial + ((((long long)chunk * gridDim.x + mt) * gridDim.y + nt) * kM + row) * kN;
-#pragma unroll 1
-    for (int c0 = 0; c0 < kN; c0 += 16) {
-      double v[16];
-      read_sum16(P, c0, v);
-      if (ok)
-#pragma unroll
-        for (int i = 0; i < 16; ++i) out[c0 + i] = v[i];
-    }
-  }
-  pipe_finish(P);
-}
 
 // M[p][q] = scale * sum_chunks P  (+ mirror for sym; + transpose-add for GGA)
 __global__ void k_tc_quad_reduce(const double *__restrict__ P, int nchunk, int mtiles, int ntiles,
@@ -921,6 +877,265 @@ __global__ void __launch_bounds__(kPsiThreads, 1)
   }
 }
 
+// ---------------------------------------------------------------------------
+// Quadrature on pre-split operands: M_pq = sum_g A_p(g) B_q(g) with A and B
+// given as TF32 hi/lo arrays [nao][ld] (A = w phi or the GGA operand, split
+// by the pass that forms it; B = phi, split once per geometry).  Grid: (tile,
+// K chunk); one warp issues TMA bulk tensor loads of the four pieces into a
+// 3-stage ring, one thread issues the MMAs (lo*hi + hi*lo + hi*hi into one
+// accumulator), four warps drain the two ping-pong TMEM accumulators every
+// `drain` stages into TMEM-resident TwoSum sums (S, C) and write the FP64
+// partial tile.  Tiles are 128 x 128; the last, partial AO block (nao % 128
+// rows) runs as an N = 16..112 MMA: as the B side directly, or -- for tiles
+// whose A side is that block (non-symmetric case) -- by swapping the roles of
+// A and B and storing the transposed result.
+// ---------------------------------------------------------------------------
+constexpr int kQtDrainWarps = 4;
+constexpr int kQtMmaWarp = kQtDrainWarps;
+constexpr int kQtTmaWarp = kQtMmaWarp + 1;
+constexpr int kQtThreads = (kQtTmaWarp + 1) * 32;
+constexpr int kQtRing = 3;
+constexpr size_t kQtStageBytes = 4 * kTile;  // A hi, A lo, B hi, B lo (B pieces may be narrower)
+constexpr size_t kQtSmem = kQtRing * kQtStageBytes + 1024;
+
+struct QtTile {
+  int arow, brow;  // first AO row of the A-side and B-side operand blocks
+  int nb;          // MMA N (B rows): 128, or the partial block rounded up to 16
+  int swap;        // A side reads the B arrays (and vice versa); store transposed
+  int mt, nt;      // destination tile of the partial sums
+};
+
+struct QtArgs {
+  QtTile tiles[12];
+  int ntile;
+  long long N;
+  int kchunk, drain, mtiles, ntiles;
+  double *partial;
+  int *err;
+};
+
+struct QtPipe {
+  uint64_t full[kQtRing], empty[kQtRing], acc_full[2], acc_empty[2];
+  uint32_t tmem_base;
+};
+
+__global__ void __launch_bounds__(kQtThreads, 1)
+    k_tc_quad_tma(QtArgs a, const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtensorMap mAl,
+                  const __grid_constant__ CUtensorMap mBh, const __grid_constant__ CUtensorMap mBl,
+                  const __grid_constant__ CUtensorMap mAh16, const __grid_constant__ CUtensorMap mAl16,
+                  const __grid_constant__ CUtensorMap mBh16, const __grid_constant__ CUtensorMap mBl16) {
+  extern __shared__ __align__(1024) char smraw[];
+  char *sm = (char *)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
+  __shared__ QtPipe P;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const QtTile T = a.tiles[blockIdx.x];
+  const int chunk = blockIdx.y;
+  const long long k0 = (long long)chunk * a.kchunk;
+  const long long k1 = min(k0 + (long long)a.kchunk, a.N);
+  const int nstages = (int)((k1 - k0 + kStageK - 1) / kStageK);
+  const int nsub = (nstages + a.drain - 1) / a.drain;
+  const int nb = T.nb;
+  if (tid == 0) {
+    for (int b = 0; b < kQtRing; ++b) {
+      mbar_init(&P.full[b], 1);
+      mbar_init(&P.empty[b], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&P.acc_full[b], 1);
+      mbar_init(&P.acc_empty[b], kQtDrainWarps * 32);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == kQtMmaWarp) tmem_alloc(&P.tmem_base, kTmemCols);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+
+  bool ok = true;
+  if (warp == kQtTmaWarp) {
+    if (lane == 0) {
+      // the A side always has 128 rows; the B side nb rows (box 16 for narrow blocks)
+      const CUtensorMap *ah = T.swap ? &mBh : &mAh, *al = T.swap ? &mBl : &mAl;
+      const CUtensorMap *bh, *bl;
+      if (nb == kN) {
+        bh = T.swap ? &mAh : &mBh;
+        bl = T.swap ? &mAl : &mBl;
+      } else {
+        bh = T.swap ? &mAh16 : &mBh16;
+        bl = T.swap ? &mAl16 : &mBl16;
+      }
+      const int bbox = nb == kN ? kN : 16;
+      const int nbox = nb / bbox;
+      const uint32_t bytes = 2u * (uint32_t)kTile + 2u * (uint32_t)nb * 128u;
+      for (int st = 0; st < nstages; ++st) {
+        const int slot = st % kQtRing, use = st / kQtRing;
+        if (ok && use > 0 && !mbar_wait(&P.empty[slot], (unsigned)((use - 1) & 1), a.err, 31)) ok = false;
+        if (!ok) break;
+        const int x = (int)(k0 + (long long)st * kStageK);
+        const uint32_t base = smem_u32(sm + slot * kQtStageBytes);
+        mbar_expect_tx(&P.full[slot], bytes);
+        tma_load_2d(base, ah, x, T.arow, &P.full[slot]);
+        tma_load_2d(base + (uint32_t)kTile, al, x, T.arow, &P.full[slot]);
+        for (int q = 0; q < nbox; ++q) {
+          const uint32_t off = (uint32_t)(q * bbox * 128);
+          tma_load_2d(base + 2u * (uint32_t)kTile + off, bh, x, T.brow + q * bbox, &P.full[slot]);
+          tma_load_2d(base + 3u * (uint32_t)kTile + off, bl, x, T.brow + q * bbox, &P.full[slot]);
+        }
+      }
+    }
+  } else if (warp == kQtMmaWarp) {
+    if (lane == 0) {
+      const uint32_t idesc = idesc_tf32(kM, nb);
+      int stage = 0;
+      for (int j = 0; j < nsub; ++j) {
+        const int ab = j & 1, ause = j >> 1;
+        if (ok && ause > 0 && !mbar_wait(&P.acc_empty[ab], (unsigned)((ause - 1) & 1), a.err, 34)) ok = false;
+        tc_fence_after();
+        const uint32_t tmem_d = P.tmem_base + (uint32_t)(ab * kN);
+        const int s_end = min(nstages, (j + 1) * a.drain);
+        bool first = true;
+        for (; stage < s_end; ++stage) {
+          const int slot = stage % kQtRing, use = stage / kQtRing;
+          if (ok && !mbar_wait(&P.full[slot], (unsigned)(use & 1), a.err, 32)) ok = false;
+          tc_fence_after();
+          if (ok) {
+            const uint32_t base = smem_u32(sm + slot * kQtStageBytes);
+            const uint32_t Ah = base, Al = base + (uint32_t)kTile, Bh = base + 2u * (uint32_t)kTile,
+                           Bl = base + 3u * (uint32_t)kTile;
+#pragma unroll
+            for (int ks = 0; ks < kStageK / 8; ++ks) {
+              const uint32_t off = ks * 32;
+              mma_tf32(tmem_d, sdesc(Al + off), sdesc(Bh + off), idesc, (first && ks == 0) ? 0 : 1);
+              mma_tf32(tmem_d, sdesc(Ah + off), sdesc(Bl + off), idesc, 1);
+              mma_tf32(tmem_d, sdesc(Ah + off), sdesc(Bh + off), idesc, 1);
+            }
+          }
+          first = false;
+          mma_commit(&P.empty[slot]);
+        }
+        mma_commit(&P.acc_full[ab]);
+      }
+    }
+  } else {
+    // drains: thread = TMEM lane (output row); nb columns
+    const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
+    for (int j = 0; j < nsub; ++j) {
+      const int b = j & 1, use = j >> 1;
+      const bool got = ok && mbar_wait(&P.acc_full[b], (unsigned)(use & 1), a.err, 33);
+      if (!got) ok = false;
+      tc_fence_after();
+      if (got) {
+#pragma unroll 1
+        for (int col = 0; col < nb; col += 16) {
+          uint32_t va[16], sa[16], ca[16];
+          tmem_ld16_nowait(P.tmem_base + lane_off + b * kN + col, va);
+          if (j > 0) {
+            tmem_ld16_nowait(P.tmem_base + lane_off + kColS + col, sa);
+            tmem_ld16_nowait(P.tmem_base + lane_off + kColC + col, ca);
+          }
+          tmem_wait_ld();
+          float sv[16], cv[16];
+#pragma unroll
+          for (int i = 0; i < 16; ++i) {
+            const float v = __uint_as_float(va[i]);
+            if (j == 0) {
+              sv[i] = v;
+              cv[i] = 0.f;
+            } else {
+              sv[i] = __uint_as_float(sa[i]);
+              cv[i] = __uint_as_float(ca[i]);
+              two_sum_add(sv[i], cv[i], v);
+            }
+          }
+          tmem_st16(P.tmem_base + lane_off + kColS + col, sv);
+          tmem_st16(P.tmem_base + lane_off + kColC + col, cv);
+        }
+        tmem_wait_st();
+      }
+      tc_fence_before();
+      mbar_arrive(&P.acc_empty[b]);
+    }
+    // FP64 partial tile: P[chunk][mt][nt][row][col]
+    const int row = warp * 32 + lane;
+    double *tile = a.partial + (((long long)chunk * a.mtiles + T.mt) * a.ntiles + T.nt) * (kM * kN);
+#pragma unroll 1
+    for (int c0 = 0; c0 < nb; c0 += 16) {
+      uint32_t sr[16], cr[16];
+      tmem_ld16_nowait(P.tmem_base + lane_off + kColS + c0, sr);
+      tmem_ld16_nowait(P.tmem_base + lane_off + kColC + c0, cr);
+      tmem_wait_ld();
+      double v[16];
+#pragma unroll
+      for (int i = 0; i < 16; ++i) v[i] = (double)__uint_as_float(sr[i]) + (double)__uint_as_float(cr[i]);
+      if (ok) {
+        if (!T.swap) {
+#pragma unroll
+          for (int i = 0; i < 16; ++i) tile[(long long)row * kN + c0 + i] = v[i];
+        } else {
+#pragma unroll
+          for (int i = 0; i < 16; ++i) tile[(long long)(c0 + i) * kN + row] = v[i];
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == kQtMmaWarp) {
+    tc_fence_after();
+    tmem_dealloc(P.tmem_base, kTmemCols);
+  }
+}
+
+// hi/lo TF32 pieces of Z = a w phi + b u . grad phi (u, dphi optional; w
+// optional, = 1): inputs with row stride ldi, outputs [nao][ldo] with zeros
+// in [N, ldo).  Grid (column blocks of 1024, rows); 4 columns per thread
+// (ldi, ldo multiples of 4, 16-byte aligned rows).
+__global__ void __launch_bounds__(256)
+    k_split_operand(const float *__restrict__ phi, const float *__restrict__ dphi,
+                    const float *__restrict__ w, const float *__restrict__ u, int nao, long long N,
+                    long long ldi, long long ldo, float a, float b, float *__restrict__ hi,
+                    float *__restrict__ lo) {
+  const int p = blockIdx.y;
+  const long long g = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * 4;
+  if (g >= ldo) return;
+  const long long j = (long long)p * ldi + g, NN = (long long)nao * ldi;
+  float z[4] = {0.f, 0.f, 0.f, 0.f};
+  if (g + 3 < N) {
+    const float4 f = *reinterpret_cast<const float4 *>(phi + j);
+    float4 wv = w ? *reinterpret_cast<const float4 *>(w + g) : make_float4(1.f, 1.f, 1.f, 1.f);
+    z[0] = a * wv.x * f.x;
+    z[1] = a * wv.y * f.y;
+    z[2] = a * wv.z * f.z;
+    z[3] = a * wv.w * f.w;
+    if (u) {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const float4 uv = *reinterpret_cast<const float4 *>(u + d * ldi + g);
+        const float4 dv = *reinterpret_cast<const float4 *>(dphi + d * NN + j);
+        z[0] += b * uv.x * dv.x;
+        z[1] += b * uv.y * dv.y;
+        z[2] += b * uv.z * dv.z;
+        z[3] += b * uv.w * dv.w;
+      }
+    }
+  } else {
+    for (int e = 0; e < 4; ++e) {
+      if (g + e >= N) break;
+      float v = (w ? a * w[g + e] : a) * phi[j + e];
+      if (u)
+        for (int d = 0; d < 3; ++d) v += b * u[d * ldi + g + e] * dphi[d * NN + j + e];
+      z[e] = v;
+    }
+  }
+  float4 h, l;
+  split2(z[0], h.x, l.x);
+  split2(z[1], h.y, l.y);
+  split2(z[2], h.z, l.z);
+  split2(z[3], h.w, l.w);
+  *reinterpret_cast<float4 *>(hi + (long long)p * ldo + g) = h;
+  *reinterpret_cast<float4 *>(lo + (long long)p * ldo + g) = l;
+}
+
 // Yhl[0][k][p], Yhl[1][k][p]: TF32 hi/lo pieces of C[p][k] sqrt(occ[k]) for
 // k < nuse, zero for k in [nuse, npsi) and p in [nao, ldk).
 __global__ void k_psi_operand(const double *__restrict__ C, const double *__restrict__ occ, int nao,
@@ -943,7 +1158,14 @@ namespace tc {
 // and 128-byte swizzle (the UMMA K-major canonical layout of a 32-element
 // K block); out-of-range rows read as zero.  The driver's encoder is looked
 // up at run time (no link-time dependency on the driver library).
+CUtensorMap tensor_map_2d_ext(const float *base, long long ld, long long cols, long long rows,
+                              int box_rows);
 CUtensorMap tensor_map_2d(const float *base, long long ld, long long rows, int box_rows) {
+  return tensor_map_2d_ext(base, ld, ld, rows, box_rows);
+}
+// as tensor_map_2d with the valid row length `cols` <= ld: columns past it read as zero
+CUtensorMap tensor_map_2d_ext(const float *base, long long ld, long long cols, long long rows,
+                              int box_rows) {
   static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
   if (!encode) {
     void *fn = nullptr;
@@ -955,7 +1177,8 @@ CUtensorMap tensor_map_2d(const float *base, long long ld, long long rows, int b
   HQ_REQUIRE(((uintptr_t)base & 15) == 0, "TMA base must be 16-byte aligned");
   HQ_REQUIRE(ld % 32 == 0, "TMA row stride must be a multiple of 32 floats");
   CUtensorMap m;
-  cuuint64_t dims[2] = {(cuuint64_t)ld, (cuuint64_t)rows};
+  HQ_REQUIRE(cols >= 1 && cols <= ld, "TMA row length out of range");
+  cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
   cuuint64_t strides[1] = {(cuuint64_t)ld * sizeof(float)};
   cuuint32_t box[2] = {(cuuint32_t)kStageK, (cuuint32_t)box_rows};
   cuuint32_t estr[2] = {1, 1};
@@ -1032,63 +1255,104 @@ size_t tc_quad_partial_doubles(int nao, long long N) {
   return (size_t)chunks * mt * nt * tc::kM * tc::kN;
 }
 
-// M = scale * sum_g A_p(g) w(g) B_q(g) (+ its transpose when add_transpose);
-// A, B fp32 [nao][ld]; w may be null.  sym: A == B with w symmetric use.
-void launch_tc_gemm_nt(const float *A, const float *B, const float *w, int nao, long long N,
-                       long long ld, bool sym, bool add_transpose, double scale, double *partial,
-                       double *M, int *err, cudaStream_t st, int nsplit, int drain) {
+// M = scale * sum_g A_p(g) B_q(g) (+ its transpose when add_transpose) from the
+// pre-split pieces Ahl, Bhl [2][nao][ld] (hi rows, then lo rows); sym: M is
+// symmetric (only tiles nt >= mt are computed; the reduce mirrors them).
+void launch_tc_quad_split(const float *Ahl, const float *Bhl, int nao, long long N, long long ld,
+                          bool sym, bool add_transpose, double scale, double *partial, double *M,
+                          int *err, cudaStream_t st, int drain) {
   HQ_STAGE(ST_QUAD, st);
-  HQ_REQUIRE(ld % 4 == 0, "row stride must be a multiple of 4 floats");
-  HQ_REQUIRE(nsplit == 2, "nsplit must be 2 (3xTF32)");
   HQ_REQUIRE(drain >= 1, "drain must be >= 1");
+  HQ_REQUIRE(ld % 32 == 0 && ld >= N, "pre-split operands need a row stride that is a multiple of 32");
+  HQ_REQUIRE(N <= (1LL << 31) - 64, "grid too large for 32-bit TMA coordinates");
   static bool attr = false;
   if (!attr) {
-    HQ_CUDA(cudaFuncSetAttribute(tc::k_tc_quadrature, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)tc::kQuadSmem));
+    HQ_CUDA(cudaFuncSetAttribute(tc::k_tc_quad_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)tc::kQtSmem));
     attr = true;
   }
-  tc::QuadArgs a;
-  a.A = tc::Operand{A, ld, nao};
-  a.B = tc::Operand{B, ld, nao};
-  a.w = w; a.nao = nao; a.sym = sym ? 1 : 0; a.drain = drain; a.ns = nsplit; a.N = N;
-  a.kchunk = tc_quad_chunk(); a.partial = partial; a.err = err;
-  int mt = ceil_div(nao, tc::kM), nt = ceil_div(nao, tc::kN);
-  int chunks = ceil_div(N, a.kchunk);
-  dim3 grid(mt, nt, chunks);
-  tc::k_tc_quadrature<<<grid, tc::kThreads, tc::kQuadSmem, st>>>(a);
+  const int nblk = ceil_div(nao, tc::kM);
+  const int last = nao - tc::kM * (nblk - 1);
+  const bool narrow = last < tc::kM;
+  const int nb_last = ceil_div(last, 16) * 16;
+  tc::QtArgs a;
+  a.ntile = 0;
+  for (int mt = 0; mt < nblk; ++mt)
+    for (int nt = 0; nt < nblk; ++nt) {
+      if (sym && nt < mt) continue;
+      const bool nm = narrow && mt == nblk - 1, nn = narrow && nt == nblk - 1;
+      tc::QtTile t;
+      t.mt = mt;
+      t.nt = nt;
+      if (nm && !nn) {  // narrow A block: compute the transposed tile
+        t.arow = nt * tc::kM;
+        t.brow = mt * tc::kM;
+        t.nb = nb_last;
+        t.swap = 1;
+      } else {
+        t.arow = mt * tc::kM;
+        t.brow = nt * tc::kN;
+        t.nb = nn ? nb_last : tc::kN;
+        t.swap = 0;
+      }
+      HQ_REQUIRE(a.ntile < 12, "too many AO blocks for the quadrature tile list");
+      a.tiles[a.ntile++] = t;
+    }
+  a.N = N;
+  a.kchunk = tc_quad_chunk();
+  a.drain = drain;
+  a.mtiles = nblk;
+  a.ntiles = nblk;
+  a.partial = partial;
+  a.err = err;
+  const long long rows = nao;
+  const float *Ah = Ahl, *Al = Ahl + (size_t)nao * ld, *Bh = Bhl, *Bl = Bhl + (size_t)nao * ld;
+  CUtensorMap mAh = tc::tensor_map_2d_ext(Ah, ld, N, rows, tc::kM);
+  CUtensorMap mAl = tc::tensor_map_2d_ext(Al, ld, N, rows, tc::kM);
+  CUtensorMap mBh = tc::tensor_map_2d_ext(Bh, ld, N, rows, tc::kN);
+  CUtensorMap mBl = tc::tensor_map_2d_ext(Bl, ld, N, rows, tc::kN);
+  CUtensorMap mAh16 = tc::tensor_map_2d_ext(Ah, ld, N, rows, 16);
+  CUtensorMap mAl16 = tc::tensor_map_2d_ext(Al, ld, N, rows, 16);
+  CUtensorMap mBh16 = tc::tensor_map_2d_ext(Bh, ld, N, rows, 16);
+  CUtensorMap mBl16 = tc::tensor_map_2d_ext(Bl, ld, N, rows, 16);
+  const int chunks = ceil_div(N, a.kchunk);
+  dim3 grid(a.ntile, chunks);
+  tc::k_tc_quad_tma<<<grid, tc::kQtThreads, tc::kQtSmem, st>>>(a, mAh, mAl, mBh, mBl, mAh16, mAl16, mBh16,
+                                                                mBl16);
   HQ_LAUNCH_CHECK();
   tc::k_tc_quad_reduce<<<ceil_div((long long)nao * nao, 256), 256, 0, st>>>(
-      partial, chunks, mt, nt, nao, a.sym, add_transpose ? 1 : 0, scale, M);
+      partial, chunks, nblk, nblk, nao, sym ? 1 : 0, add_transpose ? 1 : 0, scale, M);
   HQ_LAUNCH_CHECK();
 }
 
-// Quadrature of the Fock build: LDA  M = phi diag(w) phi^T;  GGA  M = Z phi^T +
-// phi Z^T with the operand Z = 0.5 w phi + dV u.grad phi precomputed in `zbuf`.
-__global__ void k_gga_operand32(const float *__restrict__ phi, const float *__restrict__ dphi,
-                                const float *__restrict__ w, const float *__restrict__ u, int nao,
-                                long long ld, float dV, float *__restrict__ Z) {
-  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  long long NN = (long long)nao * ld;
-  if (i >= NN) return;
-  long long g = i % ld;
-  Z[i] = 0.5f * w[g] * phi[i] + dV * (u[g] * dphi[i] + u[ld + g] * dphi[NN + i] +
-                                      u[2 * ld + g] * dphi[2 * NN + i]);
+// hi/lo pieces of a w phi + b u . grad phi into out [2][nao][ldo]
+void launch_split_operand(const float *phi, const float *dphi, const float *w, const float *u, int nao,
+                          long long N, long long ldi, long long ldo, float a, float b, float *out,
+                          cudaStream_t st) {
+  HQ_STAGE(ST_QUAD, st);
+  HQ_REQUIRE(ldi % 4 == 0 && ldo % 4 == 0 && ldo >= N && ldi >= N, "split operand: bad row strides");
+  dim3 grid(ceil_div(ldo, 1024), nao);
+  tc::k_split_operand<<<grid, 256, 0, st>>>(phi, dphi, w, u, nao, N, ldi, ldo, a, b, out,
+                                             out + (size_t)nao * ldo);
+  HQ_LAUNCH_CHECK();
 }
 
-void launch_tc_quadrature(const float *phi, const float *dphi, const float *w, const float *u,
-                          float dV, int nao, long long N, long long ld, bool gga, double scale,
-                          double *partial, double *M, int *err, cudaStream_t st, int nsplit,
-                          int drain, float *zbuf) {
+// Quadrature of the Fock build from the pre-split phi (phihl [2][nao][ld]):
+// LDA  M = (w phi) phi^T (symmetric);  GGA  M = Z phi^T + phi Z^T with
+// Z = 0.5 w phi + dV u . grad phi.  zhl [2][nao][ld] receives the split operand.
+void launch_tc_quadrature(const float *phi, const float *dphi, const float *phihl, const float *w,
+                          const float *u, float dV, int nao, long long N, long long ld, bool gga,
+                          double scale, double *partial, double *M, int *err, cudaStream_t st, int drain,
+                          float *zhl) {
+  HQ_REQUIRE(zhl && phihl, "quadrature needs the split operand buffers");
   if (!gga) {
-    launch_tc_gemm_nt(phi, phi, w, nao, N, ld, true, false, scale, partial, M, err, st, nsplit, drain);
+    launch_split_operand(phi, nullptr, w, nullptr, nao, N, ld, ld, 1.f, 0.f, zhl, st);
+    launch_tc_quad_split(zhl, phihl, nao, N, ld, true, false, scale, partial, M, err, st, drain);
     return;
   }
-  HQ_REQUIRE(zbuf && dphi && u, "GGA quadrature needs dphi, u and a Z buffer");
-  k_gga_operand32<<<ceil_div((long long)nao * ld, 256), 256, 0, st>>>(phi, dphi, w, u, nao, ld, dV,
-                                                                       zbuf);
-  HQ_LAUNCH_CHECK();
-  launch_tc_gemm_nt(zbuf, phi, nullptr, nao, N, ld, false, true, scale, partial, M, err, st, nsplit,
-                    drain);
+  HQ_REQUIRE(dphi && u, "GGA quadrature needs dphi and u");
+  launch_split_operand(phi, dphi, w, u, nao, N, ld, ld, 0.5f, dV, zhl, st);
+  launch_tc_quad_split(zhl, phihl, nao, N, ld, false, true, scale, partial, M, err, st, drain);
 }
 
 size_t tc_density_partial_doubles(int nao, long long ld, bool gga) {
@@ -1146,15 +1410,23 @@ extern "C" int hqcgb_tc_quadrature(int nao, long long N, long long ld, const flo
   cudaStream_t st = (cudaStream_t)stream;
   try {
     HQ_REQUIRE(nao >= 1 && N >= 1 && ld >= N && ld % 4 == 0 && phi && w && M, "bad argument");
+    HQ_REQUIRE(nsplit == 2, "nsplit must be 2 (3xTF32)");
+    const long long ldo = (N + 31) / 32 * 32;
     double *part = nullptr;
+    float *hl = nullptr;
     int *err = nullptr;
     HQ_CUDA(cudaMallocAsync(&part, tc_quad_partial_doubles(nao, N) * sizeof(double), st));
+    HQ_CUDA(cudaMallocAsync(&hl, 4 * (size_t)nao * ldo * sizeof(float), st));
     HQ_CUDA(cudaMallocAsync(&err, sizeof(int), st));
     HQ_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
-    launch_tc_gemm_nt(phi, phi, w, nao, N, ld, true, false, 1.0, part, M, err, st, nsplit, drain);
+    float *phl = hl, *zhl = hl + 2 * (size_t)nao * ldo;
+    launch_split_operand(phi, nullptr, nullptr, nullptr, nao, N, ld, ldo, 1.f, 0.f, phl, st);
+    launch_split_operand(phi, nullptr, w, nullptr, nao, N, ld, ldo, 1.f, 0.f, zhl, st);
+    launch_tc_quad_split(zhl, phl, nao, N, ldo, true, false, 1.0, part, M, err, st, drain);
     int h = 0;
     HQ_CUDA(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, st));
     HQ_CUDA(cudaFreeAsync(part, st));
+    HQ_CUDA(cudaFreeAsync(hl, st));
     HQ_CUDA(cudaFreeAsync(err, st));
     HQ_CUDA(cudaStreamSynchronize(st));
     if (h) throw Error{HQCGB_CUDA_ERROR, "tensor-core pipeline wait limit hit"};
