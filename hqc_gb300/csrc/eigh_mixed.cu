@@ -334,7 +334,19 @@ static void sort_eigpairs(int n, double *w, double *X, MixedEigWork &ws, cudaStr
   HQ_LAUNCH_CHECK();
 }
 
+// Rayleigh quotients l_i = s_ii / g_ii (the eigenvalue estimates of a
+// converged step, whose update is skipped).
+__global__ void k_oa_lambda(int n, const double *__restrict__ S, const double *__restrict__ G,
+                            double *__restrict__ lam) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) lam[i] = S[(long long)i * n + i] / G[(long long)i * n + i];
+}
+
 // One refinement step; returns ||X^T A X - diag|| / ||A|| before the update.
+// When that and ||I - X^T X|| are already at rounding level (< kOaConverged)
+// the step stops after the statistics: X is kept and only the eigenvalue
+// estimates are set.
+constexpr double kOaConverged = 1e-12;
 static double oa_iteration(int n, const double *A, double *X, double *w, MixedEigWork &ws,
                            cudaStream_t st, int max_cluster = kMaxClusterFock) {
   const long long nn = (long long)n * n;
@@ -346,6 +358,18 @@ static double oa_iteration(int n, const double *A, double *X, double *w, MixedEi
   HQ_CUDA(cudaMemsetAsync(red, 0, 5 * sizeof(double), st));
   k_oa_stats<<<grid, kOaThreads, 0, st>>>(n, A, ws.S, ws.G, red);
   HQ_LAUNCH_CHECK();
+  double rs[4];
+  HQ_CUDA(cudaMemcpyAsync(rs, red, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  HQ_CUDA(cudaStreamSynchronize(st));
+  const double off = std::sqrt(rs[1]) / std::max(std::sqrt(rs[0]), 1e-300);
+  // converged: off-diagonal part and orthonormality residual ||I - X^T X||_F
+  // both at rounding level (the update also re-normalises X)
+  if (off < kOaConverged && std::sqrt(rs[2]) < kOaConverged) {
+    k_oa_lambda<<<ceil_div(n, 256), 256, 0, st>>>(n, ws.S, ws.G, w);
+    HQ_LAUNCH_CHECK();
+    if (std::getenv("HQCGB_TRACE")) fprintf(stderr, "  oa off=%.3e (converged, no update)\n", off);
+    return off;
+  }
   k_oa_clusters<<<1, 1024, 0, st>>>(n, ws.S, ws.G, red, w, ws.emax, ws.iwork, ws.wbuf, max_cluster);
   HQ_LAUNCH_CHECK();
   k_oa_rotate_cols<<<grid, kOaThreads, 0, st>>>(n, X, ws.S, ws.G, ws.iwork, ws.wbuf);
@@ -357,10 +381,10 @@ static double oa_iteration(int n, const double *A, double *X, double *w, MixedEi
   HQ_LAUNCH_CHECK();
   gemm(false, false, n, n, n, 1.0, X, n, ws.E, n, nullptr, 0.0, ws.T1, n, st);  // X E
   axpby(n, 1.0, X, 1.0, ws.T1, false, X, st);                                  // X += X E
-  double em[13];
-  HQ_CUDA(cudaMemcpyAsync(em, ws.emax, 13 * sizeof(double), cudaMemcpyDeviceToHost, st));
-  HQ_CUDA(cudaStreamSynchronize(st));
   if (std::getenv("HQCGB_TRACE")) {
+    double em[13];
+    HQ_CUDA(cudaMemcpyAsync(em, ws.emax, 13 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    HQ_CUDA(cudaStreamSynchronize(st));
     static auto t_last = std::chrono::steady_clock::now();
     auto now = std::chrono::steady_clock::now();
     fprintf(stderr, "  oa off=%.3e max|E|=%.3e clusters=%g%s (%.3f ms since last)\n", em[1], em[8 + 4],
@@ -368,7 +392,7 @@ static double oa_iteration(int n, const double *A, double *X, double *w, MixedEi
             std::chrono::duration<double, std::milli>(now - t_last).count());
     t_last = now;
   }
-  return em[1];
+  return off;
 }
 
 // Full solve: FP32 stage (eigh_f32.cu; the QL solver of eigh_fp64.cu when
@@ -413,7 +437,7 @@ bool eigh_mixed(int n, const double *A, double *V, double *w, MixedEigWork &ws, 
   HQ_LAUNCH_CHECK();
   for (int it = 0; it < 8; ++it) {
     double off = oa_iteration(n, A, V, w, ws, st, wide ? kMaxCluster : kMaxClusterFock);
-    if (off < 1e-12) {
+    if (off < kOaConverged) {
       sort_eigpairs(n, w, V, ws, st);
       return true;
     }
@@ -434,7 +458,7 @@ bool eigh_mixed_warm(int n, const double *A, const double *X0, double *V, double
   for (int it = 0; it < 8; ++it) {
     double off = oa_iteration(n, A, V, w, ws, st);
     if (!(off < 2e-3)) return false;
-    if (off < 1e-12) {
+    if (off < kOaConverged) {
       sort_eigpairs(n, w, V, ws, st);
       return true;
     }

@@ -56,6 +56,7 @@ void diis_extrapolate(int space, int n, const double *Fk, const double *ek, int 
 void occupations(int n_elec, int nmo, int smearing, int method, double sigma, int search, int cycle,
                  double tol, double shift, const double *w, double *f, double *mu, cudaStream_t st);
 void entropy(int n, const double *f, double *out, cudaStream_t st);
+void launch_occ_block(const double *C, const double *occ, int n, int nuse, double *Y, cudaStream_t st);
 void inv_sqrt_cols(int n, const double *U, const double *w, double *v, int *bad, cudaStream_t st);
 void antisym(int n, const double *X, double *e, cudaStream_t st);
 

@@ -500,3 +500,19 @@ void antisym(int n, const double *X, double *e, cudaStream_t st) {
 }
 
 }  // namespace hqcgb
+
+namespace hqcgb {
+// Y[p][k] = C[p][k] sqrt(occ[k]) for k < nuse (row stride nuse): D = Y Y^T.
+__global__ void k_occ_block(const double *__restrict__ C, const double *__restrict__ occ, int n,
+                            int nuse, double *__restrict__ Y) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n * nuse) return;
+  const int p = idx / nuse, k = idx % nuse;
+  Y[idx] = C[(long long)p * n + k] * sqrt(fmax(occ[k], 0.0));
+}
+
+void launch_occ_block(const double *C, const double *occ, int n, int nuse, double *Y, cudaStream_t st) {
+  k_occ_block<<<ceil_div((long long)n * nuse, 256), 256, 0, st>>>(C, occ, n, nuse, Y);
+  HQ_LAUNCH_CHECK();
+}
+}  // namespace hqcgb

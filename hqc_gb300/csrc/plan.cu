@@ -73,6 +73,7 @@ static constexpr double kMadelungSC = 0.22578495;  // solver.py:404
 // before a compensated drain: 2 measured 14% faster than 1 on the H54
 // shapes at a relative density bias of -2.9e-7 (the tensor core truncates).
 static constexpr int kPsiDrain = 2;
+static constexpr int kThinOcc = 64;  // occupied-block GEMMs up to this many orbitals
 
 // HQCGB_TRACE=1 prints one line per SCF iteration (energy, error norm) to stderr.
 static bool trace_on() {
@@ -122,6 +123,11 @@ struct hqcgb_plan {
   float *dphiT32 = nullptr, *Yhl = nullptr;  // grid-major AO gradients; split Y^T
   double *ovq = nullptr;                     // lattice sums of the S/T Hermite products
   bool allow_warm = false;                   // warm eigen-refinement after the DIIS warm-up
+  // mixed path: occupied block Y = C_occ sqrt(f) (n x nuse_dm) when few
+  // orbitals are occupied, so that D = Y Y^T and S D F = (S Y)(F^T Y)^T run
+  // as GEMMs with K = nuse_dm
+  double *Yd = nullptr, *Y2 = nullptr, *xerr = nullptr;
+  int nuse_dm = 0;
   double *c1_prev = nullptr;                 // eigenvectors of the previous F'
   bool have_prev = false;
   // mixed Kohn-Sham forces from the occupied orbitals on the grid
@@ -294,6 +300,9 @@ static void create(const hqcgb_params *in, hqcgb_plan *p) {
     p->mew.wbuf = p->alloc<double>(2 * nn);
     p->mew.iwork = p->alloc<int>(5 * (size_t)nao + 1);
     p->c1_prev = p->alloc<double>(nn);
+    p->Yd = p->alloc<double>((size_t)nao * kThinOcc);
+    p->Y2 = p->alloc<double>((size_t)nao * kThinOcc);
+    p->xerr = p->alloc<double>(nn);
     p->F1d32 = p->alloc<float>((size_t)n * 3 * p->ng * P.n_prim * 6);
     if (p->orb_forces) {
       p->psi32 = p->alloc<float>((size_t)(p->gga ? 4 : 1) * tc_psi_max(false) * N);
@@ -412,6 +421,21 @@ static void density_matrix(Ctx &c) {
   int n = p->nao;
   occupations(P.n_atoms, n, P.smearing, P.smearing_method, P.smearing_sigma, P.search_method,
               P.search_cycle, P.search_tol, occ_shift(p), p->w, p->occ, p->mu, c.st);
+  p->nuse_dm = 0;
+  if (p->mixed) {
+    // orbitals with a non-negligible occupation come first (ascending energies)
+    HQ_CUDA(cudaMemcpyAsync(p->hocc.data(), p->occ, sizeof(double) * n, cudaMemcpyDeviceToHost, c.st));
+    HQ_CUDA(cudaStreamSynchronize(c.st));
+    int nuse = 0;
+    for (int k = 0; k < n; ++k)
+      if (p->hocc[k] > 1e-14) nuse = k + 1;
+    if (nuse >= 1 && nuse <= kThinOcc) {
+      launch_occ_block(p->C, p->occ, n, nuse, p->Yd, c.st);
+      gemm(false, true, n, n, nuse, 1.0, p->Yd, nuse, p->Yd, nuse, nullptr, 0.0, p->D, n, c.st);
+      p->nuse_dm = nuse;
+      return;
+    }
+  }
   gemm(false, true, n, n, n, 1.0, p->C, n, p->C, n, p->occ, 0.0, p->D, n, c.st);
 }
 
@@ -531,9 +555,18 @@ static double fock(Ctx &c) {
 static double err_vector(Ctx &c, double *e) {
   hqcgb_plan *p = c.p;
   int n = p->nao;
-  gemm(false, false, n, n, n, 1.0, p->S, n, p->D, n, nullptr, 0.0, p->t1, n, c.st);
-  gemm(false, false, n, n, n, 1.0, p->t1, n, p->F, n, nullptr, 0.0, p->t2, n, c.st);
-  antisym(n, p->t2, e, c.st);
+  const int k = p->nuse_dm;
+  if (k > 0) {
+    // S D F = (S Y)(F^T Y)^T for D = Y Y^T
+    gemm(false, false, n, k, n, 1.0, p->S, n, p->Yd, k, nullptr, 0.0, p->Y2, k, c.st);
+    gemm(true, false, n, k, n, 1.0, p->F, n, p->Yd, k, nullptr, 0.0, p->t1, k, c.st);
+    gemm(false, true, n, n, k, 1.0, p->Y2, k, p->t1, k, nullptr, 0.0, p->xerr, n, c.st);
+    antisym(n, p->xerr, e, c.st);
+  } else {
+    gemm(false, false, n, n, n, 1.0, p->S, n, p->D, n, nullptr, 0.0, p->t1, n, c.st);
+    gemm(false, false, n, n, n, 1.0, p->t1, n, p->F, n, nullptr, 0.0, p->t2, n, c.st);
+    antisym(n, p->t2, e, c.st);
+  }
   dot((long long)n * n, e, e, 1.0, p->scal + S_ERR2, false, c.st);
   sync_scalars(c);
   return std::sqrt(p->hscal[S_ERR2]);
