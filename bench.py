@@ -4,7 +4,7 @@ Workload (the metric's configuration): H54 as a bcc 3x3x3 lattice at rs 1.31
 with N(0, 0.1 Bohr) displacements (seed 7, a new seed per step), gth-dzvp,
 GGA-PBE, 81^3 grid (the reference's odd grid for the requested 80^3), Gamma
 point; one step = SCF + adjoint forces + Ewald of one batch of B
-configurations (default 8, run concurrently by as many engine workers)
+configurations (default 16, run concurrently by as many engine workers)
 through the public batched API.  Inputs (positions) are resident in HBM
 before the timed region; every configuration streams > 2 GB of grid data (AO
 values and gradients), far more than the 129 MB L2, so no flush is needed.
@@ -39,11 +39,13 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "mixed"])
-    ap.add_argument("--batch", type=int, default=8, help="configurations per step")
+    ap.add_argument("--batch", type=int, default=16, help="configurations per step")
     ap.add_argument("--concurrency", type=int, default=0, help="configurations at once (0: batch)")
     ap.add_argument("--no-fp64-plain", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--workload", default="h54", choices=["h54", "kpoint", "slater", "coulomb"],
+                    help="h54: the headline metric; the others measure the widened paths")
     return ap.parse_args()
 
 
@@ -346,8 +348,168 @@ def run_reference(args):
                     "restatement (oracle/) on the host cores"}
 
 
+# ---------------------------------------------------------------------------
+# Secondary workloads (one JSON line each; not the headline metric)
+# ---------------------------------------------------------------------------
+KB_HA_PER_K = 3.166811563e-6
+
+
+def _timed(fn, steps, warmup):
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(steps):
+        fn()
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / steps
+
+
+def _stage_profile(fn):
+    import torch
+    from hqc_gb300 import _lib
+    _lib.profile(1)
+    fn()
+    torch.cuda.synchronize()
+    st = _lib.stage_stats()
+    _lib.profile(0)
+    return {k: round(v[1], 3) for k, v in st.items() if v[0]}
+
+
+def _line(metric, unit, value, ms, args, config, extra):
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    d = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps,
+         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+         "vs_baseline": None, "data": "synthetic", "config": config}
+    d.update(extra)
+    if "cpu_baseline" in d:
+        d["cpu_baseline"]["cores"] = cores
+    return d
+
+
+def run_kpoint(args):
+    """Single-k SCFs of a 2x2x2 Monkhorst-Pack mesh (the configuration family
+    of H64 dzv HF at 10000 K, here H16 at 49^3 so that the FP64 exact exchange
+    finishes in seconds): one step = the 8 k-point SCFs through
+    make_solver(gamma=False).  CPU: the oracle's geometry set-up and one
+    exchange + Hartree build at one k-point, extrapolated to the GPU's
+    iteration count."""
+    import torch
+    from hqc_gb300 import make_solver
+    from hqc_gb300.workloads import uniform, box
+    n, rs, ng = 16, 1.25, 49
+    L = box(n)
+    sigma = 10000.0 * KB_HA_PER_K
+    xp = uniform(n, 11)
+    u = np.array([-0.25, 0.25]) * 2 * np.pi / (L * rs)
+    kmesh = np.array([[a, b, c] for a in u for b in u for c in u])
+    kw = dict(smearing=True, smearing_sigma=sigma, n_grid=ng, tol=1e-7)
+    s = make_solver(n, L, rs, "gth-dzv", gamma=False, **kw)
+    ms = _timed(lambda: s(xp, kmesh), args.steps, max(args.warmup, 1))
+    iters = float(np.mean(s.iterations))
+    stages = _stage_profile(lambda: s(xp, kmesh[0]))
+    from oracle.gpw import Solver
+    o = Solver(n, L, rs, "gth-dzv", **kw)
+    t0 = time.perf_counter()
+    g = o.setup_geometry(xp, kmesh[0])
+    t1 = time.perf_counter()
+    # core-Hamiltonian orbitals with the Fermi occupations (all orbitals occupied)
+    w, U = np.linalg.eigh(g["S"])
+    v = U / np.sqrt(w)[None, :]
+    e, c1 = np.linalg.eigh(v.conj().T @ (g["T"] + g["V"]) @ v)
+    C = v @ c1
+    occ = o.occ(e)
+    D = (C * occ) @ C.conj().T
+    t2 = time.perf_counter()
+    rho = o.density(D, g["phi"])[0]
+    o.hartree(rho, g["phi"])
+    o.exchange(D, C, occ, g["phi"], g["Stilde"])
+    t3 = time.perf_counter()
+    t_scf = (t1 - t0) + (t3 - t2) * (iters + 1)
+    return _line("k-point SCFs/s (H16 dzv HF Fermi 10000 K, 49^3, 2x2x2 MP mesh)", "SCFs/s",
+                 8.0 / (ms / 1000.0), ms, args,
+                 {"workload": "kpoint", "n_atoms": n, "n_ao": 2 * n, "grid": ng ** 3, "kpoints": 8,
+                  "scf_iterations_mean": iters, "precision_path": "fp64 (complex)"},
+                 {"dtype": "c128", "gpu_ms_per_scf_by_stage": stages,
+                  "cpu_baseline": {"value": 1.0 / t_scf, "unit": "SCFs/s", "kind": "port",
+                                   "sample": f"oracle geometry {t1 - t0:.1f}s + one Fock build "
+                                             f"{t3 - t2:.1f}s at one k-point, x {iters + 1:.0f}"}})
+
+
+def run_slater(args):
+    """Walker-batched Slater matrices (make_slater): H54 bcc protons, gth-dzvp
+    (270 AOs), 4096 walkers of 54 electrons; the AO values at the electrons
+    (FP64 lattice sums) and the batched products.  CPU: the oracle's AO
+    values at the points of 8 walkers."""
+    import torch
+    from hqc_gb300 import make_slater
+    from hqc_gb300.workloads import h54_bcc_pbe
+    w = h54_bcc_pbe(7)
+    n, L, rs = w["n"], w["L"], w["rs"]
+    W = 4096
+    rng = np.random.default_rng(5)
+    xe = torch.as_tensor(rng.uniform(0, L, (W, n, 3)), device="cuda")
+    xp = torch.as_tensor(w["xp"], device="cuda")
+    mo = torch.as_tensor(np.linalg.qr(rng.normal(size=(5 * n, 5 * n)))[0], device="cuda")
+    sl = make_slater(n, L, rs, "gth-dzvp")
+    ms = _timed(lambda: sl(xp, xe, mo), args.steps, max(args.warmup, 1))
+    stages = _stage_profile(lambda: sl(xp, xe, mo))
+    from oracle.gpw import Setup
+    st = Setup(n, L, rs, "gth-dzvp", n_grid=5)
+    b = st.basis
+    xs = rng.uniform(0, L, (8, n, 3)) * rs
+    t0 = time.perf_counter()
+    for x in xs:
+        for r in x:
+            for A in range(n):
+                u = r[:, None] - w["xp"][A][:, None] * rs - st.lat1d[None, :]
+                gq = np.exp(-b.alpha[None, :, None] * u[:, None, :] ** 2)
+                gq.sum(-1), (gq * u[:, None, :]).sum(-1)
+    t1 = time.perf_counter()
+    return _line("Slater walker matrices/s (H54 dzvp, 4096 walkers)", "walkers/s", W / (ms / 1000.0),
+                 ms, args, {"workload": "slater", "n_atoms": n, "n_ao": 5 * n, "walkers": W},
+                 {"dtype": "f64", "gpu_ms_by_stage": stages,
+                  "cpu_baseline": {"value": 8 / (t1 - t0), "unit": "walkers/s", "kind": "port",
+                                   "sample": "oracle 1D lattice sums at the electrons of 8 walkers "
+                                             "(the AO products and GEMMs not counted)"}})
+
+
+def run_coulomb(args):
+    """Walker-batched Ewald sums potential_energy (VMC observables): 4096
+    walkers of 54 protons + 54 electrons, Gmax 15 (14146 G vectors).  CPU:
+    the pairwise oracle on 4 walkers."""
+    from hqc_gb300 import potential_energy, kpoints
+    from hqc_gb300.workloads import box
+    from oracle.ewald import potential_energy as pe_ref
+    import torch
+    n, rs, W = 54, 1.31, 4096
+    L = box(n)
+    rng = np.random.default_rng(6)
+    x = torch.as_tensor(rng.uniform(0, L, (W, 2 * n, 3)), device="cuda")
+    G = kpoints(3, 15)
+    ms = _timed(lambda: potential_energy(x, 10.0, G, L, rs), args.steps, max(args.warmup, 1))
+    xs = x[:4].cpu().numpy()
+    t0 = time.perf_counter()
+    pe_ref(xs, 10.0, G, L, rs)
+    t1 = time.perf_counter()
+    # algorithmic work: n_particles x N_G phase evaluations per walker (sincos)
+    phases = W * 2 * n * G.shape[0]
+    return _line("Coulomb walker energies/s (54 p + 54 e, Gmax 15)", "walkers/s", W / (ms / 1000.0), ms,
+                 args, {"workload": "coulomb", "particles": 2 * n, "walkers": W, "G_vectors": int(G.shape[0])},
+                 {"dtype": "f64", "phase_evals_per_s": phases / (ms / 1000.0),
+                  "cpu_baseline": {"value": 4 / (t1 - t0), "unit": "walkers/s", "kind": "port",
+                                   "sample": "pairwise oracle on 4 walkers"}})
+
+
 def main():
     args = parse()
+    if args.impl != "reference" and args.workload != "h54":
+        line = {"kpoint": run_kpoint, "slater": run_slater, "coulomb": run_coulomb}[args.workload](args)
+        print(json.dumps(line), flush=True)
+        return
     line = run_reference(args) if args.impl == "reference" else run_ours(args)
     if line is not None:
         print(json.dumps(line), flush=True)

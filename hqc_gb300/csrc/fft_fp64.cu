@@ -18,9 +18,13 @@ namespace hqcgb {
 // line_stride == 1 the group is loaded element-major (coalesced across lines),
 // otherwise line-major (the lines are contiguous, elem_stride == 1).
 // C = double2 (FP64 path) or float2 (mixed path; twiddles rounded from FP64).
+// n1 > 1: two-factor Cooley-Tukey for ng = n1 n2 (j = n2 j1 + j2, k = k1 + n1 k2):
+//   y[j2][k1]        = W^(j2 k1) sum_j1 x[n2 j1 + j2] W^(n2 j1 k1)
+//   X[k1 + n1 k2]    = sum_j2 y[j2][k1] W^(n1 j2 k2),      W = exp(-2 pi i / ng),
+// ng (n1 + n2) multiply-adds per line instead of ng^2; n1 = 1: the direct sum.
 template <typename C>
 __global__ void k_dft_pass(C *__restrict__ c, int ng, int axis, const double2 *__restrict__ tw,
-                           int inverse, long long N) {
+                           int inverse, long long N, int n1) {
   using R = decltype(C::x);
   extern __shared__ __align__(16) unsigned char sm_raw[];
   C *buf = reinterpret_cast<C *>(sm_raw);
@@ -79,6 +83,51 @@ __global__ void k_dft_pass(C *__restrict__ c, int ng, int axis, const double2 *_
   int l = tid & 31;
   C res[16];  // ng <= 256 with 16 warps
   int nk = 0;
+  if (n1 > 1) {
+    const int n2 = ng / n1;
+    // stage A: m = j2 n1 + k1
+    for (int m = tid >> 5; m < ng; m += (blockDim.x >> 5)) {
+      const int j2 = m / n1, k1 = m - j2 * n1;
+      const int step = (n2 * k1) % ng;
+      R re = 0, im = 0;
+      int idx = 0;
+      for (int j1 = 0; j1 < n1; ++j1) {
+        C x = buf[(n2 * j1 + j2) * 32 + l];
+        C t = w[idx];
+        re += x.x * t.x - x.y * t.y;
+        im += x.x * t.y + x.y * t.x;
+        idx += step;
+        if (idx >= ng) idx -= ng;
+      }
+      C t = w[(j2 * k1) % ng];
+      res[nk].x = re * t.x - im * t.y;
+      res[nk].y = re * t.y + im * t.x;
+      ++nk;
+    }
+    __syncthreads();
+    nk = 0;
+    for (int m = tid >> 5; m < ng; m += (blockDim.x >> 5)) buf[m * 32 + l] = res[nk++];
+    __syncthreads();
+    // stage B: output k = k1 + n1 k2 from y[j2][k1] at buf[(j2 n1 + k1) * 32 + l]
+    nk = 0;
+    for (int k = tid >> 5; k < ng; k += (blockDim.x >> 5)) {
+      const int k2 = k / n1, k1 = k - k2 * n1;
+      const int step = (n1 * k2) % ng;
+      R re = 0, im = 0;
+      int idx = 0;
+      for (int j2 = 0; j2 < n2; ++j2) {
+        C x = buf[(j2 * n1 + k1) * 32 + l];
+        C t = w[idx];
+        re += x.x * t.x - x.y * t.y;
+        im += x.x * t.y + x.y * t.x;
+        idx += step;
+        if (idx >= ng) idx -= ng;
+      }
+      res[nk].x = re;
+      res[nk].y = im;
+      ++nk;
+    }
+  } else
   for (int k = tid >> 5; k < ng; k += (blockDim.x >> 5)) {
     R re = 0, im = 0;
     int idx = 0;
@@ -122,9 +171,13 @@ static void fft3d_impl(C *c, int ng, int batch, const double2 *tw, bool inverse,
     attr = smem;
   }
   int zb = (ng + 31) / 32;
+  // largest factor n1 <= sqrt(ng) (1 for a prime size: the direct sum)
+  int n1 = 1;
+  for (int f = 2; f * f <= ng; ++f)
+    if (ng % f == 0) n1 = f;
   for (int axis = 2; axis >= 0; --axis) {
     dim3 grid(axis == 2 ? ceil_div((long long)ng * ng, 32) : ng * zb, batch);
-    k_dft_pass<C><<<grid, 512, smem, st>>>(c, ng, axis, tw, inverse ? 1 : 0, N);
+    k_dft_pass<C><<<grid, 512, smem, st>>>(c, ng, axis, tw, inverse ? 1 : 0, N, n1);
     HQ_LAUNCH_CHECK();
   }
 }

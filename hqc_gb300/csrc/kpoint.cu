@@ -28,6 +28,10 @@
 namespace hqcgb {
 
 static constexpr double kMadelungK = 0.22578495;  // solver.py:404, 510
+// Exact exchange skips orbitals with occupation <= 1e-14 (besides the caller's
+// exx_occ_threshold): each adds f_i times a bounded matrix to K, below FP64
+// rounding of the sum; with Fermi smearing most virtual orbitals are such.
+static constexpr double kExxOccFloor = 1e-14;
 
 // Factor table F[A][d][i][a][s] (complex): s = 3 l + k, k = value, first and
 // second derivative of u^l exp(-alpha u^2), each lattice term times the
@@ -542,7 +546,7 @@ static void kexchange(KCtx &c) {
   HQ_CUDA(cudaMemsetAsync(p->K, 0, sizeof(double2) * n * n, c.st));
   for (int i = 0; i < p->nuse; ++i) {
     const double f = p->h_occ[i];
-    if (!(f > p->P.exx_occ_threshold)) continue;
+    if (!(f > std::max(p->P.exx_occ_threshold, kExxOccFloor))) continue;
     k_pair_kpt<<<ceil_div((long long)n * N, 256), 256, 0, c.st>>>(p->phi, p->Psi + (long long)i * N, n,
                                                                     N, p->Z, p->W);
     HQ_LAUNCH_CHECK();

@@ -69,6 +69,10 @@ void stage_mark(int stage, cudaStream_t st, bool begin) {
 using namespace hqcgb;
 
 static constexpr double kMadelungSC = 0.22578495;  // solver.py:404
+// Exact exchange skips orbitals with occupation <= 1e-14 (besides the caller's
+// exx_occ_threshold): each adds f_i times a bounded matrix to K, below FP64
+// rounding of the sum; with Fermi smearing most virtual orbitals are such.
+static constexpr double kExxOccFloor = 1e-14;
 // K blocks of 32 AOs the orbital-density kernel accumulates per TMEM slot
 // before a compensated drain: 2 measured 14% faster than 1 on the H54
 // shapes at a relative density bias of -2.9e-7 (the tensor core truncates).
@@ -462,7 +466,7 @@ static void exchange(Ctx &c, double *Zacc) {
   HQ_CUDA(cudaMemsetAsync(p->K, 0, sizeof(double) * n * n, c.st));
   for (int i = 0; i < n; ++i) {
     double f = p->h_occ[i];
-    if (!(f > p->P.exx_occ_threshold)) continue;
+    if (!(f > std::max(p->P.exx_occ_threshold, kExxOccFloor))) continue;
     launch_psi(p->C, n, i, p->phi, N, p->psi, c.st);
     launch_real_to_complex(p->phi, p->psi, N, n, p->cbuf, c.st);
     launch_fft3d(p->cbuf, p->ng, n, p->tw, false, c.st);

@@ -73,7 +73,7 @@ typedef struct {
   int diis_start_cycle;
   double diis_damp;
   int precision;           /* HQCGB_PREC_* */
-  double exx_occ_threshold;/* skip orbitals with occupation <= this in exchange */
+  double exx_occ_threshold;/* exchange skips orbitals with occupation <= max(this, 1e-14) */
   int want_forces;         /* keep derivative tables for hqcgb_forces */
 } hqcgb_params;
 
