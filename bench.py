@@ -136,6 +136,10 @@ def peaks():
     return 6800.0, 1900.0, "fallback"
 
 
+# DRAM bytes (read + write) of one k_tc_quad_tma launch at the H54 PBE shapes
+# (ncu; profiles/quadrature_h54.md)
+QUAD_TRAFFIC = 2771808512 + 149348608
+
 CONFIG = {"workload": "H54 bcc rs=1.31 gth-dzvp PBE 81^3 Gamma, SCF tol 1e-7 Ry + forces",
           "n_atoms": 54, "n_ao": 270, "grid": 531441}
 
@@ -178,6 +182,50 @@ def psi_density_roofline(hbm_gbs, src, reps=5):
             "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs, burst)" if src == "measured" else src,
             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch "
                               "(profiles/psi_density_h54.md)", "drain": drain}
+
+
+def quadrature_roofline(hbm_gbs, src, reps=5):
+    """The Fock quadrature kernel (k_tc_quad_tma: TMA loads of pre-split TF32
+    operands, tcgen05 3xTF32; the dominant multi-SM kernel of the SCF) timed
+    alone with CUDA events at the H54 PBE shapes, its non-symmetric tile set:
+    algorithmic bytes = the four TF32 pieces (Z hi/lo, phi hi/lo) read once,
+    4 x n_ao x N x 4 B, plus M (n_ao^2 x 8 B).  The split pass that forms the
+    pieces is timed separately (stage "split") and not counted here."""
+    import torch
+    from hqc_gb300 import _lib
+    nao, N = 270, 531441
+    ld = (N + 63) // 64 * 64
+    g = torch.Generator(device="cuda").manual_seed(1)
+    phi = torch.zeros(nao, ld, dtype=torch.float32, device="cuda")
+    phi[:, :N] = torch.randn(nao, N, generator=g, device="cuda")
+    dphi = torch.zeros(3 * nao, ld, dtype=torch.float32, device="cuda")
+    dphi[:, :N] = torch.randn(3 * nao, N, generator=g, device="cuda")
+    w = torch.zeros(ld, dtype=torch.float32, device="cuda")
+    w[:N] = torch.rand(N, generator=g, device="cuda")
+    u = torch.zeros(3, ld, dtype=torch.float32, device="cuda")
+    u[:, :N] = torch.randn(3, N, generator=g, device="cuda")
+    _lib.tc_quadrature_gga(phi, dphi, w, u, 1e-3, N, drain=4)  # warm
+    torch.cuda.synchronize()
+    _lib.profile(1)
+    for _ in range(reps):
+        _lib.tc_quadrature_gga(phi, dphi, w, u, 1e-3, N, drain=4)
+    torch.cuda.synchronize()
+    st = _lib.stage_stats()
+    cnt, tot = st["quadrature"]
+    _lib.profile(0)
+    avg_s = tot / cnt / 1000.0
+    algo = 4 * nao * N * 4 + nao * nao * 8
+    achieved = algo / avg_s / 1e9
+    del phi, dphi
+    torch.cuda.empty_cache()
+    return {"bound": "hbm", "achieved": achieved, "peak": hbm_gbs, "unit": "GB/s",
+            "frac": achieved / hbm_gbs, "traffic": QUAD_TRAFFIC,
+            "kernel": "k_tc_quad_tma + k_tc_quad_reduce (PBE Fock quadrature, H54 shapes)",
+            "algorithmic_bytes": algo, "avg_ms": avg_s * 1e3, "launches": cnt,
+            "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs, burst)" if src == "measured" else src,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_tc_quad_tma, "
+                              "one launch (profiles/quadrature_h54.md)", "drain": 4,
+            "split_ms": st["split"][1] / max(st["split"][0], 1)}
 
 
 def run_ours(args):
@@ -244,7 +292,8 @@ def run_ours(args):
     stage_ms = {k: round(v[1] / B, 3) for k, v in stats.items() if v[0]}
 
     hbm, bf16, src = peaks()
-    roof = psi_density_roofline(hbm, src)
+    roof = quadrature_roofline(hbm, src)
+    roof_psi = psi_density_roofline(hbm, src)
 
     # the plain FP64 single-configuration path on the last timed batch's first
     # configuration: its speed, and the mixed path's error against it
@@ -288,7 +337,7 @@ def run_ours(args):
                            scf_iterations_mean=float(np.mean(iters[B * args.warmup:])),
                            l2="inputs > L2 (every configuration streams > 2 GB of AO grids), no flush",
                            parallelism=f"replicas x{world}"),
-            "roofline": roof, "fp64_plain": fp64, "gpu_ms_per_eval_by_stage": stage_ms, "e2e": e2e,
+            "roofline": roof, "roofline_orbital_density": roof_psi, "fp64_plain": fp64, "gpu_ms_per_eval_by_stage": stage_ms, "e2e": e2e,
             "gpu_launches": launches, "clocks": clk.summary()}
     if rank == 0 and not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(iters_per_eval=float(np.mean(iters)))

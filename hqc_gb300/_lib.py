@@ -49,8 +49,9 @@ EXPORTS = ("hqcgb_plan_create", "hqcgb_plan_destroy", "hqcgb_scf", "hqcgb_scf_ba
            "hqcgb_tc_orbital_density", "hqcgb_plan_set_concurrency", "hqcgb_pes_batch",
            "hqcgb_ao_points", "hqcgb_slater", "hqcgb_kplan_create", "hqcgb_kplan_destroy",
            "hqcgb_scf_kpt", "hqcgb_scf_kpt_batch", "hqcgb_kplan_query", "hqcgb_eigh_herm",
-           "hqcgb_ao_points_kpt", "hqcgb_slater_kpt", "hqcgb_overlap", "hqcgb_coulomb_energy")
-N_STAGES = 14
+           "hqcgb_ao_points_kpt", "hqcgb_slater_kpt", "hqcgb_overlap", "hqcgb_coulomb_energy",
+           "hqcgb_tc_quadrature_gga")
+N_STAGES = 15
 
 _lib = None
 
@@ -130,6 +131,8 @@ def load():
     lib.hqcgb_tc_quadrature.argtypes = [ctypes.c_int, ctypes.c_longlong, ctypes.c_longlong,
                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                         ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+    lib.hqcgb_tc_quadrature_gga.argtypes = [ctypes.c_int, ctypes.c_longlong, ctypes.c_longlong] + \
+        [ctypes.c_void_p] * 4 + [ctypes.c_float, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
     lib.hqcgb_tc_density.argtypes = [ctypes.c_int, ctypes.c_longlong, ctypes.c_longlong,
                                      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                      ctypes.c_void_p, ctypes.c_void_p]
@@ -258,6 +261,22 @@ def tc_quadrature(phi32, w32, nsplit=2, drain=2):
     check(lib.hqcgb_tc_quadrature(nao, ld, ld, ctypes.c_void_p(phi32.data_ptr()),
                                   ctypes.c_void_p(w32.data_ptr()), nsplit, drain,
                                   ctypes.c_void_p(M.data_ptr()), st))
+    return M
+
+
+def tc_quadrature_gga(phi32, dphi32, w32, u32, dV, N=None, drain=4):
+    """M = Z phi^T + phi Z^T, Z = 0.5 w phi + dV u . grad phi (fp32 operands on
+    the device, row stride a multiple of 32): (nao, nao) float64."""
+    import torch
+    lib = load()
+    nao, ld = phi32.shape
+    N = ld if N is None else N
+    M = torch.empty(nao, nao, dtype=torch.float64, device=phi32.device)
+    st = ctypes.c_void_p(torch.cuda.current_stream(phi32.device).cuda_stream)
+    check(lib.hqcgb_tc_quadrature_gga(nao, N, ld, ctypes.c_void_p(phi32.data_ptr()),
+                                      ctypes.c_void_p(dphi32.data_ptr()), ctypes.c_void_p(w32.data_ptr()),
+                                      ctypes.c_void_p(u32.data_ptr()), float(dV), int(drain),
+                                      ctypes.c_void_p(M.data_ptr()), st))
     return M
 
 

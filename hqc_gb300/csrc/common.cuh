@@ -17,7 +17,7 @@ void count_launch(long long k = 1);
 // Per-stage device timing (CUDA events on the launching stream), enabled by
 // hqcgb_profile(1).  Stage names are listed in plan.cu (kStageNames).
 enum Stage { ST_GTO = 0, ST_PHI, ST_DENSITY, ST_QUAD, ST_FFT, ST_XC, ST_JACOBI, ST_GEMM_SMALL,
-             ST_OVERLAP, ST_FORCE_GRID, ST_EXCHANGE, ST_EWALD, ST_OTHER, ST_PSI, ST_COUNT };
+             ST_OVERLAP, ST_FORCE_GRID, ST_EXCHANGE, ST_EWALD, ST_OTHER, ST_PSI, ST_SPLIT, ST_COUNT };
 void stage_mark(int stage, cudaStream_t st, bool begin);
 struct StageScope {
   int s;

@@ -26,7 +26,7 @@ void count_launch(long long k) { g_launches += k; }
 
 static const char *kStageNames[ST_COUNT] = {"gto1d", "phi", "density", "quadrature", "fft", "xc",
                                             "jacobi", "gemm_small", "overlap", "force_grid",
-                                            "exchange", "ewald", "other", "psi_density"};
+                                            "exchange", "ewald", "other", "psi_density", "split"};
 struct StageRec {
   int stage;
   cudaEvent_t a, b;

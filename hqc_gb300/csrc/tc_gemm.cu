@@ -1247,7 +1247,7 @@ void launch_tc_psi_density(const float *phiT, const float *dphiT, const float *Y
 }
 
 // ---------------------------------------------------------------------------
-int tc_quad_chunk() { return 8192; }
+int tc_quad_chunk() { return 2048; }
 
 size_t tc_quad_partial_doubles(int nao, long long N) {
   int mt = ceil_div(nao, tc::kM), nt = ceil_div(nao, tc::kN);
@@ -1329,7 +1329,7 @@ void launch_tc_quad_split(const float *Ahl, const float *Bhl, int nao, long long
 void launch_split_operand(const float *phi, const float *dphi, const float *w, const float *u, int nao,
                           long long N, long long ldi, long long ldo, float a, float b, float *out,
                           cudaStream_t st) {
-  HQ_STAGE(ST_QUAD, st);
+  HQ_STAGE(ST_SPLIT, st);
   HQ_REQUIRE(ldi % 4 == 0 && ldo % 4 == 0 && ldo >= N && ldi >= N, "split operand: bad row strides");
   dim3 grid(ceil_div(ldo, 1024), nao);
   tc::k_split_operand<<<grid, 256, 0, st>>>(phi, dphi, w, u, nao, N, ldi, ldo, a, b, out,
@@ -1404,6 +1404,42 @@ void launch_tc_density(const float *phi, const float *phiT, const float *dphi, c
 // ---------------------------------------------------------------------------
 // C ABI: the two tensor-core contractions as library calls (tests and tools).
 // ---------------------------------------------------------------------------
+// C ABI: the GGA Fock quadrature of the mixed path, M = Z phi^T + phi Z^T with
+// Z = 0.5 w phi + dV u . grad phi (hqc/pbc/solver.py:680-694 with the PBE
+// gradient term); phi [nao][ld], dphi [3][nao][ld], w [ld], u [3][ld] fp32
+// (device), ld % 32 == 0.  Splits phi and Z into TF32 pieces, then runs the
+// tensor-core quadrature (non-symmetric tile set).
+extern "C" int hqcgb_tc_quadrature_gga(int nao, long long N, long long ld, const float *phi,
+                                       const float *dphi, const float *w, const float *u, float dV,
+                                       int drain, double *M, void *stream) {
+  using namespace hqcgb;
+  cudaStream_t st = (cudaStream_t)stream;
+  try {
+    HQ_REQUIRE(nao >= 1 && N >= 1 && ld >= N && ld % 32 == 0 && phi && dphi && w && u && M, "bad argument");
+    double *part = nullptr;
+    float *hl = nullptr;
+    int *err = nullptr;
+    HQ_CUDA(cudaMallocAsync(&part, tc_quad_partial_doubles(nao, N) * sizeof(double), st));
+    HQ_CUDA(cudaMallocAsync(&hl, 4 * (size_t)nao * ld * sizeof(float), st));
+    HQ_CUDA(cudaMallocAsync(&err, sizeof(int), st));
+    HQ_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
+    float *phl = hl, *zhl = hl + 2 * (size_t)nao * ld;
+    launch_split_operand(phi, nullptr, nullptr, nullptr, nao, N, ld, ld, 1.f, 0.f, phl, st);
+    launch_tc_quadrature(phi, dphi, phl, w, u, dV, nao, N, ld, true, 1.0, part, M, err, st, drain, zhl);
+    int h = 0;
+    HQ_CUDA(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    HQ_CUDA(cudaFreeAsync(part, st));
+    HQ_CUDA(cudaFreeAsync(hl, st));
+    HQ_CUDA(cudaFreeAsync(err, st));
+    HQ_CUDA(cudaStreamSynchronize(st));
+    if (h) throw Error{HQCGB_CUDA_ERROR, "tensor-core pipeline wait limit hit"};
+    return HQCGB_OK;
+  } catch (const Error &e) {
+    set_error(e.msg);
+    return e.status;
+  }
+}
+
 extern "C" int hqcgb_tc_quadrature(int nao, long long N, long long ld, const float *phi,
                                    const float *w, int nsplit, int drain, double *M, void *stream) {
   using namespace hqcgb;

@@ -7,7 +7,8 @@ Cases (synthetic operands with the benchmark's sizes: 270 AOs, an 81^3 grid,
 
   psi_density   orbital-form density with the gradient (tcgen05, 3xTF32)
   density_D     density-matrix form of the density (tcgen05, 3xTF32)
-  quadrature    phi diag(w) phi^T (tcgen05, 3xTF32)
+  quadrature    phi diag(w) phi^T (tcgen05, 3xTF32; symmetric tile set)
+  quadrature_gga  Z phi^T + phi Z^T with the PBE operand (the SCF's form)
   eigh_mixed    the mixed-precision eigensolver on a 270 x 270 matrix
   eigh_fp64     the FP64 eigensolver on the same matrix
 
@@ -36,7 +37,8 @@ def _operands(gga):
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["psi_density", "density_D", "quadrature", "eigh_mixed", "eigh_fp64"])
+    ap.add_argument("case", choices=["psi_density", "density_D", "quadrature", "quadrature_gga",
+                                     "eigh_mixed", "eigh_fp64"])
     ap.add_argument("--reps", type=int, default=3)
     a = ap.parse_args(argv)
     import torch
@@ -62,6 +64,15 @@ def main(argv=None):
         D = 0.5 * (D + D.T)
         for _ in range(a.reps):
             _lib.tc_density(phi, D, N, drain=1)
+    elif a.case == "quadrature_gga":
+        phi, dphi, N = _operands(True)
+        ld = phi.shape[1]
+        w = torch.zeros(ld, dtype=torch.float32, device="cuda")
+        w[:N] = torch.rand(N, device="cuda")
+        u = torch.zeros(3, ld, dtype=torch.float32, device="cuda")
+        u[:, :N] = torch.randn(3, N, device="cuda")
+        for _ in range(a.reps):
+            _lib.tc_quadrature_gga(phi, dphi, w, u, 1e-3, N, drain=4)
     else:
         phi, _, N = _operands(False)
         w = torch.zeros(phi.shape[1], dtype=torch.float32, device="cuda")

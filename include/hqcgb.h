@@ -218,6 +218,14 @@ int hqcgb_tc_quadrature(int nao, long long N, long long ld, const float *phi, co
 int hqcgb_tc_density(int nao, long long N, long long ld, const float *phi, const float *D,
                      int nsplit, int drain, double *rho, void *stream);
 
+/* The GGA (PBE) Fock quadrature of the mixed path: M = Z phi^T + phi Z^T with
+ * Z = 0.5 w phi + dV u . grad phi (hqc/pbc/solver.py:680-694 plus the gradient
+ * term); phi [nao][ld], dphi [3][nao][ld], w [ld], u [3][ld] fp32 (device),
+ * ld % 32 == 0. */
+int hqcgb_tc_quadrature_gga(int nao, long long N, long long ld, const float *phi,
+                            const float *dphi, const float *w, const float *u, float dV, int drain,
+                            double *M, void *stream);
+
 /* Orbital form of the density: rho(g) = sum_k occ_k |psi_k(g)|^2 with
  * psi_k = sum_p C[p][k] phi_p over the first nuse (<= 64) orbitals, and
  * with dphi (3 x [nao][ld]) also grad rho (3 x N) -- the density of

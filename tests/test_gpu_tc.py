@@ -127,3 +127,29 @@ def test_eigh_mixed_clustered_spectrum(n):
     np.testing.assert_allclose(w, np.linalg.eigvalsh(M), atol=1e-12 * 3)
     np.testing.assert_allclose(V.T @ V, np.eye(n), atol=1e-12)
     np.testing.assert_allclose(M @ V, V * w, atol=1e-11 * 3)
+
+
+@pytest.mark.parametrize("nao,N", [(20, 4000), (150, 9000), (270, 20000)])
+def test_tc_quadrature_gga_matches_fp64(nao, N):
+    """The PBE-form Fock quadrature (pre-split operands, non-symmetric tile
+    set with the partial AO block as an N = 16 MMA, transposed on the A side)
+    against FP64: M = Z phi^T + phi Z^T, Z = 0.5 w phi + dV u . grad phi."""
+    import torch
+    from hqc_gb300._lib import tc_quadrature_gga
+    g = torch.Generator(device="cuda").manual_seed(nao)
+    ld = (N + 31) // 32 * 32
+    phi = torch.zeros(nao, ld, dtype=torch.float32, device="cuda")
+    phi[:, :N] = torch.randn(nao, N, generator=g, device="cuda")
+    dphi = torch.zeros(3, nao, ld, dtype=torch.float32, device="cuda")
+    dphi[:, :, :N] = torch.randn(3, nao, N, generator=g, device="cuda")
+    w = torch.zeros(ld, dtype=torch.float32, device="cuda")
+    w[:N] = torch.rand(N, generator=g, device="cuda")
+    u = torch.zeros(3, ld, dtype=torch.float32, device="cuda")
+    u[:, :N] = torch.randn(3, N, generator=g, device="cuda")
+    dV = 0.01
+    M = tc_quadrature_gga(phi, dphi, w, u, dV, N, drain=1)
+    P = phi[:, :N].double()
+    Z = 0.5 * w[:N].double() * P + dV * torch.einsum("dg,dpg->pg", u[:, :N].double(), dphi[:, :, :N].double())
+    ref = Z @ P.T + P @ Z.T
+    err = (M - ref).abs().max().item() / ref.abs().max().item()
+    assert err < 2e-6, err
