@@ -347,8 +347,14 @@ __global__ void k_oa_lambda(int n, const double *__restrict__ S, const double *_
 // the step stops after the statistics: X is kept and only the eigenvalue
 // estimates are set.
 constexpr double kOaConverged = 1e-12;
+// An update whose largest correction |E_ij| is below this leaves an error of
+// order |E|^2 (quadratic convergence outside clusters, which are rotated
+// exactly): the solve ends after it without a confirming step.
+constexpr double kOaFinalUpdate = 1e-7;
 static double oa_iteration(int n, const double *A, double *X, double *w, MixedEigWork &ws,
-                           cudaStream_t st, int max_cluster = kMaxClusterFock) {
+                           cudaStream_t st, int max_cluster = kMaxClusterFock,
+                           bool *final_update = nullptr) {
+  if (final_update) *final_update = false;
   const long long nn = (long long)n * n;
   const int grid = (int)std::min<long long>(ceil_div(nn, kOaThreads), 148);
   double *red = ws.emax + 8;  // [0..4] grid reductions
@@ -381,6 +387,12 @@ static double oa_iteration(int n, const double *A, double *X, double *w, MixedEi
   HQ_LAUNCH_CHECK();
   gemm(false, false, n, n, n, 1.0, X, n, ws.E, n, nullptr, 0.0, ws.T1, n, st);  // X E
   axpby(n, 1.0, X, 1.0, ws.T1, false, X, st);                                  // X += X E
+  if (final_update) {
+    double em[13];
+    HQ_CUDA(cudaMemcpyAsync(em, ws.emax, 13 * sizeof(double), cudaMemcpyDeviceToHost, st));
+    HQ_CUDA(cudaStreamSynchronize(st));
+    *final_update = em[8 + 4] < kOaFinalUpdate && em[2] == 0;
+  }
   if (std::getenv("HQCGB_TRACE")) {
     double em[13];
     HQ_CUDA(cudaMemcpyAsync(em, ws.emax, 13 * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -436,8 +448,9 @@ bool eigh_mixed(int n, const double *A, double *V, double *w, MixedEigWork &ws, 
   k_f32_to_f64<<<ceil_div(nn, 256), 256, 0, st>>>(nn, ws.V32, V);
   HQ_LAUNCH_CHECK();
   for (int it = 0; it < 8; ++it) {
-    double off = oa_iteration(n, A, V, w, ws, st, wide ? kMaxCluster : kMaxClusterFock);
-    if (off < kOaConverged) {
+    bool fin = false;
+    double off = oa_iteration(n, A, V, w, ws, st, wide ? kMaxCluster : kMaxClusterFock, &fin);
+    if (off < kOaConverged || fin) {
       sort_eigpairs(n, w, V, ws, st);
       return true;
     }
@@ -456,9 +469,10 @@ bool eigh_mixed_warm(int n, const double *A, const double *X0, double *V, double
   HQ_CUDA(cudaMemcpyAsync(V, X0, sizeof(double) * n * n, cudaMemcpyDeviceToDevice, st));
   double prev = 1e300;
   for (int it = 0; it < 8; ++it) {
-    double off = oa_iteration(n, A, V, w, ws, st);
+    bool fin = false;
+    double off = oa_iteration(n, A, V, w, ws, st, kMaxClusterFock, &fin);
     if (!(off < 2e-3)) return false;
-    if (off < kOaConverged) {
+    if (off < kOaConverged || fin) {
       sort_eigpairs(n, w, V, ws, st);
       return true;
     }
