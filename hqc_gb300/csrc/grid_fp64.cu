@@ -240,7 +240,11 @@ void launch_quadrature(const double *A, const double *B, const double *w, int na
 //   in : rho, grho (GGA), vh (Hartree potential)
 //   out: w = dV (vh + v_rho) (quadrature weight), u = 2 v_sigma grad rho (GGA)
 //   partial sums per block: [0] sum e_xc, [1] sum vh*rho
+// F32 (mixed path): the functional and its derivatives are evaluated in FP32
+// where rho > 1e-6 (FP64 below, where FP32 would lose range); per-point
+// rounding of about 1e-7 averages out in the FP64 sums.
 // ---------------------------------------------------------------------------
+template <bool F32>
 __global__ void k_xc_pointwise(int kind, const double *__restrict__ rho,
                                const double *__restrict__ grho, const double *__restrict__ vh,
                                long long N, double dV, double *__restrict__ w,
@@ -257,7 +261,17 @@ __global__ void k_xc_pointwise(int kind, const double *__restrict__ rho,
       sig = gx * gx + gy * gy + gz * gz;
     }
     double e = 0, vr = 0, vs = 0;
-    if (kind >= 0) xc_point<double>(kind, r, sig, e, vr, vs);
+    if (kind >= 0) {
+      if (F32 && r > 1e-6) {
+        float ef, vrf, vsf;
+        xc_point<float>(kind, (float)r, (float)sig, ef, vrf, vsf);
+        e = ef;
+        vr = vrf;
+        vs = vsf;
+      } else {
+        xc_point<double>(kind, r, sig, e, vr, vs);
+      }
+    }
     double v = vh ? vh[g] : 0.0;
     if (w) w[g] = dV * (v + vr);
     if (vxc_out) vxc_out[g] = vr;
@@ -281,9 +295,12 @@ int xc_blocks(long long N) { return ceil_div(N, 256); }
 
 void launch_xc_pointwise(int kind, const double *rho, const double *grho, const double *vh,
                          long long N, double dV, double *w, double *vxc_out, double *u,
-                         double *part, cudaStream_t st) {
+                         double *part, cudaStream_t st, bool fp32) {
   HQ_STAGE(ST_XC, st);
-  k_xc_pointwise<<<xc_blocks(N), 256, 0, st>>>(kind, rho, grho, vh, N, dV, w, vxc_out, u, part);
+  if (fp32)
+    k_xc_pointwise<true><<<xc_blocks(N), 256, 0, st>>>(kind, rho, grho, vh, N, dV, w, vxc_out, u, part);
+  else
+    k_xc_pointwise<false><<<xc_blocks(N), 256, 0, st>>>(kind, rho, grho, vh, N, dV, w, vxc_out, u, part);
   HQ_LAUNCH_CHECK();
 }
 

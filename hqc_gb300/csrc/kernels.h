@@ -19,7 +19,7 @@ void launch_quadrature(const double *A, const double *B, const double *w, int na
 int xc_blocks(long long N);
 void launch_xc_pointwise(int kind, const double *rho, const double *grho, const double *vh,
                          long long N, double dV, double *w, double *vxc_out, double *u,
-                         double *part, cudaStream_t st);
+                         double *part, cudaStream_t st, bool fp32 = false);
 void launch_gga_operand(const double *phi, const double *dphi, const double *w, const double *u,
                         int nao, long long N, double dV, double *Z, cudaStream_t st);
 void launch_sum_partials(const double *part, int nblk, int stride, int nout, double scale,

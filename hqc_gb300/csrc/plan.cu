@@ -521,7 +521,7 @@ static double fock(Ctx &c) {
     }
     launch_poisson_f32(p->rho, p->vh, p->cbuf32, p->coul, p->ng, p->tw, c.st);
     launch_xc_pointwise(kind, p->rho, p->gga ? p->grho : nullptr, p->vh, N, p->dV, p->wq, p->vxc,
-                        p->gga ? p->u : nullptr, p->xpart, c.st);
+                        p->gga ? p->u : nullptr, p->xpart, c.st, true);
     launch_sum_partials(p->xpart, xc_blocks(N), 2, 2, 1.0, p->scal + S_EXC, false, c.st);
     launch_to_f32(p->wq, N, N, 1, 1.0, p->w32, p->ld, c.st);
     if (p->gga) launch_to_f32(p->u, N, N, 3, 1.0, p->u32, p->ld, c.st);
