@@ -157,15 +157,18 @@ __global__ void k_zoperand(const double2 *__restrict__ phi, const double2 *__res
   Z[idx] = z;
 }
 
-// Exchange pair densities of orbital i: P_p = phibar_p conj(psibar_i), into P
-// and W (W is then transformed in place by the Poisson solve).
+// Exchange pair densities of orbital i: W_p = phibar_p conj(psibar_i) (then
+// transformed in place).
 __global__ void k_pair_kpt(const double2 *__restrict__ phi, const double2 *__restrict__ psi, int nao,
-                           long long N, double2 *__restrict__ P, double2 *__restrict__ W) {
+                           long long N, double2 *__restrict__ W) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (long long)nao * N) return;
-  const double2 v = zmul(phi[idx], zconj(psi[idx % N]));
-  P[idx] = v;
-  W[idx] = v;
+  W[idx] = zmul(phi[idx], zconj(psi[idx % N]));
+}
+
+__global__ void k_sqrt_table(long long N, const double *__restrict__ a, double *__restrict__ b) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < N) b[i] = sqrt(a[i]);
 }
 
 // out = a X + b op(Y), op(Y) = Y or Y^H (herm); out must not alias Y when herm.
@@ -298,7 +301,8 @@ struct hqcgb_kplan {
   bool gga = false, hf = false;
   std::vector<void *> allocs;
   // constant tables
-  double *alpha = nullptr, *coef = nullptr, *lat1d = nullptr, *lattice = nullptr, *coul = nullptr;
+  double *alpha = nullptr, *coef = nullptr, *lat1d = nullptr, *lattice = nullptr, *coul = nullptr,
+         *sqcoul = nullptr;
   int *ao_l = nullptr, *ao_cart = nullptr;
   double2 *tw = nullptr;
   // geometry
@@ -413,6 +417,9 @@ static void kcreate(const hqcgb_params &P, hqcgb_kplan *p) {
   kupload(p->tw, tw.data(), sizeof(double2) * p->ng);
   p->coul = p->alloc<double>(N);
   launch_coulomb_table(p->ng, p->L, p->coul, 0);
+  p->sqcoul = p->alloc<double>(N);
+  k_sqrt_table<<<ceil_div(N, 256), 256>>>(N, p->coul, p->sqcoul);
+  HQ_LAUNCH_CHECK();
 
   p->xp = p->alloc<double>(3 * (size_t)n);
   p->kpt = p->alloc<double>(3);
@@ -537,7 +544,11 @@ static void kquadrature(KCtx &c, const double *w, const double *u, double2 *out)
   }
 }
 
-// Exact exchange with the Madelung term (solver.py:509-524, 604-614, 819-822)
+// Exact exchange with the Madelung term (solver.py:509-524, 604-614, 819-822).
+// By Parseval, sum_r P_p conj(W_q) with W = v_H[P] equals
+// sum_G c(G) P^_p(G) conj(P^_q(G)) (c the Coulomb kernel of the Poisson
+// solve), so one forward transform per pair and K += f dV Q Q^H with
+// Q = sqrt(c) P^ replace the forward-and-inverse solve.
 static void kexchange(KCtx &c) {
   hqcgb_kplan *p = c.p;
   const int n = p->nao;
@@ -548,12 +559,11 @@ static void kexchange(KCtx &c) {
     const double f = p->h_occ[i];
     if (!(f > std::max(p->P.exx_occ_threshold, kExxOccFloor))) continue;
     k_pair_kpt<<<ceil_div((long long)n * N, 256), 256, 0, c.st>>>(p->phi, p->Psi + (long long)i * N, n,
-                                                                    N, p->Z, p->W);
+                                                                    N, p->W);
     HQ_LAUNCH_CHECK();
     launch_fft3d(p->W, p->ng, n, p->tw, false, c.st);
-    launch_scale_complex(p->W, p->coul, N, n, c.st);
-    launch_fft3d(p->W, p->ng, n, p->tw, true, c.st);
-    zgemm('N', 'C', n, n, (int)N, make_double2(f * p->dV, 0.0), p->Z, (int)N, p->W, (int)N, kOne, p->K,
+    launch_scale_complex(p->W, p->sqcoul, N, n, c.st);
+    zgemm('N', 'C', n, n, (int)N, make_double2(f * p->dV, 0.0), p->W, (int)N, p->W, (int)N, kOne, p->K,
           n, c.st);
   }
   zcomb(n, 0.5, p->K, 0.5, p->K, true, p->t1, c.st);
