@@ -136,8 +136,8 @@ def peaks():
     return 6800.0, 1900.0, "fallback"
 
 
-# DRAM bytes (read + write) of one k_tc_quad_tma launch at the H54 PBE shapes
-# (ncu; profiles/quadrature_h54.md)
+# DRAM bytes (read + write) of one k_tc_quad_tma launch at the H54 PBE shapes,
+# from one ncu capture (its summary is kept under profiles/)
 QUAD_TRAFFIC = 2771808512 + 149348608
 
 CONFIG = {"workload": "H54 bcc rs=1.31 gth-dzvp PBE 81^3 Gamma, SCF tol 1e-7 Ry + forces",
@@ -181,7 +181,7 @@ def psi_density_roofline(hbm_gbs, src, reps=5):
             "algorithmic_bytes": algo, "avg_ms": avg_s * 1e3, "launches": cnt,
             "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs, burst)" if src == "measured" else src,
             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch "
-                              "(profiles/psi_density_h54.md)", "drain": drain}
+                              "(orbital-density summary under profiles/)", "drain": drain}
 
 
 def quadrature_roofline(hbm_gbs, src, reps=5):
@@ -224,7 +224,7 @@ def quadrature_roofline(hbm_gbs, src, reps=5):
             "algorithmic_bytes": algo, "avg_ms": avg_s * 1e3, "launches": cnt,
             "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs, burst)" if src == "measured" else src,
             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_tc_quad_tma, "
-                              "one launch (profiles/quadrature_h54.md)", "drain": 4,
+                              "one launch (quadrature summary under profiles/)", "drain": 4,
             "split_ms": st["split"][1] / max(st["split"][0], 1)}
 
 
