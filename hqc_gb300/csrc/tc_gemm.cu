@@ -1086,6 +1086,261 @@ __global__ void __launch_bounds__(kQtThreads, 1)
   }
 }
 
+// ---------------------------------------------------------------------------
+// Fused quadrature for a partial AO block of at most 16 AOs (n_ao % 128 in
+// [1, 16], e.g. 270 = 2 x 128 + 14): each full 128 x 128 tile CTA also
+// computes up to two N = 16 products with the 128-row blocks it already holds
+// -- (m, last) from its A block and, non-symmetric, the transposed (last, n)
+// from its B block -- loading only the 16-row narrow boxes for them.  TMEM
+// (512 columns): two slots of 128 + 16 + 16 accumulator columns, the main
+// tile's TwoSum sums S (128 columns) and the narrow products' sums and
+// carries (2 x 16 each); the carries C of the main tile live in the
+// registers of eight drain warps (two per TMEM lane group, 64 main columns
+// each).  The corner (last, last) runs in k_tc_quad_tma.
+// ---------------------------------------------------------------------------
+constexpr int kQfDrainWarps = 8;
+constexpr int kQfMmaWarp = kQfDrainWarps;
+constexpr int kQfTmaWarp = kQfMmaWarp + 1;
+constexpr int kQfThreads = (kQfTmaWarp + 1) * 32;
+constexpr uint32_t kQfSlot = kN + 32;           // main + two narrow accumulators
+constexpr uint32_t kQfColS = 2 * kQfSlot;       // main-tile sums S (128 columns)
+constexpr uint32_t kQfColXS = kQfColS + kN;     // narrow sums S (2 x 16)
+constexpr uint32_t kQfColXC = kQfColXS + 32;    // narrow carries C (2 x 16), ends at 512
+constexpr int kQfTmemCols = 512;
+constexpr size_t kQfStageBytes = 4 * kTile + 4 * 16 * 128;  // main pieces + two narrow boxes x 2 pieces
+constexpr size_t kQfSmem = kQtRing * kQfStageBytes + 1024;
+
+constexpr int kQfMaxFull = 7;  // full AO blocks handled by the fused form
+
+// Narrow products carried by the diagonal tile (m, m).
+struct QfTile {
+  int nx;              // 0..2
+  int xswap[2];        // 0: A block x narrow B box; 1: B block x narrow A box (transposed)
+  int xrow;            // first row of the narrow block
+  int xmt[2], xnt[2];  // destination tiles
+};
+
+struct QfArgs {
+  int tile_m[kQfMaxFull * kQfMaxFull], tile_n[kQfMaxFull * kQfMaxFull];  // the full tiles
+  int ntile;
+  QfTile diag[kQfMaxFull];
+  long long N;
+  int kchunk, drain, mtiles, ntiles;
+  double *partial;
+  int *err;
+};
+
+__global__ void __launch_bounds__(kQfThreads, 1)
+    k_tc_quad_fused(QfArgs a, const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtensorMap mAl,
+                    const __grid_constant__ CUtensorMap mBh, const __grid_constant__ CUtensorMap mBl,
+                    const __grid_constant__ CUtensorMap mAh16, const __grid_constant__ CUtensorMap mAl16,
+                    const __grid_constant__ CUtensorMap mBh16, const __grid_constant__ CUtensorMap mBl16) {
+  extern __shared__ __align__(1024) char smraw[];
+  char *sm = (char *)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
+  __shared__ QtPipe P;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int mt = a.tile_m[blockIdx.x], nt = a.tile_n[blockIdx.x];
+  const int nx = (mt == nt) ? a.diag[mt].nx : 0;
+  const QfTile X = a.diag[mt == nt ? mt : 0];
+  const int chunk = blockIdx.y;
+  const long long k0 = (long long)chunk * a.kchunk;
+  const long long k1 = min(k0 + (long long)a.kchunk, a.N);
+  const int nstages = (int)((k1 - k0 + kStageK - 1) / kStageK);
+  const int nsub = (nstages + a.drain - 1) / a.drain;
+  if (tid == 0) {
+    for (int b = 0; b < kQtRing; ++b) {
+      mbar_init(&P.full[b], 1);
+      mbar_init(&P.empty[b], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&P.acc_full[b], 1);
+      mbar_init(&P.acc_empty[b], kQfDrainWarps * 32);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == kQfMmaWarp) tmem_alloc(&P.tmem_base, kQfTmemCols);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+
+  bool ok = true;
+  if (warp == kQfTmaWarp) {
+    if (lane == 0) {
+      const uint32_t bytes = 4u * (uint32_t)kTile + (uint32_t)nx * 2u * 16u * 128u;
+      for (int st = 0; st < nstages; ++st) {
+        const int slot = st % kQtRing, use = st / kQtRing;
+        if (ok && use > 0 && !mbar_wait(&P.empty[slot], (unsigned)((use - 1) & 1), a.err, 41)) ok = false;
+        if (!ok) break;
+        const int x = (int)(k0 + (long long)st * kStageK);
+        const uint32_t base = smem_u32(sm + slot * kQfStageBytes);
+        mbar_expect_tx(&P.full[slot], bytes);
+        tma_load_2d(base, &mAh, x, mt * kM, &P.full[slot]);
+        tma_load_2d(base + (uint32_t)kTile, &mAl, x, mt * kM, &P.full[slot]);
+        tma_load_2d(base + 2u * (uint32_t)kTile, &mBh, x, nt * kN, &P.full[slot]);
+        tma_load_2d(base + 3u * (uint32_t)kTile, &mBl, x, nt * kN, &P.full[slot]);
+        for (int e = 0; e < nx; ++e) {
+          // narrow box: from the B arrays for an A-block product, from the A arrays for the transposed one
+          const uint32_t nb = base + 4u * (uint32_t)kTile + (uint32_t)e * 2u * 2048u;
+          if (!X.xswap[e]) {
+            tma_load_2d(nb, &mBh16, x, X.xrow, &P.full[slot]);
+            tma_load_2d(nb + 2048u, &mBl16, x, X.xrow, &P.full[slot]);
+          } else {
+            tma_load_2d(nb, &mAh16, x, X.xrow, &P.full[slot]);
+            tma_load_2d(nb + 2048u, &mAl16, x, X.xrow, &P.full[slot]);
+          }
+        }
+      }
+    }
+  } else if (warp == kQfMmaWarp) {
+    if (lane == 0) {
+      const uint32_t idesc = idesc_tf32(kM, kN), idesc16 = idesc_tf32(kM, 16);
+      int stage = 0;
+      for (int j = 0; j < nsub; ++j) {
+        const int ab = j & 1, ause = j >> 1;
+        if (ok && ause > 0 && !mbar_wait(&P.acc_empty[ab], (unsigned)((ause - 1) & 1), a.err, 44)) ok = false;
+        tc_fence_after();
+        const uint32_t tmem_d = P.tmem_base + (uint32_t)ab * kQfSlot;
+        const int s_end = min(nstages, (j + 1) * a.drain);
+        bool first = true;
+        for (; stage < s_end; ++stage) {
+          const int slot = stage % kQtRing, use = stage / kQtRing;
+          if (ok && !mbar_wait(&P.full[slot], (unsigned)(use & 1), a.err, 42)) ok = false;
+          tc_fence_after();
+          if (ok) {
+            const uint32_t base = smem_u32(sm + slot * kQfStageBytes);
+            const uint32_t Ah = base, Al = base + (uint32_t)kTile, Bh = base + 2u * (uint32_t)kTile,
+                           Bl = base + 3u * (uint32_t)kTile;
+#pragma unroll
+            for (int ks = 0; ks < kStageK / 8; ++ks) {
+              const uint32_t off = ks * 32;
+              const int acc = (first && ks == 0) ? 0 : 1;
+              mma_tf32(tmem_d, sdesc(Al + off), sdesc(Bh + off), idesc, acc);
+              mma_tf32(tmem_d, sdesc(Ah + off), sdesc(Bl + off), idesc, 1);
+              mma_tf32(tmem_d, sdesc(Ah + off), sdesc(Bh + off), idesc, 1);
+              for (int e = 0; e < nx; ++e) {
+                const uint32_t Nh = base + 4u * (uint32_t)kTile + (uint32_t)e * 4096u, Nl = Nh + 2048u;
+                // the 128-row side: A block, or the B block for the transposed product
+                const uint32_t Wh = X.xswap[e] ? Bh : Ah, Wl = X.xswap[e] ? Bl : Al;
+                const uint32_t dx = tmem_d + (uint32_t)kN + (uint32_t)e * 16u;
+                mma_tf32(dx, sdesc(Wl + off), sdesc(Nh + off), idesc16, acc);
+                mma_tf32(dx, sdesc(Wh + off), sdesc(Nl + off), idesc16, 1);
+                mma_tf32(dx, sdesc(Wh + off), sdesc(Nh + off), idesc16, 1);
+              }
+            }
+          }
+          first = false;
+          mma_commit(&P.empty[slot]);
+        }
+        mma_commit(&P.acc_full[ab]);
+      }
+    }
+  } else {
+    // drains: warp w owns TMEM lanes 32 (w % 4) .. and main columns 64 (w / 4) .. + 63;
+    // the warps of half h also own narrow product h (16 columns)
+    const int h = warp >> 2;
+    const uint32_t lane_off = (uint32_t)((warp & 3) * 32) << 16;
+    const int c0 = h * 64;
+    const bool has_x = h < nx;
+    float cm[64];
+#pragma unroll
+    for (int i = 0; i < 64; ++i) cm[i] = 0.f;
+    for (int j = 0; j < nsub; ++j) {
+      const int b = j & 1, use = j >> 1;
+      const bool got = ok && mbar_wait(&P.acc_full[b], (unsigned)(use & 1), a.err, 43);
+      if (!got) ok = false;
+      tc_fence_after();
+      if (got) {
+        const uint32_t slot = P.tmem_base + lane_off + (uint32_t)b * kQfSlot;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          uint32_t va[16], sa[16];
+          tmem_ld16_nowait(slot + c0 + q * 16, va);
+          if (j > 0) tmem_ld16_nowait(P.tmem_base + lane_off + kQfColS + c0 + q * 16, sa);
+          tmem_wait_ld();
+          float sv[16];
+#pragma unroll
+          for (int i = 0; i < 16; ++i) {
+            const float v = __uint_as_float(va[i]);
+            if (j == 0) {
+              sv[i] = v;
+            } else {
+              sv[i] = __uint_as_float(sa[i]);
+              two_sum_add(sv[i], cm[q * 16 + i], v);
+            }
+          }
+          tmem_st16(P.tmem_base + lane_off + kQfColS + c0 + q * 16, sv);
+        }
+        if (has_x) {
+          const uint32_t xsa = P.tmem_base + lane_off + kQfColXS + (uint32_t)h * 16u,
+                         xca = P.tmem_base + lane_off + kQfColXC + (uint32_t)h * 16u;
+          uint32_t va[16], sa[16], ca[16];
+          tmem_ld16_nowait(slot + kN + (uint32_t)h * 16u, va);
+          if (j > 0) {
+            tmem_ld16_nowait(xsa, sa);
+            tmem_ld16_nowait(xca, ca);
+          }
+          tmem_wait_ld();
+          float sv[16], cv[16];
+#pragma unroll
+          for (int i = 0; i < 16; ++i) {
+            const float v = __uint_as_float(va[i]);
+            if (j == 0) {
+              sv[i] = v;
+              cv[i] = 0.f;
+            } else {
+              sv[i] = __uint_as_float(sa[i]);
+              cv[i] = __uint_as_float(ca[i]);
+              two_sum_add(sv[i], cv[i], v);
+            }
+          }
+          tmem_st16(xsa, sv);
+          tmem_st16(xca, cv);
+        }
+        tmem_wait_st();
+      }
+      tc_fence_before();
+      mbar_arrive(&P.acc_empty[b]);
+    }
+    const int row = (warp & 3) * 32 + lane;
+    const long long tsz = (long long)kM * kN;
+    double *tile = a.partial + (((long long)chunk * a.mtiles + mt) * a.ntiles + nt) * tsz;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      uint32_t sr[16];
+      tmem_ld16_nowait(P.tmem_base + lane_off + kQfColS + c0 + q * 16, sr);
+      tmem_wait_ld();
+      if (ok)
+#pragma unroll
+        for (int i = 0; i < 16; ++i)
+          tile[(long long)row * kN + c0 + q * 16 + i] = (double)__uint_as_float(sr[i]) + (double)cm[q * 16 + i];
+    }
+    if (has_x) {
+      uint32_t sr[16], cr[16];
+      tmem_ld16_nowait(P.tmem_base + lane_off + kQfColXS + (uint32_t)h * 16u, sr);
+      tmem_ld16_nowait(P.tmem_base + lane_off + kQfColXC + (uint32_t)h * 16u, cr);
+      tmem_wait_ld();
+      if (ok) {
+        double *xt = a.partial + (((long long)chunk * a.mtiles + X.xmt[h]) * a.ntiles + X.xnt[h]) * tsz;
+        if (!X.xswap[h]) {
+#pragma unroll
+          for (int i = 0; i < 16; ++i)
+            xt[(long long)row * kN + i] = (double)__uint_as_float(sr[i]) + (double)__uint_as_float(cr[i]);
+        } else {
+#pragma unroll
+          for (int i = 0; i < 16; ++i)
+            xt[(long long)i * kN + row] = (double)__uint_as_float(sr[i]) + (double)__uint_as_float(cr[i]);
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == kQfMmaWarp) {
+    tc_fence_after();
+    tmem_dealloc(P.tmem_base, kQfTmemCols);
+  }
+}
+
 // hi/lo TF32 pieces of Z = a w phi + b u . grad phi (u, dphi optional; w
 // optional, = 1): inputs with row stride ldi, outputs [nao][ldo] with zeros
 // in [N, ldo).  Grid (column blocks of 1024, rows); 4 columns per thread
@@ -1275,6 +1530,78 @@ void launch_tc_quad_split(const float *Ahl, const float *Bhl, int nao, long long
   const int last = nao - tc::kM * (nblk - 1);
   const bool narrow = last < tc::kM;
   const int nb_last = ceil_div(last, 16) * 16;
+  const long long rows = nao;
+  const float *Ah = Ahl, *Al = Ahl + (size_t)nao * ld, *Bh = Bhl, *Bl = Bhl + (size_t)nao * ld;
+  CUtensorMap mAh = tc::tensor_map_2d_ext(Ah, ld, N, rows, tc::kM);
+  CUtensorMap mAl = tc::tensor_map_2d_ext(Al, ld, N, rows, tc::kM);
+  CUtensorMap mBh = tc::tensor_map_2d_ext(Bh, ld, N, rows, tc::kN);
+  CUtensorMap mBl = tc::tensor_map_2d_ext(Bl, ld, N, rows, tc::kN);
+  CUtensorMap mAh16 = tc::tensor_map_2d_ext(Ah, ld, N, rows, 16);
+  CUtensorMap mAl16 = tc::tensor_map_2d_ext(Al, ld, N, rows, 16);
+  CUtensorMap mBh16 = tc::tensor_map_2d_ext(Bh, ld, N, rows, 16);
+  CUtensorMap mBl16 = tc::tensor_map_2d_ext(Bl, ld, N, rows, 16);
+  const int chunks = ceil_div(N, tc_quad_chunk());
+  const int nfull = nblk - 1;
+  if (narrow && last <= 16 && nfull >= 1 && nfull <= tc::kQfMaxFull) {
+    // full tiles, the narrow products carried by the diagonal ones; the corner alone
+    static bool fattr = false;
+    if (!fattr) {
+      HQ_CUDA(cudaFuncSetAttribute(tc::k_tc_quad_fused, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)tc::kQfSmem));
+      fattr = true;
+    }
+    tc::QfArgs f;
+    f.ntile = 0;
+    for (int mt = 0; mt < nfull; ++mt)
+      for (int nt = 0; nt < nfull; ++nt) {
+        if (sym && nt < mt) continue;
+        f.tile_m[f.ntile] = mt;
+        f.tile_n[f.ntile] = nt;
+        ++f.ntile;
+      }
+    for (int m = 0; m < nfull; ++m) {
+      tc::QfTile &d = f.diag[m];
+      d.xrow = nfull * tc::kM;
+      d.nx = 0;
+      d.xswap[d.nx] = 0;  // (m, last) from the A block
+      d.xmt[d.nx] = m;
+      d.xnt[d.nx] = nfull;
+      ++d.nx;
+      if (!sym) {  // (last, m) from the B block, transposed
+        d.xswap[d.nx] = 1;
+        d.xmt[d.nx] = nfull;
+        d.xnt[d.nx] = m;
+        ++d.nx;
+      }
+    }
+    f.N = N;
+    f.kchunk = tc_quad_chunk();
+    f.drain = drain;
+    f.mtiles = nblk;
+    f.ntiles = nblk;
+    f.partial = partial;
+    f.err = err;
+    tc::k_tc_quad_fused<<<dim3(f.ntile, chunks), tc::kQfThreads, tc::kQfSmem, st>>>(
+        f, mAh, mAl, mBh, mBl, mAh16, mAl16, mBh16, mBl16);
+    HQ_LAUNCH_CHECK();
+    tc::QtArgs c;
+    c.ntile = 1;
+    c.tiles[0] = tc::QtTile{nfull * tc::kM, nfull * tc::kN, nb_last, 0, nfull, nfull};
+    c.N = N;
+    c.kchunk = tc_quad_chunk();
+    c.drain = drain;
+    c.mtiles = nblk;
+    c.ntiles = nblk;
+    c.partial = partial;
+    c.err = err;
+    tc::k_tc_quad_tma<<<dim3(1, chunks), tc::kQtThreads, tc::kQtSmem, st>>>(c, mAh, mAl, mBh, mBl, mAh16,
+                                                                            mAl16, mBh16, mBl16);
+    HQ_LAUNCH_CHECK();
+    tc::k_tc_quad_reduce<<<ceil_div((long long)nao * nao, 256), 256, 0, st>>>(
+        partial, chunks, nblk, nblk, nao, sym ? 1 : 0, add_transpose ? 1 : 0, scale, M);
+    HQ_LAUNCH_CHECK();
+    return;
+  }
   tc::QtArgs a;
   a.ntile = 0;
   for (int mt = 0; mt < nblk; ++mt)
@@ -1305,17 +1632,6 @@ void launch_tc_quad_split(const float *Ahl, const float *Bhl, int nao, long long
   a.ntiles = nblk;
   a.partial = partial;
   a.err = err;
-  const long long rows = nao;
-  const float *Ah = Ahl, *Al = Ahl + (size_t)nao * ld, *Bh = Bhl, *Bl = Bhl + (size_t)nao * ld;
-  CUtensorMap mAh = tc::tensor_map_2d_ext(Ah, ld, N, rows, tc::kM);
-  CUtensorMap mAl = tc::tensor_map_2d_ext(Al, ld, N, rows, tc::kM);
-  CUtensorMap mBh = tc::tensor_map_2d_ext(Bh, ld, N, rows, tc::kN);
-  CUtensorMap mBl = tc::tensor_map_2d_ext(Bl, ld, N, rows, tc::kN);
-  CUtensorMap mAh16 = tc::tensor_map_2d_ext(Ah, ld, N, rows, 16);
-  CUtensorMap mAl16 = tc::tensor_map_2d_ext(Al, ld, N, rows, 16);
-  CUtensorMap mBh16 = tc::tensor_map_2d_ext(Bh, ld, N, rows, 16);
-  CUtensorMap mBl16 = tc::tensor_map_2d_ext(Bl, ld, N, rows, 16);
-  const int chunks = ceil_div(N, a.kchunk);
   dim3 grid(a.ntile, chunks);
   tc::k_tc_quad_tma<<<grid, tc::kQtThreads, tc::kQtSmem, st>>>(a, mAh, mAl, mBh, mBl, mAh16, mAl16, mBh16,
                                                                 mBl16);

@@ -42,7 +42,8 @@ def test_tc_density_matches_fp64(nao, N):
     assert bool((rho == rho2).all()), "repeated call differs"
 
 
-@pytest.mark.parametrize("nao,N", [(1, 1000), (20, 29791), (80, 29791), (130, 4097), (270, 531441)])
+@pytest.mark.parametrize("nao,N", [(1, 1000), (20, 29791), (80, 29791), (130, 4097), (150, 4097),
+                                   (256, 4097), (270, 531441)])
 def test_tc_quadrature_matches_fp64(nao, N):
     import torch
     from hqc_gb300._lib import tc_quadrature
@@ -129,7 +130,8 @@ def test_eigh_mixed_clustered_spectrum(n):
     np.testing.assert_allclose(M @ V, V * w, atol=1e-11 * 3)
 
 
-@pytest.mark.parametrize("nao,N", [(20, 4000), (150, 9000), (270, 20000)])
+@pytest.mark.parametrize("nao,N", [(20, 4000), (129, 5000), (140, 7000), (150, 9000), (256, 6000),
+                                   (270, 20000)])
 def test_tc_quadrature_gga_matches_fp64(nao, N):
     """The PBE-form Fock quadrature (pre-split operands, non-symmetric tile
     set with the partial AO block as an N = 16 MMA, transposed on the A side)
