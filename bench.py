@@ -136,9 +136,10 @@ def peaks():
     return 6800.0, 1900.0, "fallback"
 
 
-# DRAM bytes (read + write) of one k_tc_quad_tma launch at the H54 PBE shapes,
-# from one ncu capture (its summary is kept under profiles/)
-QUAD_TRAFFIC = 2771808512 + 149348608
+# DRAM bytes (read + write) of one PBE quadrature at the H54 shapes -- the
+# fused kernel, the corner tile and the FP64 reduce, the launches the timing
+# covers -- from one ncu capture (its summary is kept under profiles/)
+QUAD_TRAFFIC = (3655161344 + 160482560) + (119371776 + 419072) + (302131200 + 538880)
 
 CONFIG = {"workload": "H54 bcc rs=1.31 gth-dzvp PBE 81^3 Gamma, SCF tol 1e-7 Ry + forces",
           "n_atoms": 54, "n_ao": 270, "grid": 531441}
@@ -185,12 +186,13 @@ def psi_density_roofline(hbm_gbs, src, reps=5):
 
 
 def quadrature_roofline(hbm_gbs, src, reps=5):
-    """The Fock quadrature kernel (k_tc_quad_tma: TMA loads of pre-split TF32
-    operands, tcgen05 3xTF32; the dominant multi-SM kernel of the SCF) timed
-    alone with CUDA events at the H54 PBE shapes, its non-symmetric tile set:
-    algorithmic bytes = the four TF32 pieces (Z hi/lo, phi hi/lo) read once,
-    4 x n_ao x N x 4 B, plus M (n_ao^2 x 8 B).  The split pass that forms the
-    pieces is timed separately (stage "split") and not counted here."""
+    """The Fock quadrature (k_tc_quad_fused + the corner tile's k_tc_quad_tma +
+    k_tc_quad_reduce: TMA loads of pre-split TF32 operands, tcgen05 3xTF32;
+    the dominant multi-SM kernel of the SCF) timed alone with CUDA events at
+    the H54 PBE shapes, its non-symmetric tile set: algorithmic bytes = the
+    four TF32 pieces (Z hi/lo, phi hi/lo) read once, 4 x n_ao x N x 4 B, plus
+    M (n_ao^2 x 8 B).  The split pass that forms the pieces is timed
+    separately (stage "split") and not counted here."""
     import torch
     from hqc_gb300 import _lib
     nao, N = 270, 531441
@@ -220,11 +222,11 @@ def quadrature_roofline(hbm_gbs, src, reps=5):
     torch.cuda.empty_cache()
     return {"bound": "hbm", "achieved": achieved, "peak": hbm_gbs, "unit": "GB/s",
             "frac": achieved / hbm_gbs, "traffic": QUAD_TRAFFIC,
-            "kernel": "k_tc_quad_tma + k_tc_quad_reduce (PBE Fock quadrature, H54 shapes)",
+            "kernel": "k_tc_quad_fused + k_tc_quad_tma (corner) + k_tc_quad_reduce (PBE Fock quadrature, H54 shapes)",
             "algorithmic_bytes": algo, "avg_ms": avg_s * 1e3, "launches": cnt,
             "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs, burst)" if src == "measured" else src,
-            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of k_tc_quad_tma, "
-                              "one launch (quadrature summary under profiles/)", "drain": 4,
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the three launches "
+                              "of one quadrature (quadrature summary under profiles/)", "drain": 4,
             "split_ms": st["split"][1] / max(st["split"][0], 1)}
 
 
