@@ -76,3 +76,43 @@ def test_xc_codes_and_reference_errors():
         xc_code("lda,pz81")
     with pytest.raises(ValueError):
         xc_code("b3lyp,x")
+
+
+def test_ewald_host_helpers_match_oracle():
+    """kpoints / Madelung (hqc/pbc/potential.py:6-33) of the package against
+    the oracle, 3D and 2D, and the simple-cubic Madelung known answer."""
+    from hqc_gb300.potential import kpoints, Madelung
+    from oracle.ewald import kpoints as kp_ref, madelung_dim
+    for dim, gmax in ((3, 15), (3, 4), (2, 10)):
+        G = kpoints(dim, gmax)
+        ref = kp_ref(dim, gmax)
+        assert G.shape == ref.shape
+        assert sorted(map(tuple, G)) == sorted(map(tuple, ref))
+        assert abs(Madelung(dim, 10.0, G) - madelung_dim(dim, 10.0, ref)) < 1e-13
+    assert abs(Madelung(3, 10.0, kpoints(3, 15)) - (-2.8372974794806)) < 1e-9
+
+
+def test_kpoint_factories_reject_unsupported_modes():
+    """make_solver(gamma=False) runs in FP64 without forces; the factories
+    refuse the other modes before any device work."""
+    from hqc_gb300 import make_solver, make_pes
+    with pytest.raises(NotImplementedError):
+        make_solver(4, 2.5, 1.5, "gth-szv", gamma=False, precision="mixed")
+    with pytest.raises(NotImplementedError):
+        make_solver(4, 2.5, 1.5, "gth-szv", gamma=False, forces=True)
+    with pytest.raises(NotImplementedError):
+        make_pes(4, 2.5, 1.5, "gth-szv", gamma=False, forces=True)
+
+
+def test_overlap_lattice_sphere_matches_reference_rule():
+    """The lattice sphere of make_overlap / the S, T sums: integer multiples
+    of L within rcut (hqc/pbc/overlap.py:126-138, solver.py:162-176)."""
+    from hqc_gb300.solver import lattice_sphere
+    L = 3.7
+    for rcut in (18.0, 24.0):
+        T = lattice_sphere(L, rcut)
+        tmax = rcut // L
+        n = np.arange(-tmax, tmax + 1)
+        ref = np.array(np.meshgrid(n, n, n)).reshape(3, -1).T * L
+        ref = ref[(ref ** 2).sum(1) <= rcut ** 2]
+        assert sorted(map(tuple, np.round(T / L).astype(int))) == sorted(map(tuple, np.round(ref / L).astype(int)))
