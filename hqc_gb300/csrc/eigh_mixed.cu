@@ -351,10 +351,17 @@ constexpr double kOaConverged = 1e-12;
 // order |E|^2 (quadratic convergence outside clusters, which are rotated
 // exactly): the solve ends after it without a confirming step.
 constexpr double kOaFinalUpdate = 1e-7;
+// Loose mode (eigenvectors that only feed the next SCF density, whose own
+// noise is ~1e-7): converged at off < 1e-9, or after an update below 1e-4
+// (error of order 1e-8).
+constexpr double kOaConvergedLoose = 1e-9;
+constexpr double kOaFinalUpdateLoose = 1e-4;
 static double oa_iteration(int n, const double *A, double *X, double *w, MixedEigWork &ws,
                            cudaStream_t st, int max_cluster = kMaxClusterFock,
-                           bool *final_update = nullptr) {
+                           bool *final_update = nullptr, bool loose = false) {
   if (final_update) *final_update = false;
+  const double conv = loose ? kOaConvergedLoose : kOaConverged;
+  const double fin_thr = loose ? kOaFinalUpdateLoose : kOaFinalUpdate;
   const long long nn = (long long)n * n;
   const int grid = (int)std::min<long long>(ceil_div(nn, kOaThreads), 148);
   double *red = ws.emax + 8;  // [0..4] grid reductions
@@ -370,7 +377,7 @@ static double oa_iteration(int n, const double *A, double *X, double *w, MixedEi
   const double off = std::sqrt(rs[1]) / std::max(std::sqrt(rs[0]), 1e-300);
   // converged: off-diagonal part and orthonormality residual ||I - X^T X||_F
   // both at rounding level (the update also re-normalises X)
-  if (off < kOaConverged && std::sqrt(rs[2]) < kOaConverged) {
+  if (off < conv && std::sqrt(rs[2]) < conv) {
     k_oa_lambda<<<ceil_div(n, 256), 256, 0, st>>>(n, ws.S, ws.G, w);
     HQ_LAUNCH_CHECK();
     if (std::getenv("HQCGB_TRACE")) fprintf(stderr, "  oa off=%.3e (converged, no update)\n", off);
@@ -391,7 +398,7 @@ static double oa_iteration(int n, const double *A, double *X, double *w, MixedEi
     double em[13];
     HQ_CUDA(cudaMemcpyAsync(em, ws.emax, 13 * sizeof(double), cudaMemcpyDeviceToHost, st));
     HQ_CUDA(cudaStreamSynchronize(st));
-    *final_update = em[8 + 4] < kOaFinalUpdate && em[2] == 0;
+    *final_update = em[8 + 4] < fin_thr && em[2] == 0;
   }
   if (std::getenv("HQCGB_TRACE")) {
     double em[13];
@@ -413,7 +420,7 @@ static double oa_iteration(int n, const double *A, double *X, double *w, MixedEi
 // Returns false when the refinement does not get there within 8 steps (the
 // caller then uses the FP64 solver).
 bool eigh_mixed(int n, const double *A, double *V, double *w, MixedEigWork &ws, cudaStream_t st,
-                bool wide) {
+                bool wide, bool loose) {
   HQ_STAGE(ST_JACOBI, st);
   long long nn = (long long)n * n;
   k_f64_to_f32<<<ceil_div(nn, 256), 256, 0, st>>>(nn, A, ws.A32);
@@ -449,8 +456,8 @@ bool eigh_mixed(int n, const double *A, double *V, double *w, MixedEigWork &ws, 
   HQ_LAUNCH_CHECK();
   for (int it = 0; it < 8; ++it) {
     bool fin = false;
-    double off = oa_iteration(n, A, V, w, ws, st, wide ? kMaxCluster : kMaxClusterFock, &fin);
-    if (off < kOaConverged || fin) {
+    double off = oa_iteration(n, A, V, w, ws, st, wide ? kMaxCluster : kMaxClusterFock, &fin, loose);
+    if (off < (loose ? kOaConvergedLoose : kOaConverged) || fin) {
       sort_eigpairs(n, w, V, ws, st);
       return true;
     }
@@ -464,15 +471,15 @@ bool eigh_mixed(int n, const double *A, double *V, double *w, MixedEigWork &ws, 
 // too far (relative off-diagonal norm above 2e-3) or the iteration stalls; the
 // caller then runs the full solve.
 bool eigh_mixed_warm(int n, const double *A, const double *X0, double *V, double *w,
-                     MixedEigWork &ws, cudaStream_t st) {
+                     MixedEigWork &ws, cudaStream_t st, bool loose) {
   HQ_STAGE(ST_JACOBI, st);
   HQ_CUDA(cudaMemcpyAsync(V, X0, sizeof(double) * n * n, cudaMemcpyDeviceToDevice, st));
   double prev = 1e300;
   for (int it = 0; it < 8; ++it) {
     bool fin = false;
-    double off = oa_iteration(n, A, V, w, ws, st, kMaxClusterFock, &fin);
+    double off = oa_iteration(n, A, V, w, ws, st, kMaxClusterFock, &fin, loose);
     if (!(off < 2e-3)) return false;
-    if (off < kOaConverged || fin) {
+    if (off < (loose ? kOaConvergedLoose : kOaConverged) || fin) {
       sort_eigpairs(n, w, V, ws, st);
       return true;
     }

@@ -117,9 +117,9 @@ struct MixedEigWork {
   int *status, *iwork;                    // iwork: 5 n + 1
 };
 bool eigh_mixed_warm(int n, const double *A, const double *X0, double *V, double *w,
-                     MixedEigWork &ws, cudaStream_t st);
+                     MixedEigWork &ws, cudaStream_t st, bool loose = false);
 bool eigh_mixed(int n, const double *A, double *V, double *w, MixedEigWork &ws, cudaStream_t st,
-                bool wide = false);
+                bool wide = false, bool loose = false);
 
 // fft (FP32 transforms)
 void launch_fft3d_f32(float2 *c, int ng, int batch, const double2 *tw, bool inverse,

@@ -375,12 +375,13 @@ static void sync_scalars(Ctx &c) {
 
 // Symmetric eigensolver: Householder + QL (eigh_fp64.cu); the Jacobi solver
 // is kept as the fallback when a QL sweep limit is hit.
-static void eigh(Ctx &c, const double *A, double *vecs, double *vals, bool wide = false) {
+static void eigh(Ctx &c, const double *A, double *vecs, double *vals, bool wide = false,
+                 bool loose = false) {
   hqcgb_plan *p = c.p;
   int n = p->nao;
   if (p->mixed) {
     // FP32 solve, then FP64 Ogita-Aishima refinement
-    if (eigh_mixed(n, A, vecs, vals, p->mew, c.st, wide)) {
+    if (eigh_mixed(n, A, vecs, vals, p->mew, c.st, wide, loose)) {
       HQ_CUDA(cudaMemsetAsync(p->jstat, 0, sizeof(int), c.st));
       return;
     }
@@ -397,7 +398,10 @@ static void eigh(Ctx &c, const double *A, double *vecs, double *vals, bool wide 
   }
 }
 
-// C, w from a Fock matrix: F' = v^T F v, eigh, C = v c'
+// C, w from a Fock matrix: F' = v^T F v, eigh, C = v c'.  In the mixed path
+// the solves inside the SCF loop stop at the loose refinement level (their
+// eigenvectors only build the next density); the returned orbitals are
+// refined to rounding level after the loop (refine_last).
 static void diagonalize(Ctx &c, const double *Fm) {
   hqcgb_plan *p = c.p;
   int n = p->nao;
@@ -409,13 +413,24 @@ static void diagonalize(Ctx &c, const double *Fm) {
   }
   // mixed: refine the previous iteration's eigenvectors when they are close
   bool done = p->mixed && p->have_prev && p->allow_warm &&
-              eigh_mixed_warm(n, p->Fp, p->c1_prev, p->c1, p->w, p->mew, c.st);
-  if (!done) eigh(c, p->Fp, p->c1, p->w);
+              eigh_mixed_warm(n, p->Fp, p->c1_prev, p->c1, p->w, p->mew, c.st, true);
+  if (!done) eigh(c, p->Fp, p->c1, p->w, false, p->mixed);
   if (p->mixed) {
     HQ_CUDA(cudaMemcpyAsync(p->c1_prev, p->c1, sizeof(double) * n * n, cudaMemcpyDeviceToDevice, c.st));
     p->have_prev = true;
   }
   if (trace_on() && p->mixed) fprintf(stderr, "eigh: %s\n", done ? "warm start" : "full solve");
+  gemm(false, false, n, n, n, 1.0, p->vorth, n, p->c1, n, nullptr, 0.0, p->C, n, c.st);
+}
+
+// Mixed path: the last solve of the loop (F' in Fp, its vectors in c1_prev)
+// refined to rounding level, then C = v c'.
+static void refine_last(Ctx &c) {
+  hqcgb_plan *p = c.p;
+  const int n = p->nao;
+  if (!eigh_mixed_warm(n, p->Fp, p->c1_prev, p->c1, p->w, p->mew, c.st, false))
+    eigh(c, p->Fp, p->c1, p->w);
+  HQ_CUDA(cudaMemcpyAsync(p->c1_prev, p->c1, sizeof(double) * n * n, cudaMemcpyDeviceToDevice, c.st));
   gemm(false, false, n, n, n, 1.0, p->vorth, n, p->c1, n, nullptr, 0.0, p->C, n, c.st);
 }
 
@@ -709,6 +724,7 @@ static int scf_one(hqcgb_plan *p, const double *xp_dev, const hqcgb_scf_out *out
     }
   }
   int converged = (loop != P.max_cycle) ? 1 : 0;
+  if (p->mixed) refine_last(c);
   // post-processing (solver.py:758-767 / 890-899); the mixed force path keeps
   // the orbitals on the grid from this last density pass
   density_matrix(c);
