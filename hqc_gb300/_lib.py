@@ -50,7 +50,7 @@ EXPORTS = ("hqcgb_plan_create", "hqcgb_plan_destroy", "hqcgb_scf", "hqcgb_scf_ba
            "hqcgb_ao_points", "hqcgb_slater", "hqcgb_kplan_create", "hqcgb_kplan_destroy",
            "hqcgb_scf_kpt", "hqcgb_scf_kpt_batch", "hqcgb_kplan_query", "hqcgb_eigh_herm",
            "hqcgb_ao_points_kpt", "hqcgb_slater_kpt", "hqcgb_overlap", "hqcgb_coulomb_energy",
-           "hqcgb_tc_quadrature_gga")
+           "hqcgb_tc_quadrature_gga", "hqcgb_diis_coefficients")
 N_STAGES = 15
 
 _lib = None
@@ -120,6 +120,7 @@ def load():
     lib.hqcgb_kplan_query.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p,
                                       ctypes.c_size_t, ctypes.c_void_p]
     lib.hqcgb_kplan_query.restype = ctypes.c_longlong
+    lib.hqcgb_diis_coefficients.argtypes = [ctypes.c_int, c_double_p, c_double_p]
     lib.hqcgb_eigh_herm.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                     ctypes.c_void_p, ctypes.c_void_p]
     lib.hqcgb_last_error.restype = ctypes.c_char_p

@@ -854,6 +854,22 @@ int hqcgb_scf_kpt_batch(hqcgb_kplan *plan, int n_cfg, const double *xp, const do
   }
 }
 
+int hqcgb_diis_coefficients(int space, const double *B, double *c) {
+  try {
+    HQ_REQUIRE(space >= 1 && space <= 32 && B && c, "bad argument");
+    std::vector<double2> Bh((size_t)space * space);
+    for (int k = 0; k < space * space; ++k) Bh[k] = make_double2(B[2 * k], B[2 * k + 1]);
+    std::vector<std::complex<double>> x = diis_coefficients(Bh, space);
+    for (int k = 0; k < space; ++k) {
+      c[2 * k] = x[k].real();
+      c[2 * k + 1] = x[k].imag();
+    }
+    return HQCGB_OK;
+  } catch (const Error &e) {
+    return kfail(e);
+  }
+}
+
 long long hqcgb_kplan_query(hqcgb_kplan *p, const char *name, void *dst, size_t bytes, void *stream) {
   try {
     HQ_REQUIRE(p && name, "null argument");

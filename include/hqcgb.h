@@ -280,6 +280,14 @@ int hqcgb_scf_kpt_batch(hqcgb_kplan *plan, int n_cfg, const double *xp, const do
 long long hqcgb_kplan_query(hqcgb_kplan *plan, const char *name, void *dst, size_t bytes,
                             void *stream);
 
+/* The k-point solver's DIIS coefficients (host computation, no device
+ * work): B [space][space] complex (interleaved, host) is the reference's
+ * unconjugated error matrix sum_mn e_i e_j (hqc/pbc/scf.py:177-188); solves
+ * [[B + eta I, -1], [-1, 0]] [c; lambda] = [0; -1] with
+ * eta = 1e-12 (tr B / space + 1) by LU with partial pivoting; c [space]
+ * complex (interleaved, host). */
+int hqcgb_diis_coefficients(int space, const double *B, double *c);
+
 /* Complex Hermitian FP64 eigensolver on `batch` row-major n x n matrices A
  * (complex, interleaved; device, not modified; both triangles are read, so A
  * must be Hermitian): ascending eigenvalues w [batch][n] and eigenvectors as

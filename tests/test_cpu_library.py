@@ -116,3 +116,31 @@ def test_overlap_lattice_sphere_matches_reference_rule():
         ref = np.array(np.meshgrid(n, n, n)).reshape(3, -1).T * L
         ref = ref[(ref ** 2).sum(1) <= rcut ** 2]
         assert sorted(map(tuple, np.round(T / L).astype(int))) == sorted(map(tuple, np.round(ref / L).astype(int)))
+
+
+def test_complex_diis_solve_matches_numpy():
+    """The k-point DIIS coefficients (host code of the library, no GPU): the
+    reference's unconjugated complex B (scf.py:177-188) with its eta
+    regularisation, against numpy.linalg.solve of the same bordered system;
+    the coefficients sum to 1."""
+    from hqc_gb300 import _lib
+    lib = _lib.load()
+    rng = np.random.default_rng(3)
+    for sp in (1, 3, 8):
+        e = rng.normal(size=(sp, 6, 6)) + 1j * rng.normal(size=(sp, 6, 6))
+        B = np.einsum("imn,jmn->ij", e, e)  # complex symmetric, no conjugation
+        eta = 1e-12 * (np.trace(B) / sp + 1.0)
+        h = np.zeros((sp + 1, sp + 1), complex)
+        h[:sp, :sp] = B + eta * np.eye(sp)
+        h[:sp, sp] = -1
+        h[sp, :sp] = -1
+        g = np.zeros(sp + 1, complex)
+        g[sp] = -1
+        ref = np.linalg.solve(h, g)[:sp]
+        Bi = np.ascontiguousarray(np.stack([B.real, B.imag], -1).reshape(-1))
+        out = np.zeros(2 * sp)
+        assert lib.hqcgb_diis_coefficients(sp, Bi.ctypes.data_as(_lib.c_double_p),
+                                           out.ctypes.data_as(_lib.c_double_p)) == 0
+        c = out[0::2] + 1j * out[1::2]
+        np.testing.assert_allclose(c, ref, rtol=1e-9, atol=1e-12)
+        assert abs(c.sum() - 1) < 1e-10
