@@ -50,7 +50,8 @@ EXPORTS = ("hqcgb_plan_create", "hqcgb_plan_destroy", "hqcgb_scf", "hqcgb_scf_ba
            "hqcgb_ao_points", "hqcgb_slater", "hqcgb_kplan_create", "hqcgb_kplan_destroy",
            "hqcgb_scf_kpt", "hqcgb_scf_kpt_batch", "hqcgb_kplan_query", "hqcgb_eigh_herm",
            "hqcgb_ao_points_kpt", "hqcgb_slater_kpt", "hqcgb_overlap", "hqcgb_coulomb_energy",
-           "hqcgb_tc_quadrature_gga", "hqcgb_diis_coefficients")
+           "hqcgb_tc_quadrature_gga", "hqcgb_diis_coefficients",
+           "hqcgb_tc_quad_tiles")
 N_STAGES = 15
 
 _lib = None
@@ -121,6 +122,7 @@ def load():
                                       ctypes.c_size_t, ctypes.c_void_p]
     lib.hqcgb_kplan_query.restype = ctypes.c_longlong
     lib.hqcgb_diis_coefficients.argtypes = [ctypes.c_int, c_double_p, c_double_p]
+    lib.hqcgb_tc_quad_tiles.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, c_int_p, c_int_p, c_int_p]
     lib.hqcgb_eigh_herm.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                     ctypes.c_void_p, ctypes.c_void_p]
     lib.hqcgb_last_error.restype = ctypes.c_char_p
@@ -250,6 +252,20 @@ def eigh_noalloc(A, w=None, V=None):
     check(lib.hqcgb_eigh_noalloc(n, ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(w.data_ptr()),
                                  ctypes.c_void_p(V.data_ptr()), st))
     return w, V
+
+
+def quad_tiles(nao, sym=True):
+    """Tile plan of the tensor-core quadrature (host only): an int array
+    (count, 7) of {kind, mt, nt, arow, brow, nb, swap} rows and the number of
+    kernel launches before the reduce."""
+    import numpy as np
+    lib = load()
+    count, launches = ctypes.c_int(0), ctypes.c_int(0)
+    check(lib.hqcgb_tc_quad_tiles(nao, int(sym), 0, None, ctypes.byref(count), ctypes.byref(launches)))
+    out = np.zeros((count.value, 7), dtype=np.int32)
+    check(lib.hqcgb_tc_quad_tiles(nao, int(sym), count.value, out.ctypes.data_as(c_int_p),
+                                  ctypes.byref(count), ctypes.byref(launches)))
+    return out, launches.value
 
 
 def tc_quadrature(phi32, w32, nsplit=2, drain=2):

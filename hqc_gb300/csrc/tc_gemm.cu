@@ -28,6 +28,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <vector>
 
 #include "common.cuh"
 #include "kernels.h"
@@ -905,8 +906,10 @@ struct QtTile {
   int mt, nt;      // destination tile of the partial sums
 };
 
+constexpr int kQtMaxTiles = 12;  // tiles per k_tc_quad_tma launch (kernel parameter space)
+
 struct QtArgs {
-  QtTile tiles[12];
+  QtTile tiles[kQtMaxTiles];
   int ntile;
   long long N;
   int kchunk, drain, mtiles, ntiles;
@@ -1510,48 +1513,39 @@ size_t tc_quad_partial_doubles(int nao, long long N) {
   return (size_t)chunks * mt * nt * tc::kM * tc::kN;
 }
 
-// M = scale * sum_g A_p(g) B_q(g) (+ its transpose when add_transpose) from the
-// pre-split pieces Ahl, Bhl [2][nao][ld] (hi rows, then lo rows); sym: M is
-// symmetric (only tiles nt >= mt are computed; the reduce mirrors them).
-void launch_tc_quad_split(const float *Ahl, const float *Bhl, int nao, long long N, long long ld,
-                          bool sym, bool add_transpose, double scale, double *partial, double *M,
-                          int *err, cudaStream_t st, int drain) {
-  HQ_STAGE(ST_QUAD, st);
-  HQ_REQUIRE(drain >= 1, "drain must be >= 1");
-  HQ_REQUIRE(ld % 32 == 0 && ld >= N, "pre-split operands need a row stride that is a multiple of 32");
-  HQ_REQUIRE(N <= (1LL << 31) - 64, "grid too large for 32-bit TMA coordinates");
-  static bool attr = false;
-  if (!attr) {
-    HQ_CUDA(cudaFuncSetAttribute(tc::k_tc_quad_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)tc::kQtSmem));
-    attr = true;
-  }
-  const int nblk = ceil_div(nao, tc::kM);
-  const int last = nao - tc::kM * (nblk - 1);
+// Tile plan of the quadrature for nao AOs in 128-row blocks: which CTA writes
+// which 128 x 128 destination tile (mt, nt) of the partial sums.
+//  * fused form (the last block has at most 16 rows and there are 1..7 full
+//    blocks): k_tc_quad_fused runs the full tiles, each diagonal CTA (m, m)
+//    also running the narrow products (m, last) and, unless symmetric,
+//    (last, m); one k_tc_quad_tma launch runs the (last, last) corner;
+//  * tile-list form otherwise: every tile of the upper triangle (sym) or of
+//    the whole square through k_tc_quad_tma, at most kQtMaxTiles per launch.
+// A tile whose A-side block is the narrow one is computed transposed
+// (swap = 1: A side from the B arrays), so the narrow block is always the
+// MMA's N side, rounded up to a multiple of 16 rows.
+struct QuadTilePlan {
+  int nblk = 0, nb_last = 0;
+  bool fused = false;
+  tc::QfArgs f{};                 // fused form: the full tiles and the diagonal extras
+  std::vector<tc::QtArgs> lists;  // k_tc_quad_tma launches, tile lists only
+};
+
+static QuadTilePlan plan_quad_tiles(int nao, bool sym) {
+  QuadTilePlan p;
+  p.nblk = ceil_div(nao, tc::kM);
+  const int last = nao - tc::kM * (p.nblk - 1);
   const bool narrow = last < tc::kM;
-  const int nb_last = ceil_div(last, 16) * 16;
-  const long long rows = nao;
-  const float *Ah = Ahl, *Al = Ahl + (size_t)nao * ld, *Bh = Bhl, *Bl = Bhl + (size_t)nao * ld;
-  CUtensorMap mAh = tc::tensor_map_2d_ext(Ah, ld, N, rows, tc::kM);
-  CUtensorMap mAl = tc::tensor_map_2d_ext(Al, ld, N, rows, tc::kM);
-  CUtensorMap mBh = tc::tensor_map_2d_ext(Bh, ld, N, rows, tc::kN);
-  CUtensorMap mBl = tc::tensor_map_2d_ext(Bl, ld, N, rows, tc::kN);
-  CUtensorMap mAh16 = tc::tensor_map_2d_ext(Ah, ld, N, rows, 16);
-  CUtensorMap mAl16 = tc::tensor_map_2d_ext(Al, ld, N, rows, 16);
-  CUtensorMap mBh16 = tc::tensor_map_2d_ext(Bh, ld, N, rows, 16);
-  CUtensorMap mBl16 = tc::tensor_map_2d_ext(Bl, ld, N, rows, 16);
-  const int chunks = ceil_div(N, tc_quad_chunk());
-  const int nfull = nblk - 1;
-  if (narrow && last <= 16 && nfull >= 1 && nfull <= tc::kQfMaxFull) {
-    // full tiles, the narrow products carried by the diagonal ones; the corner alone
-    static bool fattr = false;
-    if (!fattr) {
-      HQ_CUDA(cudaFuncSetAttribute(tc::k_tc_quad_fused, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)tc::kQfSmem));
-      fattr = true;
-    }
-    tc::QfArgs f;
-    f.ntile = 0;
+  p.nb_last = ceil_div(last, 16) * 16;
+  const int nfull = p.nblk - 1;
+  auto push = [&p](const tc::QtTile &t) {
+    if (p.lists.empty() || p.lists.back().ntile == tc::kQtMaxTiles) p.lists.push_back(tc::QtArgs{});
+    tc::QtArgs &a = p.lists.back();
+    a.tiles[a.ntile++] = t;
+  };
+  p.fused = narrow && last <= 16 && nfull >= 1 && nfull <= tc::kQfMaxFull;
+  if (p.fused) {
+    tc::QfArgs &f = p.f;
     for (int mt = 0; mt < nfull; ++mt)
       for (int nt = 0; nt < nfull; ++nt) {
         if (sym && nt < mt) continue;
@@ -1574,6 +1568,69 @@ void launch_tc_quad_split(const float *Ahl, const float *Bhl, int nao, long long
         ++d.nx;
       }
     }
+    push(tc::QtTile{nfull * tc::kM, nfull * tc::kN, p.nb_last, 0, nfull, nfull});
+    return p;
+  }
+  for (int mt = 0; mt < p.nblk; ++mt)
+    for (int nt = 0; nt < p.nblk; ++nt) {
+      if (sym && nt < mt) continue;
+      const bool nm = narrow && mt == p.nblk - 1, nn = narrow && nt == p.nblk - 1;
+      tc::QtTile t;
+      t.mt = mt;
+      t.nt = nt;
+      if (nm && !nn) {  // narrow A block: compute the transposed tile
+        t.arow = nt * tc::kM;
+        t.brow = mt * tc::kM;
+        t.nb = p.nb_last;
+        t.swap = 1;
+      } else {
+        t.arow = mt * tc::kM;
+        t.brow = nt * tc::kN;
+        t.nb = nn ? p.nb_last : tc::kN;
+        t.swap = 0;
+      }
+      push(t);
+    }
+  return p;
+}
+
+// M = scale * sum_g A_p(g) B_q(g) (+ its transpose when add_transpose) from the
+// pre-split pieces Ahl, Bhl [2][nao][ld] (hi rows, then lo rows); sym: M is
+// symmetric (only tiles nt >= mt are computed; the reduce mirrors them).
+void launch_tc_quad_split(const float *Ahl, const float *Bhl, int nao, long long N, long long ld,
+                          bool sym, bool add_transpose, double scale, double *partial, double *M,
+                          int *err, cudaStream_t st, int drain) {
+  HQ_STAGE(ST_QUAD, st);
+  HQ_REQUIRE(drain >= 1, "drain must be >= 1");
+  HQ_REQUIRE(ld % 32 == 0 && ld >= N, "pre-split operands need a row stride that is a multiple of 32");
+  HQ_REQUIRE(N <= (1LL << 31) - 64, "grid too large for 32-bit TMA coordinates");
+  static bool attr = false;
+  if (!attr) {
+    HQ_CUDA(cudaFuncSetAttribute(tc::k_tc_quad_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)tc::kQtSmem));
+    attr = true;
+  }
+  const QuadTilePlan plan = plan_quad_tiles(nao, sym);
+  const int nblk = plan.nblk;
+  const long long rows = nao;
+  const float *Ah = Ahl, *Al = Ahl + (size_t)nao * ld, *Bh = Bhl, *Bl = Bhl + (size_t)nao * ld;
+  CUtensorMap mAh = tc::tensor_map_2d_ext(Ah, ld, N, rows, tc::kM);
+  CUtensorMap mAl = tc::tensor_map_2d_ext(Al, ld, N, rows, tc::kM);
+  CUtensorMap mBh = tc::tensor_map_2d_ext(Bh, ld, N, rows, tc::kN);
+  CUtensorMap mBl = tc::tensor_map_2d_ext(Bl, ld, N, rows, tc::kN);
+  CUtensorMap mAh16 = tc::tensor_map_2d_ext(Ah, ld, N, rows, 16);
+  CUtensorMap mAl16 = tc::tensor_map_2d_ext(Al, ld, N, rows, 16);
+  CUtensorMap mBh16 = tc::tensor_map_2d_ext(Bh, ld, N, rows, 16);
+  CUtensorMap mBl16 = tc::tensor_map_2d_ext(Bl, ld, N, rows, 16);
+  const int chunks = ceil_div(N, tc_quad_chunk());
+  if (plan.fused) {
+    static bool fattr = false;
+    if (!fattr) {
+      HQ_CUDA(cudaFuncSetAttribute(tc::k_tc_quad_fused, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)tc::kQfSmem));
+      fattr = true;
+    }
+    tc::QfArgs f = plan.f;
     f.N = N;
     f.kchunk = tc_quad_chunk();
     f.drain = drain;
@@ -1584,58 +1641,19 @@ void launch_tc_quad_split(const float *Ahl, const float *Bhl, int nao, long long
     tc::k_tc_quad_fused<<<dim3(f.ntile, chunks), tc::kQfThreads, tc::kQfSmem, st>>>(
         f, mAh, mAl, mBh, mBl, mAh16, mAl16, mBh16, mBl16);
     HQ_LAUNCH_CHECK();
-    tc::QtArgs c;
-    c.ntile = 1;
-    c.tiles[0] = tc::QtTile{nfull * tc::kM, nfull * tc::kN, nb_last, 0, nfull, nfull};
-    c.N = N;
-    c.kchunk = tc_quad_chunk();
-    c.drain = drain;
-    c.mtiles = nblk;
-    c.ntiles = nblk;
-    c.partial = partial;
-    c.err = err;
-    tc::k_tc_quad_tma<<<dim3(1, chunks), tc::kQtThreads, tc::kQtSmem, st>>>(c, mAh, mAl, mBh, mBl, mAh16,
-                                                                            mAl16, mBh16, mBl16);
-    HQ_LAUNCH_CHECK();
-    tc::k_tc_quad_reduce<<<ceil_div((long long)nao * nao, 256), 256, 0, st>>>(
-        partial, chunks, nblk, nblk, nao, sym ? 1 : 0, add_transpose ? 1 : 0, scale, M);
-    HQ_LAUNCH_CHECK();
-    return;
   }
-  tc::QtArgs a;
-  a.ntile = 0;
-  for (int mt = 0; mt < nblk; ++mt)
-    for (int nt = 0; nt < nblk; ++nt) {
-      if (sym && nt < mt) continue;
-      const bool nm = narrow && mt == nblk - 1, nn = narrow && nt == nblk - 1;
-      tc::QtTile t;
-      t.mt = mt;
-      t.nt = nt;
-      if (nm && !nn) {  // narrow A block: compute the transposed tile
-        t.arow = nt * tc::kM;
-        t.brow = mt * tc::kM;
-        t.nb = nb_last;
-        t.swap = 1;
-      } else {
-        t.arow = mt * tc::kM;
-        t.brow = nt * tc::kN;
-        t.nb = nn ? nb_last : tc::kN;
-        t.swap = 0;
-      }
-      HQ_REQUIRE(a.ntile < 12, "too many AO blocks for the quadrature tile list");
-      a.tiles[a.ntile++] = t;
-    }
-  a.N = N;
-  a.kchunk = tc_quad_chunk();
-  a.drain = drain;
-  a.mtiles = nblk;
-  a.ntiles = nblk;
-  a.partial = partial;
-  a.err = err;
-  dim3 grid(a.ntile, chunks);
-  tc::k_tc_quad_tma<<<grid, tc::kQtThreads, tc::kQtSmem, st>>>(a, mAh, mAl, mBh, mBl, mAh16, mAl16, mBh16,
-                                                                mBl16);
-  HQ_LAUNCH_CHECK();
+  for (tc::QtArgs a : plan.lists) {
+    a.N = N;
+    a.kchunk = tc_quad_chunk();
+    a.drain = drain;
+    a.mtiles = nblk;
+    a.ntiles = nblk;
+    a.partial = partial;
+    a.err = err;
+    tc::k_tc_quad_tma<<<dim3(a.ntile, chunks), tc::kQtThreads, tc::kQtSmem, st>>>(a, mAh, mAl, mBh, mBl,
+                                                                                    mAh16, mAl16, mBh16, mBl16);
+    HQ_LAUNCH_CHECK();
+  }
   tc::k_tc_quad_reduce<<<ceil_div((long long)nao * nao, 256), 256, 0, st>>>(
       partial, chunks, nblk, nblk, nao, sym ? 1 : 0, add_transpose ? 1 : 0, scale, M);
   HQ_LAUNCH_CHECK();
@@ -1861,6 +1879,52 @@ extern "C" int hqcgb_tc_orbital_density(int nao, long long N, long long ld, cons
     HQ_CUDA(cudaFreeAsync(err, st));
     HQ_CUDA(cudaStreamSynchronize(st));
     if (h) throw Error{HQCGB_CUDA_ERROR, "tensor-core pipeline wait limit hit"};
+    return HQCGB_OK;
+  } catch (const Error &e) {
+    set_error(e.msg);
+    return e.status;
+  }
+}
+
+// C ABI (host only, no device work): the quadrature's tile plan for nao AOs
+// (sym: upper-triangle tiles only).  One row of 7 ints per computed product,
+// {kind, mt, nt, arow, brow, nb, swap}: kind 0 a full tile of the fused
+// kernel, 1 a narrow product carried by a fused diagonal CTA, 2 a tile of the
+// tile-list kernel; (mt, nt) the destination tile, arow / brow the first AO
+// row of the MMA's A / B side (swap = 1: A side from the B operand, stored
+// transposed), nb the MMA N.  count = rows (at most cap are written);
+// launches = quadrature kernel launches before the reduce.
+extern "C" int hqcgb_tc_quad_tiles(int nao, int sym, int cap, int *tiles, int *count, int *launches) {
+  using namespace hqcgb;
+  try {
+    HQ_REQUIRE(nao >= 1 && nao <= kMaxNao && cap >= 0 && (cap == 0 || tiles) && count && launches,
+               "bad argument");
+    const QuadTilePlan p = plan_quad_tiles(nao, sym != 0);
+    int k = 0;
+    auto row = [&](int kind, int mt, int nt, int arow, int brow, int nb, int swap) {
+      if (k < cap) {
+        int *r = tiles + 7 * (size_t)k;
+        r[0] = kind; r[1] = mt; r[2] = nt; r[3] = arow; r[4] = brow; r[5] = nb; r[6] = swap;
+      }
+      ++k;
+    };
+    if (p.fused) {
+      for (int t = 0; t < p.f.ntile; ++t)
+        row(0, p.f.tile_m[t], p.f.tile_n[t], p.f.tile_m[t] * tc::kM, p.f.tile_n[t] * tc::kN, tc::kN, 0);
+      for (int t = 0; t < p.f.ntile; ++t) {
+        if (p.f.tile_m[t] != p.f.tile_n[t]) continue;
+        const tc::QfTile &d = p.f.diag[p.f.tile_m[t]];
+        for (int x = 0; x < d.nx; ++x)
+          row(1, d.xmt[x], d.xnt[x], p.f.tile_m[t] * tc::kM, d.xrow, 16, d.xswap[x]);
+      }
+    }
+    for (const tc::QtArgs &a : p.lists)
+      for (int t = 0; t < a.ntile; ++t) {
+        const tc::QtTile &q = a.tiles[t];
+        row(2, q.mt, q.nt, q.arow, q.brow, q.nb, q.swap);
+      }
+    *count = k;
+    *launches = (p.fused ? 1 : 0) + (int)p.lists.size();
     return HQCGB_OK;
   } catch (const Error &e) {
     set_error(e.msg);

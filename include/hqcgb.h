@@ -226,6 +226,18 @@ int hqcgb_tc_quadrature_gga(int nao, long long N, long long ld, const float *phi
                             const float *dphi, const float *w, const float *u, float dV, int drain,
                             double *M, void *stream);
 
+/* Host only (no device work): the quadrature's tile plan for nao AOs in
+ * 128-row blocks (sym: upper-triangle destination tiles only).  tiles
+ * [cap][7] receives one row per product the kernels compute, {kind, mt, nt,
+ * arow, brow, nb, swap}: kind 0 a full tile of the fused kernel, 1 a narrow
+ * product carried by a fused diagonal CTA, 2 a tile of the tile-list kernel;
+ * (mt, nt) the destination tile, arow / brow the first AO rows of the MMA's
+ * A / B side (swap = 1: A side from the second operand, stored transposed),
+ * nb the MMA N.  count = number of rows (only the first cap are written),
+ * launches = quadrature kernel launches before the reduce.  Lets a caller
+ * check that every destination tile is written exactly once. */
+int hqcgb_tc_quad_tiles(int nao, int sym, int cap, int *tiles, int *count, int *launches);
+
 /* Orbital form of the density: rho(g) = sum_k occ_k |psi_k(g)|^2 with
  * psi_k = sum_p C[p][k] phi_p over the first nuse (<= 64) orbitals, and
  * with dphi (3 x [nao][ld]) also grad rho (3 x N) -- the density of

@@ -144,3 +144,39 @@ def test_complex_diis_solve_matches_numpy():
         c = out[0::2] + 1j * out[1::2]
         np.testing.assert_allclose(c, ref, rtol=1e-9, atol=1e-12)
         assert abs(c.sum() - 1) < 1e-10
+
+
+@pytest.mark.parametrize("nao", [1, 14, 16, 17, 20, 54, 127, 128, 129, 140, 144, 150, 256, 257, 270,
+                                 300, 384, 400, 512, 513, 600, 900, 912, 913, 1000, 1024])
+@pytest.mark.parametrize("sym", [True, False])
+def test_quadrature_tile_plan_covers_each_tile_once(nao, sym):
+    """The tensor-core quadrature's tile plan (host code of the library, no
+    GPU): every destination tile of M (the upper triangle when symmetric) is
+    written by exactly one product; each product's operand rows match its
+    tile (transposed products swap them); the MMA N covers the rows of the
+    B-side block in multiples of 16; the fused form is taken exactly when
+    the last block has at most 16 rows and there are 1..7 full blocks; the
+    tile-list kernel gets at most 12 tiles per launch."""
+    from hqc_gb300 import _lib
+    tiles, launches = _lib.quad_tiles(nao, sym)
+    nblk = -(-nao // 128)
+    last = nao - 128 * (nblk - 1)
+    cover = np.zeros((nblk, nblk), int)
+    for kind, mt, nt, arow, brow, nb, swap in tiles:
+        assert 0 <= mt < nblk and 0 <= nt < nblk
+        cover[mt, nt] += 1
+        a_blk, b_blk = (nt, mt) if swap else (mt, nt)
+        assert (arow, brow) == (128 * a_blk, 128 * b_blk)
+        b_rows = min(128, nao - brow)
+        assert nb % 16 == 0 and b_rows <= nb <= 128, (kind, mt, nt, nb)
+        if kind == 1:
+            assert nb == 16 and b_blk == nblk - 1
+    want = np.triu(np.ones((nblk, nblk), int)) if sym else np.ones((nblk, nblk), int)
+    np.testing.assert_array_equal(cover, want)
+    fused = last <= 16 and 1 <= nblk - 1 <= 7
+    assert (tiles[:, 0] != 2).any() == fused
+    n_list = int((tiles[:, 0] == 2).sum())
+    assert launches == int(fused) + -(-n_list // 12)
+    if fused:
+        assert n_list == 1  # the (last, last) corner alone
+

@@ -43,8 +43,11 @@ def test_tc_density_matches_fp64(nao, N):
 
 
 @pytest.mark.parametrize("nao,N", [(1, 1000), (20, 29791), (80, 29791), (130, 4097), (150, 4097),
-                                   (256, 4097), (270, 531441)])
+                                   (256, 4097), (270, 531441), (600, 3000), (900, 2500), (1000, 2500)])
 def test_tc_quadrature_matches_fp64(nao, N):
+    """LDA form (symmetric tile set).  600 and 1000 AOs need 15 and 36 tiles,
+    several tile-list launches; 900 AOs is the largest fused form (7 full
+    blocks and a 4-row block)."""
     import torch
     from hqc_gb300._lib import tc_quadrature
     phi, _, ld = _operands(nao, N, 100 + nao)
@@ -131,7 +134,7 @@ def test_eigh_mixed_clustered_spectrum(n):
 
 
 @pytest.mark.parametrize("nao,N", [(20, 4000), (129, 5000), (140, 7000), (150, 9000), (256, 6000),
-                                   (270, 20000)])
+                                   (270, 20000), (400, 3000), (600, 3000)])
 def test_tc_quadrature_gga_matches_fp64(nao, N):
     """The PBE-form Fock quadrature (pre-split operands, non-symmetric tile
     set with the partial AO block as an N = 16 MMA, transposed on the A side)
