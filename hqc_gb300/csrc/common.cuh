@@ -13,6 +13,10 @@ namespace hqcgb {
 
 void set_error(const std::string &msg);
 void count_launch(long long k = 1);
+// Raise the dynamic shared-memory limit of kernel `func` on the current
+// device to at least `bytes` (never lowers it); callable from concurrent
+// host threads.
+void ensure_dyn_smem(const void *func, size_t bytes);
 
 // Per-stage device timing (CUDA events on the launching stream), enabled by
 // hqcgb_profile(1).  Stage names are listed in plan.cu (kStageNames).

@@ -332,12 +332,7 @@ void eigh_f32(int n, float *A, float *V, float *w, float *scr, cudaStream_t st) 
   size_t sm2 = (size_t)4 * n * sizeof(float);
   size_t sm3 = (size_t)n * 33 * sizeof(float);
   HQ_REQUIRE(sm3 <= 200 * 1024, "matrix too large for the FP32 eigensolver");
-  static size_t attr3 = 0;
-  if (sm3 > 48 * 1024 && sm3 > attr3) {
-    HQ_CUDA(cudaFuncSetAttribute(k_backtransform_f32, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)sm3));
-    attr3 = sm3;
-  }
+  ensure_dyn_smem((const void *)k_backtransform_f32, sm3);
   const bool tr = std::getenv("HQCGB_TRACE") != nullptr;
   cudaEvent_t ev[4];
   if (tr)
@@ -345,12 +340,7 @@ void eigh_f32(int n, float *A, float *V, float *w, float *scr, cudaStream_t st) 
   if (tr) cudaEventRecord(ev[0], st);
   const size_t smt = ((size_t)n * (n + 1) / 2 + 5 * (size_t)n) * sizeof(float);
   if (smt <= 200 * 1024) {
-    static size_t attr1 = 0;
-    if (smt > attr1) {
-      HQ_CUDA(cudaFuncSetAttribute(k_tridiag_f32_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)smt));
-      attr1 = smt;
-    }
+    ensure_dyn_smem((const void *)k_tridiag_f32_smem, smt);
     k_tridiag_f32_smem<<<1, kTriThreads, smt, st>>>(n, A, dg, eg, taug, hv);
   } else {
     k_tridiag_f32<<<1, kTriThreads, sm1, st>>>(n, A, dg, eg, taug, hv);

@@ -103,12 +103,7 @@ void eigh_tql(int n, int batch, double *A, double *V, double *w, double *work, i
   HQ_STAGE(ST_JACOBI, st);
   size_t smem = (size_t)7 * n * sizeof(double);
   HQ_REQUIRE(smem <= 200 * 1024, "matrix too large for the eigensolver");
-  static size_t attr = 0;
-  if (smem > attr) {
-    HQ_CUDA(cudaFuncSetAttribute(k_eigh_tql<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem));
-    attr = smem;
-  }
+  ensure_dyn_smem((const void *)k_eigh_tql<double>, smem);
   k_eigh_tql<double><<<batch, kEigThreads, smem, st>>>(n, A, V, w, work, status);
   HQ_LAUNCH_CHECK();
 }
@@ -122,12 +117,7 @@ void eigh_tql_f32(int n, int batch, float *A, float *V, float *w, float *work, i
   HQ_STAGE(ST_JACOBI, st);
   size_t smem = (size_t)7 * n * sizeof(float);
   HQ_REQUIRE(smem <= 200 * 1024, "matrix too large for the eigensolver");
-  static size_t attr = 0;
-  if (smem > attr) {
-    HQ_CUDA(cudaFuncSetAttribute(k_eigh_tql<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem));
-    attr = smem;
-  }
+  ensure_dyn_smem((const void *)k_eigh_tql<float>, smem);
   k_eigh_tql<float><<<batch, kEigThreads, smem, st>>>(n, A, V, w, work, status);
   HQ_LAUNCH_CHECK();
 }

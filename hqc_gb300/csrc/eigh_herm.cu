@@ -172,11 +172,7 @@ void eigh_herm(int n, int batch, double2 *A, double2 *V, double *w, double2 *wor
   HQ_STAGE(ST_JACOBI, st);
   const size_t smem = eigh_herm_smem(n);
   HQ_REQUIRE(smem <= 200 * 1024, "matrix too large for the Hermitian eigensolver");
-  static size_t attr = 0;
-  if (smem > attr) {
-    HQ_CUDA(cudaFuncSetAttribute(k_eigh_herm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = smem;
-  }
+  ensure_dyn_smem((const void *)k_eigh_herm, smem);
   k_eigh_herm<<<batch, kHermThreads, smem, st>>>(n, A, V, w, work, status);
   HQ_LAUNCH_CHECK();
 }

@@ -404,7 +404,7 @@ static double oa_iteration(int n, const double *A, double *X, double *w, MixedEi
     double em[13];
     HQ_CUDA(cudaMemcpyAsync(em, ws.emax, 13 * sizeof(double), cudaMemcpyDeviceToHost, st));
     HQ_CUDA(cudaStreamSynchronize(st));
-    static auto t_last = std::chrono::steady_clock::now();
+    static thread_local auto t_last = std::chrono::steady_clock::now();
     auto now = std::chrono::steady_clock::now();
     fprintf(stderr, "  oa off=%.3e max|E|=%.3e clusters=%g%s (%.3f ms since last)\n", em[1], em[8 + 4],
             em[3], em[2] != 0 ? " (cluster too large)" : "",

@@ -165,11 +165,7 @@ static void fft3d_impl(C *c, int ng, int batch, const double2 *tw, bool inverse,
   HQ_REQUIRE(ng <= kMaxGrid, "grid too large for the direct DFT passes");
   long long N = (long long)ng * ng * ng;
   size_t smem = ((size_t)ng * 32 + ng) * sizeof(C);
-  static size_t attr = 0;
-  if (smem > attr) {
-    HQ_CUDA(cudaFuncSetAttribute(k_dft_pass<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr = smem;
-  }
+  ensure_dyn_smem((const void *)k_dft_pass<C>, smem);
   int zb = (ng + 31) / 32;
   // largest factor n1 <= sqrt(ng) (1 for a prime size: the direct sum)
   int n1 = 1;

@@ -156,11 +156,7 @@ void launch_density(const double *phi, const double *dphi, const double *D, int 
   HQ_STAGE(ST_DENSITY, st);
   size_t smem = ((size_t)nao * 32 + 8 * 4 * 32) * sizeof(double);
   HQ_REQUIRE(smem <= 227 * 1024, "too many AOs for the FP64 density tile");
-  static size_t attr_set = 0;
-  if (smem > attr_set) {
-    HQ_CUDA(cudaFuncSetAttribute(k_density, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr_set = smem;
-  }
+  ensure_dyn_smem((const void *)k_density, smem);
   k_density<<<ceil_div(N, 32), 256, smem, st>>>(phi, dphi, D, nao, N, rho, grho, Xout);
   HQ_LAUNCH_CHECK();
 }

@@ -6,6 +6,7 @@
 // DIIS / fixed-point loops of hqc/pbc/scf.py.  The loop control runs on the
 // host; every array operation is a kernel on the caller's stream.
 #include <atomic>
+#include <map>
 #include <mutex>
 #include <thread>
 #include <cstring>
@@ -31,7 +32,23 @@ struct StageRec {
   int stage;
   cudaEvent_t a, b;
 };
-static bool g_profile = false;
+static std::atomic<bool> g_profile{false};
+// Dynamic shared-memory limits already raised, per (device, kernel).  Batch
+// workers launch from several host threads, so check-and-raise is one
+// critical section and a limit is never lowered under a concurrent launch.
+static std::mutex g_smem_mu;
+static std::map<std::pair<int, const void *>, size_t> g_smem_set;
+
+void ensure_dyn_smem(const void *func, size_t bytes) {
+  int dev = 0;
+  HQ_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_smem_mu);
+  size_t &cur = g_smem_set[{dev, func}];
+  if (bytes <= cur) return;
+  HQ_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  cur = bytes;
+}
+
 static std::mutex g_rec_mu;  // guards g_recs and g_event_pool (batch workers record too)
 static std::vector<StageRec> g_recs;
 static std::vector<cudaEvent_t> g_event_pool;
@@ -81,12 +98,11 @@ static constexpr int kThinOcc = 64;  // occupied-block GEMMs up to this many orb
 
 // HQCGB_TRACE=1 prints one line per SCF iteration (energy, error norm) to stderr.
 static bool trace_on() {
-  static int v = -1;
-  if (v < 0) {
+  static const bool v = [] {
     const char *e = std::getenv("HQCGB_TRACE");
-    v = (e && e[0] == '1') ? 1 : 0;
-  }
-  return v == 1;
+    return e && e[0] == '1';
+  }();
+  return v;
 }
 
 struct hqcgb_plan {

@@ -1424,14 +1424,13 @@ CUtensorMap tensor_map_2d(const float *base, long long ld, long long rows, int b
 // as tensor_map_2d with the valid row length `cols` <= ld: columns past it read as zero
 CUtensorMap tensor_map_2d_ext(const float *base, long long ld, long long cols, long long rows,
                               int box_rows) {
-  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
-  if (!encode) {
+  static const PFN_cuTensorMapEncodeTiled_v12000 encode = [] {  // thread-safe one-time lookup
     void *fn = nullptr;
     cudaDriverEntryPointQueryResult q;
     HQ_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
     HQ_REQUIRE(fn && q == cudaDriverEntryPointSuccess, "cuTensorMapEncodeTiled unavailable");
-    encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
-  }
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }();
   HQ_REQUIRE(((uintptr_t)base & 15) == 0, "TMA base must be 16-byte aligned");
   HQ_REQUIRE(ld % 32 == 0, "TMA row stride must be a multiple of 32 floats");
   CUtensorMap m;
@@ -1468,20 +1467,16 @@ void launch_tc_psi_density(const float *phiT, const float *dphiT, const float *Y
   HQ_REQUIRE(npsi >= 16 && npsi <= tc::kPsiMaxN && npsi % 16 == 0, "orbital count out of range");
   HQ_REQUIRE(tc::psi_ring(npsi, grho ? 4 : 1) > 0, "orbital count too large for the TMEM layout");
   HQ_REQUIRE(ldk % tc::kStageK == 0, "AO stride must be a multiple of 32");
-  static int nsm = 0;
-  if (!nsm) {
-    HQ_CUDA(cudaFuncSetAttribute(tc::k_tc_psi_density<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)tc::kPsiSmem));
-    HQ_CUDA(cudaFuncSetAttribute(tc::k_tc_psi_density<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)tc::kPsiSmem));
-    HQ_CUDA(cudaFuncSetAttribute(tc::k_tc_psi_density<48>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)tc::kPsiSmem));
-    HQ_CUDA(cudaFuncSetAttribute(tc::k_tc_psi_density<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)tc::kPsiSmem));
-    int dev = 0;
+  static const int nsm = [] {
+    int dev = 0, v = 0;
     HQ_CUDA(cudaGetDevice(&dev));
-    HQ_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  }
+    HQ_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
+    return v;
+  }();
+  ensure_dyn_smem((const void *)tc::k_tc_psi_density<16>, tc::kPsiSmem);
+  ensure_dyn_smem((const void *)tc::k_tc_psi_density<32>, tc::kPsiSmem);
+  ensure_dyn_smem((const void *)tc::k_tc_psi_density<48>, tc::kPsiSmem);
+  ensure_dyn_smem((const void *)tc::k_tc_psi_density<64>, tc::kPsiSmem);
   tc::PsiArgs a;
   a.phiT = phiT; a.dphiT = grho ? dphiT : nullptr; a.Yhl = Yhl; a.N = N; a.ldk = ldk;
   a.npsi = npsi; a.ncomp = grho ? 4 : 1; a.rho = rho; a.grho = grho; a.err = err;
@@ -1604,12 +1599,7 @@ void launch_tc_quad_split(const float *Ahl, const float *Bhl, int nao, long long
   HQ_REQUIRE(drain >= 1, "drain must be >= 1");
   HQ_REQUIRE(ld % 32 == 0 && ld >= N, "pre-split operands need a row stride that is a multiple of 32");
   HQ_REQUIRE(N <= (1LL << 31) - 64, "grid too large for 32-bit TMA coordinates");
-  static bool attr = false;
-  if (!attr) {
-    HQ_CUDA(cudaFuncSetAttribute(tc::k_tc_quad_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)tc::kQtSmem));
-    attr = true;
-  }
+  ensure_dyn_smem((const void *)tc::k_tc_quad_tma, tc::kQtSmem);
   const QuadTilePlan plan = plan_quad_tiles(nao, sym);
   const int nblk = plan.nblk;
   const long long rows = nao;
@@ -1624,12 +1614,7 @@ void launch_tc_quad_split(const float *Ahl, const float *Bhl, int nao, long long
   CUtensorMap mBl16 = tc::tensor_map_2d_ext(Bl, ld, N, rows, 16);
   const int chunks = ceil_div(N, tc_quad_chunk());
   if (plan.fused) {
-    static bool fattr = false;
-    if (!fattr) {
-      HQ_CUDA(cudaFuncSetAttribute(tc::k_tc_quad_fused, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)tc::kQfSmem));
-      fattr = true;
-    }
+    ensure_dyn_smem((const void *)tc::k_tc_quad_fused, tc::kQfSmem);
     tc::QfArgs f = plan.f;
     f.N = N;
     f.kchunk = tc_quad_chunk();
@@ -1712,12 +1697,7 @@ void launch_tc_density(const float *phi, const float *phiT, const float *dphi, c
   HQ_REQUIRE(ld % 4 == 0, "row stride must be a multiple of 4 floats");
   HQ_REQUIRE(nsplit == 2, "nsplit must be 2 (3xTF32)");
   HQ_REQUIRE(drain >= 1, "drain must be >= 1");
-  static bool attr = false;
-  if (!attr) {
-    HQ_CUDA(cudaFuncSetAttribute(tc::k_tc_density, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)tc::kDensSmem));
-    attr = true;
-  }
+  ensure_dyn_smem((const void *)tc::k_tc_density, tc::kDensSmem);
   int mt = ceil_div(nao, tc::kM);
   int ldk = tc_ldk(nao);
   tc::DensArgs a;
