@@ -13,6 +13,7 @@ from .potential import (potential_energy_pp, potential_energy_pp_and_grad,  # no
                         potential_energy, kpoints, Madelung)
 from .overlap import make_overlap  # noqa: F401
 from .slater import make_slater  # noqa: F401
+from .autograd import PesFunction, pes_energy  # noqa: F401
 from . import basis  # noqa: F401
 
 __version__ = "0.1.0"

@@ -1,8 +1,9 @@
 """``torch.autograd.Function`` over the engine's energy + adjoint-force ABI.
 
 ``PesFunction.apply(xp, pes)`` returns E + Vpp (Rydberg) for a pes made with
-``make_pes(..., forces=True)``; its backward multiplies the incoming gradient
-by dE/dxp from ``hqcgb_forces`` + the Ewald gradient, so
+``make_pes(..., forces=True)``: a scalar for xp (n, 3), a (B,) vector for a
+batch (B, n, 3).  Its backward multiplies the incoming gradient (per
+configuration) by dE/dxp from ``hqcgb_forces`` + the Ewald gradient, so
 ``torch.autograd.grad`` works through the SCF like ``jax.grad(make_pes(...))``
 does for the reference's differentiable parts.
 """
@@ -19,7 +20,7 @@ class PesFunction(torch.autograd.Function):
     @staticmethod
     def backward(ctx, gout):
         (g,) = ctx.saved_tensors
-        return gout * g, None
+        return gout[..., None, None] * g, None
 
 
 def pes_energy(xp, pes):

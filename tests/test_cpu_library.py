@@ -180,3 +180,32 @@ def test_quadrature_tile_plan_covers_each_tile_once(nao, sym):
     if fused:
         assert n_list == 1  # the (last, last) corner alone
 
+
+def test_autograd_wrapper_chains_engine_gradient():
+    """The torch.autograd.Function over value_and_grad (host logic only): a
+    stand-in pes with E = sum x^3 per configuration and its exact gradient;
+    torch.autograd must return dE/dxp times the incoming gradient, for one
+    configuration and for a batch."""
+    import torch
+    from hqc_gb300 import pes_energy
+
+    class FakePes:
+        calls = 0
+
+        def value_and_grad(self, xp):
+            FakePes.calls += 1
+            x = torch.as_tensor(xp, dtype=torch.float64)
+            return (x ** 3).sum(dim=(-2, -1)), 3 * x ** 2
+
+    pes = FakePes()
+    x1 = torch.randn(4, 3, dtype=torch.float64, requires_grad=True)
+    (g1,) = torch.autograd.grad(2.5 * pes_energy(x1, pes), x1)
+    torch.testing.assert_close(g1, 7.5 * x1.detach() ** 2)
+    xb = torch.randn(3, 4, 3, dtype=torch.float64, requires_grad=True)
+    w = torch.tensor([1.0, -2.0, 0.5], dtype=torch.float64)
+    E = pes_energy(xb, pes)
+    assert E.shape == (3,)
+    (gb,) = torch.autograd.grad((w * E).sum(), xb)
+    torch.testing.assert_close(gb, w[:, None, None] * 3 * xb.detach() ** 2)
+    assert FakePes.calls == 2  # one engine call per forward, none in backward
+
