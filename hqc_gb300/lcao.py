@@ -11,7 +11,7 @@ def make_lcao(n, L, rs, basis, rcut=24, tol=1e-7, max_cycle=100, grid_length=0.1
               diis_space=8, diis_start_cycle=1, diis_damp=0., use_jit=True, dft=False,
               xc='lda,vwn', smearing=False, smearing_method='fermi', smearing_sigma=0.,
               search_method='newton', search_cycle=100, search_tol=1e-7, gamma=True,
-              precision='fp64', forces=False, n_grid=None, exx_occ_threshold=0.0):
+              precision='fp64', forces=False, n_grid=None, exx_occ_threshold=0.0, concurrency=1):
     solver = make_solver(n, L, rs, basis, rcut=rcut, tol=tol, max_cycle=max_cycle,
                          grid_length=grid_length, diis=diis, diis_space=diis_space,
                          diis_start_cycle=diis_start_cycle, diis_damp=diis_damp, use_jit=use_jit,
@@ -19,7 +19,7 @@ def make_lcao(n, L, rs, basis, rcut=24, tol=1e-7, max_cycle=100, grid_length=0.1
                          smearing_sigma=smearing_sigma, search_method=search_method,
                          search_cycle=search_cycle, search_tol=search_tol, gamma=gamma,
                          precision=precision, forces=forces, n_grid=n_grid,
-                         exx_occ_threshold=exx_occ_threshold)
+                         exx_occ_threshold=exx_occ_threshold, concurrency=concurrency)
 
     if gamma:
         def lcao(xp):

@@ -8,6 +8,7 @@ under Fermi smearing the electronic part is the gradient of E - sigma*Se).
 ``gamma=False`` gives ``pes(xp, kpt)`` (pes_kpt / pes_dev_kpt,
 pes.py:88-137), without forces.
 """
+import numpy as np
 import torch
 
 from .solver import make_solver, RY
@@ -31,9 +32,12 @@ def make_pes(n, L, rs, basis, rcut=24, tol=1e-7, max_cycle=100, grid_length=0.12
                          precision=precision, forces=forces, n_grid=n_grid,
                          exx_occ_threshold=exx_occ_threshold, concurrency=concurrency)
 
+    def _arr(xp):
+        return xp if isinstance(xp, torch.Tensor) else np.asarray(xp, dtype=np.float64)
+
     def _vpp(xp):
         """Ewald energy and gradient of one configuration or a batch."""
-        if getattr(xp, "ndim", 2) == 3:
+        if xp.ndim == 3:
             pairs = [potential_energy_pp_and_grad(x, L, rs, kappa=kappa, Gmax=Gmax) for x in xp]
             return torch.stack([e for e, _ in pairs]), torch.stack([g for _, g in pairs])
         return potential_energy_pp_and_grad(xp, L, rs, kappa=kappa, Gmax=Gmax)
@@ -41,6 +45,7 @@ def make_pes(n, L, rs, basis, rcut=24, tol=1e-7, max_cycle=100, grid_length=0.12
     def pes(xp, *kpt):
         if gamma == bool(kpt):
             raise TypeError("pes(xp) at the Gamma point, pes(xp, kpt) with gamma=False")
+        xp = _arr(xp)
         _, _, _, E, Ki, Vep, Vee, Se, conv = solver(xp, *kpt)
         Vpp, _ = _vpp(xp)
         if mode == "dev":
@@ -49,7 +54,8 @@ def make_pes(n, L, rs, basis, rcut=24, tol=1e-7, max_cycle=100, grid_length=0.12
 
     def value_and_grad(xp):
         """(E + Vpp, d/dxp); a batch (B, n, 3) gives (B,) and (B, n, 3)."""
-        if getattr(xp, "ndim", 2) == 3:
+        xp = _arr(xp)
+        if xp.ndim == 3:
             out = solver.batch(xp, forces=True, full=False)
             Vpp, gpp = _vpp(xp)
             return out["energies"][:, 0] * RY + Vpp, out["grad"] * (RY * rs) + gpp

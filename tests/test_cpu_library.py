@@ -209,3 +209,52 @@ def test_autograd_wrapper_chains_engine_gradient():
     torch.testing.assert_close(gb, w[:, None, None] * 3 * xb.detach() ** 2)
     assert FakePes.calls == 2  # one engine call per forward, none in backward
 
+
+
+def test_pes_host_logic_with_stand_in_engine(monkeypatch):
+    """make_pes's host logic (pes.py:78-137 of the reference) over stand-ins
+    for the engine calls: E + Vpp in 'default' mode, the 7-tuple in 'dev'
+    mode, batches and nested-list inputs, the Gamma / k-point call forms and
+    the reference's mode error."""
+    import torch
+    from hqc_gb300 import pes as pes_mod
+
+    def fake_make_solver(n, L, rs, basis, gamma=True, **kw):
+        def solver(xp, *kpt):
+            x = torch.as_tensor(xp, dtype=torch.float64)
+            E = x.sum(dim=(-2, -1)) + (float(kpt[0][0]) if kpt else 0.0)
+            one = torch.ones_like(E)
+            return None, None, None, E, 2 * one, 3 * one, 4 * one, 5 * one, one > 0
+
+        def batch(xp, forces=False, full=True):
+            x = torch.as_tensor(xp, dtype=torch.float64)
+            return {"energies": torch.stack([x.sum(dim=(-2, -1)) / 2.0] * 5, -1), "grad": x / 2.0}
+
+        solver.batch = batch
+        solver.grad = lambda: None
+        return solver
+
+    def fake_vpp(xp, L, rs, kappa=10, Gmax=15):
+        x = torch.as_tensor(xp, dtype=torch.float64)
+        return 100.0 * x.shape[0] * torch.ones((), dtype=torch.float64), torch.full_like(x, 7.0)
+
+    monkeypatch.setattr(pes_mod, "make_solver", fake_make_solver)
+    monkeypatch.setattr(pes_mod, "potential_energy_pp_and_grad", fake_vpp)
+    with pytest.raises(ValueError, match="Invalid mode"):
+        pes_mod.make_pes(2, 2.0, 1.3, "gth-szv", mode="bad")
+    xp = [[0.1, 0.2, 0.3], [0.4, 0.5, 0.6]]
+    pes = pes_mod.make_pes(2, 2.0, 1.3, "gth-szv")
+    assert abs(float(pes(xp)) - (2.1 + 200.0)) < 1e-12
+    xb = [xp, [[1.0, 0.0, 0.0], [0.0, 0.0, 0.0]]]
+    np.testing.assert_allclose(pes(xb).numpy(), [202.1, 201.0])
+    with pytest.raises(TypeError):
+        pes(xp, np.zeros(3))
+    dev = pes_mod.make_pes(2, 2.0, 1.3, "gth-szv", mode="dev")(xp)
+    assert len(dev) == 7 and abs(float(dev[4]) - 200.0) < 1e-12 and float(dev[1]) == 2.0
+    E, g = pes.value_and_grad(xb)  # batch: engine energies in Ha -> Ry, gradients per rs unit
+    np.testing.assert_allclose(E.numpy(), [2.1 + 200.0, 1.0 + 200.0])
+    np.testing.assert_allclose(g.numpy(), np.asarray(xb) / 2.0 * 2.0 * 1.3 + 7.0)
+    kp = pes_mod.make_pes(2, 2.0, 1.3, "gth-szv", gamma=False)
+    assert abs(float(kp(xp, np.array([0.5, 0.0, 0.0]))) - (2.6 + 200.0)) < 1e-12
+    with pytest.raises(TypeError):
+        kp(xp)
