@@ -61,6 +61,26 @@ struct Error {
 
 inline int ceil_div(long long a, long long b) { return (int)((a + b - 1) / b); }
 
+// Stream-ordered scratch memory, released (stream-ordered) when the scope
+// ends -- also when a call in between throws.
+class StreamBuf {
+ public:
+  StreamBuf(size_t bytes, cudaStream_t st) : st_(st) { HQ_CUDA(cudaMallocAsync(&p_, bytes, st_)); }
+  ~StreamBuf() {
+    if (p_) cudaFreeAsync(p_, st_);
+  }
+  StreamBuf(const StreamBuf &) = delete;
+  StreamBuf &operator=(const StreamBuf &) = delete;
+  template <typename T>
+  T *as(size_t byte_offset = 0) const {
+    return reinterpret_cast<T *>(static_cast<char *>(p_) + byte_offset);
+  }
+
+ private:
+  void *p_ = nullptr;
+  cudaStream_t st_;
+};
+
 constexpr int kMaxGrid = 255;        // points per axis handled by the direct DFT passes
 constexpr int kMaxNao = 1024;        // AOs per configuration
 

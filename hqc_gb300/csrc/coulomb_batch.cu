@@ -150,11 +150,10 @@ extern "C" int hqcgb_coulomb_energy(int B, int n, int dim, const double *x, doub
     if (B == 0) return HQCGB_OK;
     HQ_STAGE(ST_EWALD, st);
     const int nblk = nG > 0 ? ceil_div(nG, kCbThreads) : 0;
-    void *blk = nullptr;
     const size_t gbytes = ((size_t)nG * dim * sizeof(int) + 15) / 16 * 16;
-    HQ_CUDA(cudaMallocAsync(&blk, gbytes + (size_t)B * std::max(nblk, 1) * 3 * sizeof(double), st));
-    int *Gd = static_cast<int *>(blk);
-    double *part = reinterpret_cast<double *>(static_cast<char *>(blk) + gbytes);
+    StreamBuf blk(gbytes + (size_t)B * std::max(nblk, 1) * 3 * sizeof(double), st);
+    int *Gd = blk.as<int>();
+    double *part = blk.as<double>(gbytes);
     if (nG > 0) HQ_CUDA(cudaMemcpyAsync(Gd, G, (size_t)nG * dim * sizeof(int), cudaMemcpyHostToDevice, st));
     const size_t smem = (size_t)n * dim * sizeof(double);
     if (nblk > 0) {
@@ -164,7 +163,6 @@ extern "C" int hqcgb_coulomb_energy(int B, int n, int dim, const double *x, doub
     const double g0 = dim == 3 ? -M_PI / (kappa * kappa) : -2.0 * std::sqrt(M_PI) / kappa;
     k_coul_real_finish<<<B, kCbThreads, smem, st>>>(n, dim, x, L, rs, kappa, g0, part, nblk, out);
     HQ_LAUNCH_CHECK();
-    HQ_CUDA(cudaFreeAsync(blk, st));
     HQ_CUDA(cudaStreamSynchronize(st));
     return HQCGB_OK;
   } catch (const Error &e) {

@@ -188,18 +188,13 @@ extern "C" int hqcgb_eigh_herm(int n, int batch, const double *A, double *w, dou
   try {
     HQ_REQUIRE(A && w && V && n >= 1 && n <= kMaxNao && batch >= 1, "bad argument");
     const size_t nn = (size_t)n * n * batch;
-    double2 *work = nullptr, *Ac = nullptr;
-    int *stat = nullptr;
-    HQ_CUDA(cudaMallocAsync(&work, nn * sizeof(double2), st));
-    HQ_CUDA(cudaMallocAsync(&Ac, nn * sizeof(double2), st));
-    HQ_CUDA(cudaMallocAsync(&stat, batch * sizeof(int), st));
+    StreamBuf wbuf(nn * sizeof(double2), st), abuf(nn * sizeof(double2), st), sbuf(batch * sizeof(int), st);
+    double2 *work = wbuf.as<double2>(), *Ac = abuf.as<double2>();
+    int *stat = sbuf.as<int>();
     HQ_CUDA(cudaMemcpyAsync(Ac, A, nn * sizeof(double2), cudaMemcpyDeviceToDevice, st));
     eigh_herm(n, batch, Ac, reinterpret_cast<double2 *>(V), w, work, stat, st);
     std::vector<int> hs(batch);
     HQ_CUDA(cudaMemcpyAsync(hs.data(), stat, batch * sizeof(int), cudaMemcpyDeviceToHost, st));
-    HQ_CUDA(cudaFreeAsync(work, st));
-    HQ_CUDA(cudaFreeAsync(Ac, st));
-    HQ_CUDA(cudaFreeAsync(stat, st));
     HQ_CUDA(cudaStreamSynchronize(st));
     for (int b = 0; b < batch; ++b)
       if (hs[b] < 0) throw Error{HQCGB_EIG_FAIL, "Hermitian eigensolver did not converge"};

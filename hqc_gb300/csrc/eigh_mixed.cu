@@ -499,11 +499,10 @@ extern "C" int hqcgb_eigh_mixed(int n, const double *A, double *w, double *V, vo
     HQ_REQUIRE(A && w && V && n >= 1 && n <= kMaxNao, "bad argument");
     size_t nn = (size_t)n * n;
     MixedEigWork ws{};
-    void *blk = nullptr;
     size_t f32 = 3 * nn + 2 * (size_t)n + 64 + eigh_f32_scratch_floats(n), f64 = 6 * nn + 64,
            i32 = 5 * (size_t)n + 64;  // emax: 64
-    HQ_CUDA(cudaMallocAsync(&blk, f64 * sizeof(double) + f32 * sizeof(float) + i32 * sizeof(int), st));
-    double *d = reinterpret_cast<double *>(blk);
+    StreamBuf blk(f64 * sizeof(double) + f32 * sizeof(float) + i32 * sizeof(int), st);
+    double *d = blk.as<double>();
     ws.T1 = d; ws.S = d + nn; ws.G = d + 2 * nn; ws.E = d + 3 * nn; ws.wbuf = d + 4 * nn;
     ws.emax = d + 6 * nn;
     float *f = reinterpret_cast<float *>(d + f64);
@@ -513,7 +512,6 @@ extern "C" int hqcgb_eigh_mixed(int n, const double *A, double *w, double *V, vo
     ws.iwork = ws.status + 64;
     HQ_CUDA(cudaMemsetAsync(ws.status, 0, sizeof(int), st));
     bool ok = eigh_mixed(n, A, V, w, ws, st);
-    HQ_CUDA(cudaFreeAsync(blk, st));
     HQ_CUDA(cudaStreamSynchronize(st));
     int hs = ok ? 0 : -1;
     if (hs < 0) throw Error{HQCGB_EIG_FAIL, "eigensolver did not converge"};

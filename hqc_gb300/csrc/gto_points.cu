@@ -77,9 +77,8 @@ extern "C" int hqcgb_ao_points(int n_atoms, int nao_atom, int n_prim, const doub
                  "only s and p AOs are supported");
     if (npts == 0) return HQCGB_OK;
     const size_t nd = (size_t)n_prim + (size_t)nao_atom * n_prim + n_lat1d, ni = 2 * (size_t)nao_atom;
-    void *blk = nullptr;
-    HQ_CUDA(cudaMallocAsync(&blk, nd * sizeof(double) + ni * sizeof(int), st));
-    double *d = static_cast<double *>(blk);
+    StreamBuf blk(nd * sizeof(double) + ni * sizeof(int), st);
+    double *d = blk.as<double>();
     int *iv = reinterpret_cast<int *>(d + nd);
     HQ_CUDA(cudaMemcpyAsync(d, alpha, n_prim * sizeof(double), cudaMemcpyHostToDevice, st));
     HQ_CUDA(cudaMemcpyAsync(d + n_prim, coef, (size_t)nao_atom * n_prim * sizeof(double),
@@ -94,7 +93,6 @@ extern "C" int hqcgb_ao_points(int n_atoms, int nao_atom, int n_prim, const doub
                                                       d + n_prim + (size_t)nao_atom * n_prim, xp, npts,
                                                       pts_per_group, xe, out);
     HQ_LAUNCH_CHECK();
-    HQ_CUDA(cudaFreeAsync(blk, st));
     HQ_CUDA(cudaStreamSynchronize(st));
     return HQCGB_OK;
   } catch (const Error &e) {
@@ -133,11 +131,10 @@ extern "C" int hqcgb_slater(int n, int nao_atom, int n_prim, const double *alpha
     const int n2 = n / 2, nao = n * nao_atom;
     for (int k = 0; k < n; ++k)
       HQ_REQUIRE(state_idx[k] >= 0 && state_idx[k] < nmo, "state index out of range");
-    double *ao = nullptr, *Mu = nullptr;
-    int *idx = nullptr;
-    HQ_CUDA(cudaMallocAsync(&ao, (size_t)W * n * nao * sizeof(double), st));
-    HQ_CUDA(cudaMallocAsync(&Mu, (size_t)2 * nao * n2 * sizeof(double), st));
-    HQ_CUDA(cudaMallocAsync(&idx, (size_t)n * sizeof(int), st));
+    StreamBuf ao_buf((size_t)W * n * nao * sizeof(double), st), mu_buf((size_t)2 * nao * n2 * sizeof(double), st),
+        idx_buf((size_t)n * sizeof(int), st);
+    double *ao = ao_buf.as<double>(), *Mu = mu_buf.as<double>();
+    int *idx = idx_buf.as<int>();
     HQ_CUDA(cudaMemcpyAsync(idx, state_idx, n * sizeof(int), cudaMemcpyHostToDevice, st));
     // AO values: with shared protons every point is in group 0
     const int ppg = xp_groups == 1 ? W * n : n;
@@ -153,9 +150,6 @@ extern "C" int hqcgb_slater(int n, int nao_atom, int n_prim, const double *alpha
                           (long long)n2 * n2, W, st);
     gemm_batched_rowmajor(n2, n2, nao, ao + (size_t)n2 * nao, nao, (long long)n * nao,
                           Mu + (size_t)nao * n2, n2, 0, dn, n2, (long long)n2 * n2, W, st);
-    HQ_CUDA(cudaFreeAsync(ao, st));
-    HQ_CUDA(cudaFreeAsync(Mu, st));
-    HQ_CUDA(cudaFreeAsync(idx, st));
     HQ_CUDA(cudaStreamSynchronize(st));
     return HQCGB_OK;
   } catch (const Error &e) {
@@ -241,9 +235,8 @@ extern "C" int hqcgb_ao_points_kpt(int n_atoms, int nao_atom, int n_prim, const 
                  "only s and p AOs are supported");
     if (npts == 0) return HQCGB_OK;
     const size_t nd = (size_t)n_prim + (size_t)nao_atom * n_prim + n_lat1d, ni = 2 * (size_t)nao_atom;
-    void *blk = nullptr;
-    HQ_CUDA(cudaMallocAsync(&blk, nd * sizeof(double) + ni * sizeof(int), st));
-    double *d = static_cast<double *>(blk);
+    StreamBuf blk(nd * sizeof(double) + ni * sizeof(int), st);
+    double *d = blk.as<double>();
     int *iv = reinterpret_cast<int *>(d + nd);
     HQ_CUDA(cudaMemcpyAsync(d, alpha, n_prim * sizeof(double), cudaMemcpyHostToDevice, st));
     HQ_CUDA(cudaMemcpyAsync(d + n_prim, coef, (size_t)nao_atom * n_prim * sizeof(double),
@@ -258,7 +251,6 @@ extern "C" int hqcgb_ao_points_kpt(int n_atoms, int nao_atom, int n_prim, const 
         d + n_prim + (size_t)nao_atom * n_prim, kpt[0], kpt[1], kpt[2], xp, npts, pts_per_group, xe,
         reinterpret_cast<double2 *>(out));
     HQ_LAUNCH_CHECK();
-    HQ_CUDA(cudaFreeAsync(blk, st));
     HQ_CUDA(cudaStreamSynchronize(st));
     return HQCGB_OK;
   } catch (const Error &e) {
@@ -284,11 +276,10 @@ extern "C" int hqcgb_slater_kpt(int n, int nao_atom, int n_prim, const double *a
     const int n2 = n / 2, nao = n * nao_atom;
     for (int k = 0; k < n; ++k)
       HQ_REQUIRE(state_idx[k] >= 0 && state_idx[k] < nmo, "state index out of range");
-    double2 *ao = nullptr, *Mu = nullptr;
-    int *idx = nullptr;
-    HQ_CUDA(cudaMallocAsync(&ao, (size_t)W * n * nao * sizeof(double2), st));
-    HQ_CUDA(cudaMallocAsync(&Mu, (size_t)2 * nao * n2 * sizeof(double2), st));
-    HQ_CUDA(cudaMallocAsync(&idx, (size_t)n * sizeof(int), st));
+    StreamBuf ao_buf((size_t)W * n * nao * sizeof(double2), st),
+        mu_buf((size_t)2 * nao * n2 * sizeof(double2), st), idx_buf((size_t)n * sizeof(int), st);
+    double2 *ao = ao_buf.as<double2>(), *Mu = mu_buf.as<double2>();
+    int *idx = idx_buf.as<int>();
     HQ_CUDA(cudaMemcpyAsync(idx, state_idx, n * sizeof(int), cudaMemcpyHostToDevice, st));
     const int ppg = xp_groups == 1 ? W * n : n;
     int s = hqcgb_ao_points_kpt(n, nao_atom, n_prim, alpha, coef, ao_l, ao_cart, n_lat1d, lat1d, kpt,
@@ -305,9 +296,6 @@ extern "C" int hqcgb_slater_kpt(int n, int nao_atom, int n_prim, const double *a
     zgemm_batched_rowmajor(n2, n2, nao, ao + (size_t)n2 * nao, nao, (long long)n * nao,
                            Mu + (size_t)nao * n2, n2, 0, reinterpret_cast<double2 *>(dn), n2,
                            (long long)n2 * n2, W, st);
-    HQ_CUDA(cudaFreeAsync(ao, st));
-    HQ_CUDA(cudaFreeAsync(Mu, st));
-    HQ_CUDA(cudaFreeAsync(idx, st));
     HQ_CUDA(cudaStreamSynchronize(st));
     return HQCGB_OK;
   } catch (const Error &e) {

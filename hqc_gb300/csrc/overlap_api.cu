@@ -28,9 +28,8 @@ extern "C" int hqcgb_overlap(int n_atoms, int nao_atom, int n_prim, const double
     const size_t nq = kp ? ovl_scratch_doubles_kpt(n_atoms, n_prim) : ovl_scratch_doubles(n_atoms, n_prim);
     const size_t nd = (size_t)n_prim + (size_t)nao_atom * n_prim + 3 * (size_t)n_lattice + 3 + nq +
                       (T ? 0 : cw * nn);
-    void *blk = nullptr;
-    HQ_CUDA(cudaMallocAsync(&blk, nd * sizeof(double) + 2 * (size_t)nao_atom * sizeof(int), st));
-    double *d_alpha = static_cast<double *>(blk), *d_coef = d_alpha + n_prim,
+    StreamBuf blk(nd * sizeof(double) + 2 * (size_t)nao_atom * sizeof(int), st);
+    double *d_alpha = blk.as<double>(), *d_coef = d_alpha + n_prim,
            *d_lat = d_coef + (size_t)nao_atom * n_prim, *d_k = d_lat + 3 * (size_t)n_lattice,
            *d_q = d_k + 3, *d_t = d_q + nq;
     int *d_l = reinterpret_cast<int *>(d_alpha + nd), *d_c = d_l + nao_atom;
@@ -52,7 +51,6 @@ extern "C" int hqcgb_overlap(int n_atoms, int nao_atom, int n_prim, const double
                                T ? Tb : nullptr, nullptr, nullptr, nullptr, nullptr, d_q, st);
       }
     }
-    HQ_CUDA(cudaFreeAsync(blk, st));
     HQ_CUDA(cudaStreamSynchronize(st));
     return HQCGB_OK;
   } catch (const Error &e) {

@@ -1038,10 +1038,8 @@ int hqcgb_ewald(const double *xp, int n, double L, double rs, double kappa, int 
     HQ_REQUIRE(xp && energy && n >= 1 && L > 0 && rs > 0 && kappa > 0 && gmax >= 1, "bad argument");
     cudaStream_t st = (cudaStream_t)stream;
     HQ_REQUIRE(gmax <= 200, "Gmax too large");
-    double *work = nullptr;
-    HQ_CUDA(cudaMallocAsync(&work, sizeof(double) * ewald_work_doubles(n, gmax), st));
-    launch_ewald(xp, n, L, rs, kappa, gmax, work, energy, grad, st);
-    HQ_CUDA(cudaFreeAsync(work, st));
+    StreamBuf work(sizeof(double) * ewald_work_doubles(n, gmax), st);
+    launch_ewald(xp, n, L, rs, kappa, gmax, work.as<double>(), energy, grad, st);
     return HQCGB_OK;
   });
 }
@@ -1086,11 +1084,9 @@ int hqcgb_eigh(int n, int batch, const double *A, double *w, double *V, void *st
     HQ_REQUIRE(A && w && V && n >= 1 && n <= kMaxNao && batch >= 1, "bad argument");
     cudaStream_t st = (cudaStream_t)stream;
     size_t nn = (size_t)n * n * batch;
-    double *work = nullptr, *Ac = nullptr;
-    int *stat = nullptr;
-    HQ_CUDA(cudaMallocAsync(&work, nn * sizeof(double), st));
-    HQ_CUDA(cudaMallocAsync(&Ac, nn * sizeof(double), st));
-    HQ_CUDA(cudaMallocAsync(&stat, batch * sizeof(int), st));
+    StreamBuf wbuf(nn * sizeof(double), st), abuf(nn * sizeof(double), st), sbuf(batch * sizeof(int), st);
+    double *work = wbuf.as<double>(), *Ac = abuf.as<double>();
+    int *stat = sbuf.as<int>();
     HQ_CUDA(cudaMemcpyAsync(Ac, A, nn * sizeof(double), cudaMemcpyDeviceToDevice, st));
     eigh_tql(n, batch, Ac, V, w, work, stat, st);
     std::vector<int> hs(batch);
@@ -1109,9 +1105,6 @@ int hqcgb_eigh(int n, int batch, const double *A, double *w, double *V, void *st
         if (js < 0) status = HQCGB_EIG_FAIL;
       }
     }
-    HQ_CUDA(cudaFreeAsync(work, st));
-    HQ_CUDA(cudaFreeAsync(Ac, st));
-    HQ_CUDA(cudaFreeAsync(stat, st));
     if (status != HQCGB_OK) throw Error{status, "eigensolver did not converge"};
     return HQCGB_OK;
   });

@@ -1730,21 +1730,17 @@ extern "C" int hqcgb_tc_quadrature_gga(int nao, long long N, long long ld, const
   cudaStream_t st = (cudaStream_t)stream;
   try {
     HQ_REQUIRE(nao >= 1 && N >= 1 && ld >= N && ld % 32 == 0 && phi && dphi && w && u && M, "bad argument");
-    double *part = nullptr;
-    float *hl = nullptr;
-    int *err = nullptr;
-    HQ_CUDA(cudaMallocAsync(&part, tc_quad_partial_doubles(nao, N) * sizeof(double), st));
-    HQ_CUDA(cudaMallocAsync(&hl, 4 * (size_t)nao * ld * sizeof(float), st));
-    HQ_CUDA(cudaMallocAsync(&err, sizeof(int), st));
+    StreamBuf part_buf(tc_quad_partial_doubles(nao, N) * sizeof(double), st),
+        hl_buf(4 * (size_t)nao * ld * sizeof(float), st), err_buf(sizeof(int), st);
+    double *part = part_buf.as<double>();
+    float *hl = hl_buf.as<float>();
+    int *err = err_buf.as<int>();
     HQ_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
     float *phl = hl, *zhl = hl + 2 * (size_t)nao * ld;
     launch_split_operand(phi, nullptr, nullptr, nullptr, nao, N, ld, ld, 1.f, 0.f, phl, st);
     launch_tc_quadrature(phi, dphi, phl, w, u, dV, nao, N, ld, true, 1.0, part, M, err, st, drain, zhl);
     int h = 0;
     HQ_CUDA(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, st));
-    HQ_CUDA(cudaFreeAsync(part, st));
-    HQ_CUDA(cudaFreeAsync(hl, st));
-    HQ_CUDA(cudaFreeAsync(err, st));
     HQ_CUDA(cudaStreamSynchronize(st));
     if (h) throw Error{HQCGB_CUDA_ERROR, "tensor-core pipeline wait limit hit"};
     return HQCGB_OK;
@@ -1762,12 +1758,11 @@ extern "C" int hqcgb_tc_quadrature(int nao, long long N, long long ld, const flo
     HQ_REQUIRE(nao >= 1 && N >= 1 && ld >= N && ld % 4 == 0 && phi && w && M, "bad argument");
     HQ_REQUIRE(nsplit == 2, "nsplit must be 2 (3xTF32)");
     const long long ldo = (N + 31) / 32 * 32;
-    double *part = nullptr;
-    float *hl = nullptr;
-    int *err = nullptr;
-    HQ_CUDA(cudaMallocAsync(&part, tc_quad_partial_doubles(nao, N) * sizeof(double), st));
-    HQ_CUDA(cudaMallocAsync(&hl, 4 * (size_t)nao * ldo * sizeof(float), st));
-    HQ_CUDA(cudaMallocAsync(&err, sizeof(int), st));
+    StreamBuf part_buf(tc_quad_partial_doubles(nao, N) * sizeof(double), st),
+        hl_buf(4 * (size_t)nao * ldo * sizeof(float), st), err_buf(sizeof(int), st);
+    double *part = part_buf.as<double>();
+    float *hl = hl_buf.as<float>();
+    int *err = err_buf.as<int>();
     HQ_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
     float *phl = hl, *zhl = hl + 2 * (size_t)nao * ldo;
     launch_split_operand(phi, nullptr, nullptr, nullptr, nao, N, ld, ldo, 1.f, 0.f, phl, st);
@@ -1775,9 +1770,6 @@ extern "C" int hqcgb_tc_quadrature(int nao, long long N, long long ld, const flo
     launch_tc_quad_split(zhl, phl, nao, N, ldo, true, false, 1.0, part, M, err, st, drain);
     int h = 0;
     HQ_CUDA(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, st));
-    HQ_CUDA(cudaFreeAsync(part, st));
-    HQ_CUDA(cudaFreeAsync(hl, st));
-    HQ_CUDA(cudaFreeAsync(err, st));
     HQ_CUDA(cudaStreamSynchronize(st));
     if (h) throw Error{HQCGB_CUDA_ERROR, "tensor-core pipeline wait limit hit"};
     return HQCGB_OK;
@@ -1794,13 +1786,12 @@ extern "C" int hqcgb_tc_density(int nao, long long N, long long ld, const float 
   try {
     HQ_REQUIRE(nao >= 1 && N >= 1 && ld >= N && ld % 4 == 0 && phi && D && rho, "bad argument");
     int ldk = tc_ldk(nao);
-    double *part = nullptr;
-    float *phiT = nullptr, *D32 = nullptr;
-    int *err = nullptr;
-    HQ_CUDA(cudaMallocAsync(&part, tc_density_partial_doubles(nao, ld, false) * sizeof(double), st));
-    HQ_CUDA(cudaMallocAsync(&phiT, (size_t)N * ldk * sizeof(float), st));
-    HQ_CUDA(cudaMallocAsync(&D32, (size_t)nao * ldk * sizeof(float), st));
-    HQ_CUDA(cudaMallocAsync(&err, sizeof(int), st));
+    StreamBuf part_buf(tc_density_partial_doubles(nao, ld, false) * sizeof(double), st),
+        phiT_buf((size_t)N * ldk * sizeof(float), st), D32_buf((size_t)nao * ldk * sizeof(float), st),
+        err_buf(sizeof(int), st);
+    double *part = part_buf.as<double>();
+    float *phiT = phiT_buf.as<float>(), *D32 = D32_buf.as<float>();
+    int *err = err_buf.as<int>();
     HQ_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
     HQ_CUDA(cudaMemsetAsync(D32, 0, (size_t)nao * ldk * sizeof(float), st));
     HQ_CUDA(cudaMemcpy2DAsync(D32, ldk * sizeof(float), D, nao * sizeof(float), nao * sizeof(float),
@@ -1809,10 +1800,6 @@ extern "C" int hqcgb_tc_density(int nao, long long N, long long ld, const float 
     launch_tc_density(phi, phiT, nullptr, D32, nao, N, ld, part, rho, nullptr, err, st, nsplit, drain);
     int h = 0;
     HQ_CUDA(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, st));
-    HQ_CUDA(cudaFreeAsync(part, st));
-    HQ_CUDA(cudaFreeAsync(phiT, st));
-    HQ_CUDA(cudaFreeAsync(D32, st));
-    HQ_CUDA(cudaFreeAsync(err, st));
     HQ_CUDA(cudaStreamSynchronize(st));
     if (h) throw Error{HQCGB_CUDA_ERROR, "tensor-core pipeline wait limit hit"};
     return HQCGB_OK;
@@ -1838,11 +1825,10 @@ extern "C" int hqcgb_tc_orbital_density(int nao, long long N, long long ld, cons
     HQ_REQUIRE((dphi == nullptr) == (grho == nullptr), "dphi and grho go together");
     int ldk = tc_ldk(nao);
     int ncomp = dphi ? 4 : 1;
-    float *phiT = nullptr, *Yhl = nullptr;
-    int *err = nullptr;
-    HQ_CUDA(cudaMallocAsync(&phiT, (size_t)ncomp * N * ldk * sizeof(float), st));
-    HQ_CUDA(cudaMallocAsync(&Yhl, (size_t)2 * tc_psi_max(false) * ldk * sizeof(float), st));
-    HQ_CUDA(cudaMallocAsync(&err, sizeof(int), st));
+    StreamBuf phiT_buf((size_t)ncomp * N * ldk * sizeof(float), st),
+        Yhl_buf((size_t)2 * tc_psi_max(false) * ldk * sizeof(float), st), err_buf(sizeof(int), st);
+    float *phiT = phiT_buf.as<float>(), *Yhl = Yhl_buf.as<float>();
+    int *err = err_buf.as<int>();
     HQ_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
     launch_transpose_phi(phi, nao, N, ld, phiT, st);
     if (dphi)
@@ -1854,9 +1840,6 @@ extern "C" int hqcgb_tc_orbital_density(int nao, long long N, long long ld, cons
                           N, rho, grho, err, st, nullptr, drain);
     int h = 0;
     HQ_CUDA(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, st));
-    HQ_CUDA(cudaFreeAsync(phiT, st));
-    HQ_CUDA(cudaFreeAsync(Yhl, st));
-    HQ_CUDA(cudaFreeAsync(err, st));
     HQ_CUDA(cudaStreamSynchronize(st));
     if (h) throw Error{HQCGB_CUDA_ERROR, "tensor-core pipeline wait limit hit"};
     return HQCGB_OK;
