@@ -258,3 +258,21 @@ def test_pes_host_logic_with_stand_in_engine(monkeypatch):
     assert abs(float(kp(xp, np.array([0.5, 0.0, 0.0]))) - (2.6 + 200.0)) < 1e-12
     with pytest.raises(TypeError):
         kp(xp)
+
+
+def test_no_cpu_fallback(monkeypatch, tmp_path):
+    """The product path fails loudly instead of falling back to CPU code:
+    without the built library the loader raises, and without a GPU the
+    factories raise before any work."""
+    import torch
+    from hqc_gb300 import _lib, make_solver, make_overlap
+    monkeypatch.setattr(_lib, "_lib", None)
+    monkeypatch.setattr(_lib, "LIB_PATH", str(tmp_path / "missing.so"))
+    with pytest.raises(RuntimeError, match="no CPU fallback"):
+        _lib.load()
+    monkeypatch.undo()
+    if not torch.cuda.is_available():
+        with pytest.raises(RuntimeError, match="CUDA GPU"):
+            make_solver(2, 2.0, 1.5, "gth-szv")
+        with pytest.raises(Exception):
+            make_overlap(2, 2.0, 1.5, "gth-szv")(np.zeros((2, 3)))
