@@ -276,3 +276,23 @@ def test_no_cpu_fallback(monkeypatch, tmp_path):
             make_solver(2, 2.0, 1.5, "gth-szv")
         with pytest.raises(Exception):
             make_overlap(2, 2.0, 1.5, "gth-szv")(np.zeros((2, 3)))
+
+
+def test_plain_c_client_links_and_runs(tmp_path):
+    """tests/c_client.c, a C99 program using only include/hqcgb.h, compiles
+    with gcc, links against the library and gets the expected answers from
+    the host-side entry points (no GPU needed)."""
+    import shutil
+    import subprocess
+    from hqc_gb300 import _lib
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not available")
+    _lib.load()
+    libdir = os.path.dirname(_lib.LIB_PATH)
+    exe = str(tmp_path / "c_client")
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic",
+                    "-I", os.path.join(ROOT, "include"), os.path.join(ROOT, "tests", "c_client.c"),
+                    "-L", libdir, "-lhqcgb", "-Wl,-rpath," + libdir, "-lm", "-o", exe], check=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, r.stderr
+    assert "c_client ok" in r.stdout
