@@ -910,10 +910,14 @@ static int run_batch(hqcgb_plan *p, int n_cfg, const double *xp, const hqcgb_scf
   if (nthreads <= 1) {
     int worst = HQCGB_OK;
     for (int b = 0; b < n_cfg; ++b) {
-      hqcgb_scf_out o = slice(*out, b, p->nao);
-      int s = scf_one(p, xp + (size_t)b * 3 * p->n, &o, st);
-      if (grad) forces(p, grad + (size_t)b * 3 * p->n, st);
-      worst = std::max(worst, s);
+      try {
+        hqcgb_scf_out o = slice(*out, b, p->nao);
+        int s = scf_one(p, xp + (size_t)b * 3 * p->n, &o, st);
+        if (grad) forces(p, grad + (size_t)b * 3 * p->n, st);
+        worst = std::max(worst, s);
+      } catch (const Error &e) {  // name the configuration, as the concurrent path does
+        throw Error{e.status, "configuration " + std::to_string(b) + ": " + e.msg};
+      }
     }
     return worst;
   }
