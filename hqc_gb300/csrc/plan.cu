@@ -878,15 +878,16 @@ static hqcgb_params params_of(const hqcgb_plan *p) {
 static void ensure_workers(hqcgb_plan *p, int k) {
   while ((int)p->workers.size() < k) {
     hqcgb_params q = params_of(p);
+    cudaStream_t s;
+    HQ_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     hqcgb_plan *w = new hqcgb_plan();
     try {
       create(&q, w);
-    } catch (...) {
+    } catch (...) {  // nothing of a failed clone outlives this call
       delete w;
+      cudaStreamDestroy(s);
       throw;
     }
-    cudaStream_t s;
-    HQ_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
     p->workers.push_back(w);
     p->wstreams.push_back(s);
   }
