@@ -1133,6 +1133,21 @@ struct QfArgs {
   int *err;
 };
 
+// Layout invariants of the tensor-core kernels, checked at compile time:
+// dynamic shared memory within the 227 KB a CTA may use, TMEM columns within
+// the 512 of an SM, kernel parameters (tile lists + eight tensor maps) within
+// the classic 4 KB parameter space.
+constexpr size_t kMaxDynSmem = 227 * 1024;
+static_assert(kDensSmem <= kMaxDynSmem && kPsiSmem <= kMaxDynSmem && kQtSmem <= kMaxDynSmem &&
+                  kQfSmem <= kMaxDynSmem,
+              "dynamic shared memory above 227 KB");
+static_assert(kTmemCols <= 512 && kQfColXC + 32 == (uint32_t)kQfTmemCols && kQfTmemCols <= 512,
+              "TMEM column layout");
+static_assert(sizeof(QtArgs) + 8 * sizeof(CUtensorMap) <= 4096 &&
+                  sizeof(QfArgs) + 8 * sizeof(CUtensorMap) <= 4096,
+              "kernel parameters above 4 KB");
+static_assert(kPsiRowsPerThread * kPsiProducers == kM * 8, "splitter rows per thread");
+
 __global__ void __launch_bounds__(kQfThreads, 1)
     k_tc_quad_fused(QfArgs a, const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtensorMap mAl,
                     const __grid_constant__ CUtensorMap mBh, const __grid_constant__ CUtensorMap mBl,
