@@ -389,14 +389,14 @@ def run_reference(args):
         vals.append(cb["value"])
     v = float(np.mean(vals[args.warmup:])) if args.steps else float(vals[-1])
     cb["value"] = v
-    return {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
+    return {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
             "data": "synthetic", "config": dict(CONFIG, batch=1, concurrency=1),
             "cpu_baseline": cb,
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "reference is JAX (not installable here, no network); timed its NumPy FP64 "
-                    "restatement (oracle/) on the host cores"}
+                    "restatement (oracle/) on the host cores of rank 0, no GPU used"}
 
 
 # ---------------------------------------------------------------------------
