@@ -33,3 +33,7 @@ def scan(f, init, xs, length=None):
     if ys and isinstance(ys[0], tuple):
         return carry, tuple(_wrap(_np.stack([y[k] for y in ys])) for k in range(len(ys[0])))
     return carry, _wrap(_np.stack(ys))
+
+
+def map(f, xs):  # noqa: A001  (the jax.lax name)
+    return _wrap(_np.stack([f(x) for x in xs]))

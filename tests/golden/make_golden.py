@@ -8,7 +8,8 @@ read-only checkout.  Every number written below is therefore produced by the
 reference's own code path: ``hqc/pbc/solver.py`` (make_solver and its
 hf_gamma / dft_gamma / hf_kpt / dft_kpt drivers), ``hqc/pbc/scf.py``,
 ``hqc/tools/smearing.py``, ``hqc/tools/excor.py``, ``hqc/pbc/gto.py``,
-``hqc/pbc/potential.py``, ``hqc/pbc/lcao.py`` and ``hqc/pbc/pes.py``.
+``hqc/pbc/potential.py``, ``hqc/pbc/overlap.py``, ``hqc/pbc/slater.py``,
+``hqc/pbc/lcao.py`` and ``hqc/pbc/pes.py``.
 
 Positions come from ``numpy.random.default_rng(seed)`` (JAX's PRNG stream is
 not reproducible without jaxlib).  Output: one ``.npz`` per case in this
@@ -36,6 +37,7 @@ from hqc.pbc.lcao import make_lcao  # noqa: E402
 from hqc.pbc.pes import make_pes  # noqa: E402
 from hqc.pbc.gto import make_pbc_gto  # noqa: E402
 from hqc.pbc.overlap import make_overlap  # noqa: E402
+from hqc.pbc.slater import make_slater  # noqa: E402
 from hqc.pbc.potential import potential_energy_pp, potential_energy, kpoints, Madelung  # noqa: E402
 
 
@@ -174,6 +176,32 @@ def run_gto_kpt_case():
     return rec, dict(n=n, rs=rs, seeds=44)
 
 
+def run_slater_case():
+    """make_slater (``hqc/pbc/slater.py:7-104``): the Slater matrices of one
+    electron configuration with random orthonormal orbital coefficients, for
+    the ground state, an excited ``state_idx`` and a k-point (complex
+    coefficients).  Positions and L in rs units, as the reference takes them."""
+    n, rs, basis = 8, 1.5, "gth-dzv"
+    L = box(n)
+    rng = np.random.default_rng(45)
+    xp = rng.uniform(0.0, L, (n, 3))
+    xe = rng.uniform(0.0, L, (n, 3))
+    nao = 2 * n
+    mo = np.linalg.qr(rng.normal(size=(nao, nao)))[0]
+    moc = mo * np.exp(1j * rng.uniform(0.0, 2 * np.pi, nao))[None, :]
+    kpt = rng.uniform(-np.pi / (L * rs), np.pi / (L * rs), 3)
+    idx = np.array([0, 1, 2, 5, 0, 1, 3, 4])
+    rec = dict(xp=xp, xe=xe, L=L, mo=mo, moc=moc, kpt=kpt, idx=idx)
+    a = (jnp.array(xp), jnp.array(xe))
+    up, dn = make_slater(n, L, rs, basis)(*a, jnp.array(mo))
+    rec["up"], rec["dn"] = np.asarray(up), np.asarray(dn)
+    up, dn = make_slater(n, L, rs, basis, groundstate=False)(*a, jnp.array(mo), jnp.array(idx))
+    rec["up_x"], rec["dn_x"] = np.asarray(up), np.asarray(dn)
+    up, dn = make_slater(n, L, rs, basis, gamma=False)(*a, jnp.array(moc), jnp.array(kpt))
+    rec["up_k"], rec["dn_k"] = np.asarray(up), np.asarray(dn)
+    return rec, dict(n=n, rs=rs, basis=basis, seeds=45)
+
+
 def run_coulomb_case():
     """potential_energy (``hqc/pbc/potential.py:69-101``) of proton + electron
     walker batches, with kpoints / Madelung (6-33), as in
@@ -234,7 +262,8 @@ def run_vpp_case():
 def main(selected):
     manifest_path = os.path.join(HERE, "manifest.json")
     manifest = json.load(open(manifest_path)) if os.path.exists(manifest_path) else {}
-    jobs = list(SOLVER_CASES) + ["gto_values", "gto_values_kpt", "vpp", "coulomb_pe", "overlap"]
+    jobs = list(SOLVER_CASES) + ["gto_values", "gto_values_kpt", "vpp", "coulomb_pe", "overlap",
+                                 "slater"]
     if selected:
         jobs = [j for j in jobs if j in selected]
     for name in jobs:
@@ -247,6 +276,8 @@ def main(selected):
             rec, meta = run_coulomb_case()
         elif name == "overlap":
             rec, meta = run_overlap_case()
+        elif name == "slater":
+            rec, meta = run_slater_case()
         elif name == "vpp":
             rec, meta = run_vpp_case()
         else:

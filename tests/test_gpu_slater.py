@@ -1,7 +1,8 @@
 """make_slater (hqc/pbc/slater.py): AO values at electron positions against
 the reference's golden values (generated from its eval_pbc_ao,
 hqc/pbc/gto.py:357-369) and Slater matrices against the same products in
-FP64 on the host, for single walkers and walker batches."""
+FP64 on the host, for single walkers and walker batches; the Slater matrices
+also against the reference's own make_slater output."""
 import numpy as np
 import pytest
 
@@ -88,3 +89,21 @@ def test_slater_kpt_matrices_and_walker_batches():
     k0 = sl.ao_values(xp, xe[0], np.zeros(3)).cpu().numpy()
     np.testing.assert_allclose(k0.real, g, atol=1e-13)
     assert np.abs(k0.imag).max() == 0.0
+
+
+def test_slater_matrices_match_reference_golden():
+    """The reference's own make_slater output (ground state, an excited
+    state_idx, and a k-point with complex coefficients) for one electron
+    configuration."""
+    from hqc_gb300 import make_slater
+    meta, z = load_golden("slater")
+    n, rs, basis, L = meta["n"], meta["rs"], meta["basis"], float(z["L"])
+    up, dn = make_slater(n, L, rs, basis)(z["xp"], z["xe"], z["mo"])
+    np.testing.assert_allclose(up.cpu().numpy(), z["up"], atol=1e-11)
+    np.testing.assert_allclose(dn.cpu().numpy(), z["dn"], atol=1e-11)
+    up, dn = make_slater(n, L, rs, basis, groundstate=False)(z["xp"], z["xe"], z["mo"], z["idx"])
+    np.testing.assert_allclose(up.cpu().numpy(), z["up_x"], atol=1e-11)
+    np.testing.assert_allclose(dn.cpu().numpy(), z["dn_x"], atol=1e-11)
+    up, dn = make_slater(n, L, rs, basis, gamma=False)(z["xp"], z["xe"], z["moc"], z["kpt"])
+    np.testing.assert_allclose(up.cpu().numpy(), z["up_k"], atol=1e-11)
+    np.testing.assert_allclose(dn.cpu().numpy(), z["dn_k"], atol=1e-11)

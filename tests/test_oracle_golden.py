@@ -196,3 +196,19 @@ def test_overlap_matches_reference():
             np.testing.assert_allclose(st.overlap_kinetic(xp)[0], z[f"S_{tag}_{rcut}"], atol=1e-13)
         st = Setup(n, L, rs, basis, rcut=24, n_grid=5)
         np.testing.assert_allclose(st.overlap_kinetic(xp, kpt=z["kpt"])[0], z[f"Sk_{tag}"], atol=1e-13)
+
+
+def test_slater_matches_reference():
+    """make_slater (slater.py:7-104): the reference's Slater matrices equal the
+    oracle's AO values at the electrons times the selected orbital columns,
+    with the first n/2 electrons and state_idx entries spin-up -- the
+    convention the engine's hqcgb_slater[_kpt] follows."""
+    meta, z = load_golden("slater")
+    n, rs = meta["n"], meta["rs"]
+    st = Setup(n, float(z["L"]), rs, meta["basis"], n_grid=5)
+    h = n // 2
+    for key, mo, idx, kpt in (("", z["mo"], np.r_[:h, :h], None), ("_x", z["mo"], z["idx"], None),
+                              ("_k", z["moc"], np.r_[:h, :h], z["kpt"])):
+        ao = _ao_at_points(st, z["xp"] * rs, z["xe"] * rs, kpt)
+        np.testing.assert_allclose(ao[:h] @ mo[:, idx[:h]], z["up" + key], atol=1e-12)
+        np.testing.assert_allclose(ao[h:] @ mo[:, idx[h:]], z["dn" + key], atol=1e-12)
