@@ -16,6 +16,8 @@
 #include <cstdlib>
 #include <algorithm>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "common.cuh"
 #include "kernels.h"
 
@@ -67,7 +69,21 @@ static cudaEvent_t take_event() {
   return e;
 }
 
+// HQCGB_NVTX=1 also opens an NVTX range per stage scope (named as in
+// kStageNames), for ncu --nvtx filters and timeline tools.
+static bool nvtx_on() {
+  static const bool v = [] {
+    const char *e = std::getenv("HQCGB_NVTX");
+    return e && e[0] == '1';
+  }();
+  return v;
+}
+
 void stage_mark(int stage, cudaStream_t st, bool begin) {
+  if (nvtx_on()) {
+    if (begin) nvtxRangePushA(kStageNames[stage]);
+    else nvtxRangePop();
+  }
   if (!g_profile) return;
   if (begin) {
     if (g_open[stage]++ > 0) return;  // nested scopes of one stage count once
