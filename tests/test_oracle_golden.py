@@ -212,3 +212,18 @@ def test_slater_matches_reference():
         ao = _ao_at_points(st, z["xp"] * rs, z["xe"] * rs, kpt)
         np.testing.assert_allclose(ao[:h] @ mo[:, idx[:h]], z["up" + key], atol=1e-12)
         np.testing.assert_allclose(ao[h:] @ mo[:, idx[h:]], z["dn" + key], atol=1e-12)
+
+
+def test_h54_oracle_run_obeys_translation_sum_rule():
+    """The cached full-size oracle run of the benchmark workload
+    (tests/golden/make_oracle_h54.py): converged, and its electronic gradient
+    sums to zero over the atoms (a uniform translation of every proton leaves
+    the periodic energy unchanged, up to the grid's egg-box term) while single
+    atoms feel forces of order 0.1 Ha/Bohr."""
+    meta, z = load_golden("oracle_h54_bcc_pbe")
+    assert meta["source"] == "oracle" and meta["n_grid"] == 81 and bool(z["converged"])
+    g = z["grad"]
+    assert g.shape == (54, 3)
+    assert np.abs(g.sum(axis=0)).max() < 1e-6 < 1e-2 < np.abs(g).max()
+    # 27 doubly occupied bands below the gap
+    assert z["bands"][26] < z["bands"][27]
