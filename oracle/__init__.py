@@ -7,8 +7,10 @@ of ``bench.py`` use it, and only as the checker.
 It is a NumPy float64 restatement of the reference algorithm, written in the
 streamed (real-space) form: AO values on the grid, rho(r) = sum_pq D_pq
 phi_p phi_q, FFT Poisson for Hartree, occupied-pair-density FFT exchange plus
-the reference's G=0 Madelung term, LDA xc, and the reference's DIIS / fixed
-point SCF with its smearing and chemical-potential search quirks.  On the odd
+the reference's G=0 Madelung term, LDA and PBE xc, the reference's DIIS /
+fixed point SCF with its smearing and chemical-potential search quirks, at
+the Gamma point and at a single k-point (complex Bloch AOs, unconjugated
+complex DIIS), and the Ewald sums of ``hqc/pbc/potential.py``.  On the odd
 grids the reference supports, this form is identical by Parseval to the
 reference's rhoG/ERI formulation (``hqc/pbc/solver.py:391-479``).
 
@@ -16,6 +18,8 @@ Parity pin: ``tests/golden/*.npz`` hold outputs of the reference's own
 unmodified source, executed by ``tests/golden/make_golden.py`` over a NumPy
 stand-in for the JAX API subset it uses.  ``tests/test_oracle_golden.py``
 checks this oracle against those vectors.  The features the reference lacks
-(GGA-PBE, analytic forces) are checked by internal identities only (central
-finite differences, the uniform-gas limit) and are "parity unpinned".
+(GGA-PBE, analytic forces) are checked by internal identities only and are
+"parity unpinned": forces against central finite differences of the
+oracle's own energy, PBE against the constraints it was built to satisfy
+(``tests/test_oracle_xc.py``).
 """
