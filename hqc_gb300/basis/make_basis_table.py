@@ -10,6 +10,9 @@ keyed by basis name.  The data are the published GTH basis sets of CP2K
 GPL-2.0-or-later), copied verbatim because the numbers must be identical.
 
     python hqc_gb300/basis/make_basis_table.py [/path/to/reference]
+
+The checkout defaults to ``$HQC_REFERENCE`` (or /root/reference when unset).
+The licence notice of the extracted data is ``NOTICE`` beside the table.
 """
 import glob
 import json
@@ -19,7 +22,8 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
-def main(ref="/root/reference"):
+def main(ref=None):
+    ref = ref or os.environ.get("HQC_REFERENCE", "/root/reference")
     table = {}
     for sub in ("gth-raw", "gth-test"):
         for path in sorted(glob.glob(os.path.join(ref, "hqc", "basis", sub, "*.dat"))):

@@ -22,6 +22,8 @@
 //  * The first call on each device looks up the array's device address with
 //    cudaGetSymbolAddress (with that device current) and caches it; make that
 //    first call before starting any stream capture.
+//  * The call blocks the host: it synchronises the caller's stream to read
+//    the solver's status word (once, and twice more on the Jacobi fallback).
 #include <mutex>
 #include <string>
 

@@ -258,6 +258,8 @@ int hqcgb_tc_orbital_density(int nao, long long N, long long ld, const float *ph
  * is a static device array of about 1.6 MB per GPU, shared by every call on
  * that device (calls whose device work overlaps race on it); the first call
  * on a device looks the array up and should precede any stream capture.
+ * The call blocks the host: it synchronises the caller's stream once to read
+ * the solver's status (twice more when the Jacobi fallback runs).
  * No counterpart in the reference. */
 int hqcgb_eigh_noalloc(int n, const double *A, double *w, double *V, void *stream);
 

@@ -15,7 +15,9 @@ Positions come from ``numpy.random.default_rng(seed)`` (JAX's PRNG stream is
 not reproducible without jaxlib).  Output: one ``.npz`` per case in this
 folder plus ``manifest.json``.  Run from the repository root:
 
-    python tests/golden/make_golden.py [case-name ...]
+    HQC_REFERENCE=/path/to/hqc python tests/golden/make_golden.py [case-name ...]
+
+``HQC_REFERENCE`` names the reference checkout (default: /root/reference).
 """
 import json
 import os
@@ -26,7 +28,7 @@ import warnings
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REFERENCE = "/root/reference"
+REFERENCE = os.environ.get("HQC_REFERENCE", "/root/reference")
 sys.path.insert(0, os.path.join(HERE, "_jaxshim"))
 sys.path.insert(0, REFERENCE)
 warnings.filterwarnings("ignore")
