@@ -342,59 +342,97 @@ def run_ours(args):
             "roofline": roof, "roofline_orbital_density": roof_psi, "fp64_plain": fp64, "gpu_ms_per_eval_by_stage": stage_ms, "e2e": e2e,
             "gpu_launches": launches, "clocks": clk.summary()}
     if rank == 0 and not args.no_cpu_baseline and world == 1:
-        line["cpu_baseline"] = cpu_baseline(iters_per_eval=float(np.mean(iters)))
+        line["cpu_baseline"] = cpu_baseline()
     if world > 1:
         torch.distributed.destroy_process_group()
     return line if rank == 0 else None
 
 
-def cpu_baseline(iters_per_eval, budget_s=25.0):
-    """The NumPy oracle on the host cores on a bounded sample of the workload:
-    the AO grid (values and gradients) of one configuration plus Fock builds
-    (density, gradient, Hartree FFT Poisson, PBE, quadrature) until the
-    budget is used; one eval is extrapolated as the AO grid + (iterations + 3)
-    Fock builds (the force pass costs about three builds)."""
+class _EnoughUnits(Exception):
+    pass
+
+
+def oracle_units(min_units=0):
+    """Complete CPU evaluations of the workload by the NumPy oracle on the
+    host cores: geometry set-up, every SCF iteration of the real trajectory
+    (DIIS, tol 1e-7 Ry) and the force pass (analytic electronic gradient +
+    Ewald), each timed as one unit.  Runs until one evaluation is complete
+    and at least `min_units` units have run (a later evaluation stops at a
+    unit boundary).  Returns (units [(label, s)], evaluations [(s, iterations)])."""
     from oracle.gpw import Solver
-    w = workload(7)
-    xp = w.pop("xp") * w["rs"]
-    s = Solver(w["n"], w["L"], w["rs"], w["basis"], dft=True, xc=w["xc"],
-               grid_length=w["grid_length"], tol=1e-7)
-    t0 = time.perf_counter()
-    phi, grad, _ = s.st.ao_grid(xp, deriv=1)
-    t1 = time.perf_counter()
-    D = np.eye(s.st.nao) * (w["n"] / s.st.nao)
-    nb = 0
-    while nb < 1 or (nb < 3 and time.perf_counter() - t1 < budget_s):
-        rho = s.density(D, phi)[0]
-        s.hartree(rho, phi)
-        s.xc_terms(D, phi, grad)
-        nb += 1
-    t2 = time.perf_counter()
-    per_build = (t2 - t1) / nb
-    t_eval = (t1 - t0) + per_build * (iters_per_eval + 3)
+    from oracle.forces import electronic_gradient
+    from oracle.ewald import vpp
+    units, evals = [], []
+    last = [time.perf_counter()]
+
+    def mark(label):
+        now = time.perf_counter()
+        units.append((label, now - last[0]))
+        last[0] = now
+        if evals and len(units) >= min_units:
+            raise _EnoughUnits
+
+    seed = 7
+    try:
+        while True:
+            w = workload(seed)
+            xp = w.pop("xp")
+            t0 = last[0] = time.perf_counter()
+            s = Solver(w["n"], w["L"], w["rs"], w["basis"], dft=True, xc=w["xc"],
+                       grid_length=w["grid_length"], tol=1e-7)
+            s.on_unit = mark
+            s.solve(xp)
+            electronic_gradient(s)
+            vpp(xp, w["L"], w["rs"], grad=True)
+            now = time.perf_counter()
+            units.append(("forces", now - last[0]))
+            last[0] = now
+            evals.append((now - t0, s.iterations))
+            if len(units) >= min_units:
+                break
+            seed += 1
+    except _EnoughUnits:
+        pass
+    return units, evals
+
+
+def cpu_baseline():
+    """One complete oracle evaluation of the workload (SCF to convergence +
+    forces) on the host cores, measured once per bench run."""
+    units, evals = oracle_units(0)
+    t, it = evals[-1]
     cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
-    return {"value": 1.0 / t_eval, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"oracle AO grid {t1 - t0:.1f}s + {nb} Fock builds ({per_build:.2f}s each), "
-                      f"extrapolated to {iters_per_eval:.0f} iterations + forces"}
+    return {"value": 1.0 / t, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"one complete oracle evaluation of the first configuration, measured: "
+                      f"geometry {units[0][1]:.1f}s + {it} SCF iterations + force pass "
+                      f"{units[-1][1]:.1f}s = {t:.1f}s"}
 
 
 def run_reference(args):
+    """The reference arm: the NumPy FP64 restatement of the reference's path
+    (jax is absent) on the host cores.  A step is one unit of a complete
+    evaluation (geometry set-up, one SCF iteration or the force pass), so
+    that steps x ms_per_step is the time spent; the value is the measured
+    rate of one complete evaluation."""
     rank, world, _ = dist_info()
     if rank != 0:
         return None
-    from oracle.gpw import Solver  # noqa: F401  (the reference restatement; jax is absent)
-    vals = []
-    for _ in range(args.warmup + args.steps):
-        cb = cpu_baseline(iters_per_eval=19.0, budget_s=20.0)
-        vals.append(cb["value"])
-    v = float(np.mean(vals[args.warmup:])) if args.steps else float(vals[-1])
-    cb["value"] = v
+    units, evals = oracle_units(args.warmup + args.steps)
+    t, it = evals[-1]
+    timed = [u[1] for u in units[args.warmup:args.warmup + args.steps]]
+    v = 1.0 / t
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    cb = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+          "sample": f"complete oracle evaluations timed unit by unit (geometry, each SCF iteration, "
+                    f"force pass); value = the complete evaluation of {t:.1f}s ({it} iterations); "
+                    f"{len(units)} units run in all"}
     return {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
-            "data": "synthetic", "config": dict(CONFIG, batch=1, concurrency=1),
+            "warmup": args.warmup, "ms_per_step": 1000.0 * float(np.mean(timed)) if timed else 1000.0 * t,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "impl": "reference", "data": "synthetic", "config": dict(CONFIG, batch=1, concurrency=1),
             "cpu_baseline": cb,
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "step": "one unit of a complete evaluation: geometry set-up, one SCF iteration or the force pass",
             "note": "reference is JAX (not installable here, no network); timed its NumPy FP64 "
                     "restatement (oracle/) on the host cores of rank 0, no GPU used"}
 

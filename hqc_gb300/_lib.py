@@ -39,7 +39,7 @@ class Params(ctypes.Structure):
 class ScfOut(ctypes.Structure):
     _fields_ = [("mo_coeff", ctypes.c_void_p), ("dm", ctypes.c_void_p), ("bands", ctypes.c_void_p),
                 ("energies", ctypes.c_void_p), ("converged", ctypes.c_void_p),
-                ("iterations", ctypes.c_void_p)]
+                ("iterations", ctypes.c_void_p), ("free_energy", ctypes.c_void_p)]
 
 
 EXPORTS = ("hqcgb_plan_create", "hqcgb_plan_destroy", "hqcgb_scf", "hqcgb_scf_batch",
@@ -51,7 +51,7 @@ EXPORTS = ("hqcgb_plan_create", "hqcgb_plan_destroy", "hqcgb_scf", "hqcgb_scf_ba
            "hqcgb_scf_kpt", "hqcgb_scf_kpt_batch", "hqcgb_kplan_query", "hqcgb_eigh_herm",
            "hqcgb_ao_points_kpt", "hqcgb_slater_kpt", "hqcgb_overlap", "hqcgb_coulomb_energy",
            "hqcgb_tc_quadrature_gga", "hqcgb_diis_coefficients",
-           "hqcgb_tc_quad_tiles")
+           "hqcgb_tc_quad_tiles", "hqcgb_batch_create", "hqcgb_batch_destroy", "hqcgb_batch_run")
 N_STAGES = 15
 
 _lib = None
@@ -106,6 +106,12 @@ def load():
                                          c_int_p, ctypes.c_void_p, ctypes.c_void_p]
     lib.hqcgb_pes_batch.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
                                     ctypes.POINTER(ScfOut), ctypes.c_void_p, ctypes.c_void_p]
+    lib.hqcgb_batch_create.argtypes = [ctypes.POINTER(Params), ctypes.c_double, ctypes.c_int,
+                                       ctypes.POINTER(ctypes.c_void_p)]
+    lib.hqcgb_batch_destroy.argtypes = [ctypes.c_void_p]
+    lib.hqcgb_batch_run.argtypes = [ctypes.c_void_p, ctypes.c_int, c_int_p, c_int_p, c_double_p,
+                                    ctypes.c_void_p, ctypes.POINTER(ScfOut), ctypes.c_void_p,
+                                    ctypes.c_void_p]
     lib.hqcgb_ewald.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.c_double,
                                 ctypes.c_double, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                 ctypes.c_void_p]

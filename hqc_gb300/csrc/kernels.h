@@ -56,6 +56,9 @@ void diis_extrapolate(int space, int n, const double *Fk, const double *ek, int 
 void occupations(int n_elec, int nmo, int smearing, int method, double sigma, int search, int cycle,
                  double tol, double shift, const double *w, double *f, double *mu, cudaStream_t st);
 void entropy(int n, const double *f, double *out, cudaStream_t st);
+// entropy of the free energy E - sigma S whose gradient the forces are
+void free_entropy(int n, int method, double sigma, const double *w, const double *mu, const double *f,
+                  double *out, cudaStream_t st);
 void launch_occ_block(const double *C, const double *occ, int n, int nuse, double *Y, cudaStream_t st);
 void inv_sqrt_cols(int n, const double *U, const double *w, double *v, int *bad, cudaStream_t st);
 void antisym(int n, const double *X, double *e, cudaStream_t st);
@@ -136,10 +139,12 @@ void launch_to_f32(const double *in, long long ldi, long long N, int rows, doubl
 
 // tc_gemm.cu (tcgen05, 3xTF32)
 int tc_quad_chunk();
-size_t tc_quad_partial_doubles(int nao, long long N);
+// kchunk: grid points per CTA along the contraction (0: tc_quad_chunk())
+size_t tc_quad_partial_doubles(int nao, long long N, int kchunk = 0);
+int tc_quad_tiles(int nao, bool sym);  // destination tiles of the tile plan (upper triangle if sym)
 void launch_tc_quad_split(const float *Ahl, const float *Bhl, int nao, long long N, long long ld,
                           bool sym, bool add_transpose, double scale, double *partial, double *M,
-                          int *err, cudaStream_t st, int drain);
+                          int *err, cudaStream_t st, int drain, int kchunk = 0);
 void launch_split_operand(const float *phi, const float *dphi, const float *w, const float *u, int nao,
                           long long N, long long ldi, long long ldo, float a, float b, float *out,
                           cudaStream_t st);
@@ -170,5 +175,31 @@ void launch_force_grid_orb(const float *F32, const double *coef, const int *ao_l
 void launch_tc_density(const float *phi, const float *phiT, const float *dphi, const float *D32,
                        int nao, long long N, long long ld, double *part, double *rho, double *grho,
                        int *err, cudaStream_t st, int nsplit = 2, int drain = 3);
+
+// exchange.cu: occupied-pair exact exchange with fused FFT stages
+struct ExxGeom {
+  int n, nao, nb, nprim;       // grid points per axis, AOs, AOs per atom, primitives
+  const double2 *tw;           // FFT twiddles exp(-2 pi i k / n)
+  const double *coef;          // [nb][nprim] contraction coefficients
+  const int *ao_l, *ao_cart;   // [nb]
+  const void *wsq;             // [n][n][(n+1)/2] square roots of the pair weights (R)
+};
+int exx_factor(int n);
+bool exx_fused_supported(int n, int nprim, bool fp64);
+long long exx_pair_len(int n);  // 2 n^2 (n+1)/2: reals of one pair's half spectrum
+template <typename R>
+void launch_exx_weights(int n, double L, double dV, R *wsq, cudaStream_t st);
+template <typename R>
+void launch_psi_all(const double *C, const double *occ, int nao, int nmo, int nuse, const R *phi,
+                    long long ldphi, long long N, R *out, cudaStream_t st);
+template <typename R>
+void launch_exx_plane(const ExxGeom &G, const R *F1d, const double *X, long long ldx, const R *psi,
+                      long long ldpsi, int g, void *T, cudaStream_t st);
+template <typename R>
+void launch_exx_column_q(const ExxGeom &G, const void *T, int g, void *Q, long long ldq, bool split,
+                         cudaStream_t st);
+template <typename R>
+void launch_exx_column_grad(const ExxGeom &G, const void *T, int g, double *part, double *grad,
+                            cudaStream_t st);
 
 }  // namespace hqcgb

@@ -340,7 +340,7 @@ struct hqcgb_kplan {
 namespace hqcgb {
 
 enum { K_TRHD = 0, K_EXC = 1, K_VHRHO = 2, K_TRKD = 3, K_ERR2 = 4, K_SE = 5, K_KI = 6, K_VEP = 7,
-       K_NSLOT = 16 };
+       K_SFREE = 8, K_NSLOT = 16 };
 
 static void kupload(void *dst, const void *src, size_t bytes) {
   HQ_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
@@ -765,11 +765,13 @@ static int kscf_one(hqcgb_kplan *p, const double *xp_dev, const double *kpt_host
   kdot(c, p->T, p->D, K_KI);
   kdot(c, p->V, p->D, K_VEP);
   entropy(n, p->occ, p->scal + K_SE, st);
+  if (P.smearing) free_entropy(n, P.smearing_method, P.smearing_sigma, p->w, p->mu, p->occ, p->scal + K_SFREE, st);
   ksync(c);
   const double *s = p->hscal;
   const double Exc = P.dft ? p->dV * s[K_EXC] : -0.25 * s[K_TRKD];
   const double Vee = 0.5 * p->dV * s[K_VHRHO] + Exc;
   const double en[5] = {E1, s[K_KI], s[K_VEP], Vee, s[K_SE]};
+  const double Efree = P.smearing ? E1 - P.smearing_sigma * s[K_SFREE] : E1;
   if (out) {
     if (out->mo_coeff) HQ_CUDA(cudaMemcpyAsync(out->mo_coeff, p->C, zb, cudaMemcpyDeviceToDevice, st));
     if (out->dm) HQ_CUDA(cudaMemcpyAsync(out->dm, p->D, zb, cudaMemcpyDeviceToDevice, st));
@@ -779,6 +781,8 @@ static int kscf_one(hqcgb_kplan *p, const double *xp_dev, const double *kpt_host
       HQ_CUDA(cudaMemcpyAsync(out->converged, &converged, sizeof(int), cudaMemcpyHostToDevice, st));
     if (out->iterations)
       HQ_CUDA(cudaMemcpyAsync(out->iterations, &loop, sizeof(int), cudaMemcpyHostToDevice, st));
+    if (out->free_energy)
+      HQ_CUDA(cudaMemcpyAsync(out->free_energy, &Efree, sizeof(double), cudaMemcpyHostToDevice, st));
     HQ_CUDA(cudaStreamSynchronize(st));
   }
   p->have_state = true;
@@ -840,6 +844,7 @@ int hqcgb_scf_kpt_batch(hqcgb_kplan *plan, int n_cfg, const double *xp, const do
       if (o.energies) o.energies += (size_t)b * 5;
       if (o.converged) o.converged += b;
       if (o.iterations) o.iterations += b;
+      if (o.free_energy) o.free_energy += b;
       int s;
       try {
         s = kscf_one(plan, xp + (size_t)b * 3 * plan->n, kpts + (size_t)b * 3, &o, (cudaStream_t)stream);

@@ -470,6 +470,33 @@ void entropy(int n, const double *f, double *out, cudaStream_t st) {
   HQ_LAUNCH_CHECK();
 }
 
+// The entropy S that makes the smeared occupations stationary points of
+// E - sigma S at fixed particle number: Fermi f = 2 / (e^x + 1) -> the Fermi
+// formula above; Gaussian f = erfc(x) / 2 (capped at 1, smearing.py:52) ->
+// S = sum_i exp(-x_i^2) / (2 sqrt(pi)), x_i = (w_i - mu) / sigma.
+__global__ void k_entropy_gauss(int n, const double *__restrict__ w, const double *__restrict__ mu,
+                                double sigma, double *__restrict__ out) {
+  __shared__ double sh[32];
+  double s = 0;
+  const double m = *mu;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double x = (w[i] - m) / sigma;
+    s += exp(-x * x);
+  }
+  s = block_sum(s, sh);
+  if (threadIdx.x == 0) *out = s * 0.28209479177387814;  // 1 / (2 sqrt(pi))
+}
+
+void free_entropy(int n, int method, double sigma, const double *w, const double *mu, const double *f,
+                  double *out, cudaStream_t st) {
+  if (method == HQCGB_SMEAR_GAUSS) {
+    k_entropy_gauss<<<1, 256, 0, st>>>(n, w, mu, sigma, out);
+    HQ_LAUNCH_CHECK();
+  } else {
+    entropy(n, f, out, st);
+  }
+}
+
 // v = U diag(w^-1/2)  (solver.py:729-730)
 __global__ void k_inv_sqrt_cols(int n, const double *__restrict__ U, const double *__restrict__ w,
                                 double *__restrict__ v, int *__restrict__ bad) {

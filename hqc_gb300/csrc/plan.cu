@@ -178,6 +178,22 @@ struct hqcgb_plan {
   float2 *cbuf32 = nullptr;
   int *tc_err = nullptr;
   MixedEigWork mew{};
+  // exact exchange in the occupied-pair form (exchange.cu); R = double on
+  // the FP64 path, float on the mixed path
+  bool exx_fused = false;
+  ExxGeom exx{};
+  int exx_g = 0;               // orbitals per Fock group (Q and T capacity)
+  int exx_grad_g = 0;          // orbitals per gradient group (4 rows per AO)
+  void *exx_T = nullptr;       // plane-transformed pairs
+  void *exx_Q = nullptr;       // FP64 [nao][g 2N_h], or the TF32 pieces [2][nao][exx_ldq]
+  long long exx_ldq = 0;
+  void *exx_psi = nullptr;     // psi~_k = sqrt(f_k) psi_k, [nao][N] (R)
+  bool exx_psi_ready = false;  // psi~ of the current density already written (mixed density pass)
+  double *exx_part = nullptr;  // gradient dot products
+  double *exx_tcpart = nullptr, *exx_Kt = nullptr;  // mixed: Gram partial tiles, group sum
+  void *exx_wsq = nullptr;     // pair weights (depend on the box)
+  int exx_kchunk = 0;
+  int nuse_occ = 0;            // orbitals with occupation > 1e-14 (host copy of occ in hocc)
   double *scal = nullptr;  // device scalars
   double *hscal = nullptr; // pinned host mirror
   // last state
@@ -193,6 +209,7 @@ struct hqcgb_plan {
     return (T *)p;
   }
   // concurrent batch workers: sub-plans with their own workspaces and streams
+  int lat1d_cap = 0, lattice_cap = 0;  // device capacity of the lattice arrays (entries)
   int concurrency = 1;
   std::vector<hqcgb_plan *> workers;
   std::vector<cudaStream_t> wstreams;
@@ -207,7 +224,7 @@ struct hqcgb_plan {
 
 // scal slots
 enum { S_TRHD = 0, S_EXC = 1, S_VHRHO = 2, S_TRKD = 3, S_ERR2 = 4, S_SE = 5, S_KI = 6, S_VEP = 7,
-       S_NSLOT = 16 };
+       S_SFREE = 8, S_NSLOT = 16 };
 
 static void upload(void *dst, const void *src, size_t bytes) {
   HQ_CUDA(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice));
@@ -281,6 +298,8 @@ static void create(const hqcgb_params *in, hqcgb_plan *p) {
   upload(p->lat1d, P.lat1d, sizeof(double) * P.n_lat1d);
   p->lattice = p->alloc<double>(3 * P.n_lattice);
   upload(p->lattice, P.lattice, sizeof(double) * 3 * P.n_lattice);
+  p->lat1d_cap = P.n_lat1d;
+  p->lattice_cap = P.n_lattice;
   std::vector<double2> tw(p->ng);
   for (int k = 0; k < p->ng; ++k) {
     double a = -2.0 * M_PI * k / p->ng;
@@ -377,10 +396,46 @@ static void create(const hqcgb_params *in, hqcgb_plan *p) {
     if (!p->Z) p->Z = p->alloc<double>((size_t)nao * N);
   }
   if (fp64_forces && p->gga) p->DPsi = p->alloc<double>((size_t)nao * N);
-  p->cbuf_batch = p->hf ? nao : 1;
-  if (p->hf) p->W = p->alloc<double>((size_t)nao * N);
+  long long qcols = N;
+  p->exx_fused = p->hf && exx_fused_supported(p->ng, P.n_prim, !p->mixed);
+  if (p->exx_fused) {
+    // orbitals per group: T and Q within about 1.5 GB
+    const long long L2 = exx_pair_len(p->ng);  // reals of one pair's half spectrum
+    const size_t rb = p->mixed ? sizeof(float) : sizeof(double);
+    const double per_orb = (double)nao * L2 * (rb + 8.0);
+    p->exx_g = (int)std::max(1.0, std::min(16.0, std::floor(1.5e9 / per_orb)));
+    p->exx_g = std::min(p->exx_g, nao);
+    const int rows_cap = std::max(p->exx_g, 4) * nao;  // pair rows T holds
+    p->exx_grad_g = rows_cap / (4 * nao);
+    p->exx_T = p->alloc<char>((size_t)rows_cap * (L2 / 2) * 2 * rb);
+    p->exx_psi = p->alloc<char>((size_t)nao * N * rb);
+    p->exx_part = p->alloc<double>((size_t)p->exx_grad_g * nao * p->ng * 3);
+    void *wsq = p->alloc<char>((size_t)(L2 / 2) * rb);
+    const long long gK = (long long)p->exx_g * L2;
+    if (p->mixed) {
+      p->exx_ldq = (gK + 31) / 32 * 32;
+      p->exx_Q = p->alloc<float>((size_t)2 * nao * p->exx_ldq);
+      const int ctas = 2 * 152;
+      const int chunks = std::max(1, ctas / tc_quad_tiles(nao, true));
+      p->exx_kchunk = (int)std::max<long long>(2048, (gK + chunks - 1) / chunks / 32 * 32 + 32);
+      p->exx_tcpart = p->alloc<double>(tc_quad_partial_doubles(nao, gK, p->exx_kchunk));
+      p->exx_Kt = p->alloc<double>(nn);
+      launch_exx_weights<float>(p->ng, p->L, p->dV, (float *)wsq, 0);
+    } else {
+      p->exx_ldq = gK;
+      p->exx_Q = p->alloc<double>((size_t)nao * gK);
+      qcols = std::max(qcols, gK);
+      launch_exx_weights<double>(p->ng, p->L, p->dV, (double *)wsq, 0);
+    }
+    p->exx = ExxGeom{p->ng, nao, p->nb, p->nprim, p->tw, p->coef, p->ao_l, p->ao_cart, wsq};
+    p->exx_wsq = wsq;
+  }
+  // the per-AO pair potentials of the fallback exchange (grids beyond the
+  // fused kernels' shared memory)
+  p->cbuf_batch = (p->hf && !p->exx_fused) ? nao : 1;
+  if (p->hf && !p->exx_fused) p->W = p->alloc<double>((size_t)nao * N);
   p->cbuf = p->alloc<double2>((size_t)p->cbuf_batch * N);
-  if (!p->mixed || p->hf) p->qpart = p->alloc<double>((size_t)quad_chunks(N) * nn);
+  if (!p->mixed || p->hf) p->qpart = p->alloc<double>((size_t)quad_chunks(qcols) * nn);
   p->xpart = p->alloc<double>((size_t)2 * xc_blocks(N));
   if (P.want_forces) {
     p->fpart = p->alloc<double>(std::max((size_t)nao * force_grid_blocks(N) * 3,
@@ -473,14 +528,20 @@ static void density_matrix(Ctx &c) {
   occupations(P.n_atoms, n, P.smearing, P.smearing_method, P.smearing_sigma, P.search_method,
               P.search_cycle, P.search_tol, occ_shift(p), p->w, p->occ, p->mu, c.st);
   p->nuse_dm = 0;
-  if (p->mixed) {
-    // orbitals with a non-negligible occupation come first (ascending energies)
+  p->exx_psi_ready = false;
+  if (p->mixed || p->hf) {
+    // The one host copy of the occupations per iteration: the mixed density
+    // and the exchange of the Fock build that follows size their launches
+    // from it.  Orbitals with a non-negligible occupation come first
+    // (ascending energies).
+    p->hocc.resize(n);
     HQ_CUDA(cudaMemcpyAsync(p->hocc.data(), p->occ, sizeof(double) * n, cudaMemcpyDeviceToHost, c.st));
     HQ_CUDA(cudaStreamSynchronize(c.st));
     int nuse = 0;
     for (int k = 0; k < n; ++k)
       if (p->hocc[k] > 1e-14) nuse = k + 1;
-    if (nuse >= 1 && nuse <= kThinOcc) {
+    p->nuse_occ = nuse;
+    if (p->mixed && nuse >= 1 && nuse <= kThinOcc) {
       launch_occ_block(p->C, p->occ, n, nuse, p->Yd, c.st);
       gemm(false, true, n, n, nuse, 1.0, p->Yd, nuse, p->Yd, nuse, nullptr, 0.0, p->D, n, c.st);
       p->nuse_dm = nuse;
@@ -500,19 +561,91 @@ static void poisson(Ctx &c, const double *src, double *dst, bool keep_spectrum =
   launch_complex_real(p->cbuf, p->N, 1.0, dst, c.st);
 }
 
-// Exact exchange K (with the Madelung G=0 term), solver.py:430-431, 604-614.
-// With Zacc != nullptr also accumulates the orbital force operand
-// Z_p += f_j psi_j (D W_j)_p.
-static void exchange(Ctx &c, double *Zacc) {
+// Madelung G = 0 term of the exchange: K = Kpair + c_M S~ D S~
+// (solver.py:404, 431: eris0 = unknown1 * 4 pi / L * S~ (x) S~).
+static void exchange_madelung(Ctx &c) {
+  hqcgb_plan *p = c.p;
+  const int n = p->nao;
+  HQ_CUDA(cudaMemcpyAsync(p->t1, p->K, sizeof(double) * n * n, cudaMemcpyDeviceToDevice, c.st));
+  double cM = 4.0 * M_PI / p->L * kMadelungSC;
+  gemm(false, false, n, n, n, 1.0, p->St, n, p->D, n, nullptr, 0.0, p->t2, n, c.st);
+  gemm(false, false, n, n, n, 1.0, p->t2, n, p->St, n, nullptr, 0.0, p->K, n, c.st);
+  axpby(n, 1.0, p->t1, cM, p->K, false, p->K, c.st);
+}
+
+// Orbitals the exchange runs over: the prefix of orbitals whose occupation
+// exceeds max(exx_occ_threshold, 1e-14) (each skipped one adds f_i times a
+// bounded matrix to K, below FP64 rounding of the sum).
+static int exx_count(const hqcgb_plan *p) {
+  const double thr = std::max(p->P.exx_occ_threshold, kExxOccFloor);
+  int nuse = 0;
+  for (int k = 0; k < p->nao; ++k)
+    if (p->hocc[k] > thr) nuse = k + 1;
+  return nuse;
+}
+
+// psi~_k = sqrt(f_k) psi_k on the grid for k < nuse, unless the mixed
+// density pass already wrote them.
+static void exx_orbitals(Ctx &c, int nuse) {
+  hqcgb_plan *p = c.p;
+  if (p->exx_psi_ready || nuse == 0) return;
+  if (p->mixed)
+    launch_psi_all<float>(p->C, p->occ, p->nao, p->nao, nuse, p->phi32, p->ld, p->N,
+                          static_cast<float *>(p->exx_psi), c.st);
+  else
+    launch_psi_all<double>(p->C, p->occ, p->nao, p->nao, nuse, p->phi, p->N, p->N,
+                           static_cast<double *>(p->exx_psi), c.st);
+  p->exx_psi_ready = true;
+}
+
+// Exact exchange K (with the Madelung G=0 term), solver.py:430-431, 604-614,
+// in the occupied-pair form of exchange.cu: per group of orbitals the pair
+// planes, the column transforms that write Q, and K += Q Q^T.
+static void exchange(Ctx &c) {
+  hqcgb_plan *p = c.p;
+  const int n = p->nao;
+  const long long N = p->N;
+  HQ_STAGE(ST_EXCHANGE, c.st);
+  HQ_CUDA(cudaMemsetAsync(p->K, 0, sizeof(double) * n * n, c.st));
+  const int nuse = exx_count(p);
+  exx_orbitals(c, nuse);
+  const long long L2 = exx_pair_len(p->ng);
+  for (int j0 = 0; j0 < nuse; j0 += p->exx_g) {
+    const int g = std::min(p->exx_g, nuse - j0);
+    const long long NK = (long long)g * L2;
+    if (p->mixed) {
+      launch_exx_plane<float>(p->exx, p->F1d32, nullptr, 0, static_cast<float *>(p->exx_psi) + j0 * N, N, g,
+                              p->exx_T, c.st);
+      launch_exx_column_q<float>(p->exx, p->exx_T, g, p->exx_Q, p->exx_ldq, true, c.st);
+      const float *Q = static_cast<const float *>(p->exx_Q);
+      // drained every K = 32 stage: K is a Gram matrix of same-sign sums on
+      // its diagonal, where the tensor core's truncating FP32 accumulation
+      // would bias long accumulator chains
+      launch_tc_quad_split(Q, Q, n, NK, p->exx_ldq, true, false, 1.0, p->exx_tcpart, p->exx_Kt, p->tc_err,
+                           c.st, 1, p->exx_kchunk);
+      axpby(n, 1.0, p->K, 1.0, p->exx_Kt, false, p->K, c.st);
+    } else {
+      launch_exx_plane<double>(p->exx, p->F1d, nullptr, 0, static_cast<double *>(p->exx_psi) + j0 * N, N, g,
+                               p->exx_T, c.st);
+      launch_exx_column_q<double>(p->exx, p->exx_T, g, p->exx_Q, NK, false, c.st);
+      const double *Q = static_cast<const double *>(p->exx_Q);
+      launch_quadrature(Q, Q, nullptr, n, NK, true, 1.0, true, p->qpart, p->K, c.st);
+    }
+  }
+  exchange_madelung(c);
+}
+
+// Exact exchange on grids beyond the fused kernels' shared memory: per
+// orbital, pair densities, a full complex 3D FFT Poisson solve and the
+// real-space quadrature.  With Zacc != nullptr also accumulates the orbital
+// force operand Z_p += f_j psi_j (D W_j)_p.
+static void exchange_legacy(Ctx &c, double *Zacc) {
   hqcgb_plan *p = c.p;
   int n = p->nao;
   long long N = p->N;
-  p->h_occ.resize(n);
-  HQ_CUDA(cudaMemcpyAsync(p->h_occ.data(), p->occ, sizeof(double) * n, cudaMemcpyDeviceToHost, c.st));
-  HQ_CUDA(cudaStreamSynchronize(c.st));
   HQ_CUDA(cudaMemsetAsync(p->K, 0, sizeof(double) * n * n, c.st));
   for (int i = 0; i < n; ++i) {
-    double f = p->h_occ[i];
+    double f = p->hocc[i];
     if (!(f > std::max(p->P.exx_occ_threshold, kExxOccFloor))) continue;
     launch_psi(p->C, n, i, p->phi, N, p->psi, c.st);
     launch_real_to_complex(p->phi, p->psi, N, n, p->cbuf, c.st);
@@ -527,10 +660,29 @@ static void exchange(Ctx &c, double *Zacc) {
     }
   }
   axpby(n, 0.5, p->K, 0.5, p->K, true, p->t1, c.st);
-  double cM = 4.0 * M_PI / p->L * kMadelungSC;
-  gemm(false, false, n, n, n, 1.0, p->St, n, p->D, n, nullptr, 0.0, p->t2, n, c.st);
-  gemm(false, false, n, n, n, 1.0, p->t2, n, p->St, n, nullptr, 0.0, p->K, n, c.st);
-  axpby(n, 1.0, p->t1, cM, p->K, false, p->K, c.st);
+  HQ_CUDA(cudaMemcpyAsync(p->K, p->t1, sizeof(double) * n * n, cudaMemcpyDeviceToDevice, c.st));
+  exchange_madelung(c);
+}
+
+// Exchange part of the nuclear gradient (exchange.cu, gradient mode) for the
+// density of the last Fock build; X = D phi (FP64) on the grid.
+static void exchange_gradient(Ctx &c, double *grad) {
+  hqcgb_plan *p = c.p;
+  const long long N = p->N;
+  const int nuse = exx_count(p);
+  exx_orbitals(c, nuse);
+  for (int j0 = 0; j0 < nuse; j0 += p->exx_grad_g) {
+    const int g = std::min(p->exx_grad_g, nuse - j0);
+    if (p->mixed) {
+      launch_exx_plane<float>(p->exx, p->F1d32, p->X, N, static_cast<float *>(p->exx_psi) + j0 * N, N, g,
+                              p->exx_T, c.st);
+      launch_exx_column_grad<float>(p->exx, p->exx_T, g, p->exx_part, grad, c.st);
+    } else {
+      launch_exx_plane<double>(p->exx, p->F1d, p->X, N, static_cast<double *>(p->exx_psi) + j0 * N, N, g,
+                               p->exx_T, c.st);
+      launch_exx_column_grad<double>(p->exx, p->exx_T, g, p->exx_part, grad, c.st);
+    }
+  }
 }
 
 // Two-electron part of the Fock matrix and the energy pieces for density D.
@@ -544,18 +696,18 @@ static double fock(Ctx &c) {
   if (p->mixed) {
     // tensor-core density (3xTF32, FP32 accumulation, FP64 sums), FP32
     // Poisson, FP64 xc, tensor-core quadrature
-    // orbitals with a non-negligible occupation (sorted by energy, so first)
-    HQ_CUDA(cudaMemcpyAsync(p->hocc.data(), p->occ, sizeof(double) * n, cudaMemcpyDeviceToHost, c.st));
-    HQ_CUDA(cudaStreamSynchronize(c.st));
-    int nuse = 0;
-    for (int k = 0; k < n; ++k)
-      if (p->hocc[k] > 1e-14) nuse = k + 1;
+    // orbitals with a non-negligible occupation (sorted by energy, so first;
+    // counted from the host copy density_matrix made)
+    const int nuse = p->nuse_occ;
     if (nuse <= tc_psi_max(p->gga)) {
-      // rho = sum_k |psi_k|^2 from Y = C_occ sqrt(f) (n_use / n_ao of the work)
+      // rho = sum_k |psi_k|^2 from Y = C_occ sqrt(f) (n_use / n_ao of the work);
+      // Hartree-Fock keeps psi~_k = sqrt(f_k) psi_k for the exchange
+      float *psi_out = p->keep_psi ? p->psi32 : nullptr;
+      if (p->exx_fused && !psi_out) psi_out = static_cast<float *>(p->exx_psi);
       launch_psi_operand(p->C, p->occ, n, n, nuse, tc_ldk(n), p->Yhl, c.st);
       launch_tc_psi_density(p->phiT32, p->dphiT32, p->Yhl, tc_psi_width(nuse), tc_ldk(n), N, p->rho,
-                            p->gga ? p->grho : nullptr, p->tc_err, c.st,
-                            p->keep_psi ? p->psi32 : nullptr, kPsiDrain);
+                            p->gga ? p->grho : nullptr, p->tc_err, c.st, psi_out, kPsiDrain);
+      p->exx_psi_ready = p->exx_fused && psi_out == p->exx_psi;
       if (p->keep_psi) {
         p->npsi_kept = tc_psi_width(nuse);
         p->nuse_kept = nuse;
@@ -590,7 +742,8 @@ static double fock(Ctx &c) {
   }
   }
   if (p->hf) {
-    exchange(c, nullptr);
+    if (p->exx_fused) exchange(c);
+    else exchange_legacy(c, nullptr);
     dot((long long)n * n, p->K, p->D, 1.0, p->scal + S_TRKD, false, c.st);
     axpby(n, 1.0, p->F2e, -0.5, p->K, false, p->F2e, c.st);
   }
@@ -766,11 +919,13 @@ static int scf_one(hqcgb_plan *p, const double *xp_dev, const hqcgb_scf_out *out
   dot((long long)nn, p->T, p->D, 1.0, p->scal + S_KI, false, st);
   dot((long long)nn, p->V, p->D, 1.0, p->scal + S_VEP, false, st);
   entropy(n, p->occ, p->scal + S_SE, st);
+  if (P.smearing) free_entropy(n, P.smearing_method, P.smearing_sigma, p->w, p->mu, p->occ, p->scal + S_SFREE, st);
   sync_scalars(c);
   const double *s = p->hscal;
   double Exc = P.dft ? p->dV * s[S_EXC] : -0.25 * s[S_TRKD];
   double Vee = 0.5 * p->dV * s[S_VHRHO] + Exc;
   double en[5] = {E1, s[S_KI], s[S_VEP], Vee, s[S_SE]};
+  const double Efree = P.smearing ? E1 - P.smearing_sigma * s[S_SFREE] : E1;
   if (out) {
     if (out->mo_coeff) HQ_CUDA(cudaMemcpyAsync(out->mo_coeff, p->C, nn * 8, cudaMemcpyDeviceToDevice, st));
     if (out->dm) HQ_CUDA(cudaMemcpyAsync(out->dm, p->D, nn * 8, cudaMemcpyDeviceToDevice, st));
@@ -778,6 +933,8 @@ static int scf_one(hqcgb_plan *p, const double *xp_dev, const hqcgb_scf_out *out
     if (out->energies) HQ_CUDA(cudaMemcpyAsync(out->energies, en, sizeof(en), cudaMemcpyHostToDevice, st));
     if (out->converged) HQ_CUDA(cudaMemcpyAsync(out->converged, &converged, sizeof(int), cudaMemcpyHostToDevice, st));
     if (out->iterations) HQ_CUDA(cudaMemcpyAsync(out->iterations, &loop, sizeof(int), cudaMemcpyHostToDevice, st));
+    if (out->free_energy)
+      HQ_CUDA(cudaMemcpyAsync(out->free_energy, &Efree, sizeof(double), cudaMemcpyHostToDevice, st));
     HQ_CUDA(cudaStreamSynchronize(st));
   }
   p->have_state = true;
@@ -854,9 +1011,9 @@ static void forces(hqcgb_plan *p, double *grad, cudaStream_t st) {
   } else {
     launch_add3(N, p->vloc, p->vh, nullptr, p->veff, st);
     HQ_CUDA(cudaMemsetAsync(p->Z, 0, sizeof(double) * n * N, st));
-    // X is reused inside exchange(); keep a copy of D phi in DPsi-free form:
-    // recompute X after the exchange pass.
-    exchange(c, p->Z);
+    // the fallback exchange accumulates its orbital term into Z (it reuses X,
+    // recomputed below); the fused form adds it to grad after X = D phi
+    if (!p->exx_fused) exchange_legacy(c, p->Z);
     // Madelung term c dV (D S~ D phi)_p  folded into Z with weight cM
     gemm(false, false, n, n, n, 1.0, p->D, n, p->St, n, nullptr, 0.0, p->t1, n, st);
     gemm(false, false, n, n, n, 1.0, p->t1, n, p->D, n, nullptr, 0.0, p->t2, n, st);
@@ -864,6 +1021,7 @@ static void forces(hqcgb_plan *p, double *grad, cudaStream_t st) {
     double cM = 4.0 * M_PI / p->L * kMadelungSC;
     launch_axpy_grid((long long)n * N, N, cM, nullptr, p->X, p->Z, st);
     launch_density(p->phi, nullptr, p->D, n, N, p->rho, nullptr, p->X, st);
+    if (p->exx_fused) exchange_gradient(c, grad);
   }
   launch_force_grid(p->F1d, p->coef, p->ao_l, p->ao_cart, p->nb, p->nprim, n, p->ng, p->veff, p->X,
                     uu, p->DPsi, p->hf ? p->Z : nullptr, p->dV, p->fpart, st);
@@ -918,6 +1076,7 @@ static hqcgb_scf_out slice(const hqcgb_scf_out &o, int b, int nao) {
   if (r.energies) r.energies += 5 * b;
   if (r.converged) r.converged += b;
   if (r.iterations) r.iterations += b;
+  if (r.free_energy) r.free_energy += b;
   return r;
 }
 
@@ -974,6 +1133,188 @@ static int run_batch(hqcgb_plan *p, int n_cfg, const double *xp, const hqcgb_scf
       throw Error{status[b], "configuration " + std::to_string(b) + ": " + msg[b]};
     }
     worst = std::max(worst, status[b]);
+  }
+  return worst;
+}
+
+// ---------------------------------------------------------------------------
+// Uneven batches: configurations of different atom counts, boxes and grids
+// in one call.  The reference batches with jax.vmap over configurations of
+// one shape (test/test.py:157,179), so uneven sizes need one vmapped call per
+// shape there.  Here configurations are grouped into size classes (n_atoms,
+// n_grid); each worker thread owns one workspace per size class, whose
+// box-dependent tables are reset per configuration (set_box), and takes the
+// next configuration from a queue ordered largest first.
+// ---------------------------------------------------------------------------
+
+// Lattices of a cubic box of side L (Bohr), in the order the Python factory
+// builds them: the 1D translations of the grid GTO sums, tmax = 24 // L
+// (hqc/pbc/gto.py:47-49; make_pbc_gto is called without rcut,
+// hqc/pbc/solver.py:211,217), and the S/T sphere |t| <= rcut of the
+// meshgrid of -tmax..tmax, tmax = rcut // L (solver.py:162-176).
+static void box_lattices(double L, double rcut, std::vector<double> &lat1d, std::vector<double> &lattice) {
+  lat1d.clear();
+  const double t1 = std::floor(24.0 / L);
+  for (double t = -t1; t <= t1; t += 1.0) lat1d.push_back(t * L);
+  lattice.clear();
+  const double tm = std::floor(rcut / L);
+  std::vector<double> nt;
+  for (double t = -tm; t <= tm; t += 1.0) nt.push_back(t);
+  for (double yi : nt)
+    for (double xj : nt)
+      for (double zk : nt) {
+        const double x = xj * L, y = yi * L, z = zk * L;
+        if (x * x + y * y + z * z <= rcut * rcut) {
+          lattice.push_back(x);
+          lattice.push_back(y);
+          lattice.push_back(z);
+        }
+      }
+}
+
+// Reset the box-dependent tables of a plan to side L (Bohr): lattices,
+// Coulomb table, exchange pair weights, cell volume.  Stream-ordered on st.
+static void set_box(hqcgb_plan *p, double L, double rcut, cudaStream_t st) {
+  HQ_REQUIRE(L > 0, "L must be positive");
+  box_lattices(L, rcut, p->h_lat1d, p->h_lattice);
+  const int n1 = (int)p->h_lat1d.size(), n3 = (int)p->h_lattice.size() / 3;
+  if (n1 > p->lat1d_cap) {
+    p->lat1d = p->alloc<double>(n1);
+    p->lat1d_cap = n1;
+  }
+  if (n3 > p->lattice_cap) {
+    p->lattice = p->alloc<double>(3 * (size_t)n3);
+    p->lattice_cap = n3;
+  }
+  HQ_CUDA(cudaMemcpyAsync(p->lat1d, p->h_lat1d.data(), sizeof(double) * n1, cudaMemcpyHostToDevice, st));
+  HQ_CUDA(cudaMemcpyAsync(p->lattice, p->h_lattice.data(), sizeof(double) * 3 * n3, cudaMemcpyHostToDevice, st));
+  p->P.n_lat1d = n1;
+  p->P.n_lattice = n3;
+  p->P.L = L;
+  p->L = L;
+  p->Omega = L * L * L;
+  p->dV = p->Omega / (double)p->N;
+  launch_coulomb_table(p->ng, p->L, p->coul, st);
+  if (p->exx_fused) {
+    if (p->mixed) launch_exx_weights<float>(p->ng, p->L, p->dV, static_cast<float *>(p->exx_wsq), st);
+    else launch_exx_weights<double>(p->ng, p->L, p->dV, static_cast<double *>(p->exx_wsq), st);
+  }
+  // host copies must outlive the copies from pageable memory
+  HQ_CUDA(cudaStreamSynchronize(st));
+}
+
+struct hqcgb_batch {
+  hqcgb_params base{};
+  std::vector<double> h_alpha, h_coef;
+  std::vector<int> h_l, h_cart;
+  double rcut = 24.0;
+  int workers = 1;
+  // per worker: size class (n_atoms, n_grid) -> workspace; its stream
+  std::vector<std::map<std::pair<int, int>, hqcgb_plan *>> plans;
+  std::vector<cudaStream_t> streams;
+  ~hqcgb_batch() {
+    for (auto &m : plans)
+      for (auto &kv : m) delete kv.second;
+    for (cudaStream_t s : streams) cudaStreamDestroy(s);
+  }
+};
+
+static hqcgb_plan *batch_plan(hqcgb_batch *b, int t, int n_atoms, int n_grid, double L) {
+  auto key = std::make_pair(n_atoms, n_grid);
+  auto it = b->plans[t].find(key);
+  if (it != b->plans[t].end()) return it->second;
+  std::vector<double> l1, lat;
+  box_lattices(L, b->rcut, l1, lat);
+  hqcgb_params q = b->base;
+  q.n_atoms = n_atoms;
+  q.n_grid = n_grid;
+  q.L = L;
+  q.alpha = b->h_alpha.data();
+  q.coef = b->h_coef.data();
+  q.ao_l = b->h_l.data();
+  q.ao_cart = b->h_cart.data();
+  q.n_lat1d = (int)l1.size();
+  q.lat1d = l1.data();
+  q.n_lattice = (int)lat.size() / 3;
+  q.lattice = lat.data();
+  hqcgb_plan *p = new hqcgb_plan();
+  try {
+    create(&q, p);
+  } catch (...) {
+    delete p;
+    throw;
+  }
+  b->plans[t][key] = p;
+  return p;
+}
+
+static int run_uneven(hqcgb_batch *b, int n_cfg, const int *n_atoms, const int *n_grid, const double *L,
+                      const double *xp, const hqcgb_scf_out *out, double *grad, cudaStream_t st) {
+  std::vector<long long> xoff(n_cfg + 1, 0), aoff(n_cfg + 1, 0), moff(n_cfg + 1, 0);
+  for (int c = 0; c < n_cfg; ++c) {
+    HQ_REQUIRE(n_atoms[c] >= 1 && n_grid[c] >= 3 && L[c] > 0, "bad configuration size");
+    const long long nao = (long long)n_atoms[c] * b->base.nao_atom;
+    xoff[c + 1] = xoff[c] + 3LL * n_atoms[c];
+    aoff[c + 1] = aoff[c] + nao;
+    moff[c + 1] = moff[c] + nao * nao;
+  }
+  // largest configurations first (their workers finish last otherwise)
+  std::vector<int> order(n_cfg);
+  for (int c = 0; c < n_cfg; ++c) order[c] = c;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
+    return (long long)n_atoms[a] * n_grid[a] * n_grid[a] * n_grid[a] >
+           (long long)n_atoms[c] * n_grid[c] * n_grid[c] * n_grid[c];
+  });
+  const int nthreads = std::max(1, std::min(b->workers, n_cfg));
+  while ((int)b->plans.size() < nthreads) b->plans.emplace_back();
+  while ((int)b->streams.size() < nthreads) {
+    cudaStream_t s;
+    HQ_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    b->streams.push_back(s);
+  }
+  int dev = 0;
+  HQ_CUDA(cudaGetDevice(&dev));
+  HQ_CUDA(cudaStreamSynchronize(st));  // inputs may still be in flight on the caller's stream
+  std::atomic<int> next{0};
+  std::vector<int> status(n_cfg, HQCGB_OK);
+  std::vector<std::string> msg(n_cfg);
+  auto work = [&](int t) {
+    cudaStream_t qs = b->streams[t];
+    cudaSetDevice(dev);
+    for (int k = next++; k < n_cfg; k = next++) {
+      const int c = order[k];
+      try {
+        hqcgb_plan *q = batch_plan(b, t, n_atoms[c], n_grid[c], L[c]);
+        if (q->L != L[c]) set_box(q, L[c], b->rcut, qs);
+        hqcgb_scf_out o{};
+        if (out->mo_coeff) o.mo_coeff = out->mo_coeff + moff[c];
+        if (out->dm) o.dm = out->dm + moff[c];
+        if (out->bands) o.bands = out->bands + aoff[c];
+        if (out->energies) o.energies = out->energies + 5LL * c;
+        if (out->converged) o.converged = out->converged + c;
+        if (out->iterations) o.iterations = out->iterations + c;
+        if (out->free_energy) o.free_energy = out->free_energy + c;
+        status[c] = scf_one(q, xp + xoff[c], &o, qs);
+        if (grad) forces(q, grad + xoff[c], qs);
+        HQ_CUDA(cudaStreamSynchronize(qs));
+      } catch (const Error &e) {
+        status[c] = e.status;
+        msg[c] = e.msg;
+      } catch (const std::exception &e) {
+        status[c] = HQCGB_CUDA_ERROR;
+        msg[c] = e.what();
+      }
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nthreads; ++t) pool.emplace_back(work, t);
+  work(0);
+  for (auto &th : pool) th.join();
+  int worst = HQCGB_OK;
+  for (int c = 0; c < n_cfg; ++c) {
+    if (status[c] > HQCGB_NOT_CONVERGED)
+      throw Error{status[c], "configuration " + std::to_string(c) + ": " + msg[c]};
+    worst = std::max(worst, status[c]);
   }
   return worst;
 }
@@ -1042,6 +1383,42 @@ int hqcgb_pes_batch(hqcgb_plan *plan, int n_cfg, const double *xp, const hqcgb_s
     HQ_REQUIRE(plan && xp && out && n_cfg >= 0, "null argument");
     HQ_REQUIRE(!grad || plan->P.want_forces, "plan was created without want_forces");
     return run_batch(plan, n_cfg, xp, out, grad, (cudaStream_t)stream);
+  });
+}
+
+int hqcgb_batch_create(const hqcgb_params *base, double rcut, int workers, hqcgb_batch **batch) {
+  HQ_GUARD({
+    HQ_REQUIRE(base && batch, "null argument");
+    HQ_REQUIRE(workers >= 1 && workers <= 64, "workers must be in [1, 64]");
+    HQ_REQUIRE(rcut > 0, "rcut must be positive");
+    HQ_REQUIRE(base->nao_atom >= 1 && base->n_prim >= 1 && base->alpha && base->coef && base->ao_l &&
+                   base->ao_cart, "empty basis");
+    hqcgb_batch *b = new hqcgb_batch();
+    b->base = *base;
+    b->h_alpha.assign(base->alpha, base->alpha + base->n_prim);
+    b->h_coef.assign(base->coef, base->coef + base->nao_atom * base->n_prim);
+    b->h_l.assign(base->ao_l, base->ao_l + base->nao_atom);
+    b->h_cart.assign(base->ao_cart, base->ao_cart + base->nao_atom);
+    b->rcut = rcut;
+    b->workers = workers;
+    *batch = b;
+    return HQCGB_OK;
+  });
+}
+
+int hqcgb_batch_destroy(hqcgb_batch *batch) {
+  HQ_GUARD({
+    delete batch;
+    return HQCGB_OK;
+  });
+}
+
+int hqcgb_batch_run(hqcgb_batch *batch, int n_cfg, const int *n_atoms, const int *n_grid, const double *L,
+                    const double *xp, const hqcgb_scf_out *out, double *grad, void *stream) {
+  HQ_GUARD({
+    HQ_REQUIRE(batch && n_atoms && n_grid && L && xp && out && n_cfg >= 0, "null argument");
+    HQ_REQUIRE(!grad || batch->base.want_forces, "batch was created without want_forces");
+    return run_uneven(batch, n_cfg, n_atoms, n_grid, L, xp, out, grad, (cudaStream_t)stream);
   });
 }
 

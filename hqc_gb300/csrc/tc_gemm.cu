@@ -1517,10 +1517,15 @@ void launch_tc_psi_density(const float *phiT, const float *dphiT, const float *Y
 // ---------------------------------------------------------------------------
 int tc_quad_chunk() { return 2048; }
 
-size_t tc_quad_partial_doubles(int nao, long long N) {
+size_t tc_quad_partial_doubles(int nao, long long N, int kchunk) {
   int mt = ceil_div(nao, tc::kM), nt = ceil_div(nao, tc::kN);
-  long long chunks = ceil_div(N, tc_quad_chunk());
+  long long chunks = ceil_div(N, kchunk > 0 ? kchunk : tc_quad_chunk());
   return (size_t)chunks * mt * nt * tc::kM * tc::kN;
+}
+
+int tc_quad_tiles(int nao, bool sym) {
+  const int nb = ceil_div(nao, tc::kM);
+  return sym ? nb * (nb + 1) / 2 : nb * nb;
 }
 
 // Tile plan of the quadrature for nao AOs in 128-row blocks: which CTA writes
@@ -1609,9 +1614,11 @@ static QuadTilePlan plan_quad_tiles(int nao, bool sym) {
 // symmetric (only tiles nt >= mt are computed; the reduce mirrors them).
 void launch_tc_quad_split(const float *Ahl, const float *Bhl, int nao, long long N, long long ld,
                           bool sym, bool add_transpose, double scale, double *partial, double *M,
-                          int *err, cudaStream_t st, int drain) {
+                          int *err, cudaStream_t st, int drain, int kchunk) {
   HQ_STAGE(ST_QUAD, st);
   HQ_REQUIRE(drain >= 1, "drain must be >= 1");
+  if (kchunk <= 0) kchunk = tc_quad_chunk();
+  HQ_REQUIRE(kchunk % tc::kStageK == 0, "K chunk must be a multiple of 32");
   HQ_REQUIRE(ld % 32 == 0 && ld >= N, "pre-split operands need a row stride that is a multiple of 32");
   HQ_REQUIRE(N <= (1LL << 31) - 64, "grid too large for 32-bit TMA coordinates");
   ensure_dyn_smem((const void *)tc::k_tc_quad_tma, tc::kQtSmem);
@@ -1627,12 +1634,12 @@ void launch_tc_quad_split(const float *Ahl, const float *Bhl, int nao, long long
   CUtensorMap mAl16 = tc::tensor_map_2d_ext(Al, ld, N, rows, 16);
   CUtensorMap mBh16 = tc::tensor_map_2d_ext(Bh, ld, N, rows, 16);
   CUtensorMap mBl16 = tc::tensor_map_2d_ext(Bl, ld, N, rows, 16);
-  const int chunks = ceil_div(N, tc_quad_chunk());
+  const int chunks = ceil_div(N, kchunk);
   if (plan.fused) {
     ensure_dyn_smem((const void *)tc::k_tc_quad_fused, tc::kQfSmem);
     tc::QfArgs f = plan.f;
     f.N = N;
-    f.kchunk = tc_quad_chunk();
+    f.kchunk = kchunk;
     f.drain = drain;
     f.mtiles = nblk;
     f.ntiles = nblk;
@@ -1644,7 +1651,7 @@ void launch_tc_quad_split(const float *Ahl, const float *Bhl, int nao, long long
   }
   for (tc::QtArgs a : plan.lists) {
     a.N = N;
-    a.kchunk = tc_quad_chunk();
+    a.kchunk = kchunk;
     a.drain = drain;
     a.mtiles = nblk;
     a.ntiles = nblk;

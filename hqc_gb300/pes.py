@@ -2,9 +2,15 @@
 
 ``pes(xp)`` returns E + Vpp in Rydberg (mode 'default') or the 7-tuple
 (E + Vpp, Ki, Vep, Vee, Vpp, Se, converged) in mode 'dev'.  With
-``forces=True``, ``pes.value_and_grad(xp)`` returns (E + Vpp, d/dxp) in
-Rydberg per rs unit from the engine's adjoint (absent from the reference;
-under Fermi smearing the electronic part is the gradient of E - sigma*Se).
+``forces=True``, ``pes.value_and_grad(xp)`` returns a matching pair
+(F + Vpp, d(F + Vpp)/dxp) in Rydberg (per rs unit) from the engine's adjoint
+(absent from the reference).  F is the free energy E - sigma S whose exact
+gradient the adjoint computes: without smearing F = E, so the value is
+``pes(xp)``; with smearing S is the entropy that makes the smeared
+occupations stationary (Fermi: the reference's Se; Gaussian:
+sum exp(-x^2) / (2 sqrt(pi))), while ``pes(xp)`` keeps the reference's
+internal energy E (hqc/pbc/pes.py:86), whose gradient would need the
+occupations' response.
 ``gamma=False`` gives ``pes(xp, kpt)`` (pes_kpt / pes_dev_kpt,
 pes.py:88-137), without forces.
 """
@@ -53,15 +59,16 @@ def make_pes(n, L, rs, basis, rcut=24, tol=1e-7, max_cycle=100, grid_length=0.12
         return E + Vpp
 
     def value_and_grad(xp):
-        """(E + Vpp, d/dxp); a batch (B, n, 3) gives (B,) and (B, n, 3)."""
+        """(F + Vpp, d(F + Vpp)/dxp), F = E - sigma S (E without smearing); a
+        batch (B, n, 3) gives (B,) and (B, n, 3)."""
         xp = _arr(xp)
         if xp.ndim == 3:
             out = solver.batch(xp, forces=True, full=False)
             Vpp, gpp = _vpp(xp)
-            return out["energies"][:, 0] * RY + Vpp, out["grad"] * (RY * rs) + gpp
-        out = solver(xp)
+            return out["free_energy"] * RY + Vpp, out["grad"] * (RY * rs) + gpp
+        solver(xp)
         Vpp, gpp = _vpp(xp)
-        return out[3] + Vpp, solver.grad() + gpp
+        return solver.free_energy + Vpp, solver.grad() + gpp
 
     pes.solver = solver
     pes.value_and_grad = value_and_grad

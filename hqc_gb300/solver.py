@@ -56,6 +56,52 @@ def xc_code(xc):
     return _lib.XC[key]
 
 
+def build_params(n, L_bohr, ng, basis, rcut, tol, max_cycle, diis, diis_space, diis_start_cycle,
+                 diis_damp, dft, xc, smearing, smearing_method, smearing_sigma, search_method,
+                 search_cycle, search_tol, precision, forces, exx_occ_threshold):
+    """The engine's hqcgb_params for one system; returns (params, arrays the
+    params point into, AOs per atom)."""
+    alpha, coef, ls, carts = basis_tables(basis)
+    lat1 = lattice_1d(L_bohr)
+    lat = lattice_sphere(L_bohr, rcut)
+    keep = [alpha, coef, ls, carts, lat1, lat]
+    P = _lib.Params()
+    P.n_atoms = n
+    P.n_grid = ng
+    P.L = L_bohr
+    P.nao_atom = coef.shape[0]
+    P.n_prim = alpha.size
+    P.alpha = alpha.ctypes.data_as(_lib.c_double_p)
+    P.coef = coef.ctypes.data_as(_lib.c_double_p)
+    P.ao_l = ls.ctypes.data_as(_lib.c_int_p)
+    P.ao_cart = carts.ctypes.data_as(_lib.c_int_p)
+    P.n_lat1d = lat1.size
+    P.lat1d = lat1.ctypes.data_as(_lib.c_double_p)
+    P.n_lattice = lat.shape[0]
+    P.lattice = lat.ctypes.data_as(_lib.c_double_p)
+    P.dft = int(bool(dft))
+    P.xc = xc_code(xc) if dft else 0
+    P.smearing = int(bool(smearing))
+    if smearing:
+        assert smearing_method in SMEAR
+        assert search_method in SEARCH
+    P.smearing_method = SMEAR.get(smearing_method, 0)
+    P.smearing_sigma = float(smearing_sigma)
+    P.search_method = SEARCH.get(search_method, 0)
+    P.search_cycle = int(search_cycle)
+    P.search_tol = float(search_tol)
+    P.tol = float(tol)
+    P.max_cycle = int(max_cycle)
+    P.diis = int(bool(diis))
+    P.diis_space = int(diis_space)
+    P.diis_start_cycle = int(diis_start_cycle)
+    P.diis_damp = float(diis_damp)
+    P.precision = PRECISION[precision]
+    P.exx_occ_threshold = float(exx_occ_threshold)
+    P.want_forces = int(bool(forces))
+    return P, keep, coef.shape[0]
+
+
 class Plan:
     """Owns one engine plan (device workspace for one system size)."""
 
@@ -66,51 +112,15 @@ class Plan:
         lib = _lib.load()
         if not torch.cuda.is_available():
             raise RuntimeError("hqc_gb300 needs a CUDA GPU (no CPU fallback)")
-        alpha, coef, ls, carts = basis_tables(basis)
         self.n = n
-        self.nao_atom = coef.shape[0]
-        self.nao = n * self.nao_atom
         self.L = L_bohr
         self.ng = grid_size(L_bohr, grid_length) if n_grid is None else int(n_grid)
         self.dft = bool(dft)
-        lat1 = lattice_1d(L_bohr)
-        lat = lattice_sphere(L_bohr, rcut)
-        keep = [alpha, coef, ls, carts, lat1, lat]
-        self._keep = keep
-        P = _lib.Params()
-        P.n_atoms = n
-        P.n_grid = self.ng
-        P.L = L_bohr
-        P.nao_atom = self.nao_atom
-        P.n_prim = alpha.size
-        P.alpha = alpha.ctypes.data_as(_lib.c_double_p)
-        P.coef = coef.ctypes.data_as(_lib.c_double_p)
-        P.ao_l = ls.ctypes.data_as(_lib.c_int_p)
-        P.ao_cart = carts.ctypes.data_as(_lib.c_int_p)
-        P.n_lat1d = lat1.size
-        P.lat1d = lat1.ctypes.data_as(_lib.c_double_p)
-        P.n_lattice = lat.shape[0]
-        P.lattice = lat.ctypes.data_as(_lib.c_double_p)
-        P.dft = int(bool(dft))
-        P.xc = xc_code(xc) if dft else 0
-        P.smearing = int(bool(smearing))
-        if smearing:
-            assert smearing_method in SMEAR
-            assert search_method in SEARCH
-        P.smearing_method = SMEAR.get(smearing_method, 0)
-        P.smearing_sigma = float(smearing_sigma)
-        P.search_method = SEARCH.get(search_method, 0)
-        P.search_cycle = int(search_cycle)
-        P.search_tol = float(search_tol)
-        P.tol = float(tol)
-        P.max_cycle = int(max_cycle)
-        P.diis = int(bool(diis))
-        P.diis_space = int(diis_space)
-        P.diis_start_cycle = int(diis_start_cycle)
-        P.diis_damp = float(diis_damp)
-        P.precision = PRECISION[precision]
-        P.exx_occ_threshold = float(exx_occ_threshold)
-        P.want_forces = int(bool(forces))
+        P, self._keep, self.nao_atom = build_params(
+            n, L_bohr, self.ng, basis, rcut, tol, max_cycle, diis, diis_space, diis_start_cycle,
+            diis_damp, dft, xc, smearing, smearing_method, smearing_sigma, search_method,
+            search_cycle, search_tol, precision, forces, exx_occ_threshold)
+        self.nao = n * self.nao_atom
         self.params = P
         self.device = torch.device("cuda", torch.cuda.current_device())
         h = ctypes.c_void_p()
@@ -136,9 +146,11 @@ class Plan:
                    bands=torch.empty(nao, dtype=torch.float64, device=dev),
                    energies=torch.empty(5, dtype=torch.float64, device=dev),
                    converged=torch.zeros(1, dtype=torch.int32, device=dev),
-                   iterations=torch.zeros(1, dtype=torch.int32, device=dev))
+                   iterations=torch.zeros(1, dtype=torch.int32, device=dev),
+                   free_energy=torch.empty(1, dtype=torch.float64, device=dev))
         o = _lib.ScfOut(*[ctypes.c_void_p(out[k].data_ptr()) for k in
-                          ("mo_coeff", "dm", "bands", "energies", "converged", "iterations")])
+                          ("mo_coeff", "dm", "bands", "energies", "converged", "iterations",
+                           "free_energy")])
         xp_bohr = xp_bohr.contiguous()
         st = lib.hqcgb_scf(self.handle, ctypes.c_void_p(xp_bohr.data_ptr()), ctypes.byref(o),
                            self.stream())
@@ -156,9 +168,11 @@ class Plan:
                    bands=torch.empty(B, nao, dtype=torch.float64, device=dev),
                    energies=torch.empty(B, 5, dtype=torch.float64, device=dev),
                    converged=torch.zeros(B, dtype=torch.int32, device=dev),
-                   iterations=torch.zeros(B, dtype=torch.int32, device=dev))
+                   iterations=torch.zeros(B, dtype=torch.int32, device=dev),
+                   free_energy=torch.empty(B, dtype=torch.float64, device=dev))
         o = _lib.ScfOut(*[ctypes.c_void_p(out[k].data_ptr()) for k in
-                          ("mo_coeff", "dm", "bands", "energies", "converged", "iterations")])
+                          ("mo_coeff", "dm", "bands", "energies", "converged", "iterations",
+                           "free_energy")])
         xps_bohr = xps_bohr.contiguous()
         k = np.ascontiguousarray(kpts, dtype=np.float64).reshape(B, 3)
         st = lib.hqcgb_scf_kpt_batch(self.handle, B, ctypes.c_void_p(xps_bohr.data_ptr()),
@@ -180,13 +194,14 @@ class Plan:
         out = dict(bands=torch.empty(B, nao, dtype=torch.float64, device=dev),
                    energies=torch.empty(B, 5, dtype=torch.float64, device=dev),
                    converged=torch.zeros(B, dtype=torch.int32, device=dev),
-                   iterations=torch.zeros(B, dtype=torch.int32, device=dev))
+                   iterations=torch.zeros(B, dtype=torch.int32, device=dev),
+                   free_energy=torch.empty(B, dtype=torch.float64, device=dev))
         if full:
             out["mo_coeff"] = torch.empty(B, nao, nao, dtype=torch.float64, device=dev)
             out["dm"] = torch.empty(B, nao, nao, dtype=torch.float64, device=dev)
         ptr = lambda k: ctypes.c_void_p(out[k].data_ptr()) if k in out else ctypes.c_void_p(0)
         o = _lib.ScfOut(*[ptr(k) for k in ("mo_coeff", "dm", "bands", "energies", "converged",
-                                            "iterations")])
+                                            "iterations", "free_energy")])
         g = torch.empty(B, self.n, 3, dtype=torch.float64, device=dev) if forces else None
         xps_bohr = xps_bohr.contiguous()
         st = lib.hqcgb_pes_batch(self.handle, B, ctypes.c_void_p(xps_bohr.data_ptr()), ctypes.byref(o),
@@ -285,6 +300,7 @@ def make_solver(n: int, L: float, rs: float, basis: str,
         assert xp_t.dim() == 3 and xp_t.shape[1] == n
         out = plan.scf_batch(xp_t * rs, forces=forces, full=full)
         solver.iterations = out["iterations"].tolist()
+        solver.free_energy = out["free_energy"] * RY
         return out
 
     def solver(xp):
@@ -298,11 +314,15 @@ def make_solver(n: int, L: float, rs: float, basis: str,
         out = plan.scf(xp_t * rs)
         e = out["energies"]
         solver.iterations = int(out["iterations"].item())
+        solver.free_energy = out["free_energy"][0] * RY
         return (out["mo_coeff"], out["dm"], out["bands"] * RY, e[0] * RY, e[1] * RY, e[2] * RY,
                 e[3] * RY, e[4], out["converged"][0] != 0)
 
     def grad(xp=None):
-        """dE/dxp (Rydberg per rs unit) of the last call (needs forces=True)."""
+        """Gradient (Rydberg per rs unit) of the last call's free energy
+        ``solver.free_energy`` = E - sigma S (E itself without smearing; S the
+        entropy that makes the smeared occupations stationary); needs
+        forces=True."""
         return plan.forces() * (RY * rs)
 
     solver.plan = plan

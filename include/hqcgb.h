@@ -84,6 +84,13 @@ typedef struct {
   double *energies;   /* [5]: E, Ki, Vep, Vee (Hartree), Se (device) */
   int *converged;     /* [1] (device) */
   int *iterations;    /* [1] (device), may be NULL */
+  /* [1] (device), may be NULL: the free energy E - sigma * S (Hartree) whose
+   * gradient hqcgb_forces returns, S the entropy that makes the smearing's
+   * occupations stationary -- Fermi: Se (the energies[4] slot); Gaussian:
+   * sum_i exp(-x_i^2) / (2 sqrt(pi)), x_i = (eps_i - mu) / sigma; without
+   * smearing it equals E.  No counterpart in the reference, whose E excludes
+   * -sigma*S (hqc/pbc/scf.py:149,209). */
+  double *free_energy;
 } hqcgb_scf_out;
 
 typedef struct hqcgb_plan hqcgb_plan;
@@ -120,6 +127,35 @@ int hqcgb_plan_set_concurrency(hqcgb_plan *plan, int workers);
  * reported with its index. */
 int hqcgb_pes_batch(hqcgb_plan *plan, int n_cfg, const double *xp, const hqcgb_scf_out *out,
                     double *grad, void *stream);
+
+/* ---- uneven batches --------------------------------------------------------
+ * Energies (and gradients) of configurations that differ in atom count, box
+ * and grid, in one call.  The reference batches with jax.vmap over
+ * configurations of one shape (test/test.py:157,179); uneven sizes need one
+ * vmapped call per shape there.  A batch groups configurations into size
+ * classes (n_atoms, n_grid): each of `workers` host threads keeps one
+ * workspace per size class (created on first use, kept until
+ * hqcgb_batch_destroy) and resets its box-dependent tables per
+ * configuration. */
+typedef struct hqcgb_batch hqcgb_batch;
+
+/* base: basis and method as for hqcgb_plan_create (n_atoms, n_grid, L and
+ * the lattice fields are ignored: every configuration brings its own);
+ * rcut (Bohr): the S/T lattice sphere (make_solver's rcut, solver.py:162-176;
+ * the grid GTO sums use 24 Bohr as make_pbc_gto does). */
+int hqcgb_batch_create(const hqcgb_params *base, double rcut, int workers, hqcgb_batch **batch);
+int hqcgb_batch_destroy(hqcgb_batch *batch);
+
+/* n_cfg configurations: n_atoms, n_grid, L [n_cfg] (HOST; L in Bohr); xp the
+ * concatenation of every configuration's [n_atoms][3] positions (device,
+ * Bohr).  Outputs are concatenated the same way (each may be NULL):
+ * mo_coeff, dm [nao_c][nao_c] each; bands [nao_c] each; energies [n_cfg][5];
+ * converged, iterations, free_energy [n_cfg]; grad (want_forces) [n_atoms_c][3]
+ * each (Hartree/Bohr, the gradient of free_energy).  Returns the worst
+ * status; an error names the configuration. */
+int hqcgb_batch_run(hqcgb_batch *batch, int n_cfg, const int *n_atoms, const int *n_grid,
+                    const double *L, const double *xp, const hqcgb_scf_out *out, double *grad,
+                    void *stream);
 
 /* AO values of n_atoms protons at npts points (electron positions), Gamma
  * point: the reference's eval_pbc_ao (hqc/pbc/gto.py:326-369) with the 1D

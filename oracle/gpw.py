@@ -396,6 +396,9 @@ class Solver:
                               search_method, search_cycle, search_tol)
         self.exx_thr = exx_occ_threshold
         self.iterations = 0
+        # called with a label after the geometry set-up and after every SCF
+        # iteration (timing of a CPU evaluation's pieces); may raise to stop
+        self.on_unit = None
 
     # grid pieces --------------------------------------------------------
     def density(self, D, phi, grad=None):
@@ -466,6 +469,7 @@ class Solver:
     def solve(self, xp_rs, kpt=None):
         """One SCF; ``kpt`` (3,) in 1/Bohr selects the k-point solver."""
         g = self.setup_geometry(xp_rs, kpt)
+        self._unit("geometry")
         S, T, V, phi, grad = g["S"], g["T"], g["V"], g["phi"], g["grad"]
         cplx = np.iscomplexobj(S)
         w, u = np.linalg.eigh(S)
@@ -510,6 +514,10 @@ class Solver:
         self.last = dict(g=g, C=C, e=e, D=D, occ=occf(e), E=E, v=v)
         return C, D, e * RY, E * RY, Ki * RY, Vep * RY, Vee * RY, Se, conv
 
+    def _unit(self, label):
+        if self.on_unit is not None:
+            self.on_unit(label)
+
     def _fixed_point(self, H, D, C, e, diag, dmat, veff):
         """``fixed_point_scf`` (scf.py:21-88)."""
         E0, E1, loop = 0.0, 1.0, 0
@@ -519,6 +527,7 @@ class Solver:
             C, e = diag(H + J + Vxc)
             D = dmat(C, e)
             E0, E1, loop = E1, Enew, loop + 1
+            self._unit("scf")
         self.iterations = loop
         return C, e, E1, loop != self.max_cycle
 
@@ -541,6 +550,7 @@ class Solver:
             Fk = Fk[1:] + [F]
             ek = ek[1:] + [err]
             E0, E1, loop = E1, Enew, loop + 1
+            self._unit("scf")
         E0 = E1 - 1.0
         while ((abs(E1 - E0) > self.tol) or (np.linalg.norm(ek[-1]) > 10 * self.tol)) \
                 and loop < self.max_cycle:
@@ -566,5 +576,6 @@ class Solver:
             Fk = Fk[1:] + [F]
             ek = ek[1:] + [err]
             E0, E1, loop = E1, Enew, loop + 1
+            self._unit("scf")
         self.iterations = loop
         return C, e, E1, loop != self.max_cycle

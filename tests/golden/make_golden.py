@@ -261,11 +261,73 @@ def run_vpp_case():
     return rec, meta
 
 
+# Central finite differences of the reference's own make_pes energy
+# (pes_gamma, hqc/pbc/pes.py:78-86: E + Vpp in Ry, xp in rs units).  The
+# reference has no forces (doc/solver_algorithm.md:1210) and its SCF
+# while_loop is not reverse-differentiable, so these differences of its
+# energy are what pins the engine's analytic gradient to the reference.
+# name -> (n, rs, basis, seed, kwargs, n_coords): n_coords coordinates drawn
+# from numpy.random.default_rng(seed + 100) (None: every coordinate).  The
+# SCF and the chemical-potential search run to near machine precision so the
+# differences carry ~1e-8 Ry/rs of noise; smeared cases use the Newton search
+# (the bisection's return rule leaves N(mu) != n, so its energy has no
+# stationary free energy) and record Se so that E - sigma Se can be
+# differenced as well.
+FD_H = 1e-4
+FD_TIGHT = dict(tol=1e-10, max_cycle=300)
+FD_CASES = {
+    "fd_hf_szv": (4, 1.5, "gth-szv", 42, dict(grid_length=0.12, **FD_TIGHT), None),
+    "fd_hf_dzv": (4, 1.5, "gth-dzv", 42, dict(grid_length=0.12, **FD_TIGHT), None),
+    "fd_hf_dzv_fermi": (4, 1.5, "gth-dzv", 42,
+                        dict(grid_length=0.12, smearing=True, smearing_method="fermi",
+                             smearing_sigma=0.1, search_method="newton", search_tol=1e-13,
+                             search_cycle=200, **FD_TIGHT), None),
+    "fd_lda_dzvp": (4, 1.5, "gth-dzvp", 42,
+                    dict(grid_length=0.25, dft=True, xc="lda,vwn", **FD_TIGHT), 6),
+}
+
+
+def run_fd_case(name):
+    n, rs, basis, seed, kw, ncoord = FD_CASES[name]
+    L = box(n)
+    xp = uniform_positions(n, seed)
+    t0 = time.time()
+    pes = make_pes(n, L, rs, basis, mode="dev", **kw)
+    sigma = kw.get("smearing_sigma", 0.0) if kw.get("smearing") else 0.0
+
+    def ev(x):
+        Etot, Ki, Vep, Vee, Vpp, Se, conv = pes(jnp.array(x.copy()))
+        assert bool(np.asarray(conv)), "reference SCF did not converge"
+        return float(np.asarray(Etot)), float(np.asarray(Se)), float(np.asarray(Vpp))
+
+    coords = [(a, d) for a in range(n) for d in range(3)]
+    if ncoord is not None:
+        pick = np.random.default_rng(seed + 100).choice(len(coords), ncoord, replace=False)
+        coords = [coords[i] for i in sorted(pick)]
+    E0, S0, V0 = ev(xp)
+    dE, dF = [], []
+    for a, d in coords:
+        vals = []
+        for sgn in (1.0, -1.0):
+            x = xp.copy()
+            x[a, d] += sgn * FD_H
+            vals.append(ev(x))
+        (Ep, Sp, _), (Em, Sm, _) = vals
+        dE.append((Ep - Em) / (2 * FD_H))
+        # free energy F = E - sigma Se (sigma in Hartree, E in Ry: factor 2)
+        dF.append(((Ep - 2 * sigma * Sp) - (Em - 2 * sigma * Sm)) / (2 * FD_H))
+    rec = dict(xp=xp, n=n, rs=rs, L=L, h=FD_H, coords=np.array(coords), Etot=E0, Se=S0, Vpp=V0,
+               dEtot=np.array(dE), dFtot=np.array(dF), sigma=sigma)
+    meta = dict(factory="pes_fd", n=n, rs=rs, basis=basis, seed=seed, kwargs=kw, h=FD_H,
+                coords=len(coords), seconds=round(time.time() - t0, 2))
+    return rec, meta
+
+
 def main(selected):
     manifest_path = os.path.join(HERE, "manifest.json")
     manifest = json.load(open(manifest_path)) if os.path.exists(manifest_path) else {}
     jobs = list(SOLVER_CASES) + ["gto_values", "gto_values_kpt", "vpp", "coulomb_pe", "overlap",
-                                 "slater"]
+                                 "slater"] + list(FD_CASES)
     if selected:
         jobs = [j for j in jobs if j in selected]
     for name in jobs:
@@ -282,6 +344,8 @@ def main(selected):
             rec, meta = run_slater_case()
         elif name == "vpp":
             rec, meta = run_vpp_case()
+        elif name in FD_CASES:
+            rec, meta = run_fd_case(name)
         else:
             rec, meta = run_solver_case(name)
         np.savez(os.path.join(HERE, name + ".npz"), **rec)

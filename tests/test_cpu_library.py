@@ -228,7 +228,9 @@ def test_pes_host_logic_with_stand_in_engine(monkeypatch):
 
         def batch(xp, forces=False, full=True):
             x = torch.as_tensor(xp, dtype=torch.float64)
-            return {"energies": torch.stack([x.sum(dim=(-2, -1)) / 2.0] * 5, -1), "grad": x / 2.0}
+            # engine outputs in Hartree; the free energy differs from E (smearing)
+            return {"energies": torch.stack([x.sum(dim=(-2, -1)) / 2.0] * 5, -1), "grad": x / 2.0,
+                    "free_energy": x.sum(dim=(-2, -1)) / 2.0 - 0.25}
 
         solver.batch = batch
         solver.grad = lambda: None
@@ -251,8 +253,10 @@ def test_pes_host_logic_with_stand_in_engine(monkeypatch):
         pes(xp, np.zeros(3))
     dev = pes_mod.make_pes(2, 2.0, 1.3, "gth-szv", mode="dev")(xp)
     assert len(dev) == 7 and abs(float(dev[4]) - 200.0) < 1e-12 and float(dev[1]) == 2.0
-    E, g = pes.value_and_grad(xb)  # batch: engine energies in Ha -> Ry, gradients per rs unit
-    np.testing.assert_allclose(E.numpy(), [2.1 + 200.0, 1.0 + 200.0])
+    # batch: the engine's free energy (the gradient's own function) in Ha -> Ry,
+    # gradients per rs unit
+    E, g = pes.value_and_grad(xb)
+    np.testing.assert_allclose(E.numpy(), [2.1 - 0.5 + 200.0, 1.0 - 0.5 + 200.0])
     np.testing.assert_allclose(g.numpy(), np.asarray(xb) / 2.0 * 2.0 * 1.3 + 7.0)
     kp = pes_mod.make_pes(2, 2.0, 1.3, "gth-szv", gamma=False)
     assert abs(float(kp(xp, np.array([0.5, 0.0, 0.0]))) - (2.6 + 200.0)) < 1e-12

@@ -170,6 +170,28 @@ def test_oracle_gradient_matches_finite_differences(kw):
         assert abs(fd - g[a, d]) < 2e-6, (a, d, fd, g[a, d])
 
 
+@pytest.mark.parametrize("name", ["fd_hf_szv", "fd_hf_dzv", "fd_hf_dzv_fermi", "fd_lda_dzvp"])
+def test_oracle_gradient_matches_reference_fd(name):
+    """The oracle's analytic gradient (electronic + Ewald, Ry per rs unit)
+    against central differences of the reference's own make_pes energy
+    (tests/golden/make_golden.py, FD_CASES), and the energies themselves.
+    With Fermi smearing the gradient is that of E - sigma Se, not of the
+    reference's E: the golden records both differences."""
+    from oracle.forces import electronic_gradient
+    meta, z = load_golden(name)
+    n, rs, L = int(z["n"]), float(z["rs"]), float(z["L"])
+    s = Solver(n, L, rs, meta["basis"], **meta["kwargs"])
+    out = s.solve(z["xp"])
+    _, gpp = vpp(z["xp"], L, rs, grad=True)
+    g = electronic_gradient(s) * 2 * rs + gpp
+    c = z["coords"]
+    an = g[c[:, 0], c[:, 1]]
+    assert abs(out[3] + float(z["Vpp"]) - float(z["Etot"])) < 1e-9
+    assert np.abs(an - z["dFtot"]).max() < 3e-7
+    if float(z["sigma"]) > 0:
+        assert np.abs(an - z["dEtot"]).max() > 1e-3  # dE/dR is not the adjoint's gradient
+
+
 def test_potential_energy_matches_reference():
     """Proton + electron Ewald sums of walker batches (potential.py:69-101),
     3D and 2D, with the reference's kpoints / Madelung."""
