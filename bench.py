@@ -44,7 +44,7 @@ def parse():
     ap.add_argument("--no-fp64-plain", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", default="h54", choices=["h54", "kpoint", "slater", "coulomb"],
+    ap.add_argument("--workload", default="h54", choices=["h54", "kpoint", "slater", "coulomb", "hf"],
                     help="h54: the headline metric; the others measure the widened paths")
     return ap.parse_args()
 
@@ -593,10 +593,144 @@ def run_coulomb(args):
                                    "sample": "pairwise oracle on 4 walkers"}})
 
 
+def exchange_roofline(hbm_gbs, src, reps=5):
+    """The Hartree-Fock exchange build of one Fock matrix (k_exx_plane +
+    k_exx_column + the tcgen05 Gram K = Q Q^T + its reduce) timed alone with
+    CUDA events on its stream, at the batched workload's H32 65^3 shape after
+    one converged SCF (its real occupations).  Algorithmic bytes per
+    AO-orbital pair: the compulsory traffic of a two-pass 3D transform of a
+    real field, 2 passes x (read + write) x 8 B x N_g / 2 (half spectrum,
+    complex64) = 16 N_g."""
+    import ctypes
+    import torch
+    from hqc_gb300 import make_solver, _lib
+    from hqc_gb300.workloads import hf_uneven_batch, HF_FERMI_5000K
+    xp, L, rs, grid = hf_uneven_batch(256, 3)[-1]
+    s = make_solver(xp.shape[0], L, rs, "gth-dzv", precision="mixed", n_grid=grid, tol=1e-7,
+                    **HF_FERMI_5000K)
+    s(xp)
+    lib = _lib.load()
+    st = torch.cuda.current_stream()
+    h = s.plan.handle
+    lib.hqcgb_exchange_rebuild(h, ctypes.c_void_p(st.cuda_stream))  # warm
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(st)
+    pairs = 0
+    for _ in range(reps):
+        pairs = lib.hqcgb_exchange_rebuild(h, ctypes.c_void_p(st.cuda_stream))
+    b.record(st)
+    torch.cuda.synchronize()
+    avg_s = a.elapsed_time(b) / reps / 1000.0
+    N = grid ** 3
+    algo = pairs * 16 * N
+    achieved = algo / avg_s / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": hbm_gbs, "unit": "GB/s",
+            "frac": achieved / hbm_gbs, "traffic": None,
+            "kernel": "k_exx_plane<float> + k_exx_column<float,1> + k_tc_quad_tma (Gram) + reduce "
+                      "(HF exchange of one Fock build, H32 dzv 65^3)",
+            "algorithmic_bytes": algo, "pairs": int(pairs), "avg_ms": avg_s * 1e3, "launches": reps,
+            "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs, burst)" if src == "measured" else src}
+
+
+def run_hf(args):
+    """The batched Hartree-Fock workload (configuration family 4): 256
+    configurations, 128 H16 on 49^3 and 128 H32 on 65^3, each with its own
+    rs ~ U[1.2, 1.6], gth-dzv, Fermi smearing at 5000 K, energies + forces,
+    through one make_pes_batch call per step (new positions every step)."""
+    import torch
+    from hqc_gb300 import make_pes_batch, _lib
+    from hqc_gb300.workloads import hf_uneven_batch, HF_FERMI_5000K
+    precision = "mixed" if args.precision == "auto" else args.precision
+    count = 256
+    workers = args.concurrency or 16
+    pb = make_pes_batch("gth-dzv", precision=precision, forces=True, workers=workers, tol=1e-7,
+                        max_cycle=100, **HF_FERMI_5000K)
+    total = args.warmup + args.steps
+    host = [hf_uneven_batch(count, 3 + 1000 * s) for s in range(total + 1)]
+    dev = [[(torch.as_tensor(x, device="cuda"), L, rs, g) for x, L, rs, g in cf] for cf in host[:total]]
+    iters = []
+    for s in range(args.warmup):
+        iters.extend(pb(dev[s])["iterations"])
+    torch.cuda.synchronize()
+    _lib.load().hqcgb_launch_count(1)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        torch.cuda.synchronize()
+        a.record()
+        for s in range(args.steps):
+            r = pb(dev[args.warmup + s])
+            iters.extend(r["iterations"])
+        b.record()
+        torch.cuda.synchronize()
+    ms = a.elapsed_time(b)
+    launches = int(_lib.load().hqcgb_launch_count(0))
+    conv = float(r["converged"].float().mean())
+    # end to end: host positions in, host free energies and forces out
+    t0 = time.perf_counter()
+    r = pb(host[total])
+    _ = r["F"].cpu().numpy(), [g.cpu().numpy() for g in r["grad"]]
+    e2e_s = time.perf_counter() - t0
+    hbm, _, src = peaks()
+    roof = exchange_roofline(hbm, src)
+    n_atoms = sum(x.shape[0] for x, _, _, _ in host[total])
+    return _line("HF Fermi 5000 K energy+force evals/s (128 H16 49^3 + 128 H32 65^3 dzv, rs~U[1.2,1.6])",
+                 "evals/s", count * args.steps / (ms / 1000.0), ms / args.steps, args,
+                 {"workload": "hf_uneven_batch", "configurations": count,
+                  "classes": "128 x H16 (32 AOs, 49^3) + 128 x H32 (64 AOs, 65^3)",
+                  "precision_path": precision, "workers": workers,
+                  "scf_iterations_mean": float(np.mean(iters)), "converged_fraction": conv,
+                  "l2": "inputs > L2 (each configuration streams its AO grids and pair spectra), no flush"},
+                 {"dtype": "tf32x3+f32+f64" if precision == "mixed" else "f64", "roofline": roof,
+                  "e2e": {"value": count / e2e_s, "unit": "evals/s", "h2d_bytes_per_step": n_atoms * 3 * 8,
+                          "d2h_bytes_per_step": count * 8 + n_atoms * 3 * 8},
+                  "gpu_launches": launches, "clocks": clk.summary(),
+                  "cpu_baseline": hf_cpu_baseline(float(np.mean(iters)))})
+
+
+def hf_cpu_baseline(iters_mean):
+    """The oracle on the host cores: one complete H16 evaluation (SCF + force
+    pass) measured, and the H32 evaluation estimated from its measured
+    geometry set-up and first Fock build times the GPU run's mean iteration
+    count (an H32 SCF alone takes the oracle about 15 minutes)."""
+    from oracle.gpw import Solver
+    from oracle.forces import electronic_gradient
+    from hqc_gb300.workloads import hf_uneven_batch, HF_FERMI_5000K
+    cf = hf_uneven_batch(256, 3)
+    xp, L, rs, grid = cf[0]
+    t0 = time.perf_counter()
+    s = Solver(16, L, rs, "gth-dzv", n_grid=grid, tol=1e-7, **HF_FERMI_5000K)
+    s.solve(xp)
+    electronic_gradient(s)
+    t16 = time.perf_counter() - t0
+    xp, L, rs, grid = cf[-1]
+    t1 = time.perf_counter()
+    s = Solver(32, L, rs, "gth-dzv", n_grid=grid, tol=1e-7, **HF_FERMI_5000K)
+    g = s.setup_geometry(xp)
+    t2 = time.perf_counter()
+    w, U = np.linalg.eigh(g["S"])
+    v = U / np.sqrt(w)[None, :]
+    e, c1 = np.linalg.eigh(v.T @ (g["T"] + g["V"]) @ v)
+    C = v @ c1
+    occ = s.occ(e)
+    D = (C * occ) @ C.T
+    rho = s.density(D, g["phi"])[0]
+    s.hartree(rho, g["phi"])
+    s.exchange(D, C, occ, g["phi"], g["Stilde"])
+    t3 = time.perf_counter()
+    t32 = (t2 - t1) + (t3 - t2) * (iters_mean + 3)
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    return {"value": 2.0 / (t16 + t32), "unit": "evals/s", "cores": cores, "kind": "port",
+            "sample": f"one complete oracle H16 evaluation {t16:.1f}s (measured) and one H32 evaluation "
+                      f"estimated as geometry {t2 - t1:.1f}s + {iters_mean:.0f}+3 Fock builds of "
+                      f"{t3 - t2:.1f}s (measured once)"}
+
+
 def main():
     args = parse()
     if args.impl != "reference" and args.workload != "h54":
-        line = {"kpoint": run_kpoint, "slater": run_slater, "coulomb": run_coulomb}[args.workload](args)
+        line = {"kpoint": run_kpoint, "slater": run_slater, "coulomb": run_coulomb,
+                "hf": run_hf}[args.workload](args)
         print(json.dumps(line), flush=True)
         return
     line = run_reference(args) if args.impl == "reference" else run_ours(args)

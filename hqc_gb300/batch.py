@@ -55,15 +55,20 @@ def make_pes_batch(basis, rcut=24, tol=1e-7, max_cycle=100, diis=True, diis_spac
     _lib.check(lib.hqcgb_batch_create(ctypes.byref(P), float(rcut), int(workers), ctypes.byref(h)))
     device = torch.device("cuda", torch.cuda.current_device())
 
+    def _pos(x):
+        if isinstance(x, torch.Tensor):
+            return x.detach().to(dtype=torch.float64)
+        return torch.as_tensor(np.asarray(x, dtype=np.float64))
+
     def pes_batch(configs):
         B = len(configs)
-        n = np.array([np.asarray(c[0]).shape[0] for c in configs], dtype=np.int32)
+        xs = [_pos(c[0]) for c in configs]
+        n = np.array([x.shape[0] for x in xs], dtype=np.int32)
         grid = np.array([int(c[3]) for c in configs], dtype=np.int32)
         L_rs = np.array([float(c[1]) for c in configs])
         rs = np.array([float(c[2]) for c in configs])
         L_bohr = np.ascontiguousarray(L_rs * rs)
-        xs = [torch.as_tensor(np.asarray(c[0], dtype=np.float64)) for c in configs]
-        xp = torch.cat([x * r for x, r in zip(xs, rs)]).to(device).contiguous()
+        xp = torch.cat([x.to(device) * r for x, r in zip(xs, rs)]).contiguous()
         nao = n.astype(np.int64) * nao_atom
         aoff = np.concatenate([[0], np.cumsum(nao)])
         xoff = np.concatenate([[0], np.cumsum(n)])

@@ -16,7 +16,8 @@
 //   k_exx_plane   one x-plane of one pair: phi_p recomputed from the
 //                 separable 1D GTO factors (no AO grid is read), the pair
 //                 formed in shared memory, a real DFT along z (half
-//                 spectrum) and a two-factor complex DFT along y;
+//                 spectrum; two real lines per complex transform) and a
+//                 complex DFT along y;
 //   k_exx_column  one ky-line of one pair: the DFT along x, then the
 //                 frequency-stage multiply by sqrt(w(G) (1 or 2)); the store
 //                 stage writes Q = sqrt(.) P^ as FP64, or as the TF32 hi/lo
@@ -56,67 +57,140 @@ __device__ inline void load_twiddles(R2 *w, const double2 *tw, int n) {
   }
 }
 
-// DFT along axis 0 of `in` [n][ncol] (columns contiguous), forward sign.
-// n1 > 1: two factors n = n1 n2 (j = n2 j1 + j2, k = k1 + n1 k2):
+// Small DFTs in shared memory.  Every odd length pairs its outputs k and
+// n - k, whose twiddles are complex conjugates: with C = sum_j x_j Re W^(jk)
+// and S = sum_j x_j Im W^(jk) (complex sums),
+//   X[k] = C + i S,   X[n - k] = C - i S,
+// which halves the multiply-adds.  W = exp(-2 pi i / n), w[m] = W^m.
+template <typename R2>
+__device__ __forceinline__ R2 cmul(R2 a, R2 b) {
+  R2 r;
+  r.x = a.x * b.x - a.y * b.y;
+  r.y = a.x * b.y + a.y * b.x;
+  return r;
+}
+
+constexpr int kMaxN1 = 16, kMaxN2 = 16;  // register-blocked factor sizes
+
+// DFT along axis 0 of `in` [n][ncol] (columns contiguous), n odd.
+// n = n1 n2 with n1 <= kMaxN1, n2 <= kMaxN2 (j = n2 j1 + j2, k = k1 + n1 k2):
 //   y[j2 n1 + k1] = W^(j2 k1) sum_j1 x[n2 j1 + j2] W^(n2 j1 k1)   -> tmp
 //   X[k1 + n1 k2] = sum_j2 y[j2 n1 + k1] W^(n1 j2 k2)               -> out
-// n1 = 1: the direct sum into tmp.  Returns the buffer holding the result;
-// `in` may alias `out`.  Ends with a block barrier.
+// each thread holding one (j2, col) input group (then one (k1, col)) in
+// registers; otherwise (a prime n, n1 = 1, or a larger n2) the paired direct
+// sum into tmp.  Returns the buffer holding the result; `in` may alias
+// `out`.  Ends with a block barrier.
 template <typename R, typename R2>
 __device__ R2 *dft_axis0(const R2 *in, R2 *tmp, R2 *out, int n, int ncol, int n1, const R2 *w) {
-  const int total = n * ncol;
-  if (n1 == 1) {
-    for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+  const int n2 = n1 > 1 ? n / n1 : n;
+  if (n1 == 1 || n1 > kMaxN1 || n2 > kMaxN2) {
+    const int nh = (n + 1) / 2;
+    for (int idx = threadIdx.x; idx < nh * ncol; idx += blockDim.x) {
       const int k = idx / ncol, col = idx - k * ncol;
-      R re = 0, im = 0;
+      R2 C = in[col], S;
+      S.x = 0;
+      S.y = 0;
       int t = 0;
-      for (int j = 0; j < n; ++j) {
-        const R2 x = in[j * ncol + col], ww = w[t];
-        re += x.x * ww.x - x.y * ww.y;
-        im += x.x * ww.y + x.y * ww.x;
+      for (int j = 1; j < n; ++j) {
         t += k;
         if (t >= n) t -= n;
+        const R2 x = in[j * ncol + col], ww = w[t];
+        C.x += x.x * ww.x;
+        C.y += x.y * ww.x;
+        S.x += x.x * ww.y;
+        S.y += x.y * ww.y;
       }
-      tmp[idx].x = re;
-      tmp[idx].y = im;
+      R2 a, b;
+      a.x = C.x - S.y;
+      a.y = C.y + S.x;
+      tmp[k * ncol + col] = a;
+      if (k > 0) {
+        b.x = C.x + S.y;
+        b.y = C.y - S.x;
+        tmp[(n - k) * ncol + col] = b;
+      }
     }
     __syncthreads();
     return tmp;
   }
-  const int n2 = n / n1;
-  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
-    const int m = idx / ncol, col = idx - m * ncol;
-    const int j2 = m / n1, k1 = m - j2 * n1;
-    const int step = (n2 * k1) % n;
-    R re = 0, im = 0;
-    int t = 0;
-    for (int j1 = 0; j1 < n1; ++j1) {
-      const R2 x = in[(n2 * j1 + j2) * ncol + col], ww = w[t];
-      re += x.x * ww.x - x.y * ww.y;
-      im += x.x * ww.y + x.y * ww.x;
-      t += step;
-      if (t >= n) t -= n;
+  for (int it = threadIdx.x; it < n2 * ncol; it += blockDim.x) {
+    const int j2 = it / ncol, col = it - j2 * ncol;
+    R2 x[kMaxN1];
+#pragma unroll
+    for (int j1 = 0; j1 < kMaxN1; ++j1)
+      if (j1 < n1) x[j1] = in[(n2 * j1 + j2) * ncol + col];
+    R2 s0 = x[0];
+#pragma unroll
+    for (int j1 = 1; j1 < kMaxN1; ++j1)
+      if (j1 < n1) {
+        s0.x += x[j1].x;
+        s0.y += x[j1].y;
+      }
+    tmp[(j2 * n1) * ncol + col] = s0;
+    for (int k1 = 1; 2 * k1 < n1; ++k1) {
+      R2 C = x[0], S;
+      S.x = 0;
+      S.y = 0;
+      int t = 0;
+#pragma unroll
+      for (int j1 = 1; j1 < kMaxN1; ++j1)
+        if (j1 < n1) {
+          t += k1;
+          if (t >= n1) t -= n1;
+          const R2 ww = w[n2 * t];
+          C.x += x[j1].x * ww.x;
+          C.y += x[j1].y * ww.x;
+          S.x += x[j1].x * ww.y;
+          S.y += x[j1].y * ww.y;
+        }
+      R2 a, b;
+      a.x = C.x - S.y;
+      a.y = C.y + S.x;
+      b.x = C.x + S.y;
+      b.y = C.y - S.x;
+      tmp[(j2 * n1 + k1) * ncol + col] = cmul(a, w[(j2 * k1) % n]);
+      tmp[(j2 * n1 + n1 - k1) * ncol + col] = cmul(b, w[(j2 * (n1 - k1)) % n]);
     }
-    const R2 tw = w[(j2 * k1) % n];
-    tmp[idx].x = re * tw.x - im * tw.y;
-    tmp[idx].y = re * tw.y + im * tw.x;
   }
   __syncthreads();
-  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
-    const int k = idx / ncol, col = idx - k * ncol;
-    const int k2 = k / n1, k1 = k - k2 * n1;
-    const int step = (n1 * k2) % n;
-    R re = 0, im = 0;
-    int t = 0;
-    for (int j2 = 0; j2 < n2; ++j2) {
-      const R2 x = tmp[(j2 * n1 + k1) * ncol + col], ww = w[t];
-      re += x.x * ww.x - x.y * ww.y;
-      im += x.x * ww.y + x.y * ww.x;
-      t += step;
-      if (t >= n) t -= n;
+  for (int it = threadIdx.x; it < n1 * ncol; it += blockDim.x) {
+    const int k1 = it / ncol, col = it - k1 * ncol;
+    R2 y[kMaxN2];
+#pragma unroll
+    for (int j2 = 0; j2 < kMaxN2; ++j2)
+      if (j2 < n2) y[j2] = tmp[(j2 * n1 + k1) * ncol + col];
+    R2 s0 = y[0];
+#pragma unroll
+    for (int j2 = 1; j2 < kMaxN2; ++j2)
+      if (j2 < n2) {
+        s0.x += y[j2].x;
+        s0.y += y[j2].y;
+      }
+    out[k1 * ncol + col] = s0;
+    for (int k2 = 1; 2 * k2 < n2; ++k2) {
+      R2 C = y[0], S;
+      S.x = 0;
+      S.y = 0;
+      int t = 0;
+#pragma unroll
+      for (int j2 = 1; j2 < kMaxN2; ++j2)
+        if (j2 < n2) {
+          t += k2;
+          if (t >= n2) t -= n2;
+          const R2 ww = w[n1 * t];
+          C.x += y[j2].x * ww.x;
+          C.y += y[j2].y * ww.x;
+          S.x += y[j2].x * ww.y;
+          S.y += y[j2].y * ww.y;
+        }
+      R2 a, b;
+      a.x = C.x - S.y;
+      a.y = C.y + S.x;
+      b.x = C.x + S.y;
+      b.y = C.y - S.x;
+      out[(k1 + n1 * k2) * ncol + col] = a;
+      out[(k1 + n1 * (n2 - k2)) * ncol + col] = b;
     }
-    out[idx].x = re;
-    out[idx].y = im;
   }
   __syncthreads();
   return out;
@@ -166,23 +240,33 @@ __global__ void __launch_bounds__(256) k_exx_plane(PlaneArgs a) {
   const int n = a.n, nh = a.nh, x = blockIdx.x, r = blockIdx.y, jl = blockIdx.z;
   const size_t bufc = (size_t)n * (n + 1) / 2 + 1;  // complex slots of one plane buffer (>= n^2 reals)
   R2 *w = reinterpret_cast<R2 *>(smraw);
-  R2 *B0 = w + n;                  // real pair plane P[y][z], later the y-transform's temp
-  R2 *B1 = B0 + bufc;              // z-transformed plane C[y][kz]
+  R2 *B0 = w + n;                  // plane buffers: the packed pair lines, the
+  R2 *B1 = B0 + bufc;              // transforms' temporaries and the z-transformed plane
   R *fyz = reinterpret_cast<R *>(B1 + bufc);  // [2][nprim][n]: y and z factors
-  R *P = reinterpret_cast<R *>(B0);
   load_twiddles(w, a.tw, n);
   const long long plane = (long long)x * n * n;
   const R *psi = reinterpret_cast<const R *>(a.psi) + (long long)jl * a.ldpsi + plane;
   const long long nn = (long long)n * n;
+  // The pair plane goes straight into the packed layout of the z transform:
+  // complex column pr of Z[z][pr] holds the real y-lines 2 pr (real part) and
+  // 2 pr + 1 (imaginary part); the last column of an odd n has no partner.
+  const int npair = (n + 1) / 2;
+  R *Zr = reinterpret_cast<R *>(B0);  // Z[z][pr] as reals: [z][pr][2]
+  auto put = [&](int i, R v) {
+    const int y = i / n, z = i - y * n;
+    Zr[2 * (z * npair + (y >> 1)) + (y & 1)] = v;
+  };
+  if (n & 1)
+    for (int z = threadIdx.x; z < n; z += blockDim.x) Zr[2 * (z * npair + npair - 1) + 1] = 0;
   if (r < a.xrows) {
     const double *Xr = a.X + (long long)r * a.ldx + plane;
-    for (int i = threadIdx.x; i < nn; i += blockDim.x) P[i] = (R)Xr[i] * psi[i];
+    for (int i = threadIdx.x; i < nn; i += blockDim.x) put(i, (R)Xr[i] * psi[i]);
   } else {
-    // AO p (or its derivative along c) = sum_a coef_a fx_a(x) fy_a(y) fz_a(z)
     // Fock mode: row r is phi_p, p = r (c = -1: the value); gradient mode:
     // row nao (1 + c) + p is d_c phi_p
     const int rr = r - a.xrows;
     const int p = rr % a.nao, c = a.xrows > 0 ? rr / a.nao : -1;
+    // AO p (or its derivative along c) = sum_a coef_a fx_a(x) fy_a(y) fz_a(z)
     const int A = p / a.nb, k = p % a.nb, l = a.ao_l[k], ca = a.ao_cart[k];
     int e[3];
     for (int d = 0; d < 3; ++d) e[d] = 3 * ((l == 1 && ca == d) ? 1 : 0) + (d == c ? 1 : 0);
@@ -199,28 +283,28 @@ __global__ void __launch_bounds__(256) k_exx_plane(PlaneArgs a) {
       const int y = i / n, z = i - y * n;
       R v = 0;
       for (int pr = 0; pr < a.nprim; ++pr) v += fx[pr] * fyz[pr * n + y] * fyz[(a.nprim + pr) * n + z];
-      P[i] = v * psi[i];
+      put(i, v * psi[i]);
     }
   }
   __syncthreads();
-  // real DFT along z: C[y][kz] = sum_z P[y][z] W^(z kz), kz < nh
-  for (int i = threadIdx.x; i < n * nh; i += blockDim.x) {
-    const int y = i / nh, kz = i - y * nh;
-    const R *row = P + (long long)y * n;
-    R re = 0, im = 0;
-    int t = 0;
-    for (int z = 0; z < n; ++z) {
-      const R v = row[z];
-      re += v * w[t].x;
-      im += v * w[t].y;
-      t += kz;
-      if (t >= n) t -= n;
-    }
-    B1[i].x = re;
-    B1[i].y = im;
+  // z transform of the packed lines, then unpacked into C[y][kz], kz < nh:
+  // A[k] = (Z[k] + conj Z[n-k]) / 2 (line 2 pr), B[k] = (Z[k] - conj Z[n-k]) / 2i
+  R2 *Zt = dft_axis0<R, R2>(B0, B1, B0, n, npair, a.n1, w);
+  R2 *Cb = (Zt == B0) ? B1 : B0;
+  for (int i = threadIdx.x; i < npair * nh; i += blockDim.x) {
+    const int pr = i / nh, kz = i - pr * nh;
+    const R2 zk = Zt[kz * npair + pr], zm = Zt[(kz == 0 ? 0 : n - kz) * npair + pr];
+    R2 u, v;
+    u.x = (R)0.5 * (zk.x + zm.x);
+    u.y = (R)0.5 * (zk.y - zm.y);
+    v.x = (R)0.5 * (zk.y + zm.y);
+    v.y = (R)0.5 * (zm.x - zk.x);
+    Cb[(2 * pr) * nh + kz] = u;
+    if (2 * pr + 1 < n) Cb[(2 * pr + 1) * nh + kz] = v;
   }
   __syncthreads();
-  const R2 *res = dft_axis0<R, R2>(B1, B0, B1, n, nh, a.n1, w);
+  R2 *Ct = (Cb == B0) ? B1 : B0;
+  const R2 *res = dft_axis0<R, R2>(Cb, Ct, Cb, n, nh, a.n1, w);
   R2 *T = reinterpret_cast<R2 *>(a.T) + (((long long)jl * a.rows + r) * n + x) * (long long)n * nh;
   for (int i = threadIdx.x; i < n * nh; i += blockDim.x) T[i] = res[i];
 }

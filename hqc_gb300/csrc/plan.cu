@@ -408,7 +408,11 @@ static void create(const hqcgb_params *in, hqcgb_plan *p) {
     const int rows_cap = std::max(p->exx_g, 4) * nao;  // pair rows T holds
     p->exx_grad_g = rows_cap / (4 * nao);
     p->exx_T = p->alloc<char>((size_t)rows_cap * (L2 / 2) * 2 * rb);
-    p->exx_psi = p->alloc<char>((size_t)nao * N * rb);
+    // psi~ rows: every orbital, and at least the orbital-density kernel's
+    // padded width (a multiple of 16, up to 64), which writes them on the
+    // mixed path
+    const int psi_rows = std::max(nao, tc_psi_width(std::min(nao, tc_psi_max(false))));
+    p->exx_psi = p->alloc<char>((size_t)psi_rows * N * rb);
     p->exx_part = p->alloc<double>((size_t)p->exx_grad_g * nao * p->ng * 3);
     void *wsq = p->alloc<char>((size_t)(L2 / 2) * rb);
     const long long gK = (long long)p->exx_g * L2;
@@ -846,6 +850,7 @@ static int scf_one(hqcgb_plan *p, const double *xp_dev, const hqcgb_scf_out *out
   density_matrix(c);
   double E0 = 0.0, E1 = 1.0;
   int loop = 0;
+  bool stopped = false;  // the stopping test was met before max_cycle
   if (P.diis) {
     int sp = P.diis_space;
     fock(c);
@@ -879,11 +884,24 @@ static int scf_one(hqcgb_plan *p, const double *xp_dev, const hqcgb_scf_out *out
     // 2e-5) so that tol below the floor cannot make the loop spin to max_cycle.
     const double etol = p->mixed ? std::max(P.tol, 2e-6) : P.tol;
     const double errtol = p->mixed ? std::max(10.0 * P.tol, 2e-5) : 10.0 * P.tol;
-    while ((std::fabs(E1 - E0) > etol || enorm > errtol) && loop < P.max_cycle) {
+    auto diis_step = [&] {
       diis_extrapolate(sp, n, p->Fk, p->ek, head, P.diis_damp, p->Bm, p->dc, p->t1, st);
       HQ_CUDA(cudaMemcpyAsync(p->Fp, p->t1, nn * 8, cudaMemcpyDeviceToDevice, st));
       step(p->Fp);
       if (!std::isfinite(E1)) throw Error{HQCGB_NAN, "non-finite energy in the SCF"};
+    };
+    while ((std::fabs(E1 - E0) > etol || enorm > errtol) && loop < P.max_cycle) diis_step();
+    stopped = loop < P.max_cycle;
+    // Mixed path, stopped at the floor with the commutator still above the
+    // requested 10 tol: a few more iterations while it keeps falling by at
+    // least a fifth (the gradient's error is first order in it; at the noise
+    // floor it stops falling and the polish ends).
+    if (p->mixed && loop < P.max_cycle && enorm > 10.0 * P.tol) {
+      for (int extra = 0; extra < 6 && loop < P.max_cycle && enorm > 10.0 * P.tol; ++extra) {
+        const double prev = enorm;
+        diis_step();
+        if (enorm > 0.8 * prev) break;
+      }
     }
   } else {
     const double etol = p->mixed ? std::max(P.tol, 2e-6) : P.tol;
@@ -897,6 +915,7 @@ static int scf_one(hqcgb_plan *p, const double *xp_dev, const hqcgb_scf_out *out
       ++loop;
       if (!std::isfinite(E1)) throw Error{HQCGB_NAN, "non-finite energy in the SCF"};
     }
+    stopped = loop != P.max_cycle;
   }
   check_eig(c);
   if (p->mixed) {
@@ -908,7 +927,7 @@ static int scf_one(hqcgb_plan *p, const double *xp_dev, const hqcgb_scf_out *out
       throw Error{HQCGB_CUDA_ERROR, "tensor-core pipeline wait limit hit (code " + std::to_string(te) + ")"};
     }
   }
-  int converged = (loop != P.max_cycle) ? 1 : 0;
+  int converged = stopped ? 1 : 0;
   if (p->mixed) refine_last(c);
   // post-processing (solver.py:758-767 / 890-899); the mixed force path keeps
   // the orbitals on the grid from this last density pass
@@ -1384,6 +1403,19 @@ int hqcgb_pes_batch(hqcgb_plan *plan, int n_cfg, const double *xp, const hqcgb_s
     HQ_REQUIRE(!grad || plan->P.want_forces, "plan was created without want_forces");
     return run_batch(plan, n_cfg, xp, out, grad, (cudaStream_t)stream);
   });
+}
+
+long long hqcgb_exchange_rebuild(hqcgb_plan *plan, void *stream) {
+  try {
+    if (!plan || !plan->hf || !plan->have_state || !plan->exx_fused) return -1;
+    Ctx c{plan, (cudaStream_t)stream};
+    exchange(c);
+    HQ_CUDA(cudaStreamSynchronize(c.st));
+    return (long long)plan->nao * exx_count(plan);
+  } catch (const Error &e) {
+    set_error(e.msg);
+    return -2;
+  }
 }
 
 int hqcgb_batch_create(const hqcgb_params *base, double rcut, int workers, hqcgb_batch **batch) {

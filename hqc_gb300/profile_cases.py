@@ -11,6 +11,9 @@ Cases (synthetic operands with the benchmark's sizes: 270 AOs, an 81^3 grid,
   quadrature_gga  Z phi^T + phi Z^T with the PBE operand (the SCF's form)
   eigh_mixed    the mixed-precision eigensolver on a 270 x 270 matrix
   eigh_fp64     the FP64 eigensolver on the same matrix
+  exchange      the Hartree-Fock exchange build of one Fock matrix (pair
+                planes, column transforms, tcgen05 Gram) at the batched
+                workload's H32 dzv 65^3 shape, after one converged mixed SCF
 
 Each case runs its operation ``reps`` times (default 3) after building the
 operands, so a profiler can skip the set-up launches and capture the rest.
@@ -38,13 +41,26 @@ def _operands(gga):
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("case", choices=["psi_density", "density_D", "quadrature", "quadrature_gga",
-                                     "eigh_mixed", "eigh_fp64"])
+                                     "eigh_mixed", "eigh_fp64", "exchange"])
     ap.add_argument("--reps", type=int, default=3)
     a = ap.parse_args(argv)
     import torch
     from hqc_gb300 import _lib
     _lib.load()
-    if a.case.startswith("eigh"):
+    if a.case == "exchange":
+        import ctypes
+        from hqc_gb300 import make_solver
+        from hqc_gb300.workloads import hf_uneven_batch, HF_FERMI_5000K
+        xp, L, rs, grid = hf_uneven_batch(256, 3)[-1]
+        s = make_solver(xp.shape[0], L, rs, "gth-dzv", precision="mixed", n_grid=grid, tol=1e-7,
+                        **HF_FERMI_5000K)
+        s(xp)
+        lib = _lib.load()
+        st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        for _ in range(a.reps):
+            pairs = lib.hqcgb_exchange_rebuild(s.plan.handle, st)
+        print(f"exchange: {pairs} AO-orbital pairs per build")
+    elif a.case.startswith("eigh"):
         g = torch.Generator(device="cuda").manual_seed(2)
         M = torch.randn(NAO, NAO, dtype=torch.float64, device="cuda", generator=g)
         M = M + M.T

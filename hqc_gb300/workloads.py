@@ -73,3 +73,24 @@ def hf_fermi(n=16, rs=1.4, seed=3, count=3, grid=None):
     return dict(n=n, L=L, rs=rs, basis="gth-dzv", dft=False, grid_length=L * rs / grid,
                 smearing=True, smearing_method="fermi", smearing_sigma=sigma,
                 xps=rng.uniform(0.0, L, (count, n, 3)))
+
+
+def hf_uneven_batch(count=256, seed=3):
+    """Configuration family 4 as one uneven batch: `count` configurations,
+    the first half H16 on a 49^3 grid and the second half H32 on 65^3 (the
+    reference's odd grids for the requested 48^3 / 64^3), each with its own
+    rs ~ U[1.2, 1.6] and uniform positions in its box; gth-dzv Hartree-Fock
+    with Fermi smearing at 5000 K (``HF_FERMI_5000K``).  Returns a list of
+    (xp (n, 3) rs units, L rs units, rs, n_grid) for ``make_pes_batch``."""
+    rng = np.random.default_rng(seed)
+    cfgs = []
+    for k in range(count):
+        n, grid = (16, 49) if k < count // 2 else (32, 65)
+        rs = rng.uniform(1.2, 1.6)
+        L = box(n)
+        cfgs.append((rng.uniform(0.0, L, (n, 3)), L, rs, grid))
+    return cfgs
+
+
+HF_FERMI_5000K = dict(dft=False, smearing=True, smearing_method="fermi",
+                      smearing_sigma=0.5 * 5000 / 157888.09)

@@ -229,6 +229,15 @@ int hqcgb_ewald(const double *xp, int n, double L, double rs, double kappa, int 
 long long hqcgb_plan_query(hqcgb_plan *plan, const char *name, void *dst, size_t bytes,
                            void *stream);
 
+/* (tools) Rebuild the exact-exchange matrix of a Hartree-Fock plan for the
+ * density of its last SCF (the occupied-pair form with fused FFT stages), on
+ * `stream`, and wait for it: for timing the exchange alone.  Returns the
+ * number of AO-orbital pairs transformed, < 0 when the plan has no such
+ * state (not Hartree-Fock, no SCF yet, or a grid beyond the fused kernels).
+ * No counterpart in the reference (its exchange is an ERI contraction inside
+ * the jitted SCF, hqc/pbc/solver.py:604-614). */
+long long hqcgb_exchange_rebuild(hqcgb_plan *plan, void *stream);
+
 /* The engine's FP64 symmetric eigensolver (Householder tridiagonalisation +
  * implicit QL, Jacobi fallback) on `batch` row-major n x n matrices A
  * (device, not modified): ascending eigenvalues w [batch][n] and eigenvectors

@@ -65,8 +65,11 @@ def test_value_and_grad_is_a_derivative_pair(method, dft):
     n, rs = 4, 1.5
     L = (4 / 3 * np.pi * n) ** (1 / 3)
     xp = np.random.default_rng(21).uniform(0, L, (n, 3))
+    # Gaussian occupations are capped at 1 (smearing.py:52): a wider sigma
+    # gives the same partial filling as Fermi's
+    sigma = 0.08 if method == "fermi" else 0.25
     kw = dict(grid_length=0.2, tol=1e-11, max_cycle=300, smearing=True, smearing_method=method,
-              smearing_sigma=0.08, search_method="newton", search_tol=1e-13, search_cycle=200)
+              smearing_sigma=sigma, search_method="newton", search_tol=1e-13, search_cycle=200)
     if dft:
         kw.update(dft=True, xc="lda,vwn")
     pes = make_pes(n, L, rs, "gth-dzv", forces=True, **kw)
