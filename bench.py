@@ -242,6 +242,10 @@ def run_ours(args):
     precision = "mixed" if args.precision == "auto" else args.precision
     B = args.batch
     conc = args.concurrency or B
+    # launch shapes picked by the autotuner at this run's shapes (cached per GPU)
+    from hqc_gb300.tune import tune_quadrature
+    kchunk, ktable = tune_quadrature(270, 81)
+    tuning = {"quad_kchunk": kchunk, "measured_ms": ktable}
     w0 = workload(7)
     n, L, rs = w0["n"], w0["L"], w0["rs"]
     kw = dict(dft=True, xc=w0["xc"], grid_length=w0["grid_length"], tol=1e-7, max_cycle=100,
@@ -338,7 +342,7 @@ def run_ours(args):
             "config": dict(CONFIG, precision_path=precision, batch=B, concurrency=conc,
                            scf_iterations_mean=float(np.mean(iters[B * args.warmup:])),
                            l2="inputs > L2 (every configuration streams > 2 GB of AO grids), no flush",
-                           parallelism=f"replicas x{world}"),
+                           parallelism=f"replicas x{world}", tuning=tuning),
             "roofline": roof, "roofline_orbital_density": roof_psi, "fp64_plain": fp64, "gpu_ms_per_eval_by_stage": stage_ms, "e2e": e2e,
             "gpu_launches": launches, "clocks": clk.summary()}
     if rank == 0 and not args.no_cpu_baseline and world == 1:
@@ -641,9 +645,15 @@ def run_hf(args):
     import torch
     from hqc_gb300 import make_pes_batch, _lib
     from hqc_gb300.workloads import hf_uneven_batch, HF_FERMI_5000K
+    from hqc_gb300.tune import tune_exchange
+    from hqc_gb300.workloads import box
     precision = "mixed" if args.precision == "auto" else args.precision
     count = 256
     workers = args.concurrency or 16
+    # exchange launch shapes tuned on the dominant class (H32, 65^3) before
+    # the batch creates its workspaces
+    (group, gctas), etable = tune_exchange(32, box(32), 1.4, 65, tol=1e-7, **HF_FERMI_5000K)
+    tuning = {"exx_group": group, "exx_gram_ctas": gctas, "measured_ms": etable}
     pb = make_pes_batch("gth-dzv", precision=precision, forces=True, workers=workers, tol=1e-7,
                         max_cycle=100, **HF_FERMI_5000K)
     total = args.warmup + args.steps
@@ -678,7 +688,7 @@ def run_hf(args):
                  "evals/s", count * args.steps / (ms / 1000.0), ms / args.steps, args,
                  {"workload": "hf_uneven_batch", "configurations": count,
                   "classes": "128 x H16 (32 AOs, 49^3) + 128 x H32 (64 AOs, 65^3)",
-                  "precision_path": precision, "workers": workers,
+                  "precision_path": precision, "workers": workers, "tuning": tuning,
                   "scf_iterations_mean": float(np.mean(iters)), "converged_fraction": conv,
                   "l2": "inputs > L2 (each configuration streams its AO grids and pair spectra), no flush"},
                  {"dtype": "tf32x3+f32+f64" if precision == "mixed" else "f64", "roofline": roof,

@@ -52,7 +52,7 @@ EXPORTS = ("hqcgb_plan_create", "hqcgb_plan_destroy", "hqcgb_scf", "hqcgb_scf_ba
            "hqcgb_ao_points_kpt", "hqcgb_slater_kpt", "hqcgb_overlap", "hqcgb_coulomb_energy",
            "hqcgb_tc_quadrature_gga", "hqcgb_diis_coefficients",
            "hqcgb_tc_quad_tiles", "hqcgb_batch_create", "hqcgb_batch_destroy", "hqcgb_batch_run",
-           "hqcgb_exchange_rebuild")
+           "hqcgb_exchange_rebuild", "hqcgb_tune_set", "hqcgb_tune_get")
 N_STAGES = 15
 
 _lib = None
@@ -110,6 +110,9 @@ def load():
     lib.hqcgb_batch_create.argtypes = [ctypes.POINTER(Params), ctypes.c_double, ctypes.c_int,
                                        ctypes.POINTER(ctypes.c_void_p)]
     lib.hqcgb_batch_destroy.argtypes = [ctypes.c_void_p]
+    lib.hqcgb_tune_set.argtypes = [ctypes.c_char_p, ctypes.c_longlong]
+    lib.hqcgb_tune_get.argtypes = [ctypes.c_char_p]
+    lib.hqcgb_tune_get.restype = ctypes.c_longlong
     lib.hqcgb_exchange_rebuild.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
     lib.hqcgb_exchange_rebuild.restype = ctypes.c_longlong
     lib.hqcgb_batch_run.argtypes = [ctypes.c_void_p, ctypes.c_int, c_int_p, c_int_p, c_double_p,

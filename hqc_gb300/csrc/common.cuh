@@ -12,6 +12,8 @@
 namespace hqcgb {
 
 void set_error(const std::string &msg);
+// Run-time tuning knobs (hqcgb_tune_set): the value set for `name`, or dflt.
+long long tune_get(const char *name, long long dflt);
 void count_launch(long long k = 1);
 // Raise the dynamic shared-memory limit of kernel `func` on the current
 // device to at least `bytes` (never lowers it); callable from concurrent

@@ -25,6 +25,17 @@ namespace hqcgb {
 static thread_local std::string g_err;
 static std::atomic<long long> g_launches{0};
 void set_error(const std::string &m) { g_err = m; }
+
+// Tuning knobs: launch parameters that change no result beyond rounding
+// (K-chunk lengths, group sizes), set by the autotuner (hqc_gb300/tune.py)
+// from measurements and read by the launchers.
+static std::mutex g_tune_mu;
+static std::map<std::string, long long> g_tune;
+long long tune_get(const char *name, long long dflt) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  auto it = g_tune.find(name);
+  return it == g_tune.end() ? dflt : it->second;
+}
 void count_launch(long long k) { g_launches += k; }
 
 static const char *kStageNames[ST_COUNT] = {"gto1d", "phi", "density", "quadrature", "fft", "xc",
@@ -404,6 +415,9 @@ static void create(const hqcgb_params *in, hqcgb_plan *p) {
     const size_t rb = p->mixed ? sizeof(float) : sizeof(double);
     const double per_orb = (double)nao * L2 * (rb + 8.0);
     p->exx_g = (int)std::max(1.0, std::min(16.0, std::floor(1.5e9 / per_orb)));
+    // a tuned group size, within 1..16 and twice the memory budget
+    const long long tg = tune_get("exx_group", 0);
+    if (tg > 0) p->exx_g = (int)std::max(1.0, std::min({16.0, (double)tg, std::floor(3e9 / per_orb)}));
     p->exx_g = std::min(p->exx_g, nao);
     const int rows_cap = std::max(p->exx_g, 4) * nao;  // pair rows T holds
     p->exx_grad_g = rows_cap / (4 * nao);
@@ -419,7 +433,7 @@ static void create(const hqcgb_params *in, hqcgb_plan *p) {
     if (p->mixed) {
       p->exx_ldq = (gK + 31) / 32 * 32;
       p->exx_Q = p->alloc<float>((size_t)2 * nao * p->exx_ldq);
-      const int ctas = 2 * 152;
+      const int ctas = (int)std::max<long long>(1, tune_get("exx_gram_ctas", 2 * 152));
       const int chunks = std::max(1, ctas / tc_quad_tiles(nao, true));
       p->exx_kchunk = (int)std::max<long long>(2048, (gK + chunks - 1) / chunks / 32 * 32 + 32);
       p->exx_tcpart = p->alloc<double>(tc_quad_partial_doubles(nao, gK, p->exx_kchunk));
@@ -728,8 +742,11 @@ static double fock(Ctx &c) {
     launch_sum_partials(p->xpart, xc_blocks(N), 2, 2, 1.0, p->scal + S_EXC, false, c.st);
     launch_to_f32(p->wq, N, N, 1, 1.0, p->w32, p->ld, c.st);
     if (p->gga) launch_to_f32(p->u, N, N, 3, 1.0, p->u32, p->ld, c.st);
+    // Hartree-Fock: the Hartree potential alone is the weight, same-signed,
+    // where the truncating accumulation of 4-stage drains would bias J by
+    // ~1e-6; its grids are small, so it drains every stage
     launch_tc_quadrature(p->phi32, p->dphi32, p->phihl, p->w32, p->u32, (float)p->dV, n, N, p->ld,
-                         p->gga, 1.0, p->tcq_part, p->F2e, p->tc_err, c.st, 4, p->zhl);
+                         p->gga, 1.0, p->tcq_part, p->F2e, p->tc_err, c.st, p->hf ? 1 : 4, p->zhl);
   } else {
   launch_density(p->phi, p->gga ? p->dphi : nullptr, p->D, n, N, p->rho, p->gga ? p->grho : nullptr,
                  nullptr, c.st);
@@ -1541,6 +1558,23 @@ int hqcgb_eigh(int n, int batch, const double *A, double *w, double *V, void *st
 }
 
 const char *hqcgb_last_error(void) { return g_err.c_str(); }
+
+int hqcgb_tune_set(const char *name, long long value) {
+  HQ_GUARD({
+    HQ_REQUIRE(name, "null argument");
+    const std::string k(name);
+    static const char *known[] = {"quad_kchunk", "exx_group", "exx_gram_ctas"};
+    bool ok = false;
+    for (const char *q : known) ok = ok || k == q;
+    HQ_REQUIRE(ok, "unknown tuning knob: " + k);
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    if (value <= 0) g_tune.erase(k);
+    else g_tune[k] = value;
+    return HQCGB_OK;
+  });
+}
+
+long long hqcgb_tune_get(const char *name) { return name ? tune_get(name, 0) : 0; }
 
 int hqcgb_profile(int enable) {
   HQ_GUARD({

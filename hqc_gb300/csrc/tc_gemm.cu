@@ -1686,14 +1686,18 @@ void launch_tc_quadrature(const float *phi, const float *dphi, const float *phih
                           double scale, double *partial, double *M, int *err, cudaStream_t st, int drain,
                           float *zhl) {
   HQ_REQUIRE(zhl && phihl, "quadrature needs the split operand buffers");
+  // K chunk: a tuned multiple of the default (the partial tiles are sized
+  // for the default, so longer chunks always fit)
+  long long kc = tune_get("quad_kchunk", tc_quad_chunk());
+  if (kc < tc_quad_chunk() || kc % tc_quad_chunk() != 0 || kc > (1 << 20)) kc = tc_quad_chunk();
   if (!gga) {
     launch_split_operand(phi, nullptr, w, nullptr, nao, N, ld, ld, 1.f, 0.f, zhl, st);
-    launch_tc_quad_split(zhl, phihl, nao, N, ld, true, false, scale, partial, M, err, st, drain);
+    launch_tc_quad_split(zhl, phihl, nao, N, ld, true, false, scale, partial, M, err, st, drain, (int)kc);
     return;
   }
   HQ_REQUIRE(dphi && u, "GGA quadrature needs dphi and u");
   launch_split_operand(phi, dphi, w, u, nao, N, ld, ld, 0.5f, dV, zhl, st);
-  launch_tc_quad_split(zhl, phihl, nao, N, ld, false, true, scale, partial, M, err, st, drain);
+  launch_tc_quad_split(zhl, phihl, nao, N, ld, false, true, scale, partial, M, err, st, drain, (int)kc);
 }
 
 size_t tc_density_partial_doubles(int nao, long long ld, bool gga) {

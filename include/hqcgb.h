@@ -354,6 +354,20 @@ int hqcgb_diis_coefficients(int space, const double *B, double *c);
  * jnp.linalg.eigh (hqc/pbc/solver.py:795, 812; hqc/pbc/scf.py:69,138,198). */
 int hqcgb_eigh_herm(int n, int batch, const double *A, double *w, double *V, void *stream);
 
+/* Run-time tuning knobs, set by the autotuner (hqc_gb300/tune.py) from
+ * measurements; each changes launch shapes only (results agree to rounding):
+ *   "quad_kchunk"   grid points per CTA of the Fock quadrature (a multiple
+ *                   of 2048; default 2048),
+ *   "exx_group"     orbitals per exact-exchange group (read when a plan is
+ *                   created; default from a 1.5 GB buffer budget),
+ *   "exx_gram_ctas" CTAs of the exchange's tensor-core Gram (read when a
+ *                   plan is created; default 304).
+ * value <= 0 restores the default.  No counterpart in the reference (XLA
+ * picks its own launch shapes). */
+int hqcgb_tune_set(const char *name, long long value);
+/* The value set for a knob, 0 when it runs with its default. */
+long long hqcgb_tune_get(const char *name);
+
 /* Human-readable description of the last error on this host thread. */
 const char *hqcgb_last_error(void);
 

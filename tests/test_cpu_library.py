@@ -300,3 +300,49 @@ def test_plain_c_client_links_and_runs(tmp_path):
     r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
     assert r.returncode == 0, r.stderr
     assert "c_client ok" in r.stdout
+
+
+def test_jax_ffi_handler_matches_its_python_wrapper():
+    """The XLA FFI handler (hqc_gb300/jax_ffi/pes_ffi.cc, compiled only where
+    jaxlib is installed) and the ffi_call in hqc_gb300/jax_ffi/__init__.py
+    agree on the call signature: the same attribute names, as many results
+    as the wrapper declares, two positional arguments."""
+    import re
+    src = open(os.path.join(ROOT, "hqc_gb300", "jax_ffi", "pes_ffi.cc")).read()
+    py = open(os.path.join(ROOT, "hqc_gb300", "jax_ffi", "__init__.py")).read()
+    bind = src[src.index("XLA_FFI_DEFINE_HANDLER_SYMBOL"):]
+    attrs = re.findall(r'\.Attr<[^>]+>\("(\w+)"\)', bind)
+    assert attrs == ["plan", "L_rs", "rs", "kappa", "gmax"]
+    for a in attrs:
+        assert re.search(rf"\b{a}=np\.", py), a
+    n_ret = len(re.findall(r"\.Ret<", bind))
+    n_out = py[py.index("outs = ("):py.index("call = jax.ffi.ffi_call")].count("ShapeDtypeStruct(")
+    assert n_ret == n_out == 6
+    assert len(re.findall(r"\.Arg<", bind)) == 2
+    # the handler's results are the ABI's outputs: hqcgb_pes_batch + hqcgb_ewald
+    hdr = open(os.path.join(ROOT, "include", "hqcgb.h")).read()
+    for fn in ("hqcgb_pes_batch", "hqcgb_ewald", "hqcgb_last_error"):
+        assert fn in src and fn in hdr
+
+
+def test_tuning_knobs_and_cache(monkeypatch, tmp_path):
+    """Host side of the autotuner: knobs set and read back through the C ABI
+    (no GPU work), unknown knobs rejected, and a measured choice cached per
+    key so that a second run applies it without measuring."""
+    from hqc_gb300 import tune, _lib
+    tune.set_knob("quad_kchunk", 4096)
+    assert tune.get_knob("quad_kchunk") == 4096
+    tune.set_knob("quad_kchunk", 0)
+    assert tune.get_knob("quad_kchunk") == 0
+    with pytest.raises(_lib.HqcgbError):
+        tune.set_knob("no_such_knob", 1)
+    monkeypatch.setattr(tune, "CACHE", str(tmp_path / "tune.json"))
+    calls = []
+
+    def measure():
+        calls.append(1)
+        return 8192, {2048: 2.0, 8192: 1.0}
+
+    assert tune._cached("gpu|quad_kchunk|270|81", measure) == (8192, {2048: 2.0, 8192: 1.0})
+    assert tune._cached("gpu|quad_kchunk|270|81", measure) == (8192, None)
+    assert len(calls) == 1
