@@ -81,7 +81,7 @@ constexpr int kMaxN1 = 16, kMaxN2 = 16;  // register-blocked factor sizes
 // sum into tmp.  Returns the buffer holding the result; `in` may alias
 // `out`.  Ends with a block barrier.
 template <typename R, typename R2>
-__device__ R2 *dft_axis0(const R2 *in, R2 *tmp, R2 *out, int n, int ncol, int n1, const R2 *w) {
+__device__ R2 *dft_axis0_any(const R2 *in, R2 *tmp, R2 *out, int n, int ncol, int n1, const R2 *w) {
   const int n2 = n1 > 1 ? n / n1 : n;
   if (n1 == 1 || n1 > kMaxN1 || n2 > kMaxN2) {
     const int nh = (n + 1) / 2;
@@ -196,6 +196,124 @@ __device__ R2 *dft_axis0(const R2 *in, R2 *tmp, R2 *out, int n, int ncol, int n1
   return out;
 }
 
+// The same two-factor transform for the grids of the benchmark
+// configurations (n = N1 N2 at compile time): the inner transforms' twiddles
+// live in registers and every index is a constant, which removes most of the
+// integer work of the generic routine; work items advance without divisions.
+template <typename R, typename R2, int N1, int N2>
+__device__ R2 *dft_axis0_fixed(const R2 *in, R2 *tmp, R2 *out, int ncol, const R2 *w) {
+  constexpr int n = N1 * N2;
+  R2 w1[N1], w2[N2];  // W_N1^m = W^(N2 m), W_N2^m = W^(N1 m)
+#pragma unroll
+  for (int m = 0; m < N1; ++m) w1[m] = w[N2 * m];
+#pragma unroll
+  for (int m = 0; m < N2; ++m) w2[m] = w[N1 * m];
+  const int step_r = (int)blockDim.x / ncol, step_c = (int)blockDim.x - step_r * ncol;
+  {
+    int j2 = (int)threadIdx.x / ncol, col = (int)threadIdx.x - j2 * ncol;
+    while (j2 < N2) {
+      R2 x[N1];
+#pragma unroll
+      for (int j1 = 0; j1 < N1; ++j1) x[j1] = in[(N2 * j1 + j2) * ncol + col];
+      R2 s0 = x[0];
+#pragma unroll
+      for (int j1 = 1; j1 < N1; ++j1) {
+        s0.x += x[j1].x;
+        s0.y += x[j1].y;
+      }
+      tmp[(j2 * N1) * ncol + col] = s0;
+#pragma unroll
+      for (int k1 = 1; 2 * k1 < N1; ++k1) {
+        R2 C = x[0], S;
+        S.x = 0;
+        S.y = 0;
+#pragma unroll
+        for (int j1 = 1; j1 < N1; ++j1) {
+          const R2 ww = w1[(j1 * k1) % N1];
+          C.x += x[j1].x * ww.x;
+          C.y += x[j1].y * ww.x;
+          S.x += x[j1].x * ww.y;
+          S.y += x[j1].y * ww.y;
+        }
+        R2 a, b;
+        a.x = C.x - S.y;
+        a.y = C.y + S.x;
+        b.x = C.x + S.y;
+        b.y = C.y - S.x;
+        // j2 k1 < n: no reduction of the twiddle index
+        tmp[(j2 * N1 + k1) * ncol + col] = cmul(a, w[j2 * k1]);
+        tmp[(j2 * N1 + N1 - k1) * ncol + col] = cmul(b, w[j2 * (N1 - k1)]);
+      }
+      col += step_c;
+      j2 += step_r;
+      if (col >= ncol) {
+        col -= ncol;
+        ++j2;
+      }
+    }
+  }
+  __syncthreads();
+  {
+    int k1 = (int)threadIdx.x / ncol, col = (int)threadIdx.x - k1 * ncol;
+    while (k1 < N1) {
+      R2 y[N2];
+#pragma unroll
+      for (int j2 = 0; j2 < N2; ++j2) y[j2] = tmp[(j2 * N1 + k1) * ncol + col];
+      R2 s0 = y[0];
+#pragma unroll
+      for (int j2 = 1; j2 < N2; ++j2) {
+        s0.x += y[j2].x;
+        s0.y += y[j2].y;
+      }
+      out[k1 * ncol + col] = s0;
+#pragma unroll
+      for (int k2 = 1; 2 * k2 < N2; ++k2) {
+        R2 C = y[0], S;
+        S.x = 0;
+        S.y = 0;
+#pragma unroll
+        for (int j2 = 1; j2 < N2; ++j2) {
+          const R2 ww = w2[(j2 * k2) % N2];
+          C.x += y[j2].x * ww.x;
+          C.y += y[j2].y * ww.x;
+          S.x += y[j2].x * ww.y;
+          S.y += y[j2].y * ww.y;
+        }
+        R2 a, b;
+        a.x = C.x - S.y;
+        a.y = C.y + S.x;
+        b.x = C.x + S.y;
+        b.y = C.y - S.x;
+        out[(k1 + N1 * k2) * ncol + col] = a;
+        out[(k1 + N1 * (N2 - k2)) * ncol + col] = b;
+      }
+      col += step_c;
+      k1 += step_r;
+      if (col >= ncol) {
+        col -= ncol;
+        ++k1;
+      }
+    }
+  }
+  __syncthreads();
+  (void)n;
+  return out;
+}
+
+// Dispatch: the fixed-size transforms for 25, 33, 49, 65 and 81 points,
+// the generic routine otherwise.
+template <typename R, typename R2>
+__device__ R2 *dft_axis0(const R2 *in, R2 *tmp, R2 *out, int n, int ncol, int n1, const R2 *w) {
+  switch (n) {
+    case 25: return dft_axis0_fixed<R, R2, 5, 5>(in, tmp, out, ncol, w);
+    case 33: return dft_axis0_fixed<R, R2, 3, 11>(in, tmp, out, ncol, w);
+    case 49: return dft_axis0_fixed<R, R2, 7, 7>(in, tmp, out, ncol, w);
+    case 65: return dft_axis0_fixed<R, R2, 5, 13>(in, tmp, out, ncol, w);
+    case 81: return dft_axis0_fixed<R, R2, 9, 9>(in, tmp, out, ncol, w);
+    default: return dft_axis0_any<R, R2>(in, tmp, out, n, ncol, n1, w);
+  }
+}
+
 // dV * 4 pi / (G^2 N) (0 at G = 0), doubled for kz > 0 (the half spectrum
 // stands for +G and -G).
 __device__ inline double pair_weight(int kx, int ky, int kz, int n, double L, double dV) {
@@ -233,8 +351,12 @@ struct PlaneArgs {
 };
 
 // grid (n x-planes, rows, orbitals of the group)
+// FP32: four CTAs of 256 threads per SM (64 registers); FP64 runs one
 template <typename R>
-__global__ void __launch_bounds__(256) k_exx_plane(PlaneArgs a) {
+constexpr int exx_min_blocks() { return sizeof(R) == 4 ? 4 : 1; }
+
+template <typename R>
+__global__ void __launch_bounds__(256, exx_min_blocks<R>()) k_exx_plane(PlaneArgs a) {
   using R2 = typename C2<R>::T;
   extern __shared__ __align__(16) unsigned char smraw[];
   const int n = a.n, nh = a.nh, x = blockIdx.x, r = blockIdx.y, jl = blockIdx.z;
@@ -330,7 +452,7 @@ __device__ inline uint32_t tf32_rna_x(float x) {
 // OUT 0: FP64 Q;  OUT 1: TF32 hi/lo Q;  OUT 2: gradient dot products.
 // grid (n ky-lines, AOs (OUT 2) or rows, orbitals of the group)
 template <typename R, int OUT>
-__global__ void __launch_bounds__(256) k_exx_column(ColumnArgs a) {
+__global__ void __launch_bounds__(256, OUT == 2 ? 1 : exx_min_blocks<R>()) k_exx_column(ColumnArgs a) {
   using R2 = typename C2<R>::T;
   extern __shared__ __align__(16) unsigned char smraw[];
   const int n = a.n, nh = a.nh, ky = blockIdx.x, r = blockIdx.y, jl = blockIdx.z;

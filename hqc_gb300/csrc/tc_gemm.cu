@@ -16,14 +16,20 @@
 // significant bits) while the MMA fills the other TMEM buffer.  Long sums
 // across CTAs are reduced in FP64.
 //
-// CTA layout (288 threads): warps 0-7 are producers (load fp32 tiles from
-// global memory, split hi/lo, store them in the UMMA canonical K-major
-// 128-byte-swizzled layout) and drain/epilogue threads (warp w owns TMEM
-// lanes 32(w%4).. and column half w/4); warp 8 allocates TMEM and one of its
-// threads issues the MMAs.  Two smem stages of K = 32, two TMEM accumulators
-// of 128 columns.  Every mbarrier wait has an iteration limit: on expiry the
-// kernel records an error code in *err, stops issuing work, waits (bounded)
-// for its MMAs, frees TMEM and returns.
+// Kernels and their CTA layouts (each lists its own below):
+//   k_tc_density      288 threads: warps 0-3 copy fp32 tiles with cp.async and
+//                     split them hi/lo in shared memory, warps 4-7 drain TMEM,
+//                     warp 8 allocates TMEM and issues the MMAs;
+//   k_tc_psi_density  persistent; one warp issues TMA bulk tensor loads into
+//                     a 4-stage ring, four warps split the A box in place,
+//                     four drain, one issues the MMAs;
+//   k_tc_quad_tma /   TMA loads of operands split once by the pass that forms
+//   k_tc_quad_fused   them (k_split_operand), one MMA thread, four or eight
+//                     drain warps, FP64 partial tiles per K chunk.
+// Shared memory holds every operand in the UMMA canonical K-major
+// 128-byte-swizzled layout.  Every mbarrier wait has a time limit: on expiry
+// the kernel records an error code in *err, stops issuing work, waits
+// (bounded) for its MMAs, frees TMEM and returns.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
