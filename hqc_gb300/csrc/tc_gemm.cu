@@ -24,8 +24,9 @@
 //                     a 4-stage ring, four warps split the A box in place,
 //                     four drain, one issues the MMAs;
 //   k_tc_quad_tma /   TMA loads of operands split once by the pass that forms
-//   k_tc_quad_fused   them (k_split_operand), one MMA thread, four or eight
-//                     drain warps, FP64 partial tiles per K chunk.
+//   k_tc_quad_persist them (k_split_operand), one MMA thread, four or eight
+//                     drain warps; FP64 partial tiles per K chunk (tile-list
+//                     form) or per K slice of a persistent CTA group.
 // Shared memory holds every operand in the UMMA canonical K-major
 // 128-byte-swizzled layout.  Every mbarrier wait has a time limit: on expiry
 // the kernel records an error code in *err, stops issuing work, waits
@@ -1096,46 +1097,65 @@ __global__ void __launch_bounds__(kQtThreads, 1)
 }
 
 // ---------------------------------------------------------------------------
-// Fused quadrature for a partial AO block of at most 16 AOs (n_ao % 128 in
-// [1, 16], e.g. 270 = 2 x 128 + 14): each full 128 x 128 tile CTA also
-// computes up to two N = 16 products with the 128-row blocks it already holds
-// -- (m, last) from its A block and, non-symmetric, the transposed (last, n)
-// from its B block -- loading only the 16-row narrow boxes for them.  TMEM
-// (512 columns): two slots of 128 + 16 + 16 accumulator columns, the main
-// tile's TwoSum sums S (128 columns) and the narrow products' sums and
+// Persistent quadrature for n_ao = 128 nfull + last with last <= 16 (e.g.
+// 270 = 2 x 128 + 14) or no partial block: grid (tiles, groups).  The CTAs
+// of group g share one contiguous K slice (1/groups of the grid points) and
+// each computes one full 128 x 128 destination tile over all of it.  The
+// CTAs of a group stream the same 128-row blocks at about the same pace, so
+// a block that one of them brings in from DRAM is still in L2 when the others
+// ask for it.  The compensated sums stay in TMEM / registers over the whole
+// slice; one FP64 partial tile per CTA is written at the end and the reduce
+// adds the groups.
+//
+// The products with the partial block (at most 16 AOs, MMA N = 16) ride
+// along, at most two per CTA, spread over the tiles of a group so that each
+// CTA does about the same work:
+//   kind 0  tile (m, last)    = A block m x narrow B box;
+//   kind 1  tile (last, n)    = (B block n x narrow A box)^T, stored transposed;
+//   kind 2  tile (last, last) = narrow A box x narrow B box.  The MMA reads a
+//           128-row A window that starts at the narrow A box; its rows past
+//           16 are other operand data of the same stage, and the TMEM lanes
+//           they produce are never read.
+// TMEM (512 columns): two slots of 128 + 16 + 16 accumulator columns, the
+// main tile's TwoSum sums S (128 columns) and the narrow products' sums and
 // carries (2 x 16 each); the carries C of the main tile live in the
 // registers of eight drain warps (two per TMEM lane group, 64 main columns
-// each).  The corner (last, last) runs in k_tc_quad_tma.
+// each).
 // ---------------------------------------------------------------------------
-constexpr int kQfDrainWarps = 8;
-constexpr int kQfMmaWarp = kQfDrainWarps;
-constexpr int kQfTmaWarp = kQfMmaWarp + 1;
-constexpr int kQfThreads = (kQfTmaWarp + 1) * 32;
-constexpr uint32_t kQfSlot = kN + 32;           // main + two narrow accumulators
-constexpr uint32_t kQfColS = 2 * kQfSlot;       // main-tile sums S (128 columns)
-constexpr uint32_t kQfColXS = kQfColS + kN;     // narrow sums S (2 x 16)
-constexpr uint32_t kQfColXC = kQfColXS + 32;    // narrow carries C (2 x 16), ends at 512
-constexpr int kQfTmemCols = 512;
-constexpr size_t kQfStageBytes = 4 * kTile + 4 * 16 * 128;  // main pieces + two narrow boxes x 2 pieces
-constexpr size_t kQfSmem = kQtRing * kQfStageBytes + 1024;
+constexpr int kQpDrainWarps = 8;
+constexpr int kQpMmaWarp = kQpDrainWarps;
+constexpr int kQpTmaWarp = kQpMmaWarp + 1;
+constexpr int kQpThreads = (kQpTmaWarp + 1) * 32;
+constexpr uint32_t kQpSlot = kN + 32;           // main + two narrow accumulators
+constexpr uint32_t kQpColS = 2 * kQpSlot;       // main-tile sums S (128 columns)
+constexpr uint32_t kQpColXS = kQpColS + kN;     // narrow sums S (2 x 16)
+constexpr uint32_t kQpColXC = kQpColXS + 32;    // narrow carries C (2 x 16), ends at 512
+constexpr int kQpTmemCols = 512;
+constexpr uint32_t kQpNarrow = 16 * 128;        // one 16-row piece of a narrow box
+// Stage layout: narrow A hi, lo | narrow B hi, lo | A hi | A lo | B hi | B lo.
+// The narrow pieces come first so that the 16 KB window of a kind-2 product
+// (from either narrow A piece) ends inside the stage.
+constexpr uint32_t kQpOffNA = 0, kQpOffNB = 2 * kQpNarrow, kQpOffMain = 4 * kQpNarrow;
+constexpr size_t kQpStageBytes = 4 * kQpNarrow + 4 * kTile;
+constexpr size_t kQpSmem = kQtRing * kQpStageBytes + 1024;
+constexpr int kQpMaxFull = 6;  // full AO blocks handled by the persistent form
+constexpr int kQpMaxTiles = kQpMaxFull * kQpMaxFull;
 
-constexpr int kQfMaxFull = 7;  // full AO blocks handled by the fused form
-
-// Narrow products carried by the diagonal tile (m, m).
-struct QfTile {
-  int nx;              // 0..2
-  int xswap[2];        // 0: A block x narrow B box; 1: B block x narrow A box (transposed)
-  int xrow;            // first row of the narrow block
-  int xmt[2], xnt[2];  // destination tiles
+struct QpTile {
+  int mt, nt;          // the full destination tile
+  int nx;              // narrow products carried (0..2)
+  int kind[2];         // 0, 1 or 2 (above)
+  int xmt[2], xnt[2];  // their destination tiles
+  int loadA, loadB;    // narrow A / B boxes loaded with every stage
 };
 
-struct QfArgs {
-  int tile_m[kQfMaxFull * kQfMaxFull], tile_n[kQfMaxFull * kQfMaxFull];  // the full tiles
-  int ntile;
-  QfTile diag[kQfMaxFull];
+struct QpArgs {
+  QpTile tiles[kQpMaxTiles];
+  int ntile, groups;
+  int xrow;  // first AO row of the narrow block
   long long N;
-  int kchunk, drain, mtiles, ntiles;
-  double *partial;
+  int drain, mtiles, ntiles;
+  double *partial;  // [groups][mtiles][ntiles][128][128]
   int *err;
 };
 
@@ -1145,31 +1165,31 @@ struct QfArgs {
 // the classic 4 KB parameter space.
 constexpr size_t kMaxDynSmem = 227 * 1024;
 static_assert(kDensSmem <= kMaxDynSmem && kPsiSmem <= kMaxDynSmem && kQtSmem <= kMaxDynSmem &&
-                  kQfSmem <= kMaxDynSmem,
+                  kQpSmem <= kMaxDynSmem,
               "dynamic shared memory above 227 KB");
-static_assert(kTmemCols <= 512 && kQfColXC + 32 == (uint32_t)kQfTmemCols && kQfTmemCols <= 512,
+static_assert(kTmemCols <= 512 && kQpColXC + 32 == (uint32_t)kQpTmemCols && kQpTmemCols <= 512,
               "TMEM column layout");
 static_assert(sizeof(QtArgs) + 8 * sizeof(CUtensorMap) <= 4096 &&
-                  sizeof(QfArgs) + 8 * sizeof(CUtensorMap) <= 4096,
+                  sizeof(QpArgs) + 8 * sizeof(CUtensorMap) <= 4096,
               "kernel parameters above 4 KB");
 static_assert(kPsiRowsPerThread * kPsiProducers == kM * 8, "splitter rows per thread");
+static_assert(kQpOffNA + kQpNarrow + kTile <= kQpStageBytes, "kind-2 window leaves the stage");
 
-__global__ void __launch_bounds__(kQfThreads, 1)
-    k_tc_quad_fused(QfArgs a, const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtensorMap mAl,
-                    const __grid_constant__ CUtensorMap mBh, const __grid_constant__ CUtensorMap mBl,
-                    const __grid_constant__ CUtensorMap mAh16, const __grid_constant__ CUtensorMap mAl16,
-                    const __grid_constant__ CUtensorMap mBh16, const __grid_constant__ CUtensorMap mBl16) {
+__global__ void __launch_bounds__(kQpThreads, 1)
+    k_tc_quad_persist(QpArgs a, const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtensorMap mAl,
+                      const __grid_constant__ CUtensorMap mBh, const __grid_constant__ CUtensorMap mBl,
+                      const __grid_constant__ CUtensorMap mAh16, const __grid_constant__ CUtensorMap mAl16,
+                      const __grid_constant__ CUtensorMap mBh16, const __grid_constant__ CUtensorMap mBl16) {
   extern __shared__ __align__(1024) char smraw[];
   char *sm = (char *)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
   __shared__ QtPipe P;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int mt = a.tile_m[blockIdx.x], nt = a.tile_n[blockIdx.x];
-  const int nx = (mt == nt) ? a.diag[mt].nx : 0;
-  const QfTile X = a.diag[mt == nt ? mt : 0];
-  const int chunk = blockIdx.y;
-  const long long k0 = (long long)chunk * a.kchunk;
-  const long long k1 = min(k0 + (long long)a.kchunk, a.N);
-  const int nstages = (int)((k1 - k0 + kStageK - 1) / kStageK);
+  const QpTile T = a.tiles[blockIdx.x];
+  const int g = blockIdx.y;
+  // this group's K slice: stages [s0, s0 + nstages) of 32 points
+  const long long NS = (a.N + kStageK - 1) / kStageK;
+  const long long s0 = NS * g / a.groups;
+  const int nstages = (int)(NS * (g + 1) / a.groups - s0);
   const int nsub = (nstages + a.drain - 1) / a.drain;
   if (tid == 0) {
     for (int b = 0; b < kQtRing; ++b) {
@@ -1178,44 +1198,41 @@ __global__ void __launch_bounds__(kQfThreads, 1)
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&P.acc_full[b], 1);
-      mbar_init(&P.acc_empty[b], kQfDrainWarps * 32);
+      mbar_init(&P.acc_empty[b], kQpDrainWarps * 32);
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == kQfMmaWarp) tmem_alloc(&P.tmem_base, kQfTmemCols);
+  if (warp == kQpMmaWarp) tmem_alloc(&P.tmem_base, kQpTmemCols);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
 
   bool ok = true;
-  if (warp == kQfTmaWarp) {
+  if (warp == kQpTmaWarp) {
     if (lane == 0) {
-      const uint32_t bytes = 4u * (uint32_t)kTile + (uint32_t)nx * 2u * 16u * 128u;
+      const uint32_t bytes = 4u * (uint32_t)kTile + (uint32_t)(T.loadA + T.loadB) * 2u * kQpNarrow;
       for (int st = 0; st < nstages; ++st) {
         const int slot = st % kQtRing, use = st / kQtRing;
         if (ok && use > 0 && !mbar_wait(&P.empty[slot], (unsigned)((use - 1) & 1), a.err, 41)) ok = false;
         if (!ok) break;
-        const int x = (int)(k0 + (long long)st * kStageK);
-        const uint32_t base = smem_u32(sm + slot * kQfStageBytes);
+        const int x = (int)((s0 + st) * kStageK);
+        const uint32_t base = smem_u32(sm + slot * kQpStageBytes), mb = base + kQpOffMain;
         mbar_expect_tx(&P.full[slot], bytes);
-        tma_load_2d(base, &mAh, x, mt * kM, &P.full[slot]);
-        tma_load_2d(base + (uint32_t)kTile, &mAl, x, mt * kM, &P.full[slot]);
-        tma_load_2d(base + 2u * (uint32_t)kTile, &mBh, x, nt * kN, &P.full[slot]);
-        tma_load_2d(base + 3u * (uint32_t)kTile, &mBl, x, nt * kN, &P.full[slot]);
-        for (int e = 0; e < nx; ++e) {
-          // narrow box: from the B arrays for an A-block product, from the A arrays for the transposed one
-          const uint32_t nb = base + 4u * (uint32_t)kTile + (uint32_t)e * 2u * 2048u;
-          if (!X.xswap[e]) {
-            tma_load_2d(nb, &mBh16, x, X.xrow, &P.full[slot]);
-            tma_load_2d(nb + 2048u, &mBl16, x, X.xrow, &P.full[slot]);
-          } else {
-            tma_load_2d(nb, &mAh16, x, X.xrow, &P.full[slot]);
-            tma_load_2d(nb + 2048u, &mAl16, x, X.xrow, &P.full[slot]);
-          }
+        tma_load_2d(mb, &mAh, x, T.mt * kM, &P.full[slot]);
+        tma_load_2d(mb + (uint32_t)kTile, &mAl, x, T.mt * kM, &P.full[slot]);
+        tma_load_2d(mb + 2u * (uint32_t)kTile, &mBh, x, T.nt * kN, &P.full[slot]);
+        tma_load_2d(mb + 3u * (uint32_t)kTile, &mBl, x, T.nt * kN, &P.full[slot]);
+        if (T.loadA) {
+          tma_load_2d(base + kQpOffNA, &mAh16, x, a.xrow, &P.full[slot]);
+          tma_load_2d(base + kQpOffNA + kQpNarrow, &mAl16, x, a.xrow, &P.full[slot]);
+        }
+        if (T.loadB) {
+          tma_load_2d(base + kQpOffNB, &mBh16, x, a.xrow, &P.full[slot]);
+          tma_load_2d(base + kQpOffNB + kQpNarrow, &mBl16, x, a.xrow, &P.full[slot]);
         }
       }
     }
-  } else if (warp == kQfMmaWarp) {
+  } else if (warp == kQpMmaWarp) {
     if (lane == 0) {
       const uint32_t idesc = idesc_tf32(kM, kN), idesc16 = idesc_tf32(kM, 16);
       int stage = 0;
@@ -1223,7 +1240,7 @@ __global__ void __launch_bounds__(kQfThreads, 1)
         const int ab = j & 1, ause = j >> 1;
         if (ok && ause > 0 && !mbar_wait(&P.acc_empty[ab], (unsigned)((ause - 1) & 1), a.err, 44)) ok = false;
         tc_fence_after();
-        const uint32_t tmem_d = P.tmem_base + (uint32_t)ab * kQfSlot;
+        const uint32_t tmem_d = P.tmem_base + (uint32_t)ab * kQpSlot;
         const int s_end = min(nstages, (j + 1) * a.drain);
         bool first = true;
         for (; stage < s_end; ++stage) {
@@ -1231,9 +1248,11 @@ __global__ void __launch_bounds__(kQfThreads, 1)
           if (ok && !mbar_wait(&P.full[slot], (unsigned)(use & 1), a.err, 42)) ok = false;
           tc_fence_after();
           if (ok) {
-            const uint32_t base = smem_u32(sm + slot * kQfStageBytes);
-            const uint32_t Ah = base, Al = base + (uint32_t)kTile, Bh = base + 2u * (uint32_t)kTile,
-                           Bl = base + 3u * (uint32_t)kTile;
+            const uint32_t base = smem_u32(sm + slot * kQpStageBytes), mb = base + kQpOffMain;
+            const uint32_t Ah = mb, Al = mb + (uint32_t)kTile, Bh = mb + 2u * (uint32_t)kTile,
+                           Bl = mb + 3u * (uint32_t)kTile;
+            const uint32_t nAh = base + kQpOffNA, nAl = nAh + kQpNarrow, nBh = base + kQpOffNB,
+                           nBl = nBh + kQpNarrow;
 #pragma unroll
             for (int ks = 0; ks < kStageK / 8; ++ks) {
               const uint32_t off = ks * 32;
@@ -1241,10 +1260,12 @@ __global__ void __launch_bounds__(kQfThreads, 1)
               mma_tf32(tmem_d, sdesc(Al + off), sdesc(Bh + off), idesc, acc);
               mma_tf32(tmem_d, sdesc(Ah + off), sdesc(Bl + off), idesc, 1);
               mma_tf32(tmem_d, sdesc(Ah + off), sdesc(Bh + off), idesc, 1);
-              for (int e = 0; e < nx; ++e) {
-                const uint32_t Nh = base + 4u * (uint32_t)kTile + (uint32_t)e * 4096u, Nl = Nh + 2048u;
-                // the 128-row side: A block, or the B block for the transposed product
-                const uint32_t Wh = X.xswap[e] ? Bh : Ah, Wl = X.xswap[e] ? Bl : Al;
+              for (int e = 0; e < T.nx; ++e) {
+                const int kind = T.kind[e];
+                // the 128-row side and the 16-row narrow box of this product
+                const uint32_t Wh = kind == 0 ? Ah : (kind == 1 ? Bh : nAh);
+                const uint32_t Wl = kind == 0 ? Al : (kind == 1 ? Bl : nAl);
+                const uint32_t Nh = kind == 1 ? nAh : nBh, Nl = kind == 1 ? nAl : nBl;
                 const uint32_t dx = tmem_d + (uint32_t)kN + (uint32_t)e * 16u;
                 mma_tf32(dx, sdesc(Wl + off), sdesc(Nh + off), idesc16, acc);
                 mma_tf32(dx, sdesc(Wh + off), sdesc(Nl + off), idesc16, 1);
@@ -1264,7 +1285,7 @@ __global__ void __launch_bounds__(kQfThreads, 1)
     const int h = warp >> 2;
     const uint32_t lane_off = (uint32_t)((warp & 3) * 32) << 16;
     const int c0 = h * 64;
-    const bool has_x = h < nx;
+    const bool has_x = h < T.nx;
     float cm[64];
 #pragma unroll
     for (int i = 0; i < 64; ++i) cm[i] = 0.f;
@@ -1274,12 +1295,12 @@ __global__ void __launch_bounds__(kQfThreads, 1)
       if (!got) ok = false;
       tc_fence_after();
       if (got) {
-        const uint32_t slot = P.tmem_base + lane_off + (uint32_t)b * kQfSlot;
+        const uint32_t slot = P.tmem_base + lane_off + (uint32_t)b * kQpSlot;
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
           uint32_t va[16], sa[16];
           tmem_ld16_nowait(slot + c0 + q * 16, va);
-          if (j > 0) tmem_ld16_nowait(P.tmem_base + lane_off + kQfColS + c0 + q * 16, sa);
+          if (j > 0) tmem_ld16_nowait(P.tmem_base + lane_off + kQpColS + c0 + q * 16, sa);
           tmem_wait_ld();
           float sv[16];
 #pragma unroll
@@ -1292,11 +1313,11 @@ __global__ void __launch_bounds__(kQfThreads, 1)
               two_sum_add(sv[i], cm[q * 16 + i], v);
             }
           }
-          tmem_st16(P.tmem_base + lane_off + kQfColS + c0 + q * 16, sv);
+          tmem_st16(P.tmem_base + lane_off + kQpColS + c0 + q * 16, sv);
         }
         if (has_x) {
-          const uint32_t xsa = P.tmem_base + lane_off + kQfColXS + (uint32_t)h * 16u,
-                         xca = P.tmem_base + lane_off + kQfColXC + (uint32_t)h * 16u;
+          const uint32_t xsa = P.tmem_base + lane_off + kQpColXS + (uint32_t)h * 16u,
+                         xca = P.tmem_base + lane_off + kQpColXC + (uint32_t)h * 16u;
           uint32_t va[16], sa[16], ca[16];
           tmem_ld16_nowait(slot + kN + (uint32_t)h * 16u, va);
           if (j > 0) {
@@ -1327,11 +1348,11 @@ __global__ void __launch_bounds__(kQfThreads, 1)
     }
     const int row = (warp & 3) * 32 + lane;
     const long long tsz = (long long)kM * kN;
-    double *tile = a.partial + (((long long)chunk * a.mtiles + mt) * a.ntiles + nt) * tsz;
+    double *tile = a.partial + (((long long)g * a.mtiles + T.mt) * a.ntiles + T.nt) * tsz;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       uint32_t sr[16];
-      tmem_ld16_nowait(P.tmem_base + lane_off + kQfColS + c0 + q * 16, sr);
+      tmem_ld16_nowait(P.tmem_base + lane_off + kQpColS + c0 + q * 16, sr);
       tmem_wait_ld();
       if (ok)
 #pragma unroll
@@ -1340,12 +1361,13 @@ __global__ void __launch_bounds__(kQfThreads, 1)
     }
     if (has_x) {
       uint32_t sr[16], cr[16];
-      tmem_ld16_nowait(P.tmem_base + lane_off + kQfColXS + (uint32_t)h * 16u, sr);
-      tmem_ld16_nowait(P.tmem_base + lane_off + kQfColXC + (uint32_t)h * 16u, cr);
+      tmem_ld16_nowait(P.tmem_base + lane_off + kQpColXS + (uint32_t)h * 16u, sr);
+      tmem_ld16_nowait(P.tmem_base + lane_off + kQpColXC + (uint32_t)h * 16u, cr);
       tmem_wait_ld();
-      if (ok) {
-        double *xt = a.partial + (((long long)chunk * a.mtiles + X.xmt[h]) * a.ntiles + X.xnt[h]) * tsz;
-        if (!X.xswap[h]) {
+      const int kind = T.kind[h];
+      if (ok && (kind != 2 || row < 16)) {
+        double *xt = a.partial + (((long long)g * a.mtiles + T.xmt[h]) * a.ntiles + T.xnt[h]) * tsz;
+        if (kind != 1) {
 #pragma unroll
           for (int i = 0; i < 16; ++i)
             xt[(long long)row * kN + i] = (double)__uint_as_float(sr[i]) + (double)__uint_as_float(cr[i]);
@@ -1359,9 +1381,9 @@ __global__ void __launch_bounds__(kQfThreads, 1)
   }
   tc_fence_before();
   __syncthreads();
-  if (warp == kQfMmaWarp) {
+  if (warp == kQpMmaWarp) {
     tc_fence_after();
-    tmem_dealloc(P.tmem_base, kQfTmemCols);
+    tmem_dealloc(P.tmem_base, kQpTmemCols);
   }
 }
 
@@ -1536,10 +1558,14 @@ int tc_quad_tiles(int nao, bool sym) {
 
 // Tile plan of the quadrature for nao AOs in 128-row blocks: which CTA writes
 // which 128 x 128 destination tile (mt, nt) of the partial sums.
-//  * fused form (the last block has at most 16 rows and there are 1..7 full
-//    blocks): k_tc_quad_fused runs the full tiles, each diagonal CTA (m, m)
-//    also running the narrow products (m, last) and, unless symmetric,
-//    (last, m); one k_tc_quad_tma launch runs the (last, last) corner;
+//  * persistent form (1..6 full blocks and a last block of at most 16 rows,
+//    or none): k_tc_quad_persist runs the full tiles; the narrow products
+//    (kind 0 (m, last), kind 1 (last, n) transposed, kind 2 the corner) are
+//    spread over them, at most two per CTA:
+//      non-symmetric: (m, last) on (m, m); (last, n) on ((n + 1) % nfull, n);
+//      symmetric:     (m, last) on (m, m + 1) (or (m, m) for the last block);
+//      the corner on the first tile carrying the fewest;
+//    a shape where some CTA would carry three takes the tile-list form;
 //  * tile-list form otherwise: every tile of the upper triangle (sym) or of
 //    the whole square through k_tc_quad_tma, at most kQtMaxTiles per launch.
 // A tile whose A-side block is the narrow one is computed transposed
@@ -1547,10 +1573,58 @@ int tc_quad_tiles(int nao, bool sym) {
 // MMA's N side, rounded up to a multiple of 16 rows.
 struct QuadTilePlan {
   int nblk = 0, nb_last = 0;
-  bool fused = false;
-  tc::QfArgs f{};                 // fused form: the full tiles and the diagonal extras
+  bool persist = false;
+  tc::QpArgs f{};                 // persistent form: the full tiles and the narrow products they carry
   std::vector<tc::QtArgs> lists;  // k_tc_quad_tma launches, tile lists only
 };
+
+static bool plan_persist(int nao, bool sym, tc::QpArgs &f) {
+  const int nblk = ceil_div(nao, tc::kM);
+  const int last = nao - tc::kM * (nblk - 1);
+  const bool narrow = last < tc::kM;
+  const int nfull = narrow ? nblk - 1 : nblk;
+  if ((narrow && last > 16) || nfull < 1 || nfull > tc::kQpMaxFull) return false;
+  f = tc::QpArgs{};
+  f.xrow = nfull * tc::kM;
+  for (int mt = 0; mt < nfull; ++mt)
+    for (int nt = 0; nt < nfull; ++nt) {
+      if (sym && nt < mt) continue;
+      tc::QpTile &t = f.tiles[f.ntile++];
+      t.mt = mt;
+      t.nt = nt;
+    }
+  if (!narrow) return true;
+  auto find = [&f](int mt, int nt) {
+    for (int i = 0; i < f.ntile; ++i)
+      if (f.tiles[i].mt == mt && f.tiles[i].nt == nt) return i;
+    return -1;
+  };
+  bool fits = true;
+  auto add = [&](int i, int kind, int xmt, int xnt) {
+    if (i < 0 || f.tiles[i].nx >= 2) {
+      fits = false;
+      return;
+    }
+    tc::QpTile &t = f.tiles[i];
+    t.kind[t.nx] = kind;
+    t.xmt[t.nx] = xmt;
+    t.xnt[t.nx] = xnt;
+    ++t.nx;
+    if (kind != 0) t.loadA = 1;
+    if (kind != 1) t.loadB = 1;
+  };
+  for (int m = 0; m < nfull && fits; ++m)
+    add(sym && m + 1 < nfull ? find(m, m + 1) : find(m, m), 0, m, nfull);
+  if (!sym)
+    for (int n = 0; n < nfull && fits; ++n) add(find(nfull > 1 ? (n + 1) % nfull : n, n), 1, nfull, n);
+  if (fits) {
+    int best = 0;
+    for (int i = 1; i < f.ntile; ++i)
+      if (f.tiles[i].nx < f.tiles[best].nx) best = i;
+    add(best, 2, nfull, nfull);
+  }
+  return fits;
+}
 
 static QuadTilePlan plan_quad_tiles(int nao, bool sym) {
   QuadTilePlan p;
@@ -1558,40 +1632,15 @@ static QuadTilePlan plan_quad_tiles(int nao, bool sym) {
   const int last = nao - tc::kM * (p.nblk - 1);
   const bool narrow = last < tc::kM;
   p.nb_last = ceil_div(last, 16) * 16;
-  const int nfull = p.nblk - 1;
+  if (plan_persist(nao, sym, p.f)) {
+    p.persist = true;
+    return p;
+  }
   auto push = [&p](const tc::QtTile &t) {
     if (p.lists.empty() || p.lists.back().ntile == tc::kQtMaxTiles) p.lists.push_back(tc::QtArgs{});
     tc::QtArgs &a = p.lists.back();
     a.tiles[a.ntile++] = t;
   };
-  p.fused = narrow && last <= 16 && nfull >= 1 && nfull <= tc::kQfMaxFull;
-  if (p.fused) {
-    tc::QfArgs &f = p.f;
-    for (int mt = 0; mt < nfull; ++mt)
-      for (int nt = 0; nt < nfull; ++nt) {
-        if (sym && nt < mt) continue;
-        f.tile_m[f.ntile] = mt;
-        f.tile_n[f.ntile] = nt;
-        ++f.ntile;
-      }
-    for (int m = 0; m < nfull; ++m) {
-      tc::QfTile &d = f.diag[m];
-      d.xrow = nfull * tc::kM;
-      d.nx = 0;
-      d.xswap[d.nx] = 0;  // (m, last) from the A block
-      d.xmt[d.nx] = m;
-      d.xnt[d.nx] = nfull;
-      ++d.nx;
-      if (!sym) {  // (last, m) from the B block, transposed
-        d.xswap[d.nx] = 1;
-        d.xmt[d.nx] = nfull;
-        d.xnt[d.nx] = m;
-        ++d.nx;
-      }
-    }
-    push(tc::QtTile{nfull * tc::kM, nfull * tc::kN, p.nb_last, 0, nfull, nfull});
-    return p;
-  }
   for (int mt = 0; mt < p.nblk; ++mt)
     for (int nt = 0; nt < p.nblk; ++nt) {
       if (sym && nt < mt) continue;
@@ -1615,6 +1664,21 @@ static QuadTilePlan plan_quad_tiles(int nao, bool sym) {
   return p;
 }
 
+// K slices (CTA groups) of the persistent quadrature: one CTA per SM for
+// the whole launch (the autotuner's "quad_groups" when set), at most one
+// slice per 64 stages and at most the chunk count the partial buffer holds.
+static int quad_groups(int ntile, long long N) {
+  int dev = 0, sms = 0;
+  HQ_CUDA(cudaGetDevice(&dev));
+  HQ_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  long long g = std::max(1, sms / std::max(1, ntile));
+  const long long t = tune_get("quad_groups", 0);
+  if (t > 0) g = t;
+  g = std::min<long long>(g, std::max<long long>(1, ceil_div(N, (long long)tc::kStageK * 64)));
+  g = std::min<long long>(g, ceil_div(N, (long long)tc_quad_chunk()));
+  return (int)std::max<long long>(1, g);
+}
+
 // M = scale * sum_g A_p(g) B_q(g) (+ its transpose when add_transpose) from the
 // pre-split pieces Ahl, Bhl [2][nao][ld] (hi rows, then lo rows); sym: M is
 // symmetric (only tiles nt >= mt are computed; the reduce mirrors them).
@@ -1627,7 +1691,6 @@ void launch_tc_quad_split(const float *Ahl, const float *Bhl, int nao, long long
   HQ_REQUIRE(kchunk % tc::kStageK == 0, "K chunk must be a multiple of 32");
   HQ_REQUIRE(ld % 32 == 0 && ld >= N, "pre-split operands need a row stride that is a multiple of 32");
   HQ_REQUIRE(N <= (1LL << 31) - 64, "grid too large for 32-bit TMA coordinates");
-  ensure_dyn_smem((const void *)tc::k_tc_quad_tma, tc::kQtSmem);
   const QuadTilePlan plan = plan_quad_tiles(nao, sym);
   const int nblk = plan.nblk;
   const long long rows = nao;
@@ -1640,35 +1703,39 @@ void launch_tc_quad_split(const float *Ahl, const float *Bhl, int nao, long long
   CUtensorMap mAl16 = tc::tensor_map_2d_ext(Al, ld, N, rows, 16);
   CUtensorMap mBh16 = tc::tensor_map_2d_ext(Bh, ld, N, rows, 16);
   CUtensorMap mBl16 = tc::tensor_map_2d_ext(Bl, ld, N, rows, 16);
-  const int chunks = ceil_div(N, kchunk);
-  if (plan.fused) {
-    ensure_dyn_smem((const void *)tc::k_tc_quad_fused, tc::kQfSmem);
-    tc::QfArgs f = plan.f;
+  int nparts = 0;  // partial tiles per destination tile
+  if (plan.persist) {
+    ensure_dyn_smem((const void *)tc::k_tc_quad_persist, tc::kQpSmem);
+    tc::QpArgs f = plan.f;
+    f.groups = quad_groups(f.ntile, N);
     f.N = N;
-    f.kchunk = kchunk;
     f.drain = drain;
     f.mtiles = nblk;
     f.ntiles = nblk;
     f.partial = partial;
     f.err = err;
-    tc::k_tc_quad_fused<<<dim3(f.ntile, chunks), tc::kQfThreads, tc::kQfSmem, st>>>(
+    nparts = f.groups;
+    tc::k_tc_quad_persist<<<dim3(f.ntile, f.groups), tc::kQpThreads, tc::kQpSmem, st>>>(
         f, mAh, mAl, mBh, mBl, mAh16, mAl16, mBh16, mBl16);
     HQ_LAUNCH_CHECK();
-  }
-  for (tc::QtArgs a : plan.lists) {
-    a.N = N;
-    a.kchunk = kchunk;
-    a.drain = drain;
-    a.mtiles = nblk;
-    a.ntiles = nblk;
-    a.partial = partial;
-    a.err = err;
-    tc::k_tc_quad_tma<<<dim3(a.ntile, chunks), tc::kQtThreads, tc::kQtSmem, st>>>(a, mAh, mAl, mBh, mBl,
-                                                                                    mAh16, mAl16, mBh16, mBl16);
-    HQ_LAUNCH_CHECK();
+  } else {
+    ensure_dyn_smem((const void *)tc::k_tc_quad_tma, tc::kQtSmem);
+    nparts = (int)ceil_div(N, (long long)kchunk);
+    for (tc::QtArgs a : plan.lists) {
+      a.N = N;
+      a.kchunk = kchunk;
+      a.drain = drain;
+      a.mtiles = nblk;
+      a.ntiles = nblk;
+      a.partial = partial;
+      a.err = err;
+      tc::k_tc_quad_tma<<<dim3(a.ntile, nparts), tc::kQtThreads, tc::kQtSmem, st>>>(
+          a, mAh, mAl, mBh, mBl, mAh16, mAl16, mBh16, mBl16);
+      HQ_LAUNCH_CHECK();
+    }
   }
   tc::k_tc_quad_reduce<<<ceil_div((long long)nao * nao, 256), 256, 0, st>>>(
-      partial, chunks, nblk, nblk, nao, sym ? 1 : 0, add_transpose ? 1 : 0, scale, M);
+      partial, nparts, nblk, nblk, nao, sym ? 1 : 0, add_transpose ? 1 : 0, scale, M);
   HQ_LAUNCH_CHECK();
 }
 
@@ -1883,9 +1950,9 @@ extern "C" int hqcgb_tc_orbital_density(int nao, long long N, long long ld, cons
 
 // C ABI (host only, no device work): the quadrature's tile plan for nao AOs
 // (sym: upper-triangle tiles only).  One row of 7 ints per computed product,
-// {kind, mt, nt, arow, brow, nb, swap}: kind 0 a full tile of the fused
-// kernel, 1 a narrow product carried by a fused diagonal CTA, 2 a tile of the
-// tile-list kernel; (mt, nt) the destination tile, arow / brow the first AO
+// {kind, mt, nt, arow, brow, nb, swap}: kind 0 a full tile of the
+// persistent kernel, 1 a narrow product carried by one of its CTAs, 2 a tile
+// of the tile-list kernel; (mt, nt) the destination tile, arow / brow the first AO
 // row of the MMA's A / B side (swap = 1: A side from the B operand, stored
 // transposed), nb the MMA N.  count = rows (at most cap are written);
 // launches = quadrature kernel launches before the reduce.
@@ -1903,14 +1970,16 @@ extern "C" int hqcgb_tc_quad_tiles(int nao, int sym, int cap, int *tiles, int *c
       }
       ++k;
     };
-    if (p.fused) {
+    if (p.persist) {
       for (int t = 0; t < p.f.ntile; ++t)
-        row(0, p.f.tile_m[t], p.f.tile_n[t], p.f.tile_m[t] * tc::kM, p.f.tile_n[t] * tc::kN, tc::kN, 0);
+        row(0, p.f.tiles[t].mt, p.f.tiles[t].nt, p.f.tiles[t].mt * tc::kM, p.f.tiles[t].nt * tc::kN, tc::kN, 0);
       for (int t = 0; t < p.f.ntile; ++t) {
-        if (p.f.tile_m[t] != p.f.tile_n[t]) continue;
-        const tc::QfTile &d = p.f.diag[p.f.tile_m[t]];
-        for (int x = 0; x < d.nx; ++x)
-          row(1, d.xmt[x], d.xnt[x], p.f.tile_m[t] * tc::kM, d.xrow, 16, d.xswap[x]);
+        const tc::QpTile &q = p.f.tiles[t];
+        for (int x = 0; x < q.nx; ++x) {
+          // the MMA's 128-row side: A block (kind 0), B block (kind 1, transposed), narrow A box (kind 2)
+          const int arow = q.kind[x] == 0 ? q.mt * tc::kM : (q.kind[x] == 1 ? q.nt * tc::kN : p.f.xrow);
+          row(1, q.xmt[x], q.xnt[x], arow, p.f.xrow, 16, q.kind[x] == 1 ? 1 : 0);
+        }
       }
     }
     for (const tc::QtArgs &a : p.lists)
@@ -1919,7 +1988,7 @@ extern "C" int hqcgb_tc_quad_tiles(int nao, int sym, int cap, int *tiles, int *c
         row(2, q.mt, q.nt, q.arow, q.brow, q.nb, q.swap);
       }
     *count = k;
-    *launches = (p.fused ? 1 : 0) + (int)p.lists.size();
+    *launches = (p.persist ? 1 : 0) + (int)p.lists.size();
     return HQCGB_OK;
   } catch (const Error &e) {
     set_error(e.msg);

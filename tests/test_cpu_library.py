@@ -153,14 +153,18 @@ def test_quadrature_tile_plan_covers_each_tile_once(nao, sym):
     """The tensor-core quadrature's tile plan (host code of the library, no
     GPU): every destination tile of M (the upper triangle when symmetric) is
     written by exactly one product; each product's operand rows match its
-    tile (transposed products swap them); the MMA N covers the rows of the
-    B-side block in multiples of 16; the fused form is taken exactly when
-    the last block has at most 16 rows and there are 1..7 full blocks; the
-    tile-list kernel gets at most 12 tiles per launch."""
+    tile (transposed products swap them; the corner reads the narrow block on
+    both sides); the MMA N covers the rows of the B-side block in multiples of
+    16; the persistent form is taken exactly when there are 1..6 full blocks,
+    the last block has at most 16 rows (or there is none) and no CTA would
+    carry more than two narrow products; the tile-list kernel gets at most 12
+    tiles per launch."""
     from hqc_gb300 import _lib
     tiles, launches = _lib.quad_tiles(nao, sym)
     nblk = -(-nao // 128)
     last = nao - 128 * (nblk - 1)
+    narrow = last < 128
+    nfull = nblk - 1 if narrow else nblk
     cover = np.zeros((nblk, nblk), int)
     for kind, mt, nt, arow, brow, nb, swap in tiles:
         assert 0 <= mt < nblk and 0 <= nt < nblk
@@ -173,12 +177,15 @@ def test_quadrature_tile_plan_covers_each_tile_once(nao, sym):
             assert nb == 16 and b_blk == nblk - 1
     want = np.triu(np.ones((nblk, nblk), int)) if sym else np.ones((nblk, nblk), int)
     np.testing.assert_array_equal(cover, want)
-    fused = last <= 16 and 1 <= nblk - 1 <= 7
-    assert (tiles[:, 0] != 2).any() == fused
+    persist = (last <= 16 or not narrow) and 1 <= nfull <= 6 and not (nfull == 1 and narrow and not sym)
+    assert (tiles[:, 0] != 2).any() == persist
     n_list = int((tiles[:, 0] == 2).sum())
-    assert launches == int(fused) + -(-n_list // 12)
-    if fused:
-        assert n_list == 1  # the (last, last) corner alone
+    assert launches == int(persist) + -(-n_list // 12)
+    if persist:
+        assert n_list == 0
+        # one narrow product per tile of the partial block: (m, last) for
+        # every full block m, (last, n) too when not symmetric, and the corner
+        assert int((tiles[:, 0] == 1).sum()) == (0 if not narrow else (nfull + 1 if sym else 2 * nfull + 1))
 
 
 def test_autograd_wrapper_chains_engine_gradient():

@@ -43,11 +43,13 @@ def test_tc_density_matches_fp64(nao, N):
 
 
 @pytest.mark.parametrize("nao,N", [(1, 1000), (20, 29791), (80, 29791), (130, 4097), (150, 4097),
-                                   (256, 4097), (270, 531441), (600, 3000), (900, 2500), (1000, 2500)])
+                                   (256, 4097), (270, 531441), (600, 3000), (784, 2500), (900, 2500),
+                                   (1000, 2500)])
 def test_tc_quadrature_matches_fp64(nao, N):
-    """LDA form (symmetric tile set).  600 and 1000 AOs need 15 and 36 tiles,
-    several tile-list launches; 900 AOs is the largest fused form (7 full
-    blocks and a 4-row block)."""
+    """LDA form (symmetric tile set).  130, 256, 270 and 784 AOs take the
+    persistent form (784: six full blocks and a 16-row block, the largest);
+    600, 900 and 1000 AOs need 15, 36 and 36 tiles, several tile-list
+    launches."""
     import torch
     from hqc_gb300._lib import tc_quadrature
     phi, _, ld = _operands(nao, N, 100 + nao)
