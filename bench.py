@@ -244,8 +244,8 @@ def run_ours(args):
     conc = args.concurrency or B
     # launch shapes picked by the autotuner at this run's shapes (cached per GPU)
     from hqc_gb300.tune import tune_quadrature
-    kchunk, ktable = tune_quadrature(270, 81)
-    tuning = {"quad_kchunk": kchunk, "measured_ms": ktable}
+    (qknob, qval), ktable = tune_quadrature(270, 81)
+    tuning = {qknob: qval, "measured_ms": ktable}
     w0 = workload(7)
     n, L, rs = w0["n"], w0["L"], w0["rs"]
     kw = dict(dft=True, xc=w0["xc"], grid_length=w0["grid_length"], tol=1e-7, max_cycle=100,

@@ -142,9 +142,11 @@ int tc_quad_chunk();
 // kchunk: grid points per CTA along the contraction (0: tc_quad_chunk())
 size_t tc_quad_partial_doubles(int nao, long long N, int kchunk = 0);
 int tc_quad_tiles(int nao, bool sym);  // destination tiles of the tile plan (upper triangle if sym)
+// blocked: the pieces are K-blocked [ld / 32][nao][32] (as launch_split_operand
+// writes them); otherwise row-major [nao][ld]
 void launch_tc_quad_split(const float *Ahl, const float *Bhl, int nao, long long N, long long ld,
                           bool sym, bool add_transpose, double scale, double *partial, double *M,
-                          int *err, cudaStream_t st, int drain, int kchunk = 0);
+                          int *err, cudaStream_t st, int drain, int kchunk = 0, bool blocked = false);
 void launch_split_operand(const float *phi, const float *dphi, const float *w, const float *u, int nao,
                           long long N, long long ldi, long long ldo, float a, float b, float *out,
                           cudaStream_t st);

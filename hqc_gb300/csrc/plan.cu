@@ -909,11 +909,14 @@ static int scf_one(hqcgb_plan *p, const double *xp_dev, const hqcgb_scf_out *out
     };
     while ((std::fabs(E1 - E0) > etol || enorm > errtol) && loop < P.max_cycle) diis_step();
     stopped = loop < P.max_cycle;
-    // Mixed path, stopped at the floor with the commutator still above the
-    // requested 10 tol: a few more iterations while it keeps falling by at
-    // least a fifth (the gradient's error is first order in it; at the noise
-    // floor it stops falling and the polish ends).
-    if (p->mixed && loop < P.max_cycle && enorm > 10.0 * P.tol) {
+    // Mixed path with smearing, stopped at the floor with the commutator
+    // still above the requested 10 tol: a few more iterations while it keeps
+    // falling by at least a fifth (the gradient's error is first order in it;
+    // at the noise floor it stops falling and the polish ends).  Without
+    // smearing the floored stop already leaves the forces well inside their
+    // bound (H54 PBE: 2.4e-7 Ha/Bohr), and the polish would only add
+    // iterations.
+    if (p->mixed && P.smearing && loop < P.max_cycle && enorm > 10.0 * P.tol) {
       for (int extra = 0; extra < 6 && loop < P.max_cycle && enorm > 10.0 * P.tol; ++extra) {
         const double prev = enorm;
         diis_step();
@@ -1563,7 +1566,7 @@ int hqcgb_tune_set(const char *name, long long value) {
   HQ_GUARD({
     HQ_REQUIRE(name, "null argument");
     const std::string k(name);
-    static const char *known[] = {"quad_kchunk", "exx_group", "exx_gram_ctas"};
+    static const char *known[] = {"quad_kchunk", "quad_groups", "exx_group", "exx_gram_ctas", "psi_ring"};
     bool ok = false;
     for (const char *q : known) ok = ok || k == q;
     HQ_REQUIRE(ok, "unknown tuning knob: " + k);

@@ -243,6 +243,20 @@ __device__ inline void two_sum_add(float &s, float &c, float v) {
   s = t;
 }
 
+// Compensated dot-product step in FP32 (Ogita-Rump-Oishi Dot2): (s, c) +=
+// x y, the product split exactly by an FMA and added by TwoSum, so the sum
+// (double)s + (double)c keeps about twice FP32's precision.  Used for the
+// per-point sums of the orbital density: GB300 runs FP64 at 1/64 of the FP32
+// rate, and FP64 accumulation there made the epilogue the kernel's limit.
+__device__ __forceinline__ void dot2_add(float &s, float &c, float x, float y) {
+  const float p = __fmul_rn(x, y);
+  const float e = fmaf(x, y, -p);
+  const float t = __fadd_rn(s, p);
+  const float z = __fsub_rn(t, s);
+  c = __fadd_rn(c, __fadd_rn(__fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z)), e));
+  s = t;
+}
+
 // Shared skeleton: `fill(stage_index, smem_stage_base)` is executed by the
 // 256 worker threads; after every `drain` stages the workers add the TMEM
 // sub-chunk sum into (s[64], c[64]) -- their row (lane) and column half.
@@ -326,13 +340,16 @@ __device__ inline void cp_async_commit() { asm volatile("cp.async.commit_group;"
 template <int N>
 __device__ inline void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
-// Generic K-major operand description: element (row, k) at ptr[row * ld + k];
-// rows >= rows_valid and k >= k_end read as zero.  Every row start and every
-// 4-element chunk is 16-byte aligned (ld % 4 == 0, k offsets multiples of 4).
+// Generic K-major operand description: element (row, k) at
+// ptr[row * ld + (k / 32) * kstride + k % 32] -- row-major with ld = row
+// stride and kstride = 32, or K-blocked ([k / 32][row][32]) with ld = 32 and
+// kstride = rows x 32; rows >= rows_valid and k >= k_end read as zero.  Every
+// row start and every 4-element chunk is 16-byte aligned.
 struct Operand {
   const float *ptr;
   long long ld;
   int rows_valid;
+  long long kstride;
 };
 
 constexpr int kStages = 3;  // smem ring depth; copies run 2 stages ahead
@@ -373,8 +390,8 @@ __device__ __forceinline__ bool run_pipe(Pipe &P, char *sm, float4 *wslot, const
       for (int j = 0; j < 8; ++j) {
         int r = (tid >> 3) + 16 * j;
         uint32_t off = swz(r, cch);
-        const float *ga = arow[j] + (kin ? kk : 0);
-        const float *gb = brow[j] + (kin ? kk : 0);
+        const float *ga = arow[j] + (kin ? (kk / kStageK) * A.kstride : 0);
+        const float *gb = brow[j] + (kin ? (kk / kStageK) * B.kstride : 0);
         if (kin && ((avalid >> j) & 1u)) cp_async16(base + off, ga);
         else cp_async_zero16(base + off, arow[j]);
         if (kin && ((bvalid >> j) & 1u)) cp_async16(base + kMaxSplit * kTile + off, gb);
@@ -474,20 +491,31 @@ __device__ inline void pipe_finish(Pipe &P) {
 // FP64 partial tiles of the quadrature: P[chunk][tile_m][tile_n][128][128].
 constexpr size_t kWslotBytes = kStages * kProducers * sizeof(float4);
 
-// M[p][q] = scale * sum_chunks P  (+ mirror for sym; + transpose-add for GGA)
+// M[p][q] = scale * sum_chunks P  (+ mirror for sym; + transpose-add for GGA);
+// the tile (corner, corner), when corner >= 0, sums ncorner partial tiles
 __global__ void k_tc_quad_reduce(const double *__restrict__ P, int nchunk, int mtiles, int ntiles,
                                  int nao, int sym, int add_transpose, double scale,
-                                 double *__restrict__ M) {
+                                 double *__restrict__ M, int corner, int ncorner) {
   int idx = blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= nao * nao) return;
   int p = idx / nao, q = idx % nao;
   auto get = [&](int pp, int qq) {
     if (sym && (qq / kN) < (pp / kM)) { int t = pp; pp = qq; qq = t; }
     int tm = pp / kM, tn = qq / kN, r = pp % kM, cc = qq % kN;
-    double s = 0;
-    for (int k = 0; k < nchunk; ++k)
-      s += P[((((long long)k * mtiles + tm) * ntiles + tn) * kM + r) * kN + cc];
-    return s;
+    const int nk = (tm == corner && tn == corner) ? ncorner : nchunk;
+    const long long stride = (long long)mtiles * ntiles * kM * kN;
+    const double *src = P + (((long long)tm * ntiles + tn) * kM + r) * kN + cc;
+    // four independent partial sums keep four loads in flight
+    double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+    int k = 0;
+    for (; k + 4 <= nk; k += 4) {
+      s0 += src[(k + 0) * stride];
+      s1 += src[(k + 1) * stride];
+      s2 += src[(k + 2) * stride];
+      s3 += src[(k + 3) * stride];
+    }
+    for (; k < nk; ++k) s0 += src[k * stride];
+    return (s0 + s1) + (s2 + s3);
   };
   // sym: the (p, q) and (q, p) elements of a diagonal tile round differently
   // (the weight multiplies one operand before its TF32 split), so both are
@@ -500,8 +528,8 @@ __global__ void k_tc_quad_reduce(const double *__restrict__ P, int nchunk, int m
 
 // ---------------------------------------------------------------------------
 // Density: X = D phi on tiles (128 AOs) x (128 grid points), K = AO, from the
-// K-major operands D[p][q] (row stride ldk) and phiT[g][q] (grid-major copy,
-// row stride ldk).  Epilogue: part[mt][g] = sum_{p in tile} phi_p(g) X_p(g)
+// K-major operands D[p][q] (row stride ldk) and phiT (the grid-major copy,
+// K-blocked: phiT[q / 32][g][q % 32]).  Epilogue: part[mt][g] = sum_{p in tile} phi_p(g) X_p(g)
 // and, for GGA, part_g[c][mt][g] = 2 sum_p dphi_c,p(g) X_p(g) (FP64).
 // ---------------------------------------------------------------------------
 struct DensArgs {
@@ -600,9 +628,13 @@ __global__ void k_tc_density_reduce(const double *__restrict__ part, const doubl
   }
 }
 
-// phiT[g][q] (row stride ldk) = phi[q][g] for g < N, q < nao; zero for q in [nao, ldk)
+// Grid-major copy of phi in K-blocks of 32 AOs: phiT[q / 32][g][q % 32] =
+// phi[q][g] for g < N, q < nao; zero for q in [nao, ldk).  A 128-point x
+// 32-AO box of it is one contiguous 16 KB run of memory, so the tensor-core
+// kernels' TMA loads stream whole DRAM pages instead of 128 rows of 128 bytes
+// spread over the row stride.
 __global__ void k_transpose_phi(const float *__restrict__ phi, int nao, long long N, long long ld,
-                                float *__restrict__ phiT, int ldk) {
+                                float *__restrict__ phiT) {
   __shared__ float t[32][33];
   long long g0 = (long long)blockIdx.x * 32;
   int q0 = blockIdx.y * 32;
@@ -613,10 +645,10 @@ __global__ void k_transpose_phi(const float *__restrict__ phi, int nao, long lon
     t[r][tx] = (q < nao && g < N) ? phi[(long long)q * ld + g] : 0.f;
   }
   __syncthreads();
+  // K-blocked: AO block blockIdx.y, grid point g, AO q0 + tx (128 contiguous bytes per g)
   for (int r = ty; r < 32; r += 8) {
     long long g = g0 + r;
-    int q = q0 + tx;
-    if (g < N && q < ldk) phiT[g * ldk + q] = t[tx][r];
+    if (g < N) phiT[((long long)blockIdx.y * N + g) * 32 + tx] = t[tx][r];
   }
 }
 
@@ -627,9 +659,9 @@ __global__ void k_transpose_phi(const float *__restrict__ phi, int nao, long lon
 // sum_pq D_pq phi_p phi_q of D = C diag(f) C^T (hqc/pbc/solver.py:566-577,
 // 690) at npsi / n_ao of the GEMM work.
 //
-// Tiles: M = 128 grid points (A = rows of the grid-major phiT / dphiT,
-// K-major), N = npsi (B = the TF32 hi/lo pieces of Y^T, pre-split in global
-// memory), K = AO in stages of 32.  Persistent CTAs loop over grid tiles;
+// Tiles: M = 128 grid points (A = rows of the grid-major, K-blocked phiT /
+// dphiT: [component][AO block][g][32]), N = npsi (B = the TF32 hi/lo pieces
+// of Y^T, pre-split in global memory), K = AO in stages of 32.  Persistent CTAs loop over grid tiles;
 // stage s of a CTA is (tile, component, K block).
 //
 // Accuracy.  The tensor core's FP32 accumulation truncates, so sums of many
@@ -638,7 +670,8 @@ __global__ void k_transpose_phi(const float *__restrict__ phi, int nao, long lon
 // products and the 2^-11 smaller cross products in separate accumulators --
 // and the epilogue warps drain each group into compensated (TwoSum) FP32
 // sums held in registers for the current component; psi = S + C is rounded
-// to FP32 once (unbiased) and rho, grad rho are summed in FP64.
+// to FP32 once (unbiased) and rho, grad rho are summed as compensated FP32
+// dot products (dot2_add), rounded to FP64 at the end.
 // Loads: bulk tensor copies (TMA) issued by one thread into a 4-stage ring.
 // TMEM: a ring of up to 8 accumulator slots of 2 npsi columns.
 // ---------------------------------------------------------------------------
@@ -686,6 +719,16 @@ __device__ inline void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, 
       "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
       " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
       "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+// TMA: one box of a 3D tensor map (the K-blocked operand layouts: x = the 32
+// elements of a K block, y = row, z = K block).
+__device__ inline void tma_load_3d(uint32_t dst, const CUtensorMap *map, int x, int y, int z,
+                                   uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
       : "memory");
 }
 __device__ inline void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
@@ -749,10 +792,10 @@ __global__ void __launch_bounds__(kPsiThreads, 1)
         const int g0 = (int)((blockIdx.x + t * gridDim.x) * (long long)kM);
         const uint32_t base = smem_u32(sm + slot * kPsiStageBytes);
         mbar_expect_tx(&P.loaded[slot], bytes);
-        if (comp == 0) tma_load_2d(base, &tmA, kb * kStageK, g0, &P.loaded[slot]);
-        else tma_load_2d(base, &tmD, kb * kStageK, (int)((comp - 1) * a.N) + g0, &P.loaded[slot]);
+        if (comp == 0) tma_load_3d(base, &tmA, 0, g0, kb, &P.loaded[slot]);
+        else tma_load_3d(base, &tmD, 0, g0, (comp - 1) * nkb + kb, &P.loaded[slot]);
         tma_load_2d(base + (uint32_t)kPsiAPieces, &tmY, kb * kStageK, 0, &P.loaded[slot]);
-        tma_load_2d(base + (uint32_t)(kPsiAPieces + kPsiBPiece), &tmY, kb * kStageK, NPSI,
+        tma_load_2d(base + (uint32_t)kPsiAPieces + (uint32_t)NPSI * 128u, &tmY, kb * kStageK, NPSI,
                     &P.loaded[slot]);
       }
     }
@@ -786,7 +829,7 @@ __global__ void __launch_bounds__(kPsiThreads, 1)
     for (long long t = 0; t < my_tiles; ++t) {
       const long long g = (blockIdx.x + t * gridDim.x) * (long long)kM + row;
       float p0[NPSI];
-      double rho = 0, gr[3] = {0, 0, 0};
+      float rs = 0.f, rc = 0.f, gs[3] = {0.f, 0.f, 0.f}, gc[3] = {0.f, 0.f, 0.f};
       for (int comp = 0; comp < a.ncomp; ++comp) {
         float sv[NPSI], cv[NPSI];
         for (int g0 = 0; g0 < nkb; g0 += DR, ++G) {
@@ -821,27 +864,38 @@ __global__ void __launch_bounds__(kPsiThreads, 1)
         }
         // component complete: value = S + C (FP32, rounded once)
         if (ok) {
+          float cs = 0.f, cc = 0.f;  // this component's compensated sum over the orbitals
 #pragma unroll
           for (int k = 0; k < NPSI; ++k) {
             const float v = sv[k] + cv[k];
-            if (comp == 0) {
-              p0[k] = v;
-              rho += (double)v * (double)v;
-            } else {
-              gr[comp - 1] += (double)p0[k] * (double)v;
-            }
+            if (comp == 0) p0[k] = v;
+            dot2_add(cs, cc, comp == 0 ? v : p0[k], v);
             if (a.psi_out && g < a.N) a.psi_out[(long long)(comp * NPSI + k) * a.N + g] = v;
+          }
+          if (comp == 0) {
+            rs = cs;
+            rc = cc;
+          } else if (comp == 1) {
+            gs[0] = cs;
+            gc[0] = cc;
+          } else if (comp == 2) {
+            gs[1] = cs;
+            gc[1] = cc;
+          } else {
+            gs[2] = cs;
+            gc[2] = cc;
           }
         }
       }
       if (ok && g < a.N) {
-        a.rho[g] = rho;
+        a.rho[g] = (double)rs + (double)rc;
         if (a.ncomp > 1)
-          for (int c = 0; c < 3; ++c) a.grho[(long long)c * a.N + g] = 2.0 * gr[c];
+#pragma unroll
+          for (int c = 0; c < 3; ++c) a.grho[(long long)c * a.N + g] = 2.0 * ((double)gs[c] + (double)gc[c]);
       }
     }
   } else if (lane == 0) {
-    const uint32_t idesc = idesc_tf32(kM, NPSI);
+    const uint32_t idesc = idesc_tf32(kM, NPSI), idesc2 = idesc_tf32(kM, 2 * NPSI);
     long long st = 0, G = 0;
     for (long long t = 0; t < my_tiles; ++t) {
       for (int comp = 0; comp < a.ncomp; ++comp) {
@@ -860,17 +914,267 @@ __global__ void __launch_bounds__(kPsiThreads, 1)
             if (ok) {
               const uint32_t base = smem_u32(sm + slot * kPsiStageBytes);
               const uint32_t Ah = base, Al = base + kTile;
-              const uint32_t Bh = base + (uint32_t)kPsiAPieces, Bl = Bh + (uint32_t)kPsiBPiece;
+              const uint32_t Bh = base + (uint32_t)kPsiAPieces, Bl = Bh + (uint32_t)NPSI * 128u;
+              // descriptors advance by 32 bytes (2 units of 16) per K step of 8.
+              // Y^T's lo rows follow its hi rows, so one MMA of N = 2 npsi
+              // gives hi*hi (into the big slot) and hi*lo (into the small slot
+              // right after it); lo*hi adds into the small slot.
+              const uint64_t dAh = sdesc(Ah), dAl = sdesc(Al), dBh = sdesc(Bh);
+              (void)Bl;
 #pragma unroll
               for (int ks = 0; ks < kStageK / 8; ++ks) {
-                const uint32_t off = ks * 32;
+                const uint64_t o = 2u * (uint32_t)ks;
                 const int acc = (kb > g0 || ks > 0) ? 1 : 0;
-                mma_tf32(dsmall, sdesc(Al + off), sdesc(Bh + off), idesc, acc);
-                mma_tf32(dsmall, sdesc(Ah + off), sdesc(Bl + off), idesc, 1);
-                mma_tf32(dbig, sdesc(Ah + off), sdesc(Bh + off), idesc, acc);
+                mma_tf32(dbig, dAh + o, dBh + o, idesc2, acc);
+                mma_tf32(dsmall, dAl + o, dBh + o, idesc, 1);
               }
             }
             mma_commit(&P.empty[slot]);
+          }
+          mma_commit(&P.acc_full[b]);
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == kPsiMmaWarp) {
+    tc_fence_after();
+    tmem_dealloc(P.tmem_base, tcols);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Orbital density, resident-Y form (npsi <= 32): the same contraction and
+// epilogue as k_tc_psi_density with the pipeline rearranged so that more
+// bytes are in flight per SM.
+//  * Y^T (both TF32 pieces, every K block) is loaded once per CTA and stays
+//    in shared memory (npsi x ldk x 8 B, 72 KB at npsi = 32, 288 AOs).
+//  * The TMA ring holds only raw fp32 A boxes (16 KB each, kPsrRing deep);
+//    the splitter warps copy a box into one of two split buffers as TF32
+//    hi/lo pieces and release the ring slot at once, so a slot is busy for
+//    the load latency plus one read rather than until its MMAs complete.
+//  * The MMA reads A from the split buffer and B from the resident Y.
+// ---------------------------------------------------------------------------
+constexpr int kPsrMaxN = 32;
+constexpr int kPsrRing = 5;                                          // raw A boxes in flight
+__host__ __device__ constexpr size_t psr_y_bytes(int npsi, int ldk) {
+  return (size_t)(ldk / kStageK) * 2 * npsi * 128;
+}
+constexpr size_t kPsrYMax = psr_y_bytes(kPsrMaxN, 288);               // 72 KB: up to 288 AOs
+constexpr size_t kPsrSmem = kPsrYMax + kPsrRing * kTile + 2 * 2 * kTile + 1024;
+
+struct PsrPipe {
+  uint64_t raw_full[kPsrRing], raw_empty[kPsrRing], sp_full[2], sp_empty[2], y_full;
+  uint64_t acc_full[8], acc_empty[8];
+  uint32_t tmem_base;
+};
+
+template <int NPSI>
+__global__ void __launch_bounds__(kPsiThreads, 1)
+    k_tc_psi_density_r(PsiArgs a, const __grid_constant__ CUtensorMap tmA,
+                       const __grid_constant__ CUtensorMap tmD, const __grid_constant__ CUtensorMap tmY) {
+  extern __shared__ __align__(1024) char smraw[];
+  char *sm = (char *)(((uintptr_t)smraw + 1023) & ~(uintptr_t)1023);
+  char *ysm = sm;                                    // [kb][hi | lo][NPSI rows x 128 B]
+  char *raw = sm + kPsrYMax;                         // [kPsrRing][16 KB]
+  char *spl = raw + kPsrRing * kTile;                // [2][hi 16 KB | lo 16 KB]
+  __shared__ PsrPipe P;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int nkb = a.ldk / kStageK;
+  const long long ntiles = (a.N + kM - 1) / kM;
+  const long long my_tiles = ntiles > blockIdx.x ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+  const int per_tile = a.ncomp * nkb;
+  const long long S = my_tiles * per_tile;
+  const int RA = psi_ring(NPSI, a.ncomp);
+  const int DR = a.drain;
+  const int ncols = RA * 2 * NPSI;
+  int tcols = 32;
+  while (tcols < ncols) tcols <<= 1;
+  constexpr uint32_t kYPiece = (uint32_t)NPSI * 128u;
+
+  if (tid == 0) {
+    for (int b = 0; b < kPsrRing; ++b) {
+      mbar_init(&P.raw_full[b], 1);
+      mbar_init(&P.raw_empty[b], kPsiProducers);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&P.sp_full[b], kPsiProducers);
+      mbar_init(&P.sp_empty[b], 1);
+    }
+    mbar_init(&P.y_full, 1);
+    for (int b = 0; b < 8; ++b) {
+      mbar_init(&P.acc_full[b], 1);
+      mbar_init(&P.acc_empty[b], kDrainers);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == kPsiMmaWarp) tmem_alloc(&P.tmem_base, tcols);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+
+  bool ok = true;
+  if (warp == kPsiTmaWarp) {
+    if (lane == 0) {
+      // the whole Y^T once, then the raw A boxes of stage (tile, component, K block)
+      mbar_expect_tx(&P.y_full, (uint32_t)nkb * 2u * kYPiece);
+      for (int kb = 0; kb < nkb; ++kb) {
+        const uint32_t yb = smem_u32(ysm) + (uint32_t)kb * 2u * kYPiece;
+        tma_load_2d(yb, &tmY, kb * kStageK, 0, &P.y_full);
+        tma_load_2d(yb + kYPiece, &tmY, kb * kStageK, NPSI, &P.y_full);
+      }
+      for (long long st = 0; st < S; ++st) {
+        const int slot = (int)(st % kPsrRing);
+        const long long use = st / kPsrRing;
+        if (ok && use > 0 && !mbar_wait(&P.raw_empty[slot], (unsigned)((use - 1) & 1), a.err, 55))
+          ok = false;
+        if (!ok) break;
+        const long long t = st / per_tile;
+        const int r = (int)(st % per_tile), comp = r / nkb, kb = r % nkb;
+        const int g0 = (int)((blockIdx.x + t * gridDim.x) * (long long)kM);
+        const uint32_t dst = smem_u32(raw + slot * kTile);
+        mbar_expect_tx(&P.raw_full[slot], (uint32_t)kTile);
+        if (comp == 0) tma_load_3d(dst, &tmA, 0, g0, kb, &P.raw_full[slot]);
+        else tma_load_3d(dst, &tmD, 0, g0, (comp - 1) * nkb + kb, &P.raw_full[slot]);
+      }
+    }
+  } else if (warp < kPsiPW) {
+    // splitters: raw box -> TF32 hi / lo pieces in the split buffer st % 2
+    const int cch = tid & 7;
+    for (long long st = 0; st < S; ++st) {
+      const int slot = (int)(st % kPsrRing), sb = (int)(st & 1);
+      if (ok && !mbar_wait(&P.raw_full[slot], (unsigned)((st / kPsrRing) & 1), a.err, 51)) ok = false;
+      if (ok && st >= 2 && !mbar_wait(&P.sp_empty[sb], (unsigned)(((st >> 1) - 1) & 1), a.err, 52)) ok = false;
+      if (ok) {
+        const char *src = raw + slot * kTile;
+        char *dst = spl + sb * 2 * kTile;
+        float4 v[kPsiRowsPerThread];
+#pragma unroll
+        for (int j = 0; j < kPsiRowsPerThread; ++j) {
+          const int row = (tid >> 3) + (kPsiProducers / 8) * j;
+          v[j] = *reinterpret_cast<const float4 *>(src + swz(row, cch));
+        }
+        mbar_arrive(&P.raw_empty[slot]);  // the box is in registers: the slot can be refilled
+#pragma unroll
+        for (int j = 0; j < kPsiRowsPerThread; ++j) {
+          const int row = (tid >> 3) + (kPsiProducers / 8) * j;
+          store_split4(dst, row, cch, v[j]);
+        }
+      } else {
+        mbar_arrive(&P.raw_empty[slot]);
+      }
+      fence_proxy_async();
+      mbar_arrive(&P.sp_full[sb]);
+    }
+  } else if (warp < kPsiPW + 4) {
+    // drains and epilogue, as in k_tc_psi_density
+    const int row = (warp & 3) * 32 + lane;
+    const uint32_t tbase = P.tmem_base + ((uint32_t)((warp & 3) * 32) << 16);
+    long long G = 0;
+    for (long long t = 0; t < my_tiles; ++t) {
+      const long long g = (blockIdx.x + t * gridDim.x) * (long long)kM + row;
+      float p0[NPSI];
+      float rs = 0.f, rc = 0.f, gs[3] = {0.f, 0.f, 0.f}, gc[3] = {0.f, 0.f, 0.f};
+      for (int comp = 0; comp < a.ncomp; ++comp) {
+        float sv[NPSI], cv[NPSI];
+        for (int g0 = 0; g0 < nkb; g0 += DR, ++G) {
+          const int b = (int)(G % RA);
+          const long long use = G / RA;
+          bool got = ok && mbar_wait(&P.acc_full[b], (unsigned)(use & 1), a.err, 53);
+          if (!got) ok = false;
+          tc_fence_after();
+          if (got) {
+            const uint32_t slot = tbase + (uint32_t)(b * 2 * NPSI);
+#pragma unroll
+            for (int c0 = 0; c0 < NPSI; c0 += 16) {
+              uint32_t vb[16], vs[16];
+              tmem_ld16_nowait(slot + c0, vb);
+              tmem_ld16_nowait(slot + NPSI + c0, vs);
+              tmem_wait_ld();
+#pragma unroll
+              for (int i = 0; i < 16; ++i) {
+                const float big = __uint_as_float(vb[i]), small = __uint_as_float(vs[i]);
+                if (g0 == 0) {
+                  sv[c0 + i] = big;
+                  cv[c0 + i] = small;
+                } else {
+                  two_sum_add(sv[c0 + i], cv[c0 + i], big);
+                  cv[c0 + i] += small;
+                }
+              }
+            }
+          }
+          tc_fence_before();
+          mbar_arrive(&P.acc_empty[b]);
+        }
+        if (ok) {
+          float cs = 0.f, cc = 0.f;  // this component's compensated sum over the orbitals
+#pragma unroll
+          for (int k = 0; k < NPSI; ++k) {
+            const float v = sv[k] + cv[k];
+            if (comp == 0) p0[k] = v;
+            dot2_add(cs, cc, comp == 0 ? v : p0[k], v);
+            if (a.psi_out && g < a.N) a.psi_out[(long long)(comp * NPSI + k) * a.N + g] = v;
+          }
+          if (comp == 0) {
+            rs = cs;
+            rc = cc;
+          } else if (comp == 1) {
+            gs[0] = cs;
+            gc[0] = cc;
+          } else if (comp == 2) {
+            gs[1] = cs;
+            gc[1] = cc;
+          } else {
+            gs[2] = cs;
+            gc[2] = cc;
+          }
+        }
+      }
+      if (ok && g < a.N) {
+        a.rho[g] = (double)rs + (double)rc;
+        if (a.ncomp > 1)
+#pragma unroll
+          for (int c = 0; c < 3; ++c) a.grho[(long long)c * a.N + g] = 2.0 * ((double)gs[c] + (double)gc[c]);
+      }
+    }
+  } else if (lane == 0) {
+    const uint32_t idesc = idesc_tf32(kM, NPSI), idesc2 = idesc_tf32(kM, 2 * NPSI);
+    if (!mbar_wait(&P.y_full, 0u, a.err, 56)) ok = false;
+    long long st = 0, G = 0;
+    for (long long t = 0; t < my_tiles; ++t) {
+      for (int comp = 0; comp < a.ncomp; ++comp) {
+        for (int g0 = 0; g0 < nkb; g0 += DR, ++G) {
+          const int b = (int)(G % RA);
+          const long long ause = G / RA;
+          if (ok && ause > 0 && !mbar_wait(&P.acc_empty[b], (unsigned)((ause - 1) & 1), a.err, 54))
+            ok = false;
+          tc_fence_after();
+          const uint32_t dbig = P.tmem_base + (uint32_t)(b * 2 * NPSI), dsmall = dbig + NPSI;
+          const int g1 = min(g0 + DR, nkb);
+          for (int kb = g0; kb < g1; ++kb, ++st) {
+            const int sb = (int)(st & 1);
+            if (ok && !mbar_wait(&P.sp_full[sb], (unsigned)((st >> 1) & 1), a.err, 57)) ok = false;
+            tc_fence_after();
+            if (ok) {
+              const uint32_t Ah = smem_u32(spl + sb * 2 * kTile), Al = Ah + (uint32_t)kTile;
+              const uint32_t Bh = smem_u32(ysm) + (uint32_t)kb * 2u * kYPiece, Bl = Bh + kYPiece;
+              // descriptors advance by 32 bytes (2 units of 16) per K step of 8.
+              // Y^T's lo rows follow its hi rows, so one MMA of N = 2 npsi
+              // gives hi*hi (into the big slot) and hi*lo (into the small slot
+              // right after it); lo*hi adds into the small slot.
+              const uint64_t dAh = sdesc(Ah), dAl = sdesc(Al), dBh = sdesc(Bh);
+              (void)Bl;
+#pragma unroll
+              for (int ks = 0; ks < kStageK / 8; ++ks) {
+                const uint64_t o = 2u * (uint32_t)ks;
+                const int acc = (kb > g0 || ks > 0) ? 1 : 0;
+                mma_tf32(dbig, dAh + o, dBh + o, idesc2, acc);
+                mma_tf32(dsmall, dAl + o, dBh + o, idesc, 1);
+              }
+            }
+            mma_commit(&P.sp_empty[sb]);
           }
           mma_commit(&P.acc_full[b]);
         }
@@ -918,6 +1222,7 @@ constexpr int kQtMaxTiles = 12;  // tiles per k_tc_quad_tma launch (kernel param
 struct QtArgs {
   QtTile tiles[kQtMaxTiles];
   int ntile;
+  int blocked;  // operands K-blocked ([K / 32][row][32], 3D maps) rather than row-major
   long long N;
   int kchunk, drain, mtiles, ntiles;
   double *partial;
@@ -984,12 +1289,16 @@ __global__ void __launch_bounds__(kQtThreads, 1)
         const int x = (int)(k0 + (long long)st * kStageK);
         const uint32_t base = smem_u32(sm + slot * kQtStageBytes);
         mbar_expect_tx(&P.full[slot], bytes);
-        tma_load_2d(base, ah, x, T.arow, &P.full[slot]);
-        tma_load_2d(base + (uint32_t)kTile, al, x, T.arow, &P.full[slot]);
+        auto load = [&](uint32_t dst, const CUtensorMap *m, int row) {
+          if (a.blocked) tma_load_3d(dst, m, 0, row, x / kStageK, &P.full[slot]);
+          else tma_load_2d(dst, m, x, row, &P.full[slot]);
+        };
+        load(base, ah, T.arow);
+        load(base + (uint32_t)kTile, al, T.arow);
         for (int q = 0; q < nbox; ++q) {
           const uint32_t off = (uint32_t)(q * bbox * 128);
-          tma_load_2d(base + 2u * (uint32_t)kTile + off, bh, x, T.brow + q * bbox, &P.full[slot]);
-          tma_load_2d(base + 3u * (uint32_t)kTile + off, bl, x, T.brow + q * bbox, &P.full[slot]);
+          load(base + 2u * (uint32_t)kTile + off, bh, T.brow + q * bbox);
+          load(base + 3u * (uint32_t)kTile + off, bl, T.brow + q * bbox);
         }
       }
     }
@@ -1012,12 +1321,13 @@ __global__ void __launch_bounds__(kQtThreads, 1)
             const uint32_t base = smem_u32(sm + slot * kQtStageBytes);
             const uint32_t Ah = base, Al = base + (uint32_t)kTile, Bh = base + 2u * (uint32_t)kTile,
                            Bl = base + 3u * (uint32_t)kTile;
+            const uint64_t dAh = sdesc(Ah), dAl = sdesc(Al), dBh = sdesc(Bh), dBl = sdesc(Bl);
 #pragma unroll
             for (int ks = 0; ks < kStageK / 8; ++ks) {
-              const uint32_t off = ks * 32;
-              mma_tf32(tmem_d, sdesc(Al + off), sdesc(Bh + off), idesc, (first && ks == 0) ? 0 : 1);
-              mma_tf32(tmem_d, sdesc(Ah + off), sdesc(Bl + off), idesc, 1);
-              mma_tf32(tmem_d, sdesc(Ah + off), sdesc(Bh + off), idesc, 1);
+              const uint64_t o = 2u * (uint32_t)ks;
+              mma_tf32(tmem_d, dAl + o, dBh + o, idesc, (first && ks == 0) ? 0 : 1);
+              mma_tf32(tmem_d, dAh + o, dBl + o, idesc, 1);
+              mma_tf32(tmem_d, dAh + o, dBh + o, idesc, 1);
             }
           }
           first = false;
@@ -1100,62 +1410,58 @@ __global__ void __launch_bounds__(kQtThreads, 1)
 // Persistent quadrature for n_ao = 128 nfull + last with last <= 16 (e.g.
 // 270 = 2 x 128 + 14) or no partial block: grid (tiles, groups).  The CTAs
 // of group g share one contiguous K slice (1/groups of the grid points) and
-// each computes one full 128 x 128 destination tile over all of it.  The
-// CTAs of a group stream the same 128-row blocks at about the same pace, so
-// a block that one of them brings in from DRAM is still in L2 when the others
-// ask for it.  The compensated sums stay in TMEM / registers over the whole
-// slice; one FP64 partial tile per CTA is written at the end and the reduce
-// adds the groups.
+// each computes one full 128 x 128 destination tile over all of it, so the
+// CTAs of a group stream the same 128-row blocks at about the same pace.  The
+// compensated sums stay in TMEM / registers over the whole slice; one FP64
+// partial tile per CTA is written at the end and the reduce adds the groups.
+// Operands are K-blocked ([K / 32][row][32]): every TMA box is one
+// contiguous run of memory.
 //
-// The products with the partial block (at most 16 AOs, MMA N = 16) ride
-// along, at most two per CTA, spread over the tiles of a group so that each
-// CTA does about the same work:
-//   kind 0  tile (m, last)    = A block m x narrow B box;
-//   kind 1  tile (last, n)    = (B block n x narrow A box)^T, stored transposed;
-//   kind 2  tile (last, last) = narrow A box x narrow B box.  The MMA reads a
-//           128-row A window that starts at the narrow A box; its rows past
-//           16 are other operand data of the same stage, and the TMEM lanes
-//           they produce are never read.
-// TMEM (512 columns): two slots of 128 + 16 + 16 accumulator columns, the
-// main tile's TwoSum sums S (128 columns) and the narrow products' sums and
-// carries (2 x 16 each); the carries C of the main tile live in the
-// registers of eight drain warps (two per TMEM lane group, 64 main columns
-// each).
+// The products with the partial block (at most 16 AOs) ride in the main MMA
+// as its columns 128..143 (N = 144), the 16-row box stored right after the
+// 128-row B block in shared memory:
+//   tile (m, m), not swapped:  A = A block m, B = [B block m; narrow B]
+//                              -> tiles (m, m) and (m, last);
+//   swapped tile (m, n):       A = B block n, B = [A block m; narrow A]
+//                              -> (m, n)^T and (last, n)^T, stored transposed;
+// other tiles run with N = 128.  The (last, last) corner is computed apart
+// (k_quad_corner).  TMEM (512 columns): two accumulator slots of 128 + 32
+// columns, the main tile's TwoSum sums S (128 columns) and the narrow
+// columns' sums and carries (16 each); the carries C of the main tile live in
+// the registers of eight drain warps (two per TMEM lane group, 64 main
+// columns each).
 // ---------------------------------------------------------------------------
 constexpr int kQpDrainWarps = 8;
 constexpr int kQpMmaWarp = kQpDrainWarps;
 constexpr int kQpTmaWarp = kQpMmaWarp + 1;
 constexpr int kQpThreads = (kQpTmaWarp + 1) * 32;
-constexpr uint32_t kQpSlot = kN + 32;           // main + two narrow accumulators
+constexpr uint32_t kQpSlot = kN + 32;           // 128 main + 16 narrow accumulator columns (+16 unused)
 constexpr uint32_t kQpColS = 2 * kQpSlot;       // main-tile sums S (128 columns)
-constexpr uint32_t kQpColXS = kQpColS + kN;     // narrow sums S (2 x 16)
-constexpr uint32_t kQpColXC = kQpColXS + 32;    // narrow carries C (2 x 16), ends at 512
+constexpr uint32_t kQpColXS = kQpColS + kN;     // narrow sums S (16)
+constexpr uint32_t kQpColXC = kQpColXS + 16;    // narrow carries C (16)
 constexpr int kQpTmemCols = 512;
 constexpr uint32_t kQpNarrow = 16 * 128;        // one 16-row piece of a narrow box
-// Stage layout: narrow A hi, lo | narrow B hi, lo | A hi | A lo | B hi | B lo.
-// The narrow pieces come first so that the 16 KB window of a kind-2 product
-// (from either narrow A piece) ends inside the stage.
-constexpr uint32_t kQpOffNA = 0, kQpOffNB = 2 * kQpNarrow, kQpOffMain = 4 * kQpNarrow;
-constexpr size_t kQpStageBytes = 4 * kQpNarrow + 4 * kTile;
+// Stage layout: A hi | A lo | B hi + narrow hi | B lo + narrow lo.
+constexpr uint32_t kQpOffBh = 2 * kTile, kQpOffBl = 3 * kTile + kQpNarrow;
+constexpr size_t kQpStageBytes = 4 * kTile + 2 * kQpNarrow;
 constexpr size_t kQpSmem = kQtRing * kQpStageBytes + 1024;
 constexpr int kQpMaxFull = 6;  // full AO blocks handled by the persistent form
 constexpr int kQpMaxTiles = kQpMaxFull * kQpMaxFull;
 
 struct QpTile {
-  int mt, nt;          // the full destination tile
-  int nx;              // narrow products carried (0..2)
-  int kind[2];         // 0, 1 or 2 (above)
-  int xmt[2], xnt[2];  // their destination tiles
-  int loadA, loadB;    // narrow A / B boxes loaded with every stage
+  int mt, nt;  // the full destination tile
+  int swap;    // computed transposed: A side from the B operand, B side from the A operand
+  int nb;      // MMA N: 128, or 144 with the narrow box
 };
 
 struct QpArgs {
   QpTile tiles[kQpMaxTiles];
   int ntile, groups;
-  int xrow;  // first AO row of the narrow block
+  int blocked;  // operands K-blocked ([K / 32][row][32], 3D maps) rather than row-major
+  int xrow;     // first AO row of the narrow block
   long long N;
   int drain, mtiles, ntiles;
-  double *partial;  // [groups][mtiles][ntiles][128][128]
+  double *partial;  // [parts][mtiles][ntiles][128][128]
   int *err;
 };
 
@@ -1167,13 +1473,15 @@ constexpr size_t kMaxDynSmem = 227 * 1024;
 static_assert(kDensSmem <= kMaxDynSmem && kPsiSmem <= kMaxDynSmem && kQtSmem <= kMaxDynSmem &&
                   kQpSmem <= kMaxDynSmem,
               "dynamic shared memory above 227 KB");
-static_assert(kTmemCols <= 512 && kQpColXC + 32 == (uint32_t)kQpTmemCols && kQpTmemCols <= 512,
+static_assert(kTmemCols <= 512 && kQpColXC + 16 <= (uint32_t)kQpTmemCols && kQpTmemCols <= 512,
               "TMEM column layout");
 static_assert(sizeof(QtArgs) + 8 * sizeof(CUtensorMap) <= 4096 &&
                   sizeof(QpArgs) + 8 * sizeof(CUtensorMap) <= 4096,
               "kernel parameters above 4 KB");
 static_assert(kPsiRowsPerThread * kPsiProducers == kM * 8, "splitter rows per thread");
-static_assert(kQpOffNA + kQpNarrow + kTile <= kQpStageBytes, "kind-2 window leaves the stage");
+static_assert(kPsrSmem <= kMaxDynSmem, "resident-Y orbital density above 227 KB");
+static_assert(kQpOffBh % 1024 == 0 && kQpOffBl % 1024 == 0 && kQpStageBytes % 1024 == 0,
+              "operand pieces must start on 1024-byte boundaries (128-byte swizzle atoms)");
 
 __global__ void __launch_bounds__(kQpThreads, 1)
     k_tc_quad_persist(QpArgs a, const __grid_constant__ CUtensorMap mAh, const __grid_constant__ CUtensorMap mAl,
@@ -1186,6 +1494,7 @@ __global__ void __launch_bounds__(kQpThreads, 1)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const QpTile T = a.tiles[blockIdx.x];
   const int g = blockIdx.y;
+  const bool wide = T.nb > kN;  // the narrow box rides as MMA columns 128..143
   // this group's K slice: stages [s0, s0 + nstages) of 32 points
   const long long NS = (a.N + kStageK - 1) / kStageK;
   const long long s0 = NS * g / a.groups;
@@ -1210,31 +1519,37 @@ __global__ void __launch_bounds__(kQpThreads, 1)
   bool ok = true;
   if (warp == kQpTmaWarp) {
     if (lane == 0) {
-      const uint32_t bytes = 4u * (uint32_t)kTile + (uint32_t)(T.loadA + T.loadB) * 2u * kQpNarrow;
+      // A side: 128 rows of the A operand (or of the B operand when swapped);
+      // B side: 128 rows of the other operand, then its narrow box
+      const CUtensorMap *ah = T.swap ? &mBh : &mAh, *al = T.swap ? &mBl : &mAl;
+      const CUtensorMap *bh = T.swap ? &mAh : &mBh, *bl = T.swap ? &mAl : &mBl;
+      const CUtensorMap *xh = T.swap ? &mAh16 : &mBh16, *xl = T.swap ? &mAl16 : &mBl16;
+      const int arow = (T.swap ? T.nt : T.mt) * kM, brow = (T.swap ? T.mt : T.nt) * kN;
+      const uint32_t bytes = 4u * (uint32_t)kTile + (wide ? 2u * kQpNarrow : 0u);
       for (int st = 0; st < nstages; ++st) {
         const int slot = st % kQtRing, use = st / kQtRing;
         if (ok && use > 0 && !mbar_wait(&P.empty[slot], (unsigned)((use - 1) & 1), a.err, 41)) ok = false;
         if (!ok) break;
         const int x = (int)((s0 + st) * kStageK);
-        const uint32_t base = smem_u32(sm + slot * kQpStageBytes), mb = base + kQpOffMain;
+        const uint32_t base = smem_u32(sm + slot * kQpStageBytes);
         mbar_expect_tx(&P.full[slot], bytes);
-        tma_load_2d(mb, &mAh, x, T.mt * kM, &P.full[slot]);
-        tma_load_2d(mb + (uint32_t)kTile, &mAl, x, T.mt * kM, &P.full[slot]);
-        tma_load_2d(mb + 2u * (uint32_t)kTile, &mBh, x, T.nt * kN, &P.full[slot]);
-        tma_load_2d(mb + 3u * (uint32_t)kTile, &mBl, x, T.nt * kN, &P.full[slot]);
-        if (T.loadA) {
-          tma_load_2d(base + kQpOffNA, &mAh16, x, a.xrow, &P.full[slot]);
-          tma_load_2d(base + kQpOffNA + kQpNarrow, &mAl16, x, a.xrow, &P.full[slot]);
-        }
-        if (T.loadB) {
-          tma_load_2d(base + kQpOffNB, &mBh16, x, a.xrow, &P.full[slot]);
-          tma_load_2d(base + kQpOffNB + kQpNarrow, &mBl16, x, a.xrow, &P.full[slot]);
+        auto load = [&](uint32_t dst, const CUtensorMap *m, int row) {
+          if (a.blocked) tma_load_3d(dst, m, 0, row, (int)(s0 + st), &P.full[slot]);
+          else tma_load_2d(dst, m, x, row, &P.full[slot]);
+        };
+        load(base, ah, arow);
+        load(base + (uint32_t)kTile, al, arow);
+        load(base + kQpOffBh, bh, brow);
+        load(base + kQpOffBl, bl, brow);
+        if (wide) {
+          load(base + kQpOffBh + (uint32_t)kTile, xh, a.xrow);
+          load(base + kQpOffBl + (uint32_t)kTile, xl, a.xrow);
         }
       }
     }
   } else if (warp == kQpMmaWarp) {
     if (lane == 0) {
-      const uint32_t idesc = idesc_tf32(kM, kN), idesc16 = idesc_tf32(kM, 16);
+      const uint32_t idesc = idesc_tf32(kM, T.nb);
       int stage = 0;
       for (int j = 0; j < nsub; ++j) {
         const int ab = j & 1, ause = j >> 1;
@@ -1248,29 +1563,19 @@ __global__ void __launch_bounds__(kQpThreads, 1)
           if (ok && !mbar_wait(&P.full[slot], (unsigned)(use & 1), a.err, 42)) ok = false;
           tc_fence_after();
           if (ok) {
-            const uint32_t base = smem_u32(sm + slot * kQpStageBytes), mb = base + kQpOffMain;
-            const uint32_t Ah = mb, Al = mb + (uint32_t)kTile, Bh = mb + 2u * (uint32_t)kTile,
-                           Bl = mb + 3u * (uint32_t)kTile;
-            const uint32_t nAh = base + kQpOffNA, nAl = nAh + kQpNarrow, nBh = base + kQpOffNB,
-                           nBl = nBh + kQpNarrow;
+            // descriptors: offsets in 16-byte units from the stage base (every
+            // piece starts on a 1024-byte boundary, so no carry leaves the
+            // 14-bit address field); K steps of 8 advance by 2 units
+            const uint64_t d0 = sdesc(smem_u32(sm + slot * kQpStageBytes));
+            const uint64_t dAh = d0, dAl = d0 + (kTile >> 4), dBh = d0 + (kQpOffBh >> 4),
+                           dBl = d0 + (kQpOffBl >> 4);
 #pragma unroll
             for (int ks = 0; ks < kStageK / 8; ++ks) {
-              const uint32_t off = ks * 32;
+              const uint64_t o = 2u * (uint32_t)ks;
               const int acc = (first && ks == 0) ? 0 : 1;
-              mma_tf32(tmem_d, sdesc(Al + off), sdesc(Bh + off), idesc, acc);
-              mma_tf32(tmem_d, sdesc(Ah + off), sdesc(Bl + off), idesc, 1);
-              mma_tf32(tmem_d, sdesc(Ah + off), sdesc(Bh + off), idesc, 1);
-              for (int e = 0; e < T.nx; ++e) {
-                const int kind = T.kind[e];
-                // the 128-row side and the 16-row narrow box of this product
-                const uint32_t Wh = kind == 0 ? Ah : (kind == 1 ? Bh : nAh);
-                const uint32_t Wl = kind == 0 ? Al : (kind == 1 ? Bl : nAl);
-                const uint32_t Nh = kind == 1 ? nAh : nBh, Nl = kind == 1 ? nAl : nBl;
-                const uint32_t dx = tmem_d + (uint32_t)kN + (uint32_t)e * 16u;
-                mma_tf32(dx, sdesc(Wl + off), sdesc(Nh + off), idesc16, acc);
-                mma_tf32(dx, sdesc(Wh + off), sdesc(Nl + off), idesc16, 1);
-                mma_tf32(dx, sdesc(Wh + off), sdesc(Nh + off), idesc16, 1);
-              }
+              mma_tf32(tmem_d, dAl + o, dBh + o, idesc, acc);
+              mma_tf32(tmem_d, dAh + o, dBl + o, idesc, 1);
+              mma_tf32(tmem_d, dAh + o, dBh + o, idesc, 1);
             }
           }
           first = false;
@@ -1281,11 +1586,11 @@ __global__ void __launch_bounds__(kQpThreads, 1)
     }
   } else {
     // drains: warp w owns TMEM lanes 32 (w % 4) .. and main columns 64 (w / 4) .. + 63;
-    // the warps of half h also own narrow product h (16 columns)
+    // the warps of half 0 also own the 16 narrow columns
     const int h = warp >> 2;
     const uint32_t lane_off = (uint32_t)((warp & 3) * 32) << 16;
     const int c0 = h * 64;
-    const bool has_x = h < T.nx;
+    const bool has_x = wide && h == 0;
     float cm[64];
 #pragma unroll
     for (int i = 0; i < 64; ++i) cm[i] = 0.f;
@@ -1316,10 +1621,9 @@ __global__ void __launch_bounds__(kQpThreads, 1)
           tmem_st16(P.tmem_base + lane_off + kQpColS + c0 + q * 16, sv);
         }
         if (has_x) {
-          const uint32_t xsa = P.tmem_base + lane_off + kQpColXS + (uint32_t)h * 16u,
-                         xca = P.tmem_base + lane_off + kQpColXC + (uint32_t)h * 16u;
+          const uint32_t xsa = P.tmem_base + lane_off + kQpColXS, xca = P.tmem_base + lane_off + kQpColXC;
           uint32_t va[16], sa[16], ca[16];
-          tmem_ld16_nowait(slot + kN + (uint32_t)h * 16u, va);
+          tmem_ld16_nowait(slot + kN, va);
           if (j > 0) {
             tmem_ld16_nowait(xsa, sa);
             tmem_ld16_nowait(xca, ca);
@@ -1354,24 +1658,32 @@ __global__ void __launch_bounds__(kQpThreads, 1)
       uint32_t sr[16];
       tmem_ld16_nowait(P.tmem_base + lane_off + kQpColS + c0 + q * 16, sr);
       tmem_wait_ld();
-      if (ok)
+      if (ok) {
+        if (!T.swap) {
 #pragma unroll
-        for (int i = 0; i < 16; ++i)
-          tile[(long long)row * kN + c0 + q * 16 + i] = (double)__uint_as_float(sr[i]) + (double)cm[q * 16 + i];
+          for (int i = 0; i < 16; ++i)
+            tile[(long long)row * kN + c0 + q * 16 + i] = (double)__uint_as_float(sr[i]) + (double)cm[q * 16 + i];
+        } else {
+#pragma unroll
+          for (int i = 0; i < 16; ++i)
+            tile[(long long)(c0 + q * 16 + i) * kN + row] = (double)__uint_as_float(sr[i]) + (double)cm[q * 16 + i];
+        }
+      }
     }
     if (has_x) {
       uint32_t sr[16], cr[16];
-      tmem_ld16_nowait(P.tmem_base + lane_off + kQpColXS + (uint32_t)h * 16u, sr);
-      tmem_ld16_nowait(P.tmem_base + lane_off + kQpColXC + (uint32_t)h * 16u, cr);
+      tmem_ld16_nowait(P.tmem_base + lane_off + kQpColXS, sr);
+      tmem_ld16_nowait(P.tmem_base + lane_off + kQpColXC, cr);
       tmem_wait_ld();
-      const int kind = T.kind[h];
-      if (ok && (kind != 2 || row < 16)) {
-        double *xt = a.partial + (((long long)g * a.mtiles + T.xmt[h]) * a.ntiles + T.xnt[h]) * tsz;
-        if (kind != 1) {
+      if (ok) {
+        const int last = a.xrow / kM;
+        if (!T.swap) {  // tile (mt, last): rows of the A block, narrow columns
+          double *xt = a.partial + (((long long)g * a.mtiles + T.mt) * a.ntiles + last) * tsz;
 #pragma unroll
           for (int i = 0; i < 16; ++i)
             xt[(long long)row * kN + i] = (double)__uint_as_float(sr[i]) + (double)__uint_as_float(cr[i]);
-        } else {
+        } else {  // tile (last, nt): narrow rows, columns of the B block
+          double *xt = a.partial + (((long long)g * a.mtiles + last) * a.ntiles + T.nt) * tsz;
 #pragma unroll
           for (int i = 0; i < 16; ++i)
             xt[(long long)i * kN + row] = (double)__uint_as_float(sr[i]) + (double)__uint_as_float(cr[i]);
@@ -1387,10 +1699,79 @@ __global__ void __launch_bounds__(kQpThreads, 1)
   }
 }
 
+// The (last, last) corner of the quadrature for a partial block of at most
+// 16 AOs, on the CUDA cores: C[p][q] = sum_g A_p(g) B_q(g) over K-blocked
+// hi/lo pieces (x = hi + lo in FP32), a 32-term FMA chain per K block added
+// into compensated (TwoSum) FP32 sums.  CTA c sums K blocks
+// [c nkb / gridDim.x, (c + 1) nkb / gridDim.x), kCornerKB of them per pass
+// (each thread keeps eight 16-byte loads of the next pass in flight while
+// the current one computes), and writes
+// its FP64 partial tile P[part0 + c][last][last]; thread (p, q) =
+// (tid / 16, tid % 16).
+constexpr int kCornerKB = 4;
+__global__ void __launch_bounds__(256) k_quad_corner(const float *__restrict__ Ahl, const float *__restrict__ Bhl,
+                                                     int nao, long long nkb, int xrow, int nrow, double *partial,
+                                                     int part0, int mtiles, int ntiles) {
+  __shared__ float sa[16][kCornerKB * 32 + 4], sb[16][kCornerKB * 32 + 4];
+  const int tid = threadIdx.x, p = tid >> 4, q = tid & 15;
+  const long long piece = nkb * nao * 32;  // floats per piece (hi, then lo)
+  const long long kb0 = nkb * blockIdx.x / gridDim.x, kb1 = nkb * (blockIdx.x + 1) / gridDim.x;
+  float s = 0.f, c = 0.f;
+  // kCornerKB K blocks x 16 rows x 8 float4 per operand and piece: 2 per
+  // thread; the next pass is loaded into registers while this one computes
+  float4 ra[2][2], rb[2][2];  // [slot h][hi, lo]
+  auto fetch = [&](long long kb) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int i = tid + 256 * h, kl = i >> 7, r = (i >> 3) & 15, e = (i & 7) * 4;
+      const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+      ra[h][0] = ra[h][1] = rb[h][0] = rb[h][1] = z;
+      if (r < nrow && kb + kl < kb1) {
+        const long long o = ((kb + kl) * nao + xrow + r) * 32 + e;
+        ra[h][0] = *reinterpret_cast<const float4 *>(Ahl + o);
+        ra[h][1] = *reinterpret_cast<const float4 *>(Ahl + piece + o);
+        rb[h][0] = *reinterpret_cast<const float4 *>(Bhl + o);
+        rb[h][1] = *reinterpret_cast<const float4 *>(Bhl + piece + o);
+      }
+    }
+  };
+  if (kb0 < kb1) fetch(kb0);
+  for (long long kb = kb0; kb < kb1; kb += kCornerKB) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int i = tid + 256 * h, kl = i >> 7, r = (i >> 3) & 15, e = (i & 7) * 4;
+      float *da = &sa[r][kl * 32 + e], *db = &sb[r][kl * 32 + e];
+      da[0] = ra[h][0].x + ra[h][1].x;
+      da[1] = ra[h][0].y + ra[h][1].y;
+      da[2] = ra[h][0].z + ra[h][1].z;
+      da[3] = ra[h][0].w + ra[h][1].w;
+      db[0] = rb[h][0].x + rb[h][1].x;
+      db[1] = rb[h][0].y + rb[h][1].y;
+      db[2] = rb[h][0].z + rb[h][1].z;
+      db[3] = rb[h][0].w + rb[h][1].w;
+    }
+    __syncthreads();
+    if (kb + kCornerKB < kb1) fetch(kb + kCornerKB);
+#pragma unroll
+    for (int kl = 0; kl < kCornerKB; ++kl) {
+      float t = 0.f;
+#pragma unroll
+      for (int k = 0; k < 32; ++k) t = fmaf(sa[p][kl * 32 + k], sb[q][kl * 32 + k], t);
+      two_sum_add(s, c, t);
+    }
+    __syncthreads();
+  }
+  const int last = xrow / kM;
+  double *tile = partial + (((long long)(part0 + blockIdx.x) * mtiles + last) * ntiles + last) * ((long long)kM * kN);
+  tile[(long long)p * kN + q] = (double)s + (double)c;
+}
+
 // hi/lo TF32 pieces of Z = a w phi + b u . grad phi (u, dphi optional; w
-// optional, = 1): inputs with row stride ldi, outputs [nao][ldo] with zeros
-// in [N, ldo).  Grid (column blocks of 1024, rows); 4 columns per thread
-// (ldi, ldo multiples of 4, 16-byte aligned rows).
+// optional, = 1): inputs with row stride ldi; outputs K-blocked,
+// [ldo / 32][nao][32] per piece, with zeros in [N, ldo), so that the
+// quadrature's 128-row x 32-point TMA boxes are contiguous 16 KB runs.
+// Grid (column blocks of 1024, rows); 4 columns per thread (ldi a multiple of
+// 4, ldo of 32, 16-byte aligned rows).
 __global__ void __launch_bounds__(256)
     k_split_operand(const float *__restrict__ phi, const float *__restrict__ dphi,
                     const float *__restrict__ w, const float *__restrict__ u, int nao, long long N,
@@ -1433,8 +1814,9 @@ __global__ void __launch_bounds__(256)
   split2(z[1], h.y, l.y);
   split2(z[2], h.z, l.z);
   split2(z[3], h.w, l.w);
-  *reinterpret_cast<float4 *>(hi + (long long)p * ldo + g) = h;
-  *reinterpret_cast<float4 *>(lo + (long long)p * ldo + g) = l;
+  const long long o = ((g >> 5) * nao + p) * 32 + (g & 31);
+  *reinterpret_cast<float4 *>(hi + o) = h;
+  *reinterpret_cast<float4 *>(lo + o) = l;
 }
 
 // Yhl[0][k][p], Yhl[1][k][p]: TF32 hi/lo pieces of C[p][k] sqrt(occ[k]) for
@@ -1461,6 +1843,11 @@ namespace tc {
 // up at run time (no link-time dependency on the driver library).
 CUtensorMap tensor_map_2d_ext(const float *base, long long ld, long long cols, long long rows,
                               int box_rows);
+// K-blocked fp32 operand [nkb][rows][32] as a 3D TMA map (x: the 32
+// elements of a K block, y: row, z: K block) with boxes of 32 x box_rows x 1
+// -- one contiguous run of box_rows x 128 bytes -- and 128-byte swizzle;
+// rows past `rows` read as zero.
+CUtensorMap tensor_map_3d_kblk(const float *base, long long rows, long long nkb, int box_rows);
 CUtensorMap tensor_map_2d(const float *base, long long ld, long long rows, int box_rows) {
   return tensor_map_2d_ext(base, ld, ld, rows, box_rows);
 }
@@ -1486,6 +1873,27 @@ CUtensorMap tensor_map_2d_ext(const float *base, long long ld, long long cols, l
                       box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                       CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) throw Error{HQCGB_CUDA_ERROR, "cuTensorMapEncodeTiled failed"};
+  return m;
+}
+CUtensorMap tensor_map_3d_kblk(const float *base, long long rows, long long nkb, int box_rows) {
+  static const PFN_cuTensorMapEncodeTiled_v12000 encode = [] {
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    HQ_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
+    HQ_REQUIRE(fn && q == cudaDriverEntryPointSuccess, "cuTensorMapEncodeTiled unavailable");
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }();
+  HQ_REQUIRE(((uintptr_t)base & 15) == 0, "TMA base must be 16-byte aligned");
+  HQ_REQUIRE(rows >= 1 && nkb >= 1 && rows < (1LL << 31) && nkb < (1LL << 31), "TMA extents out of range");
+  CUtensorMap m;
+  cuuint64_t dims[3] = {(cuuint64_t)kStageK, (cuuint64_t)rows, (cuuint64_t)nkb};
+  cuuint64_t strides[2] = {(cuuint64_t)kStageK * sizeof(float), (cuuint64_t)rows * kStageK * sizeof(float)};
+  cuuint32_t box[3] = {(cuuint32_t)kStageK, (cuuint32_t)box_rows, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = encode(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(base), dims, strides,
+                      box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) throw Error{HQCGB_CUDA_ERROR, "cuTensorMapEncodeTiled (3D) failed"};
   return m;
 }
 }  // namespace tc
@@ -1528,11 +1936,25 @@ void launch_tc_psi_density(const float *phiT, const float *dphiT, const float *Y
   HQ_REQUIRE(!grho || dphiT, "GGA density needs the gradient operand");
   HQ_REQUIRE(N <= (1LL << 29), "grid too large for 32-bit TMA row coordinates");
   // boxes of 32 fp32 (128 B, the swizzle span) x rows; row strides ldk * 4 B
-  CUtensorMap tmA = tc::tensor_map_2d(phiT, ldk, N, tc::kM);
-  CUtensorMap tmD = tc::tensor_map_2d(grho ? dphiT : phiT, ldk, grho ? 3 * N : N, tc::kM);
+  // phiT / dphiT are K-blocked ([component][AO block][g][32]): 3D maps whose
+  // 128-point x 32-AO boxes are contiguous
+  CUtensorMap tmA = tc::tensor_map_3d_kblk(phiT, N, ldk / tc::kStageK, tc::kM);
+  CUtensorMap tmD = tc::tensor_map_3d_kblk(grho ? dphiT : phiT, N, (grho ? 3 : 1) * (ldk / tc::kStageK), tc::kM);
   CUtensorMap tmY = tc::tensor_map_2d(Yhl, ldk, 2LL * npsi, npsi);
   long long ntiles = ceil_div(N, tc::kM);
   int grid = (int)std::min<long long>(ntiles, nsm);
+  // resident-Y form when Y^T fits its shared-memory region (knob
+  // "psi_ring" = 1 selects the ring form for comparison)
+  const bool resident = npsi <= tc::kPsrMaxN && tc::psr_y_bytes(npsi, ldk) <= tc::kPsrYMax &&
+                        tune_get("psi_ring", 0) == 0;
+  if (resident) {
+    ensure_dyn_smem((const void *)tc::k_tc_psi_density_r<16>, tc::kPsrSmem);
+    ensure_dyn_smem((const void *)tc::k_tc_psi_density_r<32>, tc::kPsrSmem);
+    if (npsi == 16) tc::k_tc_psi_density_r<16><<<grid, tc::kPsiThreads, tc::kPsrSmem, st>>>(a, tmA, tmD, tmY);
+    else tc::k_tc_psi_density_r<32><<<grid, tc::kPsiThreads, tc::kPsrSmem, st>>>(a, tmA, tmD, tmY);
+    HQ_LAUNCH_CHECK();
+    return;
+  }
   switch (npsi) {
     case 16: tc::k_tc_psi_density<16><<<grid, tc::kPsiThreads, tc::kPsiSmem, st>>>(a, tmA, tmD, tmY); break;
     case 32: tc::k_tc_psi_density<32><<<grid, tc::kPsiThreads, tc::kPsiSmem, st>>>(a, tmA, tmD, tmY); break;
@@ -1558,14 +1980,15 @@ int tc_quad_tiles(int nao, bool sym) {
 
 // Tile plan of the quadrature for nao AOs in 128-row blocks: which CTA writes
 // which 128 x 128 destination tile (mt, nt) of the partial sums.
-//  * persistent form (1..6 full blocks and a last block of at most 16 rows,
-//    or none): k_tc_quad_persist runs the full tiles; the narrow products
-//    (kind 0 (m, last), kind 1 (last, n) transposed, kind 2 the corner) are
-//    spread over them, at most two per CTA:
-//      non-symmetric: (m, last) on (m, m); (last, n) on ((n + 1) % nfull, n);
-//      symmetric:     (m, last) on (m, m + 1) (or (m, m) for the last block);
-//      the corner on the first tile carrying the fewest;
-//    a shape where some CTA would carry three takes the tile-list form;
+//  * persistent form (K-blocked operands; 1..6 full blocks and a last block
+//    of at most 16 rows, or none): k_tc_quad_persist runs the full tiles; the
+//    products with the partial block ride as MMA columns 128..143:
+//      (m, last) on tile (m, m);
+//      non-symmetric: (last, n) on tile ((n + 1) % nfull, n), computed
+//      transposed (its A side from the B operand);
+//    the (last, last) corner runs in k_quad_corner.  One full block and a
+//    partial one, non-symmetric, would need tile (0, 0) both ways: tile-list
+//    form;
 //  * tile-list form otherwise: every tile of the upper triangle (sym) or of
 //    the whole square through k_tc_quad_tma, at most kQtMaxTiles per launch.
 // A tile whose A-side block is the narrow one is computed transposed
@@ -1574,7 +1997,8 @@ int tc_quad_tiles(int nao, bool sym) {
 struct QuadTilePlan {
   int nblk = 0, nb_last = 0;
   bool persist = false;
-  tc::QpArgs f{};                 // persistent form: the full tiles and the narrow products they carry
+  bool corner = false;            // persistent form with a partial block: k_quad_corner
+  tc::QpArgs f{};                 // persistent form: the full tiles
   std::vector<tc::QtArgs> lists;  // k_tc_quad_tma launches, tile lists only
 };
 
@@ -1584,6 +2008,7 @@ static bool plan_persist(int nao, bool sym, tc::QpArgs &f) {
   const bool narrow = last < tc::kM;
   const int nfull = narrow ? nblk - 1 : nblk;
   if ((narrow && last > 16) || nfull < 1 || nfull > tc::kQpMaxFull) return false;
+  if (narrow && !sym && nfull == 1) return false;
   f = tc::QpArgs{};
   f.xrow = nfull * tc::kM;
   for (int mt = 0; mt < nfull; ++mt)
@@ -1592,48 +2017,28 @@ static bool plan_persist(int nao, bool sym, tc::QpArgs &f) {
       tc::QpTile &t = f.tiles[f.ntile++];
       t.mt = mt;
       t.nt = nt;
+      t.swap = 0;
+      t.nb = tc::kN;
+      if (!narrow) continue;
+      if (mt == nt) {
+        t.nb = tc::kN + 16;  // (m, last)
+      } else if (!sym && mt == (nt + 1) % nfull) {
+        t.swap = 1;          // (m, n)^T and (last, n)^T
+        t.nb = tc::kN + 16;
+      }
     }
-  if (!narrow) return true;
-  auto find = [&f](int mt, int nt) {
-    for (int i = 0; i < f.ntile; ++i)
-      if (f.tiles[i].mt == mt && f.tiles[i].nt == nt) return i;
-    return -1;
-  };
-  bool fits = true;
-  auto add = [&](int i, int kind, int xmt, int xnt) {
-    if (i < 0 || f.tiles[i].nx >= 2) {
-      fits = false;
-      return;
-    }
-    tc::QpTile &t = f.tiles[i];
-    t.kind[t.nx] = kind;
-    t.xmt[t.nx] = xmt;
-    t.xnt[t.nx] = xnt;
-    ++t.nx;
-    if (kind != 0) t.loadA = 1;
-    if (kind != 1) t.loadB = 1;
-  };
-  for (int m = 0; m < nfull && fits; ++m)
-    add(sym && m + 1 < nfull ? find(m, m + 1) : find(m, m), 0, m, nfull);
-  if (!sym)
-    for (int n = 0; n < nfull && fits; ++n) add(find(nfull > 1 ? (n + 1) % nfull : n, n), 1, nfull, n);
-  if (fits) {
-    int best = 0;
-    for (int i = 1; i < f.ntile; ++i)
-      if (f.tiles[i].nx < f.tiles[best].nx) best = i;
-    add(best, 2, nfull, nfull);
-  }
-  return fits;
+  return true;
 }
 
-static QuadTilePlan plan_quad_tiles(int nao, bool sym) {
+static QuadTilePlan plan_quad_tiles(int nao, bool sym, bool allow_persist = true) {
   QuadTilePlan p;
   p.nblk = ceil_div(nao, tc::kM);
   const int last = nao - tc::kM * (p.nblk - 1);
   const bool narrow = last < tc::kM;
   p.nb_last = ceil_div(last, 16) * 16;
-  if (plan_persist(nao, sym, p.f)) {
+  if (allow_persist && plan_persist(nao, sym, p.f)) {
     p.persist = true;
+    p.corner = narrow;
     return p;
   }
   auto push = [&p](const tc::QtTile &t) {
@@ -1684,29 +2089,31 @@ static int quad_groups(int ntile, long long N) {
 // symmetric (only tiles nt >= mt are computed; the reduce mirrors them).
 void launch_tc_quad_split(const float *Ahl, const float *Bhl, int nao, long long N, long long ld,
                           bool sym, bool add_transpose, double scale, double *partial, double *M,
-                          int *err, cudaStream_t st, int drain, int kchunk) {
+                          int *err, cudaStream_t st, int drain, int kchunk, bool blocked) {
   HQ_STAGE(ST_QUAD, st);
   HQ_REQUIRE(drain >= 1, "drain must be >= 1");
   if (kchunk <= 0) kchunk = tc_quad_chunk();
   HQ_REQUIRE(kchunk % tc::kStageK == 0, "K chunk must be a multiple of 32");
   HQ_REQUIRE(ld % 32 == 0 && ld >= N, "pre-split operands need a row stride that is a multiple of 32");
   HQ_REQUIRE(N <= (1LL << 31) - 64, "grid too large for 32-bit TMA coordinates");
-  const QuadTilePlan plan = plan_quad_tiles(nao, sym);
+  const QuadTilePlan plan = plan_quad_tiles(nao, sym, blocked);  // the persistent form reads K-blocked pieces
   const int nblk = plan.nblk;
   const long long rows = nao;
   const float *Ah = Ahl, *Al = Ahl + (size_t)nao * ld, *Bh = Bhl, *Bl = Bhl + (size_t)nao * ld;
-  CUtensorMap mAh = tc::tensor_map_2d_ext(Ah, ld, N, rows, tc::kM);
-  CUtensorMap mAl = tc::tensor_map_2d_ext(Al, ld, N, rows, tc::kM);
-  CUtensorMap mBh = tc::tensor_map_2d_ext(Bh, ld, N, rows, tc::kN);
-  CUtensorMap mBl = tc::tensor_map_2d_ext(Bl, ld, N, rows, tc::kN);
-  CUtensorMap mAh16 = tc::tensor_map_2d_ext(Ah, ld, N, rows, 16);
-  CUtensorMap mAl16 = tc::tensor_map_2d_ext(Al, ld, N, rows, 16);
-  CUtensorMap mBh16 = tc::tensor_map_2d_ext(Bh, ld, N, rows, 16);
-  CUtensorMap mBl16 = tc::tensor_map_2d_ext(Bl, ld, N, rows, 16);
-  int nparts = 0;  // partial tiles per destination tile
+  // row-major pieces: 2D maps whose columns past N read as zero; K-blocked
+  // pieces ([ld / 32][nao][32], zero-padded past N): 3D maps
+  auto map = [&](const float *b, int box) {
+    return blocked ? tc::tensor_map_3d_kblk(b, rows, ld / tc::kStageK, box)
+                   : tc::tensor_map_2d_ext(b, ld, N, rows, box);
+  };
+  CUtensorMap mAh = map(Ah, tc::kM), mAl = map(Al, tc::kM), mBh = map(Bh, tc::kN), mBl = map(Bl, tc::kN);
+  CUtensorMap mAh16 = map(Ah, 16), mAl16 = map(Al, 16), mBh16 = map(Bh, 16), mBl16 = map(Bl, 16);
+  int nparts = 0;    // partial tiles per destination tile
+  int ncorner = -1;  // of the (last, last) tile, when k_quad_corner computes it
   if (plan.persist) {
     ensure_dyn_smem((const void *)tc::k_tc_quad_persist, tc::kQpSmem);
     tc::QpArgs f = plan.f;
+    f.blocked = blocked ? 1 : 0;
     f.groups = quad_groups(f.ntile, N);
     f.N = N;
     f.drain = drain;
@@ -1718,10 +2125,22 @@ void launch_tc_quad_split(const float *Ahl, const float *Bhl, int nao, long long
     tc::k_tc_quad_persist<<<dim3(f.ntile, f.groups), tc::kQpThreads, tc::kQpSmem, st>>>(
         f, mAh, mAl, mBh, mBl, mAh16, mAl16, mBh16, mBl16);
     HQ_LAUNCH_CHECK();
+    if (plan.corner) {
+      // two CTAs per SM, within the partial tiles the buffer holds
+      int dev = 0, sms = 0;
+      HQ_CUDA(cudaGetDevice(&dev));
+      HQ_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+      const long long nkb = ld / tc::kStageK;
+      ncorner = (int)std::max<long long>(
+          1, std::min<long long>({2LL * sms, nkb, ceil_div(N, (long long)tc_quad_chunk())}));
+      tc::k_quad_corner<<<ncorner, 256, 0, st>>>(Ahl, Bhl, nao, nkb, f.xrow, nao - f.xrow, partial, 0, nblk, nblk);
+      HQ_LAUNCH_CHECK();
+    }
   } else {
     ensure_dyn_smem((const void *)tc::k_tc_quad_tma, tc::kQtSmem);
     nparts = (int)ceil_div(N, (long long)kchunk);
     for (tc::QtArgs a : plan.lists) {
+      a.blocked = blocked ? 1 : 0;
       a.N = N;
       a.kchunk = kchunk;
       a.drain = drain;
@@ -1735,7 +2154,8 @@ void launch_tc_quad_split(const float *Ahl, const float *Bhl, int nao, long long
     }
   }
   tc::k_tc_quad_reduce<<<ceil_div((long long)nao * nao, 256), 256, 0, st>>>(
-      partial, nparts, nblk, nblk, nao, sym ? 1 : 0, add_transpose ? 1 : 0, scale, M);
+      partial, nparts, nblk, nblk, nao, sym ? 1 : 0, add_transpose ? 1 : 0, scale, M,
+      ncorner >= 0 ? nblk - 1 : -1, ncorner);
   HQ_LAUNCH_CHECK();
 }
 
@@ -1744,7 +2164,7 @@ void launch_split_operand(const float *phi, const float *dphi, const float *w, c
                           long long N, long long ldi, long long ldo, float a, float b, float *out,
                           cudaStream_t st) {
   HQ_STAGE(ST_SPLIT, st);
-  HQ_REQUIRE(ldi % 4 == 0 && ldo % 4 == 0 && ldo >= N && ldi >= N, "split operand: bad row strides");
+  HQ_REQUIRE(ldi % 4 == 0 && ldo % 32 == 0 && ldo >= N && ldi >= N, "split operand: bad row strides");
   dim3 grid(ceil_div(ldo, 1024), nao);
   tc::k_split_operand<<<grid, 256, 0, st>>>(phi, dphi, w, u, nao, N, ldi, ldo, a, b, out,
                                              out + (size_t)nao * ldo);
@@ -1765,12 +2185,12 @@ void launch_tc_quadrature(const float *phi, const float *dphi, const float *phih
   if (kc < tc_quad_chunk() || kc % tc_quad_chunk() != 0 || kc > (1 << 20)) kc = tc_quad_chunk();
   if (!gga) {
     launch_split_operand(phi, nullptr, w, nullptr, nao, N, ld, ld, 1.f, 0.f, zhl, st);
-    launch_tc_quad_split(zhl, phihl, nao, N, ld, true, false, scale, partial, M, err, st, drain, (int)kc);
+    launch_tc_quad_split(zhl, phihl, nao, N, ld, true, false, scale, partial, M, err, st, drain, (int)kc, true);
     return;
   }
   HQ_REQUIRE(dphi && u, "GGA quadrature needs dphi and u");
   launch_split_operand(phi, dphi, w, u, nao, N, ld, ld, 0.5f, dV, zhl, st);
-  launch_tc_quad_split(zhl, phihl, nao, N, ld, false, true, scale, partial, M, err, st, drain, (int)kc);
+  launch_tc_quad_split(zhl, phihl, nao, N, ld, false, true, scale, partial, M, err, st, drain, (int)kc, true);
 }
 
 size_t tc_density_partial_doubles(int nao, long long ld, bool gga) {
@@ -1784,7 +2204,7 @@ void launch_transpose_phi(const float *phi, int nao, long long N, long long ld, 
                           cudaStream_t st) {
   int ldk = tc_ldk(nao);
   dim3 grid(ceil_div(N, 32), ceil_div(ldk, 32));
-  tc::k_transpose_phi<<<grid, 256, 0, st>>>(phi, nao, N, ld, phiT, ldk);
+  tc::k_transpose_phi<<<grid, 256, 0, st>>>(phi, nao, N, ld, phiT);
   HQ_LAUNCH_CHECK();
 }
 
@@ -1800,8 +2220,8 @@ void launch_tc_density(const float *phi, const float *phiT, const float *dphi, c
   int mt = ceil_div(nao, tc::kM);
   int ldk = tc_ldk(nao);
   tc::DensArgs a;
-  a.D = tc::Operand{D32, ldk, nao};
-  a.phiT = tc::Operand{phiT, ldk, (int)N};
+  a.D = tc::Operand{D32, ldk, nao, tc::kStageK};
+  a.phiT = tc::Operand{phiT, tc::kStageK, (int)N, N * tc::kStageK};
   a.phi = phi; a.dphi = grho ? dphi : nullptr; a.nao = nao;
   a.kpad = ldk; a.drain = drain; a.ns = nsplit; a.N = N; a.ld = ld; a.part = part;
   a.part_g = grho ? part + (size_t)mt * ld : nullptr; a.err = err;
@@ -1866,7 +2286,7 @@ extern "C" int hqcgb_tc_quadrature(int nao, long long N, long long ld, const flo
     float *phl = hl, *zhl = hl + 2 * (size_t)nao * ldo;
     launch_split_operand(phi, nullptr, nullptr, nullptr, nao, N, ld, ldo, 1.f, 0.f, phl, st);
     launch_split_operand(phi, nullptr, w, nullptr, nao, N, ld, ldo, 1.f, 0.f, zhl, st);
-    launch_tc_quad_split(zhl, phl, nao, N, ldo, true, false, 1.0, part, M, err, st, drain);
+    launch_tc_quad_split(zhl, phl, nao, N, ldo, true, false, 1.0, part, M, err, st, drain, 0, true);
     int h = 0;
     HQ_CUDA(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, st));
     HQ_CUDA(cudaStreamSynchronize(st));
@@ -1951,11 +2371,13 @@ extern "C" int hqcgb_tc_orbital_density(int nao, long long N, long long ld, cons
 // C ABI (host only, no device work): the quadrature's tile plan for nao AOs
 // (sym: upper-triangle tiles only).  One row of 7 ints per computed product,
 // {kind, mt, nt, arow, brow, nb, swap}: kind 0 a full tile of the
-// persistent kernel, 1 a narrow product carried by one of its CTAs, 2 a tile
-// of the tile-list kernel; (mt, nt) the destination tile, arow / brow the first AO
+// persistent kernel, 1 a narrow product (the MMA columns 128..143 of a
+// persistent CTA, or the corner of k_quad_corner), 2 a tile of the tile-list
+// kernel; (mt, nt) the destination tile, arow / brow the first AO
 // row of the MMA's A / B side (swap = 1: A side from the B operand, stored
 // transposed), nb the MMA N.  count = rows (at most cap are written);
-// launches = quadrature kernel launches before the reduce.
+// launches = tensor-core quadrature kernel launches before the reduce (the
+// CUDA-core corner kernel not counted).
 extern "C" int hqcgb_tc_quad_tiles(int nao, int sym, int cap, int *tiles, int *count, int *launches) {
   using namespace hqcgb;
   try {
@@ -1973,14 +2395,15 @@ extern "C" int hqcgb_tc_quad_tiles(int nao, int sym, int cap, int *tiles, int *c
     if (p.persist) {
       for (int t = 0; t < p.f.ntile; ++t)
         row(0, p.f.tiles[t].mt, p.f.tiles[t].nt, p.f.tiles[t].mt * tc::kM, p.f.tiles[t].nt * tc::kN, tc::kN, 0);
+      const int last = p.f.xrow / tc::kM;
       for (int t = 0; t < p.f.ntile; ++t) {
         const tc::QpTile &q = p.f.tiles[t];
-        for (int x = 0; x < q.nx; ++x) {
-          // the MMA's 128-row side: A block (kind 0), B block (kind 1, transposed), narrow A box (kind 2)
-          const int arow = q.kind[x] == 0 ? q.mt * tc::kM : (q.kind[x] == 1 ? q.nt * tc::kN : p.f.xrow);
-          row(1, q.xmt[x], q.xnt[x], arow, p.f.xrow, 16, q.kind[x] == 1 ? 1 : 0);
-        }
+        if (q.nb == tc::kN) continue;
+        // the narrow columns of a wide CTA: (mt, last), or (last, nt) transposed
+        if (!q.swap) row(1, q.mt, last, q.mt * tc::kM, p.f.xrow, 16, 0);
+        else row(1, last, q.nt, q.nt * tc::kN, p.f.xrow, 16, 1);
       }
+      if (p.corner) row(1, last, last, p.f.xrow, p.f.xrow, 16, 0);  // k_quad_corner
     }
     for (const tc::QtArgs &a : p.lists)
       for (int t = 0; t < a.ntile; ++t) {

@@ -4,10 +4,14 @@ this GPU at the shapes of the run at hand, and remembers the choice.
 Knobs (``hqcgb_tune_set``; each changes launch shapes only, so results agree
 to rounding):
 
-* ``quad_kchunk``: grid points per CTA of the tensor-core Fock quadrature.
-  Longer chunks mean fewer FP64 partial tiles to reduce but fewer CTAs and a
-  larger working set per CTA; the best value depends on the AO count and
-  grid.  Timed on the PBE quadrature (``hqcgb_tc_quadrature_gga``) with
+* ``quad_groups``: K slices of the persistent tensor-core Fock quadrature
+  (one CTA group of the destination tiles per slice; at most one CTA per
+  SM).  Fewer slices leave SMs to the kernels of concurrent configurations;
+  more slices use the whole GPU for one quadrature.
+* ``quad_kchunk``: grid points per CTA of the tile-list form (AO counts the
+  persistent form does not take).  Longer chunks mean fewer FP64 partial
+  tiles to reduce but fewer CTAs and a larger working set per CTA.
+  Both are timed on the PBE quadrature (``hqcgb_tc_quadrature_gga``) with
   synthetic operands of the run's shape.
 * ``exx_group`` and ``exx_gram_ctas``: orbitals per exact-exchange group and
   the CTA count of its tensor-core Gram matrix.  Timed on the exchange build
@@ -83,9 +87,19 @@ def _cached(key, measure, use_cache=True):
 
 
 def tune_quadrature(nao, ng, candidates=(2048, 4096, 8192, 16384), reps=4, use_cache=True):
-    """K chunk of the PBE Fock quadrature at nao AOs on an ng^3 grid; sets
-    and returns it (with the timing table when it was measured)."""
-    key = f"{torch.cuda.get_device_name()}|quad_kchunk|{nao}|{ng}"
+    """Launch shape of the PBE Fock quadrature at nao AOs on an ng^3 grid:
+    the number of K slices (CTA groups) when the shape takes the persistent
+    form, else the K chunk of the tile-list form.  Sets the knob and returns
+    (knob, value) (with the timing table when it was measured)."""
+    tiles, _ = _lib.quad_tiles(nao, False)
+    ntile = int((tiles[:, 0] == 0).sum())
+    if ntile:
+        sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+        full = max(1, sms // ntile)
+        knob, cands = "quad_groups", sorted({max(1, full // 2), max(1, (3 * full) // 4), full})
+    else:
+        knob, cands = "quad_kchunk", candidates
+    key = f"{torch.cuda.get_device_name()}|{knob}|{nao}|{ng}"
 
     def measure():
         N = ng ** 3
@@ -100,16 +114,16 @@ def tune_quadrature(nao, ng, candidates=(2048, 4096, 8192, 16384), reps=4, use_c
         u = torch.zeros(3, ld, dtype=torch.float32, device="cuda")
         u[:, :N] = torch.randn(3, N, generator=g, device="cuda")
         table = {}
-        for c in candidates:
-            set_knob("quad_kchunk", c)
+        for c in cands:
+            set_knob(knob, c)
             table[c] = _time_ms(lambda: _lib.tc_quadrature_gga(phi, dphi, w, u, 1e-3, N, drain=4), reps)
         del phi, dphi
         torch.cuda.empty_cache()
         return int(min(table, key=table.get)), table
 
     best, table = _cached(key, measure, use_cache)
-    set_knob("quad_kchunk", best)
-    return best, table
+    set_knob(knob, best)
+    return (knob, best), table
 
 
 def tune_exchange(n, L, rs, grid, basis="gth-dzv", groups=(4, 8, 16), ctas=(152, 304, 608), reps=3,

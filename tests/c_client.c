@@ -29,10 +29,12 @@ int main(void) {
   if (fabs(c[0] - 0.8) > 1e-9 || fabs(c[2] - 0.2) > 1e-9 || fabs(c[1]) > 1e-12 || fabs(c[3]) > 1e-12)
     return fail("diis coefficients wrong");
 
-  /* the quadrature tile plan of 270 AOs (2 full blocks + 14): the fused form */
+  /* the quadrature tile plan of 270 AOs (2 full blocks + 14), symmetric: the
+   * persistent form, 3 full tiles + (0, last), (1, last) and the corner in
+   * one launch */
   int tiles[64 * 7], count = 0, launches = 0;
   if (hqcgb_tc_quad_tiles(270, 1, 64, tiles, &count, &launches) != HQCGB_OK) return fail("tile plan failed");
-  if (count != 6 || launches != 2) return fail("unexpected tile plan for 270 AOs");
+  if (count != 6 || launches != 1) return fail("unexpected tile plan for 270 AOs");
 
   printf("c_client ok\n");
   return 0;

@@ -48,11 +48,19 @@ def test_fp64_exchange_matrix_matches_oracle(n, basis, grid):
 
 @pytest.mark.parametrize("n,grid", [(8, 24.0), (16, 48.0)])
 def test_mixed_hf_matches_fp64(n, grid):
+    """Mixed Hartree-Fock (FP32 pair transforms, tensor-core Gram) against
+    FP64 on configuration family 4 (Fermi smearing at 5000 K).  The chemical
+    potential is found by Newton's method: with the reference's default
+    bisection (search_tol 1e-7, hqc/tools/smearing.py:61-104) the occupations
+    are a step function of the Fock matrix at that resolution, and the FP64
+    SCF of the H16 case stalls with its commutator near 6e-7, above the
+    10 tol = 1e-7 its stopping test asks for, so there would be no converged
+    FP64 answer to compare with."""
     from hqc_gb300 import make_solver
     from hqc_gb300.workloads import hf_fermi
     w = hf_fermi(n=n, grid=grid, count=1)
     kw = {k: w[k] for k in ("dft", "grid_length", "smearing", "smearing_method", "smearing_sigma")}
-    kw.update(tol=1e-8, max_cycle=100, forces=True)
+    kw.update(tol=1e-8, max_cycle=100, forces=True, search_method="newton")
     xp = w["xps"][0]
     s64 = make_solver(w["n"], w["L"], w["rs"], w["basis"], precision="fp64", **kw)
     s32 = make_solver(w["n"], w["L"], w["rs"], w["basis"], precision="mixed", **kw)
@@ -60,4 +68,4 @@ def test_mixed_hf_matches_fp64(n, grid):
     dE = abs(float(o32[3]) - float(o64[3])) / 2 / n
     dF = np.abs(_np(s32.plan.forces()) - _np(s64.plan.forces())).max()
     print(f"H{n} HF Fermi: mixed vs fp64 dE = {dE:.2e} Ha/atom, dF = {dF:.2e} Ha/Bohr")
-    assert bool(o32[8]) and dE < 1e-6 and dF < 1e-5
+    assert bool(o64[8]) and bool(o32[8]) and dE < 1e-6 and dF < 1e-5
