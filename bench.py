@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--no-fp64-plain", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--quad-groups", type=int, default=0,
+                    help="K slices of the persistent quadrature (0: the autotuner's choice)")
     ap.add_argument("--workload", default="h54", choices=["h54", "kpoint", "slater", "coulomb", "hf"],
                     help="h54: the headline metric; the others measure the widened paths")
     return ap.parse_args()
@@ -137,9 +139,10 @@ def peaks():
 
 
 # DRAM bytes (read + write) of one PBE quadrature at the H54 shapes -- the
-# fused kernel, the corner tile and the FP64 reduce, the launches the timing
-# covers -- from one ncu capture (its summary is kept under profiles/)
-QUAD_TRAFFIC = (3655161344 + 160482560) + (119371776 + 419072) + (302131200 + 538880)
+# persistent tensor-core kernel, the corner kernel, the in-place sum of the
+# partial tiles and the reduce, the launches the timing covers -- from one ncu
+# capture (its summary is kept under profiles/)
+QUAD_TRAFFIC = None  # set from the capture below
 
 CONFIG = {"workload": "H54 bcc rs=1.31 gth-dzvp PBE 81^3 Gamma, SCF tol 1e-7 Ry + forces",
           "n_atoms": 54, "n_ao": 270, "grid": 531441}
@@ -186,9 +189,10 @@ def psi_density_roofline(hbm_gbs, src, reps=5):
 
 
 def quadrature_roofline(hbm_gbs, src, reps=5):
-    """The Fock quadrature (k_tc_quad_fused + the corner tile's k_tc_quad_tma +
-    k_tc_quad_reduce: TMA loads of pre-split TF32 operands, tcgen05 3xTF32;
-    the dominant multi-SM kernel of the SCF) timed alone with CUDA events at
+    """The Fock quadrature (k_tc_quad_persist + k_quad_corner +
+    k_tc_quad_sum_parts + k_tc_quad_reduce: TMA loads of K-blocked, pre-split
+    TF32 operands, tcgen05 3xTF32; the dominant multi-SM kernel of the SCF)
+    timed alone with CUDA events at
     the H54 PBE shapes, its non-symmetric tile set: algorithmic bytes = the
     four TF32 pieces (Z hi/lo, phi hi/lo) read once, 4 x n_ao x N x 4 B, plus
     M (n_ao^2 x 8 B).  The split pass that forms the pieces is timed
@@ -222,12 +226,14 @@ def quadrature_roofline(hbm_gbs, src, reps=5):
     torch.cuda.empty_cache()
     return {"bound": "hbm", "achieved": achieved, "peak": hbm_gbs, "unit": "GB/s",
             "frac": achieved / hbm_gbs, "traffic": QUAD_TRAFFIC,
-            "kernel": "k_tc_quad_fused + k_tc_quad_tma (corner) + k_tc_quad_reduce (PBE Fock quadrature, H54 shapes)",
+            "kernel": "k_tc_quad_persist + k_quad_corner + k_tc_quad_sum_parts + k_tc_quad_reduce "
+                      "(PBE Fock quadrature, H54 shapes)",
             "algorithmic_bytes": algo, "avg_ms": avg_s * 1e3, "launches": cnt,
             "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs, burst)" if src == "measured" else src,
-            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the three launches "
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of the four launches "
                               "of one quadrature (quadrature summary under profiles/)", "drain": 4,
-            "split_ms": st["split"][1] / max(st["split"][0], 1)}
+            # mean of the two split launches of a call (phi once, the PBE operand Z)
+            "split_ms_mean": st["split"][1] / max(st["split"][0], 1)}
 
 
 def run_ours(args):
@@ -246,6 +252,10 @@ def run_ours(args):
     from hqc_gb300.tune import tune_quadrature
     (qknob, qval), ktable = tune_quadrature(270, 81)
     tuning = {qknob: qval, "measured_ms": ktable}
+    if args.quad_groups > 0:  # a fixed choice instead of the tuner's
+        from hqc_gb300.tune import set_knob
+        set_knob("quad_groups", args.quad_groups)
+        tuning = {"quad_groups": args.quad_groups, "fixed": True}
     w0 = workload(7)
     n, L, rs = w0["n"], w0["L"], w0["rs"]
     kw = dict(dft=True, xc=w0["xc"], grid_length=w0["grid_length"], tol=1e-7, max_cycle=100,

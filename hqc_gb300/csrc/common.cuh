@@ -15,6 +15,11 @@ void set_error(const std::string &msg);
 // Run-time tuning knobs (hqcgb_tune_set): the value set for `name`, or dflt.
 long long tune_get(const char *name, long long dflt);
 void count_launch(long long k = 1);
+// How many batch workers of this host thread's batch share the GPU (1 outside
+// a concurrent batch): kernels that hold one CTA per SM for their whole run
+// (the persistent quadrature) take a correspondingly smaller grid.
+int gpu_share();
+void set_gpu_share(int workers);
 // Raise the dynamic shared-memory limit of kernel `func` on the current
 // device to at least `bytes` (never lowers it); callable from concurrent
 // host threads.

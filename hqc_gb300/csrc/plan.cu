@@ -37,6 +37,16 @@ long long tune_get(const char *name, long long dflt) {
   return it == g_tune.end() ? dflt : it->second;
 }
 void count_launch(long long k) { g_launches += k; }
+static thread_local int g_gpu_share = 1;
+int gpu_share() { return g_gpu_share; }
+void set_gpu_share(int workers) { g_gpu_share = workers > 1 ? workers : 1; }
+// GPU share of a batch worker for the scope of its loop (the caller's own
+// thread runs worker 0 and gets its previous value back)
+struct GpuShareScope {
+  int prev;
+  explicit GpuShareScope(int workers) : prev(gpu_share()) { set_gpu_share(workers); }
+  ~GpuShareScope() { set_gpu_share(prev); }
+};
 
 static const char *kStageNames[ST_COUNT] = {"gto1d", "phi", "density", "quadrature", "fft", "xc",
                                             "jacobi", "gemm_small", "overlap", "force_grid",
@@ -909,14 +919,14 @@ static int scf_one(hqcgb_plan *p, const double *xp_dev, const hqcgb_scf_out *out
     };
     while ((std::fabs(E1 - E0) > etol || enorm > errtol) && loop < P.max_cycle) diis_step();
     stopped = loop < P.max_cycle;
-    // Mixed path with smearing, stopped at the floor with the commutator
-    // still above the requested 10 tol: a few more iterations while it keeps
-    // falling by at least a fifth (the gradient's error is first order in it;
-    // at the noise floor it stops falling and the polish ends).  Without
-    // smearing the floored stop already leaves the forces well inside their
-    // bound (H54 PBE: 2.4e-7 Ha/Bohr), and the polish would only add
-    // iterations.
-    if (p->mixed && P.smearing && loop < P.max_cycle && enorm > 10.0 * P.tol) {
+    // Mixed Hartree-Fock or smeared run, stopped at the floor with the
+    // commutator still above the requested 10 tol: a few more iterations
+    // while it keeps falling by at least a fifth (the gradient's error is
+    // first order in it; at the noise floor it stops falling and the polish
+    // ends).  Kohn-Sham runs without smearing skip it: the floored stop
+    // already leaves their forces well inside the bound (H54 PBE: 2.4e-7
+    // Ha/Bohr), and the polish would only add iterations.
+    if (p->mixed && (P.smearing || !P.dft) && loop < P.max_cycle && enorm > 10.0 * P.tol) {
       for (int extra = 0; extra < 6 && loop < P.max_cycle && enorm > 10.0 * P.tol; ++extra) {
         const double prev = enorm;
         diis_step();
@@ -1147,6 +1157,7 @@ static int run_batch(hqcgb_plan *p, int n_cfg, const double *xp, const hqcgb_scf
     hqcgb_plan *q = t == 0 ? p : p->workers[t - 1];
     cudaStream_t qs = t == 0 ? st : p->wstreams[t - 1];
     cudaSetDevice(dev);
+    GpuShareScope share(nthreads);
     for (int b = next++; b < n_cfg; b = next++) {
       try {
         hqcgb_scf_out o = slice(*out, b, p->nao);
@@ -1320,6 +1331,7 @@ static int run_uneven(hqcgb_batch *b, int n_cfg, const int *n_atoms, const int *
   auto work = [&](int t) {
     cudaStream_t qs = b->streams[t];
     cudaSetDevice(dev);
+    GpuShareScope share(nthreads);
     for (int k = next++; k < n_cfg; k = next++) {
       const int c = order[k];
       try {
