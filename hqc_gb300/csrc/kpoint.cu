@@ -17,6 +17,21 @@
 // WITHOUT conjugation (scf.py:178), solved in complex arithmetic, and the
 // Fock matrices handed to the eigensolver are symmetrised, (F + F^H) / 2, as
 // jnp.linalg.eigh does with its input.
+//
+// Mixed precision (Hartree-Fock and LDA).  Every complex grid contraction
+// runs on the real tensor-core kernels of tc_gemm.cu through the real
+// embedding of the complex AO grid, X = [Re phibar; Im phibar] (2 n_ao rows,
+// FP32):
+//   quadrature  G = X diag(w) X^T,  M = (G_rr + G_ii) + i (G_ir - G_ri)
+//               (the same for S~ with w = dV and for Vep with w = dV v_loc);
+//   orbitals    psi~ = [Re; Im] of sqrt(f) C^H phibar = Y'^T X with
+//               Y' = [[Cr, -Ci]; [Ci, Cr]] sqrt(f), 32 orbitals (64 real
+//               columns) per orbital-density launch; rho = sum of the squares;
+//   exchange    FP32 pair densities phibar_p conj(psi~_i), FP32 transforms,
+//               Q = sqrt(c) P^ split into TF32 hi/lo rows [Re Q; Im Q], and
+//               K += dV [(G_rr + G_ii) + i (G_ir - G_ri)] from the Gram
+//               matrix G of those rows (3xTF32, FP64 partial sums).
+// The eigensolver, DIIS, occupations and energies stay FP64.
 #include <algorithm>
 #include <complex>
 #include <vector>
@@ -289,6 +304,123 @@ static std::vector<std::complex<double>> diis_coefficients(const std::vector<dou
   return x;
 }
 
+// ---- mixed precision: the real embedding X = [Re phibar; Im phibar] -------
+
+__device__ inline float tf32_rna_k(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+// x ~ hi + lo, both TF32 rounded to nearest
+__device__ inline void split_tf32(float x, float &hi, float &lo) {
+  hi = tf32_rna_k(x);
+  lo = tf32_rna_k(x - hi);
+}
+
+// X[p][g] = Re phibar_p(g), X[n + p][g] = Im phibar_p(g) (FP32, row stride
+// ld, zero for g in [N, ld))
+__global__ void k_kx_embed(const double2 *__restrict__ phi, int nao, long long N, long long ld,
+                           float *__restrict__ X) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)nao * ld) return;
+  const int p = (int)(idx / ld);
+  const long long g = idx - (long long)p * ld;
+  const double2 v = g < N ? phi[(long long)p * N + g] : make_double2(0.0, 0.0);
+  X[(long long)p * ld + g] = (float)v.x;
+  X[((long long)nao + p) * ld + g] = (float)v.y;
+}
+
+// w[g] = c for g < N, 0 in [N, ld)
+__global__ void k_kx_fill(long long N, long long ld, float c, float *__restrict__ w) {
+  const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g < ld) w[g] = g < N ? c : 0.f;
+}
+
+// out[p][q] (+)= scale ((G_pq + G_(n+p)(n+q)) + i (G_(n+p)q - G_p(n+q))): the
+// complex n x n matrix of the real 2n x 2n embedded product
+__global__ void k_kx_combine(int n, const double *__restrict__ G, double scale, int accumulate,
+                             double2 *__restrict__ out) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= n * n) return;
+  const int p = idx / n, q = idx % n, m = 2 * n;
+  const double re = G[(long long)p * m + q] + G[(long long)(n + p) * m + n + q];
+  const double im = G[(long long)(n + p) * m + q] - G[(long long)p * m + n + q];
+  double2 v = make_double2(scale * re, scale * im);
+  if (accumulate) v = zadd(out[idx], v);
+  out[idx] = v;
+}
+
+// TF32 hi/lo pieces of Y' for orbitals i0 .. i0 + m - 1 (m <= 32): column c < m
+// the real part of orbital i0 + c, column m + c its imaginary part, zero
+// columns up to npsi; rows p' < 2n (zero up to ldk).  Yhl [2][npsi][ldk].
+__global__ void k_kx_psi_operand(const double2 *__restrict__ C, const double *__restrict__ occ, int n,
+                                 int i0, int m, int npsi, int ldk, float *__restrict__ Yhl) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= npsi * ldk) return;
+  const int c = idx / ldk, pp = idx % ldk;
+  float x = 0.f;
+  if (c < 2 * m && pp < 2 * n) {
+    const bool im = c >= m;
+    const int k = i0 + (im ? c - m : c);
+    const int p = pp < n ? pp : pp - n;
+    const double2 cv = C[(long long)p * n + k];
+    const double sf = sqrt(fmax(occ[k], 0.0));
+    double v;
+    if (!im) v = pp < n ? cv.x : cv.y;   // Re psi~: Cr on Re phibar, Ci on Im phibar
+    else v = pp < n ? -cv.y : cv.x;      // Im psi~: -Ci on Re phibar, Cr on Im phibar
+    x = (float)(sf * v);
+  }
+  float hi, lo;
+  split_tf32(x, hi, lo);
+  Yhl[idx] = hi;
+  Yhl[(long long)npsi * ldk + idx] = lo;
+}
+
+// Pair densities of orbital j of a group: P[j][p][g] = phibar_p conj(psi~_j)
+// (FP32 complex) from the embedded rows of X and psi~ = pr + i pi.
+__global__ void k_kx_pair(const float *__restrict__ X, long long ld, const float *__restrict__ pr,
+                          const float *__restrict__ pim, int n, long long N, float2 *__restrict__ P) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)n * N) return;
+  const int p = (int)(idx / N);
+  const long long g = idx - (long long)p * N;
+  const float xr = X[(long long)p * ld + g], xi = X[((long long)n + p) * ld + g];
+  const float a = pr[g], b = pim[g];
+  P[idx] = make_float2(xr * a + xi * b, xi * a - xr * b);
+}
+
+// Q = sqrt(c) P^ of orbital j of a group as TF32 hi/lo rows: Re Q_p into row
+// p, Im Q_p into row n + p, columns j ldq + G; zero for G in [N, ldq).
+// Qhl [2][2n][ldQ] with ldQ = g ldq.
+__global__ void k_kx_qsplit(const float2 *__restrict__ P, const double *__restrict__ sqc, int n, long long N,
+                            long long ldq, int j, long long ldQ, float *__restrict__ Qhl) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)n * ldq) return;
+  const int p = (int)(idx / ldq);
+  const long long G = idx - (long long)p * ldq;
+  float re = 0.f, im = 0.f;
+  if (G < N) {
+    const float2 v = P[(long long)p * N + G];
+    const float c = (float)sqc[G];
+    re = c * v.x;
+    im = c * v.y;
+  }
+  const long long o = (long long)j * ldq + G, piece = 2LL * n * ldQ;
+  float hi, lo;
+  split_tf32(re, hi, lo);
+  Qhl[(long long)p * ldQ + o] = hi;
+  Qhl[piece + (long long)p * ldQ + o] = lo;
+  split_tf32(im, hi, lo);
+  Qhl[((long long)n + p) * ldQ + o] = hi;
+  Qhl[piece + ((long long)n + p) * ldQ + o] = lo;
+}
+
+// a += b (n doubles)
+__global__ void k_kx_add(long long n, const double *__restrict__ b, double *__restrict__ a) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) a[i] += b[i];
+}
+
 }  // namespace hqcgb
 
 using namespace hqcgb;
@@ -298,8 +430,20 @@ struct hqcgb_kplan {
   int n = 0, nb = 0, nao = 0, ng = 0, nprim = 0;
   long long N = 0;
   double L = 0, Omega = 0, dV = 0;
-  bool gga = false, hf = false;
+  bool gga = false, hf = false, mixed = false;
   std::vector<void *> allocs;
+  // mixed precision: the real embedding X [2n][ld] (FP32), its TF32 pieces
+  // (K-blocked), the quadrature operand pieces, the grid-major K-blocked copy
+  // of X, Y' pieces, the orbitals psi~ ([chunk][64][N]: 32 orbitals, real
+  // rows then imaginary rows), pair densities and Q pieces of an orbital
+  // group, FP64 partial tiles and the 2n x 2n product
+  long long ld = 0, ldq = 0;
+  int ldk2 = 0, xg = 1;
+  float *X32 = nullptr, *Xhl = nullptr, *zhl = nullptr, *w32 = nullptr, *XT = nullptr, *Yhl = nullptr,
+        *psi32 = nullptr, *Qhl = nullptr;
+  float2 *Pc = nullptr;
+  double *part = nullptr, *G = nullptr, *rhoc = nullptr;
+  int *tc_err = nullptr;
   // constant tables
   double *alpha = nullptr, *coef = nullptr, *lat1d = nullptr, *lattice = nullptr, *coul = nullptr,
          *sqcoul = nullptr;
@@ -370,7 +514,9 @@ static void kcreate(const hqcgb_params &P, hqcgb_kplan *p) {
   HQ_REQUIRE(P.diis_space >= 1 && P.diis_space <= 32, "diis_space must be in [1, 32]");
   HQ_REQUIRE(P.max_cycle >= 0, "max_cycle must be >= 0");
   HQ_REQUIRE(!P.smearing || P.smearing_sigma > 0, "smearing_sigma must be > 0 with smearing");
-  HQ_REQUIRE(P.precision == HQCGB_PREC_FP64, "the k-point solver runs in FP64 only");
+  HQ_REQUIRE(P.precision == HQCGB_PREC_FP64 || P.precision == HQCGB_PREC_MIXED, "unknown precision");
+  HQ_REQUIRE(P.precision == HQCGB_PREC_FP64 || !(P.dft && P.xc == HQCGB_XC_PBE),
+             "the mixed k-point solver covers Hartree-Fock and LDA (PBE runs in FP64)");
   HQ_REQUIRE(!P.want_forces, "the k-point solver has no forces");
   for (int k = 0; k < P.nao_atom; ++k) {
     HQ_REQUIRE(P.ao_l[k] == 0 || P.ao_l[k] == 1, "only s and p AOs are supported");
@@ -427,9 +573,12 @@ static void kcreate(const hqcgb_params &P, hqcgb_kplan *p) {
   p->phi = p->alloc<double2>((size_t)nao * N);
   if (p->gga) p->dphi = p->alloc<double2>((size_t)3 * nao * N);
   p->ph = p->alloc<double2>((size_t)n * 3 * p->ng);
-  p->Z = p->alloc<double2>((size_t)nao * N);
-  if (p->hf) p->W = p->alloc<double2>((size_t)nao * N);
-  p->Psi = p->alloc<double2>((size_t)nao * N);
+  p->mixed = P.precision == HQCGB_PREC_MIXED;
+  if (!p->mixed) {  // FP64 operand, pair-density and orbital grids (the mixed path keeps FP32 ones)
+    p->Z = p->alloc<double2>((size_t)nao * N);
+    if (p->hf) p->W = p->alloc<double2>((size_t)nao * N);
+    p->Psi = p->alloc<double2>((size_t)nao * N);
+  }
   if (p->gga) p->dPsi = p->alloc<double2>((size_t)3 * nao * N);
   p->cbuf = p->alloc<double2>(N);
   for (double2 **m : {&p->S, &p->T, &p->V, &p->H, &p->St, &p->vorth, &p->F, &p->F2e, &p->K, &p->Fp,
@@ -459,6 +608,35 @@ static void kcreate(const hqcgb_params &P, hqcgb_kplan *p) {
   p->scal = p->alloc<double>(K_NSLOT);
   HQ_CUDA(cudaMallocHost(&p->hscal, K_NSLOT * sizeof(double)));
   p->h_occ.resize(nao);
+  if (p->mixed) {
+    const int n2 = 2 * nao;
+    HQ_REQUIRE(n2 <= 288 * 4, "too many AOs for the mixed k-point path");
+    p->ld = (N + 63) / 64 * 64;
+    p->ldq = (N + 31) / 32 * 32;
+    p->ldk2 = tc_ldk(n2);
+    p->X32 = p->alloc<float>((size_t)n2 * p->ld);
+    p->Xhl = p->alloc<float>((size_t)2 * n2 * p->ld);
+    p->zhl = p->alloc<float>((size_t)2 * n2 * p->ld);
+    p->w32 = p->alloc<float>(p->ld);
+    p->XT = p->alloc<float>((size_t)N * p->ldk2);
+    p->Yhl = p->alloc<float>((size_t)2 * 64 * p->ldk2);
+    const int nchunk = (nao + 31) / 32;
+    p->psi32 = p->alloc<float>((size_t)nchunk * 64 * N);
+    p->rhoc = p->alloc<double>(N);
+    p->tc_err = p->alloc<int>(1);
+    HQ_CUDA(cudaMemset(p->tc_err, 0, sizeof(int)));
+    p->G = p->alloc<double>((size_t)n2 * n2);
+    size_t parts = tc_quad_partial_doubles(n2, N);
+    if (p->hf) {
+      // orbitals per exchange group: pair densities and Q pieces within ~3 GB
+      const double per_orb = (double)nao * N * sizeof(float2) + 2.0 * n2 * p->ldq * sizeof(float);
+      p->xg = (int)std::max(1.0, std::min(8.0, std::floor(3e9 / per_orb)));
+      p->Pc = p->alloc<float2>((size_t)p->xg * nao * N);
+      p->Qhl = p->alloc<float>((size_t)2 * n2 * p->xg * p->ldq);
+      parts = std::max(parts, tc_quad_partial_doubles(n2, (long long)p->xg * p->ldq));
+    }
+    p->part = p->alloc<double>(parts);
+  }
   HQ_CUDA(cudaDeviceSynchronize());
 }
 
@@ -527,12 +705,98 @@ static void kpoisson_real(KCtx &c, const double *src, double *dst) {
   launch_complex_real(p->cbuf, p->N, 1.0, dst, c.st);
 }
 
+// Mixed path: out (+)= scale (Z Phibar^H) with Z = w32 phibar, through the
+// tensor-core quadrature of the embedded rows X (FP64 partial sums).
+static void kx_quad(KCtx &c, int drain, double2 *out, bool accumulate = false, double scale = 1.0) {
+  hqcgb_kplan *p = c.p;
+  const int n = p->nao;
+  launch_tc_quadrature(p->X32, nullptr, p->Xhl, p->w32, nullptr, (float)p->dV, 2 * n, p->N, p->ld, false,
+                       1.0, p->part, p->G, p->tc_err, c.st, drain, p->zhl);
+  k_kx_combine<<<ceil_div((long long)n * n, 256), 256, 0, c.st>>>(n, p->G, scale, accumulate ? 1 : 0, out);
+  HQ_LAUNCH_CHECK();
+}
+
+// Mixed path: orbitals with occupation above kExxOccFloor (the occupations
+// fall with the band energy, so they come first), 32 per orbital-density
+// launch, their sqrt(f)-weighted values on the grid into psi32 and rho.
+static int kx_density(KCtx &c) {
+  hqcgb_kplan *p = c.p;
+  const int n = p->nao;
+  const long long N = p->N;
+  HQ_STAGE(ST_DENSITY, c.st);
+  int nd = 0;
+  for (int k = 0; k < n; ++k)
+    if (p->h_occ[k] > kExxOccFloor) nd = k + 1;
+  if (nd == 0) HQ_CUDA(cudaMemsetAsync(p->rho, 0, sizeof(double) * N, c.st));
+  for (int c0 = 0; c0 < nd; c0 += 32) {
+    const int m = std::min(32, nd - c0), npsi = tc_psi_width(2 * m);
+    k_kx_psi_operand<<<ceil_div(npsi * p->ldk2, 256), 256, 0, c.st>>>(p->C, p->occ, n, c0, m, npsi, p->ldk2,
+                                                                       p->Yhl);
+    HQ_LAUNCH_CHECK();
+    double *dst = c0 == 0 ? p->rho : p->rhoc;
+    launch_tc_psi_density(p->XT, nullptr, p->Yhl, npsi, p->ldk2, N, dst, nullptr, p->tc_err, c.st,
+                          p->psi32 + (size_t)(c0 / 32) * 64 * N, 2);
+    if (c0 > 0) {
+      k_kx_add<<<ceil_div(N, 256), 256, 0, c.st>>>(N, p->rhoc, p->rho);
+      HQ_LAUNCH_CHECK();
+    }
+  }
+  return nd;
+}
+
+// Mixed exact exchange: per group of xg orbitals the FP32 pair densities and
+// transforms, Q pieces, and the tensor-core Gram matrix added into K (then
+// the Madelung term as in the FP64 path).
+static void kx_exchange(KCtx &c, int nd) {
+  hqcgb_kplan *p = c.p;
+  const int n = p->nao;
+  const long long N = p->N;
+  HQ_STAGE(ST_EXCHANGE, c.st);
+  HQ_CUDA(cudaMemsetAsync(p->K, 0, sizeof(double2) * n * n, c.st));
+  const double thr = std::max(p->P.exx_occ_threshold, kExxOccFloor);
+  std::vector<int> used;
+  for (int i = 0; i < nd; ++i)
+    if (p->h_occ[i] > thr) used.push_back(i);
+  for (size_t g0 = 0; g0 < used.size(); g0 += p->xg) {
+    const int g = (int)std::min<size_t>(p->xg, used.size() - g0);
+    for (int j = 0; j < g; ++j) {
+      const int i = used[g0 + j], ch = i / 32, jj = i % 32, m = std::min(32, nd - ch * 32);
+      const float *pr = p->psi32 + ((size_t)ch * 64 + jj) * N, *pim = p->psi32 + ((size_t)ch * 64 + m + jj) * N;
+      k_kx_pair<<<ceil_div((long long)n * N, 256), 256, 0, c.st>>>(p->X32, p->ld, pr, pim, n, N,
+                                                                   p->Pc + (size_t)j * n * N);
+      HQ_LAUNCH_CHECK();
+    }
+    launch_fft3d_f32(p->Pc, p->ng, g * n, p->tw, false, c.st);
+    const long long ldQ = (long long)g * p->ldq;
+    for (int j = 0; j < g; ++j) {
+      k_kx_qsplit<<<ceil_div((long long)n * p->ldq, 256), 256, 0, c.st>>>(p->Pc + (size_t)j * n * N, p->sqcoul, n,
+                                                                          N, p->ldq, j, ldQ, p->Qhl);
+      HQ_LAUNCH_CHECK();
+    }
+    // drained every K stage: a Gram matrix's diagonal is a same-signed sum
+    launch_tc_quad_split(p->Qhl, p->Qhl, 2 * n, ldQ, ldQ, true, false, 1.0, p->part, p->G, p->tc_err, c.st, 1,
+                         0, false);
+    k_kx_combine<<<ceil_div((long long)n * n, 256), 256, 0, c.st>>>(n, p->G, p->dV, 1, p->K);
+    HQ_LAUNCH_CHECK();
+  }
+  zcomb(n, 0.5, p->K, 0.5, p->K, true, p->t1, c.st);
+  const double cM = 4.0 * M_PI / p->L * kMadelungK;
+  zgemm('N', 'N', n, n, n, kOne, p->St, n, p->D, n, kZero, p->t2, n, c.st);
+  zgemm('N', 'N', n, n, n, kOne, p->t2, n, p->St, n, kZero, p->K, n, c.st);
+  zcomb(n, 1.0, p->t1, cM, p->K, false, p->K, c.st);
+}
+
 // F2e = Z Phibar^H (+ its Hermitian conjugate with GGA), Z from w (and u)
 static void kquadrature(KCtx &c, const double *w, const double *u, double2 *out) {
   hqcgb_kplan *p = c.p;
   const int n = p->nao;
   const long long N = p->N;
   HQ_STAGE(ST_QUAD, c.st);
+  if (p->mixed) {  // LDA / Hartree only (PBE k-points run in FP64)
+    launch_to_f32(w, N, N, 1, 1.0, p->w32, p->ld, c.st);
+    kx_quad(c, p->hf ? 1 : 4, out);
+    return;
+  }
   k_zoperand<<<ceil_div((long long)n * N, 256), 256, 0, c.st>>>(p->phi, p->dphi, w, u, n, N,
                                                                   u ? 0.5 : 1.0, p->dV, p->Z);
   HQ_LAUNCH_CHECK();
@@ -585,7 +849,10 @@ static double kfock(KCtx &c) {
   for (int k = 0; k < n; ++k)
     if (p->h_occ[k] > 0.0) nuse = k + 1;
   p->nuse = nuse;
-  {
+  int nd = 0;
+  if (p->mixed) {
+    nd = kx_density(c);
+  } else {
     HQ_STAGE(ST_DENSITY, c.st);
     if (nuse > 0) {
       zgemm('C', 'N', nuse, (int)N, n, kOne, p->C, n, p->phi, (int)N, kZero, p->Psi, (int)N, c.st);
@@ -605,7 +872,8 @@ static double kfock(KCtx &c) {
   launch_sum_partials(p->xpart, xc_blocks(N), 2, 2, 1.0, p->scal + K_EXC, false, c.st);
   kquadrature(c, p->wq, p->gga ? p->u : nullptr, p->F2e);
   if (p->hf) {
-    kexchange(c);
+    if (p->mixed) kx_exchange(c, nd);
+    else kexchange(c);
     kdot(c, p->K, p->D, K_TRKD);
     zcomb(n, 1.0, p->F2e, -0.5, p->K, false, p->F2e, c.st);
   }
@@ -651,13 +919,23 @@ static void kgeometry(KCtx &c, const double *xp_dev, const double *kpt_host) {
                                                                    p->nb, p->nprim, n, p->ng, p->phi,
                                                                    p->dphi);
     HQ_LAUNCH_CHECK();
+    if (p->mixed) {  // the embedded FP32 rows, their TF32 pieces and the grid-major copy
+      k_kx_embed<<<ceil_div((long long)n * p->ld, 256), 256, 0, c.st>>>(p->phi, n, N, p->ld, p->X32);
+      HQ_LAUNCH_CHECK();
+      launch_split_operand(p->X32, nullptr, nullptr, nullptr, 2 * n, N, p->ld, p->ld, 1.f, 0.f, p->Xhl, c.st);
+      launch_transpose_phi(p->X32, 2 * n, N, p->ld, p->XT, c.st);
+    }
   }
   launch_overlap_kinetic_kpt(p->xp, p->n, p->nb, p->nprim, p->alpha, p->coef, p->ao_l, p->ao_cart,
                              p->lattice, P.n_lattice, p->kpt, p->S, p->T, p->ovq, c.st);
   launch_vloc_G(p->xp, p->n, p->ng, p->L, p->ph, p->cbuf, c.st);
   launch_fft3d(p->cbuf, p->ng, 1, p->tw, true, c.st);
   launch_complex_real(p->cbuf, N, 1.0, p->vloc, c.st);
-  {
+  if (p->mixed) {
+    HQ_STAGE(ST_QUAD, c.st);
+    launch_to_f32(p->vloc, N, N, 1, p->dV, p->w32, p->ld, c.st);
+    kx_quad(c, 1, p->V);
+  } else {
     HQ_STAGE(ST_QUAD, c.st);
     k_zoperand<<<ceil_div((long long)n * N, 256), 256, 0, c.st>>>(p->phi, nullptr, p->vloc, nullptr, n,
                                                                     N, p->dV, 0.0, p->Z);
@@ -665,9 +943,14 @@ static void kgeometry(KCtx &c, const double *xp_dev, const double *kpt_host) {
     zgemm('N', 'C', n, n, (int)N, kOne, p->Z, (int)N, p->phi, (int)N, kZero, p->V, n, c.st);
   }
   zcomb(n, 1.0, p->T, 1.0, p->V, false, p->H, c.st);
-  if (p->hf)
+  if (p->hf && p->mixed) {
+    k_kx_fill<<<ceil_div(p->ld, 256), 256, 0, c.st>>>(N, p->ld, (float)p->dV, p->w32);
+    HQ_LAUNCH_CHECK();
+    kx_quad(c, 1, p->St);
+  } else if (p->hf) {
     zgemm('N', 'C', n, n, (int)N, make_double2(p->dV, 0.0), p->phi, (int)N, p->phi, (int)N, kZero, p->St,
           n, c.st);
+  }
   // S^{-1/2} as U w^{-1/2} (solver.py:795-796)
   HQ_CUDA(cudaMemsetAsync(p->ibad, 0, sizeof(int), c.st));
   keigh(c, p->S, p->c1, p->ws);
@@ -740,14 +1023,19 @@ static int kscf_one(hqcgb_kplan *p, const double *xp_dev, const double *kpt_host
     // plain iterations filling the DIIS history (scf.py:124-169)
     while (loop < P.diis_start_cycle + sp) step(p->Fk + head * nn);
     E0 = E1 - 1.0;
-    while ((std::fabs(E1 - E0) > P.tol || enorm > 10.0 * P.tol) && loop < P.max_cycle) {
+    // mixed: the stopping tests are floored at the FP32 noise of the Fock
+    // build, as on the Gamma-point path
+    const double etol = p->mixed ? std::max(P.tol, 2e-6) : P.tol;
+    const double errtol = p->mixed ? std::max(10.0 * P.tol, 2e-5) : 10.0 * P.tol;
+    while ((std::fabs(E1 - E0) > etol || enorm > errtol) && loop < P.max_cycle) {
       kdiis_extrapolate(c, head, p->t2);  // t2 is free until the exchange step
       step(p->t2);
       if (!std::isfinite(E1)) throw Error{HQCGB_NAN, "non-finite energy in the SCF"};
     }
   } else {
     // fixed_point_scf (scf.py:21-88)
-    while (std::fabs(E1 - E0) > P.tol && loop < P.max_cycle) {
+    const double etol = p->mixed ? std::max(P.tol, 2e-6) : P.tol;
+    while (std::fabs(E1 - E0) > etol && loop < P.max_cycle) {
       const double En = kfock(c);
       kdiagonalize(c, p->F);
       kdensity_matrix(c);
@@ -758,6 +1046,15 @@ static int kscf_one(hqcgb_kplan *p, const double *xp_dev, const double *kpt_host
     }
   }
   kcheck_eig(c);
+  if (p->mixed) {
+    int te = 0;
+    HQ_CUDA(cudaMemcpyAsync(&te, p->tc_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    HQ_CUDA(cudaStreamSynchronize(st));
+    if (te) {
+      HQ_CUDA(cudaMemsetAsync(p->tc_err, 0, sizeof(int), st));
+      throw Error{HQCGB_CUDA_ERROR, "tensor-core pipeline wait limit hit (code " + std::to_string(te) + ")"};
+    }
+  }
   const int converged = (loop != P.max_cycle) ? 1 : 0;
   // post-processing (solver.py:824-837 / 950-962)
   kdensity_matrix(c);

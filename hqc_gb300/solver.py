@@ -273,20 +273,24 @@ def make_solver(n: int, L: float, rs: float, basis: str,
 
     ``gamma=False`` returns ``solver(xp, kpt)`` for one k-point (kpt (3,) in
     1/Bohr, first Brillouin zone (-pi/(L rs), pi/(L rs)); solver.py:769-962):
-    the same tuple with complex128 mo_coeff and dm.  It runs in FP64 without
-    forces; a batch of xp (B, n, 3) and/or kpt (B, 3) broadcasts like
-    ``jax.vmap``.
+    the same tuple with complex128 mo_coeff and dm.  It has no forces;
+    ``precision='mixed'`` (Hartree-Fock and LDA) runs its grid contractions on
+    the tensor cores (complex operands as real/imaginary rows, FP32 pair
+    transforms) with the FP64 eigensolver; a batch of xp (B, n, 3) and/or kpt
+    (B, 3) broadcasts like ``jax.vmap``.
     """
     L_bohr = float(L) * float(rs)
     if not gamma:
-        if precision != "fp64":
-            raise NotImplementedError("the k-point solver runs in FP64 only (precision='fp64')")
+        if precision not in ("fp64", "mixed"):
+            raise ValueError(f"unknown precision {precision!r}")
+        if precision == "mixed" and dft and _lib.XC.get(xc.lower().replace(" ", "")) == 10:
+            raise NotImplementedError("the mixed k-point solver covers Hartree-Fock and LDA")
         if forces:
             raise NotImplementedError("the k-point solver has no forces")
         return _make_kpoint_solver(n, L_bohr, rs, basis, rcut, tol, max_cycle, grid_length, diis,
                                    diis_space, diis_start_cycle, diis_damp, dft, xc, smearing,
                                    smearing_method, smearing_sigma, search_method, search_cycle,
-                                   search_tol, n_grid, exx_occ_threshold)
+                                   search_tol, n_grid, exx_occ_threshold, precision)
     plan = Plan(n, L_bohr, basis, rcut, tol, max_cycle, grid_length, diis, diis_space,
                 diis_start_cycle, diis_damp, dft, xc, smearing, smearing_method, smearing_sigma,
                 search_method, search_cycle, search_tol, precision=precision, forces=forces,
@@ -335,10 +339,10 @@ def make_solver(n: int, L: float, rs: float, basis: str,
 def _make_kpoint_solver(n, L_bohr, rs, basis, rcut, tol, max_cycle, grid_length, diis, diis_space,
                         diis_start_cycle, diis_damp, dft, xc, smearing, smearing_method,
                         smearing_sigma, search_method, search_cycle, search_tol, n_grid,
-                        exx_occ_threshold):
+                        exx_occ_threshold, precision="fp64"):
     plan = Plan(n, L_bohr, basis, rcut, tol, max_cycle, grid_length, diis, diis_space,
                 diis_start_cycle, diis_damp, dft, xc, smearing, smearing_method, smearing_sigma,
-                search_method, search_cycle, search_tol, precision="fp64", forces=False,
+                search_method, search_cycle, search_tol, precision=precision, forces=False,
                 n_grid=n_grid, exx_occ_threshold=exx_occ_threshold, kpoint=True)
 
     def solver(xp, kpt):

@@ -313,7 +313,9 @@ int hqcgb_eigh_noalloc(int n, const double *A, double *w, double *V, void *strea
 typedef struct hqcgb_kplan hqcgb_kplan;
 
 /* Factory of the k-point solver: the same parameters as hqcgb_plan_create
- * (precision must be HQCGB_PREC_FP64, want_forces 0).  Replaces the
+ * (want_forces 0; precision HQCGB_PREC_FP64, or HQCGB_PREC_MIXED for
+ * Hartree-Fock and LDA: grid contractions on the tensor cores through the
+ * real embedding of the complex AO grid, FP64 eigensolver).  Replaces the
  * table-building part of make_solver(gamma=False) (hqc/pbc/solver.py:209-231,
  * 378-389). */
 int hqcgb_kplan_create(const hqcgb_params *params, hqcgb_kplan **plan);

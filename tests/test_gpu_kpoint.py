@@ -158,3 +158,48 @@ def test_kpoint_time_reversal_and_batch():
     pes = make_pes(*args, **kw)
     Vpp = float(potential_energy_pp(z["xp"], float(z["L"]), meta["rs"]))
     assert abs(float(pes(z["xp"], k)) - (float(a[3]) + Vpp)) < 1e-10
+
+
+# Mixed-precision k-point solver (Hartree-Fock and LDA): grid contractions on
+# the tensor cores through the real embedding of the complex AO grid, FP32
+# pair transforms for the exchange, FP64 eigensolver.  Bound: the metric's
+# 1e-6 Ha/atom on the energy; occupied bands within 2e-5 Ry.
+MIXED_CASES = [
+    ("golden", "hf_kpt_dzv", None),
+    ("golden", "dft_kpt_dzv", None),
+    ("random", 16, dict(smearing=True, smearing_method="fermi", smearing_sigma=0.5 * 10000 / 157888.09,
+                        search_method="newton", grid_length=None)),
+]
+
+
+@pytest.mark.parametrize("kind,case,kw", MIXED_CASES)
+def test_kpoint_mixed_matches_fp64(kind, case, kw):
+    from hqc_gb300 import make_solver
+    if kind == "golden":
+        meta, z = load_golden(case)
+        n = meta["n"]
+        s64 = _kpt_solver(meta, z)
+        s32 = _kpt_solver(meta, z, precision="mixed")
+        xp, kpt = z["xp"], z["kpt"]
+        nocc = n // 2
+    else:
+        n, rs = case, 1.4
+        L = (4 * np.pi * n / 3) ** (1 / 3)
+        rng = np.random.default_rng(11)
+        xp = rng.uniform(0, L, size=(n, 3))
+        kpt = rng.uniform(-np.pi / L / rs, np.pi / L / rs, 3)
+        common = dict(kw, grid_length=L * rs / 48.0, tol=1e-7, max_cycle=100, gamma=False)
+        s64 = make_solver(n, L, rs, "gth-dzv", **common)
+        s32 = make_solver(n, L, rs, "gth-dzv", precision="mixed", **common)
+        nocc = n // 2
+    o64, o32 = s64(xp, kpt), s32(xp, kpt)
+    dE = abs(float(o32[3]) - float(o64[3])) / 2 / n
+    dB = np.abs(_np(o32[2])[:nocc] - _np(o64[2])[:nocc]).max()
+    print(f"{case}: mixed vs fp64 dE = {dE:.2e} Ha/atom, occupied bands {dB:.2e} Ry, converged "
+          f"{bool(o64[8])}/{bool(o32[8])} in {s64.iterations}/{s32.iterations} iterations")
+    assert bool(o64[8]) and bool(o32[8])
+    assert dE < 1e-6
+    assert dB < 2e-5
+    # the density matrix is Hermitian to rounding
+    D = _np(o32[1])
+    assert np.abs(D - np.conj(D.T)).max() < 1e-10
