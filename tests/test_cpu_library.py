@@ -159,9 +159,10 @@ def test_quadrature_tile_plan_covers_each_tile_once(nao, sym):
     tile (transposed products swap them; the corner reads the narrow block on
     both sides); the MMA N covers the rows of the B-side block in multiples of
     16; the persistent form is taken exactly when there are 1..6 full blocks,
-    the last block has at most 16 rows (or there is none) and no CTA would
-    carry more than two narrow products; the tile-list kernel gets at most 12
-    tiles per launch."""
+    the last block has at most 16 rows (or there is none), and not for one
+    full block plus a partial one in the non-symmetric case (its only tile
+    would need both orientations); the tile-list kernel gets at most 12 tiles
+    per launch."""
     from hqc_gb300 import _lib
     tiles, launches = _lib.quad_tiles(nao, sym)
     nblk = -(-nao // 128)
