@@ -511,7 +511,7 @@ class Solver:
         Vep = _tr(V, D)
         Vee = 0.5 * _tr(J, D) + Exc
         Se = entropy(occf(e))
-        self.last = dict(g=g, C=C, e=e, D=D, occ=occf(e), E=E, v=v)
+        self.last = dict(g=g, C=C, e=e, D=D, occ=occf(e), E=E, v=v, kpt=kpt)
         return C, D, e * RY, E * RY, Ki * RY, Vep * RY, Vee * RY, Se, conv
 
     def _unit(self, label):

@@ -284,6 +284,15 @@ FD_CASES = {
                              search_cycle=200, **FD_TIGHT), None),
     "fd_lda_dzvp": (4, 1.5, "gth-dzvp", 42,
                     dict(grid_length=0.25, dft=True, xc="lda,vwn", **FD_TIGHT), 6),
+    # single k-point (pes_kpt, hqc/pbc/pes.py:88-98): the k-point is drawn as
+    # in the hf_kpt_dzv solver case and held fixed while the protons move
+    "fd_hf_kpt_dzv_fermi": (4, 1.5, "gth-dzv", 42,
+                            dict(grid_length=0.2, gamma=False, smearing=True,
+                                 smearing_method="fermi", smearing_sigma=0.1,
+                                 search_method="newton", search_tol=1e-13, search_cycle=200,
+                                 **FD_TIGHT), 8),
+    "fd_lda_kpt_dzv": (4, 1.5, "gth-dzv", 42,
+                       dict(grid_length=0.2, gamma=False, dft=True, xc="lda,vwn", **FD_TIGHT), 6),
 }
 
 
@@ -294,9 +303,13 @@ def run_fd_case(name):
     t0 = time.time()
     pes = make_pes(n, L, rs, basis, mode="dev", **kw)
     sigma = kw.get("smearing_sigma", 0.0) if kw.get("smearing") else 0.0
+    kpt = None
+    if not kw.get("gamma", True):
+        kpt = np.random.default_rng(seed + 1).uniform(-np.pi / L / rs, np.pi / L / rs, 3)
 
     def ev(x):
-        Etot, Ki, Vep, Vee, Vpp, Se, conv = pes(jnp.array(x.copy()))
+        args = (jnp.array(x.copy()),) if kpt is None else (jnp.array(x.copy()), jnp.array(kpt))
+        Etot, Ki, Vep, Vee, Vpp, Se, conv = pes(*args)
         assert bool(np.asarray(conv)), "reference SCF did not converge"
         return float(np.asarray(Etot)), float(np.asarray(Se)), float(np.asarray(Vpp))
 
@@ -318,6 +331,8 @@ def run_fd_case(name):
         dF.append(((Ep - 2 * sigma * Sp) - (Em - 2 * sigma * Sm)) / (2 * FD_H))
     rec = dict(xp=xp, n=n, rs=rs, L=L, h=FD_H, coords=np.array(coords), Etot=E0, Se=S0, Vpp=V0,
                dEtot=np.array(dE), dFtot=np.array(dF), sigma=sigma)
+    if kpt is not None:
+        rec["kpt"] = kpt
     meta = dict(factory="pes_fd", n=n, rs=rs, basis=basis, seed=seed, kwargs=kw, h=FD_H,
                 coords=len(coords), seconds=round(time.time() - t0, 2))
     return rec, meta

@@ -22,7 +22,9 @@ def test_h54_adjoint_matches_fp64_finite_differences():
     w = h54_bcc_pbe()
     n, L, rs, xp = w["n"], w["L"], w["rs"], w["xp"]
     kw = dict(dft=True, xc="pbe", grid_length=w["grid_length"], max_cycle=100, forces=True)
-    p64 = make_pes(n, L, rs, w["basis"], precision="fp64", tol=1e-10, **kw)
+    # the 24 displaced energies run as one batch, 8 configurations at a time
+    # (bitwise the single-call results: tests/test_gpu_batch.py)
+    p64 = make_pes(n, L, rs, w["basis"], precision="fp64", tol=1e-10, concurrency=8, **kw)
     p32 = make_pes(n, L, rs, w["basis"], precision="mixed", tol=1e-7, **kw)
     _, g64 = p64.value_and_grad(xp)
     _, g32 = p32.value_and_grad(xp)
@@ -32,15 +34,18 @@ def test_h54_adjoint_matches_fp64_finite_differences():
     rng = np.random.default_rng(12)
     pick = rng.choice(3 * n, 12, replace=False)
     h = 1e-4 / rs                                    # 1e-4 Bohr in rs units
-    err64, err32 = [], []
+    xs = []
     for idx in pick:
         a, d = divmod(int(idx), 3)
-        e = []
         for sgn in (1.0, -1.0):
             x = xp.copy()
             x[a, d] += sgn * h
-            e.append(float(p64(x)))
-        fd = (e[0] - e[1]) / (2 * h) * to_ha_bohr
+            xs.append(x)
+    e = p64(np.stack(xs)).cpu().numpy()
+    err64, err32 = [], []
+    for i, idx in enumerate(pick):
+        a, d = divmod(int(idx), 3)
+        fd = (e[2 * i] - e[2 * i + 1]) / (2 * h) * to_ha_bohr
         err64.append(abs(fd - g64[a, d]))
         err32.append(abs(fd - g32[a, d]))
     print(f"H54 FD (12 coordinates, h = 1e-4 Bohr): max |FP64 adjoint - FD| = {max(err64):.2e}, "

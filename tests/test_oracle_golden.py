@@ -170,18 +170,21 @@ def test_oracle_gradient_matches_finite_differences(kw):
         assert abs(fd - g[a, d]) < 2e-6, (a, d, fd, g[a, d])
 
 
-@pytest.mark.parametrize("name", ["fd_hf_szv", "fd_hf_dzv", "fd_hf_dzv_fermi", "fd_lda_dzvp"])
+@pytest.mark.parametrize("name", ["fd_hf_szv", "fd_hf_dzv", "fd_hf_dzv_fermi", "fd_lda_dzvp",
+                                  "fd_hf_kpt_dzv_fermi", "fd_lda_kpt_dzv"])
 def test_oracle_gradient_matches_reference_fd(name):
     """The oracle's analytic gradient (electronic + Ewald, Ry per rs unit)
     against central differences of the reference's own make_pes energy
     (tests/golden/make_golden.py, FD_CASES), and the energies themselves.
     With Fermi smearing the gradient is that of E - sigma Se, not of the
-    reference's E: the golden records both differences."""
+    reference's E: the golden records both differences.  The ``kpt`` cases
+    difference pes_kpt (pes.py:88-98) at a fixed k-point."""
     from oracle.forces import electronic_gradient
     meta, z = load_golden(name)
     n, rs, L = int(z["n"]), float(z["rs"]), float(z["L"])
-    s = Solver(n, L, rs, meta["basis"], **meta["kwargs"])
-    out = s.solve(z["xp"])
+    kw = {k: v for k, v in meta["kwargs"].items() if k != "gamma"}
+    s = Solver(n, L, rs, meta["basis"], **kw)
+    out = s.solve(z["xp"], z["kpt"] if "kpt" in z else None)
     _, gpp = vpp(z["xp"], L, rs, grad=True)
     g = electronic_gradient(s) * 2 * rs + gpp
     c = z["coords"]
