@@ -142,7 +142,7 @@ def peaks():
 # persistent tensor-core kernel, the corner kernel, the in-place sum of the
 # partial tiles and the reduce, the launches the timing covers -- from one ncu
 # capture (its summary is kept under profiles/)
-QUAD_TRAFFIC = None  # set from the capture below
+QUAD_TRAFFIC = (2299031552 + 2275328) + (119074304 + 135936) + 542464 + 39990784 + 635136
 
 CONFIG = {"workload": "H54 bcc rs=1.31 gth-dzvp PBE 81^3 Gamma, SCF tol 1e-7 Ry + forces",
           "n_atoms": 54, "n_ao": 270, "grid": 531441}
@@ -180,8 +180,8 @@ def psi_density_roofline(hbm_gbs, src, reps=5):
     del phi, dphi
     torch.cuda.empty_cache()
     return {"bound": "hbm", "achieved": achieved, "peak": hbm_gbs, "unit": "GB/s",
-            "frac": achieved / hbm_gbs, "traffic": 2449540000 + 21869568,
-            "kernel": "k_tc_psi_density<32> (orbital-form density + gradient, H54 shapes)",
+            "frac": achieved / hbm_gbs, "traffic": 2449091000 + 19750144,
+            "kernel": "k_tc_psi_density_r<32> (orbital-form density + gradient, resident Y, H54 shapes)",
             "algorithmic_bytes": algo, "avg_ms": avg_s * 1e3, "launches": cnt,
             "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs, burst)" if src == "measured" else src,
             "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch "
@@ -545,12 +545,17 @@ def run_kpoint(args):
 def run_kpoint_h64(args):
     """Configuration family 5 at its size: H64 dzv (128 AOs), rs 1.25,
     uniform positions (seed 11), Hartree-Fock with Fermi smearing at 10000 K
-    on the odd 73^3 grid, 2x2x2 Monkhorst-Pack mesh; one step = the 8
-    single-k SCFs through make_solver(gamma=False), mixed precision by default
-    (grid contractions on the tensor cores through the real embedding of the
-    complex AO grid, FP32 pair transforms, FP64 eigensolver).  Energies only:
-    the k-point solver has no forces."""
-    from hqc_gb300 import make_solver
+    on the odd 73^3 grid, 2x2x2 Monkhorst-Pack mesh, through
+    make_pes(gamma=False, forces=True).value_and_grad(xp, kpts), mixed
+    precision by default (grid contractions on the tensor cores through the
+    real embedding of the complex AO grid, FP32 pair transforms, FP64
+    eigensolver; the force pass in FP64 with FP32 exchange-gradient
+    transforms).  A step is one evaluation (single-k SCF + gradient): the
+    warm-up runs `warmup` (at least 3) of them, the timed region `steps` of
+    them as one batch over the mesh's k-points in order (the default 3 steps
+    is widened to 8: the whole mesh)."""
+    import torch
+    from hqc_gb300 import make_pes, _lib
     from hqc_gb300.workloads import uniform, box
     precision = "mixed" if args.precision == "auto" else args.precision
     n, rs, ng = 64, 1.25, 73
@@ -560,19 +565,45 @@ def run_kpoint_h64(args):
     u = np.array([-0.25, 0.25]) * 2 * np.pi / (L * rs)
     kmesh = np.array([[a, b, c] for a in u for b in u for c in u])
     kw = dict(smearing=True, smearing_sigma=sigma, n_grid=ng, tol=1e-7)
-    s = make_solver(n, L, rs, "gth-dzv", gamma=False, precision=precision, **kw)
-    ms = _timed(lambda: s(xp, kmesh), args.steps, max(args.warmup, 1))
-    iters = float(np.mean(s.iterations))
-    stages = _stage_profile(lambda: s(xp, kmesh[0]))
-    return _line("k-point SCFs/s (H64 dzv HF Fermi 10000 K, 73^3, 2x2x2 MP mesh)", "SCFs/s",
-                 8.0 / (ms / 1000.0), ms, args,
+    pes = make_pes(n, L, rs, "gth-dzv", gamma=False, forces=True, precision=precision, **kw)
+    xd = torch.as_tensor(xp, device="cuda")
+    steps = args.steps if args.steps != 3 else 8
+    warm = max(args.warmup, 3)
+    t0 = time.perf_counter()
+    for w in range(warm):
+        pes.value_and_grad(xd, kmesh[w % 8])
+        print(f"kpoint_h64 warm-up {w}: {time.perf_counter() - t0:.1f}s, "
+              f"{pes.solver.iterations} iterations", file=sys.stderr, flush=True)
+    torch.cuda.synchronize()
+    ks = kmesh[np.arange(steps) % 8]
+    _lib.load().hqcgb_launch_count(1)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        torch.cuda.synchronize()
+        a.record()
+        F, g = pes.value_and_grad(xd, ks)
+        b.record()
+        torch.cuda.synchronize()
+    ms = a.elapsed_time(b) / steps
+    iters = list(pes.solver.iterations)
+    launches = int(_lib.load().hqcgb_launch_count(0))
+    # end to end: host positions in, host free energy and forces out, one evaluation
+    t0 = time.perf_counter()
+    F1, g1 = pes.value_and_grad(xp, kmesh[0])
+    _ = float(F1), g1.cpu().numpy()
+    e2e_s = time.perf_counter() - t0
+    return _line("k-point energy+force evals/s (H64 dzv HF Fermi 10000 K, 73^3, 2x2x2 MP mesh)", "evals/s",
+                 1000.0 / ms, ms, args,
                  {"workload": "kpoint_h64", "n_atoms": n, "n_ao": 2 * n, "grid": ng ** 3, "kpoints": 8,
-                  "scf_iterations_mean": iters, "precision_path": precision},
-                 {"dtype": "tf32x3+f32+f64" if precision == "mixed" else "c128",
-                  "gpu_ms_per_scf_by_stage": stages,
+                  "evaluations_timed": steps, "scf_iterations": iters, "precision_path": precision,
+                  "l2": "inputs > L2 (each SCF streams its complex AO grid and pair spectra), no flush"},
+                 {"dtype": "tf32x3+f32+f64" if precision == "mixed" else "c128", "steps": steps,
+                  "warmup": warm, "gpu_launches": launches, "clocks": clk.summary(),
+                  "e2e": {"value": 1.0 / e2e_s, "unit": "evals/s", "h2d_bytes_per_step": n * 3 * 8 + 3 * 8,
+                          "d2h_bytes_per_step": 8 + n * 3 * 8},
                   "cpu_baseline": None,
-                  "cpu_baseline_note": "not run: the oracle's exact exchange at this size takes minutes "
-                                       "per Fock build"})
+                  "cpu_baseline_note": "not run: one oracle Fock build with exact exchange at this size "
+                                       "takes minutes on the host cores"})
 
 
 def run_slater(args):

@@ -52,7 +52,8 @@ EXPORTS = ("hqcgb_plan_create", "hqcgb_plan_destroy", "hqcgb_scf", "hqcgb_scf_ba
            "hqcgb_ao_points_kpt", "hqcgb_slater_kpt", "hqcgb_overlap", "hqcgb_coulomb_energy",
            "hqcgb_tc_quadrature_gga", "hqcgb_diis_coefficients",
            "hqcgb_tc_quad_tiles", "hqcgb_batch_create", "hqcgb_batch_destroy", "hqcgb_batch_run",
-           "hqcgb_exchange_rebuild", "hqcgb_tune_set", "hqcgb_tune_get")
+           "hqcgb_exchange_rebuild", "hqcgb_tune_set", "hqcgb_tune_get", "hqcgb_forces_kpt",
+           "hqcgb_pes_kpt_batch")
 N_STAGES = 15
 
 _lib = None
@@ -130,6 +131,9 @@ def load():
                                   ctypes.POINTER(ScfOut), ctypes.c_void_p]
     lib.hqcgb_scf_kpt_batch.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, c_double_p,
                                         ctypes.POINTER(ScfOut), ctypes.c_void_p]
+    lib.hqcgb_forces_kpt.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    lib.hqcgb_pes_kpt_batch.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, c_double_p,
+                                        ctypes.POINTER(ScfOut), ctypes.c_void_p, ctypes.c_void_p]
     lib.hqcgb_kplan_query.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_void_p,
                                       ctypes.c_size_t, ctypes.c_void_p]
     lib.hqcgb_kplan_query.restype = ctypes.c_longlong

@@ -171,11 +171,15 @@ __global__ void k_ovl_contract(int n, int nb, int nprim, const double *__restric
   }
 }
 
-// k-point contraction: complex S, T (interleaved) from the phase-weighted sums.
+// k-point contraction: complex S, T (interleaved) from the phase-weighted
+// sums and, with gpart, Re[conj(D_pq) dT_pq - conj(W_pq) dS_pq] per (i, j, p, q)
+// (Re tr(D dT) for Hermitian D: sum_pq D_qp dT_pq = sum_pq conj(D_pq) dT_pq).
 __global__ void k_ovl_contract_kpt(int n, int nb, int nprim, const double *__restrict__ alpha,
                                    const double *__restrict__ coef, const int *__restrict__ ao_l,
                                    const int *__restrict__ ao_cart, const double *__restrict__ Q,
-                                   double2 *__restrict__ S, double2 *__restrict__ T) {
+                                   double2 *__restrict__ S, double2 *__restrict__ T,
+                                   const double2 *__restrict__ D, const double2 *__restrict__ W,
+                                   double *__restrict__ gpart) {
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= (long long)n * n * nb * nb) return;
   const int q = (int)(idx % nb), p = (int)((idx / nb) % nb);
@@ -186,7 +190,11 @@ __global__ void k_ovl_contract_kpt(int n, int nb, int nprim, const double *__res
   if (lp) mb[ao_cart[p]] += 1;
   if (lq) mb[ao_cart[q]] += 1;
   const int ks = midx_of(mb[0], mb[1], mb[2]);
+  const bool grad = gpart != nullptr;
+  int kc[3];
+  for (int c = 0; c < 3; ++c) kc[c] = midx_of(mb[0] + (c == 0), mb[1] + (c == 1), mb[2] + (c == 2));
   double sS = 0, sT = 0, sSi = 0, sTi = 0;
+  double gS[3] = {0, 0, 0}, gT[3] = {0, 0, 0}, gSi[3] = {0, 0, 0}, gTi[3] = {0, 0, 0};
   const double *Qij = Q + ((long long)i * n + j) * np2 * (4 * kNq);
   for (int a = 0; a < nprim; ++a) {
     double ca = coef[p * nprim + a];
@@ -202,11 +210,24 @@ __global__ void k_ovl_contract_kpt(int n, int nb, int nprim, const double *__res
       sT += cc * qv[kNq + ks];
       sSi += cc * qv[2 * kNq + ks];
       sTi += cc * qv[3 * kNq + ks];
+      if (grad)
+        for (int c = 0; c < 3; ++c) {
+          gS[c] += cc * qv[kc[c]];
+          gT[c] += cc * qv[kNq + kc[c]];
+          gSi[c] += cc * qv[2 * kNq + kc[c]];
+          gTi[c] += cc * qv[3 * kNq + kc[c]];
+        }
     }
   }
   const long long pq = (long long)(i * nb + p) * nao + (j * nb + q);
-  S[pq] = make_double2(sS, sSi);
-  T[pq] = make_double2(-0.5 * sT, -0.5 * sTi);
+  if (S) S[pq] = make_double2(sS, sSi);
+  if (T) T[pq] = make_double2(-0.5 * sT, -0.5 * sTi);
+  if (grad) {
+    const double2 dd = D[pq], ww = W[pq];
+    for (int c = 0; c < 3; ++c)
+      gpart[idx * 3 + c] = (i == j) ? 0.0
+                                    : -0.5 * (dd.x * gT[c] + dd.y * gTi[c]) - (ww.x * gS[c] + ww.y * gSi[c]);
+  }
 }
 
 size_t ovl_scratch_doubles(int n, int nprim) {
@@ -264,16 +285,25 @@ void launch_overlap_kinetic(const double *xp, int n, int nb, int nprim, const do
 void launch_overlap_kinetic_kpt(const double *xp, int n, int nb, int nprim, const double *alpha,
                                 const double *coef, const int *ao_l, const int *ao_cart,
                                 const double *lattice, int nlat, const double *kpt, double2 *S,
-                                double2 *T, double *Q, cudaStream_t st) {
+                                double2 *T, double *Q, cudaStream_t st, const double2 *D,
+                                const double2 *W, double *gpart, double *grad) {
   HQ_STAGE(ST_OVERLAP, st);
   const long long terms = (long long)n * n * nprim * nprim;
-  k_ovl_lattice<10, true><<<ceil_div(terms, 128), 128, 0, st>>>(xp, n, nprim, alpha, lattice, nlat,
-                                                                kpt, Q);
+  if (gpart)
+    k_ovl_lattice<20, true><<<ceil_div(terms, 128), 128, 0, st>>>(xp, n, nprim, alpha, lattice, nlat,
+                                                                  kpt, Q);
+  else
+    k_ovl_lattice<10, true><<<ceil_div(terms, 128), 128, 0, st>>>(xp, n, nprim, alpha, lattice, nlat,
+                                                                  kpt, Q);
   HQ_LAUNCH_CHECK();
   const long long total = (long long)n * n * nb * nb;
   k_ovl_contract_kpt<<<ceil_div(total, 128), 128, 0, st>>>(n, nb, nprim, alpha, coef, ao_l, ao_cart,
-                                                          Q, S, T);
+                                                          Q, S, T, D, W, gpart);
   HQ_LAUNCH_CHECK();
+  if (gpart) {
+    k_reduce_pair_grad<<<n, 256, 0, st>>>(gpart, n, nb, grad);
+    HQ_LAUNCH_CHECK();
+  }
 }
 
 // ---------------------------------------------------------------------------

@@ -97,10 +97,30 @@ void zgemm_batched_rowmajor(int M, int N, int K, const double2 *A, int lda, long
                             const double2 *B, int ldb, long long sb, double2 *C, int ldc,
                             long long sc, int batch, cudaStream_t st);
 size_t ovl_scratch_doubles_kpt(int n, int nprim);
+// With gpart (n*n*nb*nb*3 doubles) also grad[A][c] += Re tr(D dT/dR_A) - Re tr(W dS/dR_A)
+// for Hermitian D, W (S and T may then be NULL).
 void launch_overlap_kinetic_kpt(const double *xp, int n, int nb, int nprim, const double *alpha,
                                 const double *coef, const int *ao_l, const int *ao_cart,
                                 const double *lattice, int nlat, const double *kpt, double2 *S,
-                                double2 *T, double *Q, cudaStream_t st);
+                                double2 *T, double *Q, cudaStream_t st, const double2 *D = nullptr,
+                                const double2 *W = nullptr, double *gpart = nullptr,
+                                double *grad = nullptr);
+// forces_kpt.cu
+void launch_rho_from_x_kpt(const double2 *phi, const double2 *dphi, const double2 *X, int nao, long long N,
+                           double *rho, double *grho, cudaStream_t st);
+void launch_gga_zop_kpt(const double2 *dphi, const double *u, int nao, long long N, double2 *out,
+                        cudaStream_t st);
+void launch_force_grid_kpt(const double2 *F1d, const double *coef, const int *ao_l, const int *ao_cart,
+                           int nao_atom, int nprim, int nao, int ng, const double *veff, const double2 *X,
+                           const double *u, const double2 *DPsi, const double2 *Zm, double dV, double *part,
+                           cudaStream_t st);
+template <class C>  // C = double2 or float2
+void launch_kx_grad_fields(const double2 *F1d, const double *coef, const int *ao_l, const int *ao_cart,
+                           int nao_atom, int nprim, int nao, int ng, const double2 *X, const double2 *psi,
+                           C *out, cudaStream_t st);
+template <class C>
+void launch_kx_grad_contract(const C *Fh, const double *coul, int nao, long long N, double scale, double *part,
+                             cudaStream_t st);
 // eigh_herm.cu
 void eigh_herm(int n, int batch, double2 *A, double2 *V, double *w, double2 *work, int *status,
                cudaStream_t st);

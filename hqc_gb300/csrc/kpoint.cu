@@ -463,6 +463,12 @@ struct hqcgb_kplan {
   double *rho = nullptr, *grho = nullptr, *vh = nullptr, *wq = nullptr, *vxc = nullptr, *u = nullptr,
          *vloc = nullptr, *xpart = nullptr, *scal = nullptr, *hscal = nullptr;
   int *jstat = nullptr, *ibad = nullptr;
+  // nuclear gradient (want_forces): X = D phibar, a second AO-grid buffer
+  // (GGA operand or Madelung term), FP64 orbitals and the four
+  // exchange-gradient fields of the mixed / Hartree-Fock plans, partial sums
+  double2 *fX = nullptr, *fY = nullptr, *fPsi = nullptr, *fbuf = nullptr;
+  float2 *fbuf32 = nullptr;  // mixed plan: the exchange-gradient fields in FP32
+  double *fveff = nullptr, *fpart = nullptr, *vpart = nullptr, *gpart = nullptr;
   std::vector<double> h_occ;
   int nuse = 0;
   bool have_state = false;
@@ -517,7 +523,6 @@ static void kcreate(const hqcgb_params &P, hqcgb_kplan *p) {
   HQ_REQUIRE(P.precision == HQCGB_PREC_FP64 || P.precision == HQCGB_PREC_MIXED, "unknown precision");
   HQ_REQUIRE(P.precision == HQCGB_PREC_FP64 || !(P.dft && P.xc == HQCGB_XC_PBE),
              "the mixed k-point solver covers Hartree-Fock and LDA (PBE runs in FP64)");
-  HQ_REQUIRE(!P.want_forces, "the k-point solver has no forces");
   for (int k = 0; k < P.nao_atom; ++k) {
     HQ_REQUIRE(P.ao_l[k] == 0 || P.ao_l[k] == 1, "only s and p AOs are supported");
     HQ_REQUIRE(P.ao_cart[k] >= 0 && P.ao_cart[k] < 3, "bad cartesian index");
@@ -580,6 +585,7 @@ static void kcreate(const hqcgb_params &P, hqcgb_kplan *p) {
     p->Psi = p->alloc<double2>((size_t)nao * N);
   }
   if (p->gga) p->dPsi = p->alloc<double2>((size_t)3 * nao * N);
+  HQ_REQUIRE(!(P.want_forces && p->gga) || !p->mixed, "PBE k-points run in FP64");
   p->cbuf = p->alloc<double2>(N);
   for (double2 **m : {&p->S, &p->T, &p->V, &p->H, &p->St, &p->vorth, &p->F, &p->F2e, &p->K, &p->Fp,
                       &p->C, &p->c1, &p->D, &p->t1, &p->t2, &p->err, &p->jA, &p->jwork})
@@ -603,6 +609,19 @@ static void kcreate(const hqcgb_params &P, hqcgb_kplan *p) {
     p->u = p->alloc<double>(3 * N);
   }
   p->xpart = p->alloc<double>((size_t)2 * xc_blocks(N));
+  if (P.want_forces) {
+    p->fX = p->alloc<double2>((size_t)nao * N);
+    p->fY = p->alloc<double2>((size_t)nao * N);
+    if (p->hf) {
+      p->fPsi = p->alloc<double2>((size_t)nao * N);
+      if (p->mixed) p->fbuf32 = p->alloc<float2>((size_t)4 * nao * N);
+      else p->fbuf = p->alloc<double2>((size_t)4 * nao * N);
+    }
+    p->fveff = p->alloc<double>(N);
+    p->fpart = p->alloc<double>((size_t)nao * force_grid_blocks(N) * 3);
+    p->vpart = p->alloc<double>((size_t)3 * n * vloc_force_blocks(N));
+    p->gpart = p->alloc<double>((size_t)n * n * P.nao_atom * P.nao_atom * 3);
+  }
   p->jstat = p->alloc<int>(1);
   p->ibad = p->alloc<int>(1);
   p->scal = p->alloc<double>(K_NSLOT);
@@ -999,6 +1018,7 @@ static int kscf_one(hqcgb_kplan *p, const double *xp_dev, const double *kpt_host
   kdensity_matrix(c);
   double E0 = 0.0, E1 = 1.0;
   int loop = 0;
+  bool stopped = false;  // the stopping test was met before max_cycle
   if (P.diis) {
     const int sp = P.diis_space;
     kfock(c);
@@ -1027,10 +1047,24 @@ static int kscf_one(hqcgb_kplan *p, const double *xp_dev, const double *kpt_host
     // build, as on the Gamma-point path
     const double etol = p->mixed ? std::max(P.tol, 2e-6) : P.tol;
     const double errtol = p->mixed ? std::max(10.0 * P.tol, 2e-5) : 10.0 * P.tol;
-    while ((std::fabs(E1 - E0) > etol || enorm > errtol) && loop < P.max_cycle) {
+    auto diis_step = [&] {
       kdiis_extrapolate(c, head, p->t2);  // t2 is free until the exchange step
       step(p->t2);
       if (!std::isfinite(E1)) throw Error{HQCGB_NAN, "non-finite energy in the SCF"};
+    };
+    while ((std::fabs(E1 - E0) > etol || enorm > errtol) && loop < P.max_cycle) diis_step();
+    stopped = loop < P.max_cycle;
+    // Mixed Hartree-Fock or smeared run stopped at the floor with the
+    // commutator still above the requested 10 tol: a few more iterations
+    // while it keeps falling by at least a fifth (the gradient's error is
+    // first order in it; at the FP32 noise floor it stops falling), as on
+    // the Gamma-point path.
+    if (p->mixed && (P.smearing || p->hf) && stopped && enorm > 10.0 * P.tol) {
+      for (int extra = 0; extra < 6 && loop < P.max_cycle && enorm > 10.0 * P.tol; ++extra) {
+        const double prev = enorm;
+        diis_step();
+        if (enorm > 0.8 * prev) break;
+      }
     }
   } else {
     // fixed_point_scf (scf.py:21-88)
@@ -1044,6 +1078,7 @@ static int kscf_one(hqcgb_kplan *p, const double *xp_dev, const double *kpt_host
       ++loop;
       if (!std::isfinite(E1)) throw Error{HQCGB_NAN, "non-finite energy in the SCF"};
     }
+    stopped = loop != P.max_cycle;
   }
   kcheck_eig(c);
   if (p->mixed) {
@@ -1055,7 +1090,7 @@ static int kscf_one(hqcgb_kplan *p, const double *xp_dev, const double *kpt_host
       throw Error{HQCGB_CUDA_ERROR, "tensor-core pipeline wait limit hit (code " + std::to_string(te) + ")"};
     }
   }
-  const int converged = (loop != P.max_cycle) ? 1 : 0;
+  const int converged = stopped ? 1 : 0;
   // post-processing (solver.py:824-837 / 950-962)
   kdensity_matrix(c);
   kfock(c);
@@ -1084,6 +1119,95 @@ static int kscf_one(hqcgb_kplan *p, const double *xp_dev, const double *kpt_host
   }
   p->have_state = true;
   return converged ? HQCGB_OK : HQCGB_NOT_CONVERGED;
+}
+
+// out[k] = a[k] b[k]
+__global__ void k_vmul(int n, const double *__restrict__ a, const double *__restrict__ b,
+                       double *__restrict__ out) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) out[k] = a[k] * b[k];
+}
+
+// Nuclear gradient dE/dR (Hartree/Bohr) of the last k-point SCF, FP64 on
+// both precisions (the mixed plan's converged D, the FP64 Bloch AO grid;
+// the mixed plan transforms the exchange-gradient fields in FP32):
+//   Re tr(D dT) - Re tr(W dS)                    W = C diag(f eps) C^H
+//   + structure-factor term of v_loc (rho real, as at the Gamma point)
+//   + grid terms of forces_kpt.cu (V_eff, GGA, Madelung, exact exchange).
+// Gradient of E - sigma S under smearing (hqcgb_scf_out.free_energy).
+static void kforces(hqcgb_kplan *p, double *grad, cudaStream_t st) {
+  KCtx c{p, st};
+  const hqcgb_params &P = p->P;
+  HQ_REQUIRE(P.want_forces, "k-point plan was created without want_forces");
+  if (!p->have_state) throw Error{HQCGB_NO_STATE, "hqcgb_forces_kpt called before a successful SCF"};
+  const int n = p->nao, na = p->n;
+  const long long N = p->N;
+  HQ_CUDA(cudaMemsetAsync(grad, 0, sizeof(double) * 3 * na, st));
+  // energy-weighted density matrix -> t2, then the S/T lattice-sum terms
+  k_vmul<<<ceil_div(n, 256), 256, 0, st>>>(n, p->occ, p->w, p->ws);
+  HQ_LAUNCH_CHECK();
+  k_zscale_cols<<<ceil_div((long long)n * n, 256), 256, 0, st>>>(n, p->C, p->ws, p->t1);
+  HQ_LAUNCH_CHECK();
+  zgemm('N', 'C', n, n, n, kOne, p->t1, n, p->C, n, kZero, p->t2, n, st);
+  launch_overlap_kinetic_kpt(p->xp, na, p->nb, p->nprim, p->alpha, p->coef, p->ao_l, p->ao_cart, p->lattice,
+                             P.n_lattice, p->kpt, nullptr, nullptr, p->ovq, st, p->D, p->t2, p->gpart, grad);
+  // X = D phibar, rho (and grad rho) from it in FP64
+  zgemm('N', 'N', n, (int)N, n, kOne, p->D, n, p->phi, (int)N, kZero, p->fX, (int)N, st);
+  launch_rho_from_x_kpt(p->phi, p->gga ? p->dphi : nullptr, p->fX, n, N, p->rho, p->gga ? p->grho : nullptr,
+                        st);
+  // structure-factor derivative of the local potential
+  launch_real_to_complex(p->rho, nullptr, N, 1, p->cbuf, st);
+  launch_fft3d(p->cbuf, p->ng, 1, p->tw, false, st);
+  launch_vloc_force(p->ph, p->cbuf, na, p->ng, p->L, p->vpart, st);
+  launch_sum_partials(p->vpart, vloc_force_blocks(N), 3 * na, 3 * na, 1.0, grad, true, st);
+  // V_eff = v_loc + v_H (+ v_xc)
+  kpoisson_real(c, p->rho, p->vh);
+  if (P.dft)
+    launch_xc_pointwise(P.xc, p->rho, p->gga ? p->grho : nullptr, p->vh, N, p->dV, p->wq, p->vxc,
+                        p->gga ? p->u : nullptr, p->xpart, st);
+  launch_add3(N, p->vloc, p->vh, P.dft ? p->vxc : nullptr, p->fveff, st);
+  const double2 *dpsi = nullptr, *zm = nullptr;
+  if (p->gga) {  // (D conj(u . grad phi))_p = (D (u . grad phibar))_p
+    launch_gga_zop_kpt(p->dphi, p->u, n, N, p->fY, st);
+    zgemm('N', 'N', n, (int)N, n, kOne, p->D, n, p->fY, (int)N, kZero, p->Z, (int)N, st);
+    dpsi = p->Z;
+  }
+  if (p->hf) {  // Madelung term: Zm = c_M (D S~ D) phibar
+    const double cM = 4.0 * M_PI / p->L * kMadelungK;
+    zgemm('N', 'N', n, n, n, kOne, p->D, n, p->St, n, kZero, p->t1, n, st);
+    zgemm('N', 'N', n, n, n, kOne, p->t1, n, p->D, n, kZero, p->t2, n, st);
+    zgemm('N', 'N', n, (int)N, n, make_double2(cM, 0.0), p->t2, n, p->phi, (int)N, kZero, p->fY, (int)N, st);
+    zm = p->fY;
+  }
+  launch_force_grid_kpt(p->F1d, p->coef, p->ao_l, p->ao_cart, p->nb, p->nprim, n, p->ng, p->fveff, p->fX,
+                        p->gga ? p->u : nullptr, dpsi, zm, p->dV, p->fpart, st);
+  if (p->hf) {
+    // exact exchange: the occupied orbitals in FP64, then per orbital the four
+    // fields, one batched forward transform and the G-space contraction
+    const double thr = std::max(P.exx_occ_threshold, kExxOccFloor);
+    int nd = 0;
+    for (int k = 0; k < n; ++k)
+      if (p->h_occ[k] > thr) nd = k + 1;
+    if (nd > 0)
+      zgemm('C', 'N', nd, (int)N, n, kOne, p->C, n, p->phi, (int)N, kZero, p->fPsi, (int)N, st);
+    for (int i = 0; i < nd; ++i) {
+      const double f = p->h_occ[i];
+      if (!(f > thr)) continue;
+      if (p->mixed) {  // FP32 transforms, FP64 sums
+        launch_kx_grad_fields(p->F1d, p->coef, p->ao_l, p->ao_cart, p->nb, p->nprim, n, p->ng, p->fX,
+                              p->fPsi + (long long)i * N, p->fbuf32, st);
+        launch_fft3d_f32(p->fbuf32, p->ng, 4 * n, p->tw, false, st);
+        launch_kx_grad_contract(p->fbuf32, p->coul, n, N, f * p->dV, p->fpart, st);
+      } else {
+        launch_kx_grad_fields(p->F1d, p->coef, p->ao_l, p->ao_cart, p->nb, p->nprim, n, p->ng, p->fX,
+                              p->fPsi + (long long)i * N, p->fbuf, st);
+        launch_fft3d(p->fbuf, p->ng, 4 * n, p->tw, false, st);
+        launch_kx_grad_contract(p->fbuf, p->coul, n, N, f * p->dV, p->fpart, st);
+      }
+    }
+  }
+  launch_force_grid_reduce(p->fpart, n, p->nb, force_grid_blocks(N), grad, st);
+  HQ_CUDA(cudaStreamSynchronize(st));
 }
 
 static int kfail(const Error &e) {
@@ -1145,6 +1269,48 @@ int hqcgb_scf_kpt_batch(hqcgb_kplan *plan, int n_cfg, const double *xp, const do
       int s;
       try {
         s = kscf_one(plan, xp + (size_t)b * 3 * plan->n, kpts + (size_t)b * 3, &o, (cudaStream_t)stream);
+      } catch (const Error &e) {
+        throw Error{e.status, "configuration " + std::to_string(b) + ": " + e.msg};
+      }
+      worst = std::max(worst, s);
+    }
+    return worst;
+  } catch (const Error &e) {
+    return kfail(e);
+  }
+}
+
+int hqcgb_forces_kpt(hqcgb_kplan *plan, double *grad, void *stream) {
+  try {
+    HQ_REQUIRE(plan && grad, "null argument");
+    kforces(plan, grad, (cudaStream_t)stream);
+    return HQCGB_OK;
+  } catch (const Error &e) {
+    return kfail(e);
+  }
+}
+
+int hqcgb_pes_kpt_batch(hqcgb_kplan *plan, int n_cfg, const double *xp, const double *kpts,
+                        const hqcgb_scf_out *out, double *grad, void *stream) {
+  try {
+    HQ_REQUIRE(plan && xp && kpts && out && n_cfg >= 0, "null argument");
+    HQ_REQUIRE(!grad || plan->P.want_forces, "k-point plan was created without want_forces");
+    const int nao = plan->nao;
+    int worst = HQCGB_OK;
+    for (int b = 0; b < n_cfg; ++b) {
+      hqcgb_scf_out o = *out;
+      const size_t zz = 2 * (size_t)nao * nao;
+      if (o.mo_coeff) o.mo_coeff += b * zz;
+      if (o.dm) o.dm += b * zz;
+      if (o.bands) o.bands += (size_t)b * nao;
+      if (o.energies) o.energies += (size_t)b * 5;
+      if (o.converged) o.converged += b;
+      if (o.iterations) o.iterations += b;
+      if (o.free_energy) o.free_energy += b;
+      int s;
+      try {
+        s = kscf_one(plan, xp + (size_t)b * 3 * plan->n, kpts + (size_t)b * 3, &o, (cudaStream_t)stream);
+        if (grad) kforces(plan, grad + (size_t)b * 3 * plan->n, (cudaStream_t)stream);
       } catch (const Error &e) {
         throw Error{e.status, "configuration " + std::to_string(b) + ": " + e.msg};
       }

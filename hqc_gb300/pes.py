@@ -12,7 +12,8 @@ sum exp(-x^2) / (2 sqrt(pi))), while ``pes(xp)`` keeps the reference's
 internal energy E (hqc/pbc/pes.py:86), whose gradient would need the
 occupations' response.
 ``gamma=False`` gives ``pes(xp, kpt)`` (pes_kpt / pes_dev_kpt,
-pes.py:88-137), without forces.
+pes.py:88-137) and, with ``forces=True``, ``pes.value_and_grad(xp, kpt)``:
+the single-k free energy plus Vpp and its gradient at the fixed k-point.
 """
 import numpy as np
 import torch
@@ -58,10 +59,24 @@ def make_pes(n, L, rs, basis, rcut=24, tol=1e-7, max_cycle=100, grid_length=0.12
             return E + Vpp, Ki, Vep, Vee, Vpp, Se, conv
         return E + Vpp
 
-    def value_and_grad(xp):
+    def value_and_grad(xp, *kpt):
         """(F + Vpp, d(F + Vpp)/dxp), F = E - sigma S (E without smearing); a
-        batch (B, n, 3) gives (B,) and (B, n, 3)."""
+        batch (B, n, 3) gives (B,) and (B, n, 3).  With gamma=False the
+        k-point comes second: a batch of xp and/or kpt (B, 3) broadcasts."""
+        if gamma == bool(kpt):
+            raise TypeError("value_and_grad(xp) at the Gamma point, value_and_grad(xp, kpt) with gamma=False")
         xp = _arr(xp)
+        if kpt:
+            out = solver.batch(xp, kpt[0], forces=True)
+            B = out["grad"].shape[0]
+            xb = xp if xp.ndim == 3 else (xp.unsqueeze(0) if isinstance(xp, torch.Tensor) else xp[None])
+            Vpp, gpp = _vpp(xb)
+            if xb.shape[0] != B:
+                Vpp, gpp = Vpp.expand(B), gpp.expand(B, n, 3)
+            F, g = out["free_energy"] * RY + Vpp, out["grad"] + gpp
+            batched = xp.ndim == 3 or np.asarray(kpt[0].cpu() if isinstance(kpt[0], torch.Tensor)
+                                                 else kpt[0]).ndim == 2
+            return (F, g) if batched else (F[0], g[0])
         if xp.ndim == 3:
             out = solver.batch(xp, forces=True, full=False)
             Vpp, gpp = _vpp(xp)

@@ -157,9 +157,11 @@ class Plan:
         _lib.check(st, allow=(0, 1))
         return out
 
-    def scf_kpt(self, xps_bohr, kpts):
+    def scf_kpt(self, xps_bohr, kpts, forces=False):
         """k-point SCFs: xps_bohr (B, n, 3) on the device, kpts (B, 3) in
-        1/Bohr (host array); mo_coeff and dm come back complex128."""
+        1/Bohr (host array); mo_coeff and dm come back complex128.  With
+        ``forces`` also "grad" (B, n, 3), dE/dR in Hartree/Bohr of each
+        single-k free energy (hqcgb_pes_kpt_batch)."""
         lib = _lib.load()
         nao, dev = self.nao, self.device
         B = xps_bohr.shape[0]
@@ -175,10 +177,23 @@ class Plan:
                            "free_energy")])
         xps_bohr = xps_bohr.contiguous()
         k = np.ascontiguousarray(kpts, dtype=np.float64).reshape(B, 3)
-        st = lib.hqcgb_scf_kpt_batch(self.handle, B, ctypes.c_void_p(xps_bohr.data_ptr()),
-                                     k.ctypes.data_as(_lib.c_double_p), ctypes.byref(o), self.stream())
+        if forces:
+            out["grad"] = torch.empty(B, self.n, 3, dtype=torch.float64, device=dev)
+            st = lib.hqcgb_pes_kpt_batch(self.handle, B, ctypes.c_void_p(xps_bohr.data_ptr()),
+                                         k.ctypes.data_as(_lib.c_double_p), ctypes.byref(o),
+                                         ctypes.c_void_p(out["grad"].data_ptr()), self.stream())
+        else:
+            st = lib.hqcgb_scf_kpt_batch(self.handle, B, ctypes.c_void_p(xps_bohr.data_ptr()),
+                                         k.ctypes.data_as(_lib.c_double_p), ctypes.byref(o), self.stream())
         _lib.check(st, allow=(0, 1))
         return out
+
+    def forces_kpt(self):
+        """dE/dR (Hartree/Bohr, (n, 3) on the device) of the last k-point SCF."""
+        lib = _lib.load()
+        g = torch.empty(self.n, 3, dtype=torch.float64, device=self.device)
+        _lib.check(lib.hqcgb_forces_kpt(self.handle, ctypes.c_void_p(g.data_ptr()), self.stream()))
+        return g
 
     def set_concurrency(self, workers):
         """Configurations a batch call runs at once (each extra one clones the
@@ -273,11 +288,14 @@ def make_solver(n: int, L: float, rs: float, basis: str,
 
     ``gamma=False`` returns ``solver(xp, kpt)`` for one k-point (kpt (3,) in
     1/Bohr, first Brillouin zone (-pi/(L rs), pi/(L rs)); solver.py:769-962):
-    the same tuple with complex128 mo_coeff and dm.  It has no forces;
+    the same tuple with complex128 mo_coeff and dm.
     ``precision='mixed'`` (Hartree-Fock and LDA) runs its grid contractions on
     the tensor cores (complex operands as real/imaginary rows, FP32 pair
     transforms) with the FP64 eigensolver; a batch of xp (B, n, 3) and/or kpt
-    (B, 3) broadcasts like ``jax.vmap``.
+    (B, 3) broadcasts like ``jax.vmap``.  With ``forces=True``,
+    ``solver.grad()`` is the gradient (Rydberg per rs unit) of the last
+    single-k call's free energy ``solver.free_energy`` and
+    ``solver.batch(xp, kpt, forces=True)`` returns them per configuration.
     """
     L_bohr = float(L) * float(rs)
     if not gamma:
@@ -285,12 +303,10 @@ def make_solver(n: int, L: float, rs: float, basis: str,
             raise ValueError(f"unknown precision {precision!r}")
         if precision == "mixed" and dft and _lib.XC.get(xc.lower().replace(" ", "")) == 10:
             raise NotImplementedError("the mixed k-point solver covers Hartree-Fock and LDA")
-        if forces:
-            raise NotImplementedError("the k-point solver has no forces")
         return _make_kpoint_solver(n, L_bohr, rs, basis, rcut, tol, max_cycle, grid_length, diis,
                                    diis_space, diis_start_cycle, diis_damp, dft, xc, smearing,
                                    smearing_method, smearing_sigma, search_method, search_cycle,
-                                   search_tol, n_grid, exx_occ_threshold, precision)
+                                   search_tol, n_grid, exx_occ_threshold, precision, forces)
     plan = Plan(n, L_bohr, basis, rcut, tol, max_cycle, grid_length, diis, diis_space,
                 diis_start_cycle, diis_damp, dft, xc, smearing, smearing_method, smearing_sigma,
                 search_method, search_cycle, search_tol, precision=precision, forces=forces,
@@ -339,21 +355,37 @@ def make_solver(n: int, L: float, rs: float, basis: str,
 def _make_kpoint_solver(n, L_bohr, rs, basis, rcut, tol, max_cycle, grid_length, diis, diis_space,
                         diis_start_cycle, diis_damp, dft, xc, smearing, smearing_method,
                         smearing_sigma, search_method, search_cycle, search_tol, n_grid,
-                        exx_occ_threshold, precision="fp64"):
+                        exx_occ_threshold, precision="fp64", forces=False):
     plan = Plan(n, L_bohr, basis, rcut, tol, max_cycle, grid_length, diis, diis_space,
                 diis_start_cycle, diis_damp, dft, xc, smearing, smearing_method, smearing_sigma,
-                search_method, search_cycle, search_tol, precision=precision, forces=False,
+                search_method, search_cycle, search_tol, precision=precision, forces=forces,
                 n_grid=n_grid, exx_occ_threshold=exx_occ_threshold, kpoint=True)
 
-    def solver(xp, kpt):
+    def _broadcast(xp, kpt):
         xp_t = _as_device(xp, plan.device)
         k = np.asarray(kpt.detach().cpu() if isinstance(kpt, torch.Tensor) else kpt, dtype=np.float64)
         batched = xp_t.dim() == 3 or k.ndim == 2
         B = max(xp_t.shape[0] if xp_t.dim() == 3 else 1, k.shape[0] if k.ndim == 2 else 1)
         xps = xp_t.expand(B, n, 3) if xp_t.dim() == 3 else xp_t.reshape(1, n, 3).expand(B, n, 3)
         ks = np.broadcast_to(k.reshape(-1, 3), (B, 3))
-        out = plan.scf_kpt(xps.contiguous() * rs, ks)
+        return xps.contiguous(), ks, batched
+
+    def batch(xp, kpt, forces=False):
+        """Every (xp, kpt) pair of the broadcast batch; with ``forces`` also
+        "grad" (B, n, 3) in Rydberg per rs unit."""
+        xps, ks, _ = _broadcast(xp, kpt)
+        out = plan.scf_kpt(xps * rs, ks, forces=forces)
         solver.iterations = out["iterations"].tolist()
+        solver.free_energy = out["free_energy"] * RY
+        if forces:
+            out["grad"] = out["grad"] * (RY * rs)
+        return out
+
+    def solver(xp, kpt):
+        xps, ks, batched = _broadcast(xp, kpt)
+        out = plan.scf_kpt(xps * rs, ks)
+        solver.iterations = out["iterations"].tolist()
+        solver.free_energy = out["free_energy"] * RY if batched else out["free_energy"][0] * RY
         e = out["energies"]
         res = (out["mo_coeff"], out["dm"], out["bands"] * RY, e[:, 0] * RY, e[:, 1] * RY,
                e[:, 2] * RY, e[:, 3] * RY, e[:, 4], out["converged"] != 0)
@@ -362,6 +394,13 @@ def _make_kpoint_solver(n, L_bohr, rs, basis, rcut, tol, max_cycle, grid_length,
             solver.iterations = solver.iterations[0]
         return res
 
+    def grad(xp=None):
+        """Gradient (Rydberg per rs unit) of the last single-k call's free
+        energy ``solver.free_energy``; needs forces=True."""
+        return plan.forces_kpt() * (RY * rs)
+
     solver.plan = plan
+    solver.grad = grad
+    solver.batch = batch
     solver.n_grid = plan.ng
     return solver

@@ -313,11 +313,11 @@ int hqcgb_eigh_noalloc(int n, const double *A, double *w, double *V, void *strea
 typedef struct hqcgb_kplan hqcgb_kplan;
 
 /* Factory of the k-point solver: the same parameters as hqcgb_plan_create
- * (want_forces 0; precision HQCGB_PREC_FP64, or HQCGB_PREC_MIXED for
- * Hartree-Fock and LDA: grid contractions on the tensor cores through the
- * real embedding of the complex AO grid, FP64 eigensolver).  Replaces the
- * table-building part of make_solver(gamma=False) (hqc/pbc/solver.py:209-231,
- * 378-389). */
+ * (precision HQCGB_PREC_FP64, or HQCGB_PREC_MIXED for Hartree-Fock and LDA:
+ * grid contractions on the tensor cores through the real embedding of the
+ * complex AO grid, FP64 eigensolver; want_forces keeps what
+ * hqcgb_forces_kpt needs).  Replaces the table-building part of
+ * make_solver(gamma=False) (hqc/pbc/solver.py:209-231, 378-389). */
 int hqcgb_kplan_create(const hqcgb_params *params, hqcgb_kplan **plan);
 int hqcgb_kplan_destroy(hqcgb_kplan *plan);
 
@@ -333,6 +333,21 @@ int hqcgb_scf_kpt(hqcgb_kplan *plan, const double *xp, const double *kpt,
  * reference's jax.vmap(solver) over (xp, kpt)).  Returns the worst status. */
 int hqcgb_scf_kpt_batch(hqcgb_kplan *plan, int n_cfg, const double *xp, const double *kpts,
                         const hqcgb_scf_out *out, void *stream);
+
+/* Nuclear gradient dE/dR [n_atoms][3] (Hartree/Bohr, device) of the last
+ * k-point SCF at its fixed k-point: the gradient of E - sigma*Se of that
+ * single-k energy (hf_kpt / dft_kpt, hqc/pbc/solver.py:769-962; pes_kpt,
+ * hqc/pbc/pes.py:88-98, minus the proton Ewald term).  FP64 on both
+ * precisions.  No counterpart in the reference (forces are absent there,
+ * doc/solver_algorithm.md:1210). */
+int hqcgb_forces_kpt(hqcgb_kplan *plan, double *grad, void *stream);
+
+/* hqcgb_scf_kpt_batch plus, when grad is not NULL, each configuration's
+ * gradient into grad [n_cfg][n_atoms][3] (Hartree/Bohr, device): the
+ * energy-and-force evaluation of a k-mesh (the reference's jax.vmap of
+ * pes_kpt over (xp, kpt), pes.py:88-98). */
+int hqcgb_pes_kpt_batch(hqcgb_kplan *plan, int n_cfg, const double *xp, const double *kpts,
+                        const hqcgb_scf_out *out, double *grad, void *stream);
 
 /* Copy an internal buffer of the last k-point SCF into dst (device): "S",
  * "T", "V", "H", "D", "F", "K", "St" (complex nao x nao), "phi" (conjugated

@@ -93,18 +93,16 @@ def test_ewald_host_helpers_match_oracle():
 
 
 def test_kpoint_factories_reject_unsupported_modes():
-    """make_solver(gamma=False) has no forces and no mixed PBE path; the
-    factories refuse those modes (and unknown precisions) before any device
-    work."""
+    """make_solver(gamma=False) has no mixed PBE path (with or without
+    forces); the factories refuse it (and unknown precisions) before any
+    device work."""
     from hqc_gb300 import make_solver, make_pes
     with pytest.raises(NotImplementedError):
         make_solver(4, 2.5, 1.5, "gth-szv", gamma=False, precision="mixed", dft=True, xc="pbe")
     with pytest.raises(ValueError):
         make_solver(4, 2.5, 1.5, "gth-szv", gamma=False, precision="half")
     with pytest.raises(NotImplementedError):
-        make_solver(4, 2.5, 1.5, "gth-szv", gamma=False, forces=True)
-    with pytest.raises(NotImplementedError):
-        make_pes(4, 2.5, 1.5, "gth-szv", gamma=False, forces=True)
+        make_pes(4, 2.5, 1.5, "gth-szv", gamma=False, forces=True, precision="mixed", dft=True, xc="pbe")
 
 
 def test_overlap_lattice_sphere_matches_reference_rule():
