@@ -488,7 +488,7 @@ def _line(metric, unit, value, ms, args, config, extra):
          "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
          "vs_baseline": None, "data": "synthetic", "config": config}
     d.update(extra)
-    if "cpu_baseline" in d:
+    if d.get("cpu_baseline"):
         d["cpu_baseline"]["cores"] = cores
     return d
 
