@@ -86,7 +86,7 @@ def test_kmesh_batch_matches_single_calls(precision):
     This small box (H8 in 3.3 Bohr, 25^3, Fermi sigma 0.03 Ha) is a stress
     case for the mixed k-point forces: measured 9.3e-5 Ha/Bohr on a GB300,
     above the 1e-5 target, which the reference's finite-difference cases
-    above meet (1.6e-6 and 0.4e-6 Ha/Bohr); the error follows the SCF's
+    above meet (5e-7 and 4e-7 Ha/Bohr); the error follows the SCF's
     residual at the mixed path's noise floor, amplified by the narrow
     smearing.  Seed 8: every k-point's FP64 SCF converges (19-48
     iterations, the oracle's counts too); some other seeds give k-points
