@@ -273,6 +273,58 @@ def test_pes_host_logic_with_stand_in_engine(monkeypatch):
         kp(xp)
 
 
+def test_kpoint_value_and_grad_host_logic(monkeypatch):
+    """pes.value_and_grad(xp, kpt) over a stand-in k-point engine: one
+    configuration at one k-point gives a scalar and an (n, 3) gradient; a
+    k-mesh or a batch of configurations gives a leading batch axis, with
+    the Ewald term of each configuration (expanded over the mesh when one
+    configuration is shared); the free energy comes back in Rydberg and the
+    Gamma-point call form is refused."""
+    import torch
+    from hqc_gb300 import pes as pes_mod
+
+    def fake_make_solver(n, L, rs, basis, gamma=True, **kw):
+        assert gamma is False and kw.get("forces")
+
+        def batch(xp, kpt, forces=False):
+            x = torch.as_tensor(xp, dtype=torch.float64)
+            k = np.asarray(kpt, dtype=np.float64).reshape(-1, 3)
+            B = max(x.shape[0] if x.dim() == 3 else 1, k.shape[0])
+            xs = x.expand(B, n, 3) if x.dim() == 3 else x.reshape(1, n, 3).expand(B, n, 3)
+            kk = torch.as_tensor(np.broadcast_to(k, (B, 3))[:, 0].copy())
+            # Hartree free energies; gradients already in Ry per rs unit
+            return {"free_energy": xs.sum(dim=(-2, -1)) / 2.0 + kk, "grad": xs + kk[:, None, None]}
+
+        def solver(xp, kpt):
+            raise AssertionError("value_and_grad goes through solver.batch")
+
+        solver.batch = batch
+        return solver
+
+    def fake_vpp(xp, L, rs, kappa=10, Gmax=15):
+        x = torch.as_tensor(xp, dtype=torch.float64)
+        return 100.0 * x.shape[0] * torch.ones((), dtype=torch.float64), torch.full_like(x, 7.0)
+
+    monkeypatch.setattr(pes_mod, "make_solver", fake_make_solver)
+    monkeypatch.setattr(pes_mod, "potential_energy_pp_and_grad", fake_vpp)
+    pes = pes_mod.make_pes(2, 2.0, 1.3, "gth-szv", gamma=False, forces=True)
+    xp = np.array([[0.1, 0.2, 0.3], [0.4, 0.5, 0.6]])
+    F, g = pes.value_and_grad(xp, np.array([0.5, 0.0, 0.0]))
+    assert F.dim() == 0 and g.shape == (2, 3)
+    assert abs(float(F) - ((2.1 / 2.0 + 0.5) * 2.0 + 200.0)) < 1e-12
+    np.testing.assert_allclose(g.numpy(), xp + 0.5 + 7.0)
+    mesh = np.array([[0.1 * k, 0.0, 0.0] for k in range(8)])
+    F, g = pes.value_and_grad(torch.as_tensor(xp), mesh)
+    assert F.shape == (8,) and g.shape == (8, 2, 3)
+    np.testing.assert_allclose(F.numpy(), (2.1 / 2.0 + mesh[:, 0]) * 2.0 + 200.0)
+    xb = np.stack([xp, xp + 1.0])
+    F, g = pes.value_and_grad(xb, np.zeros(3))
+    assert F.shape == (2,) and g.shape == (2, 2, 3)
+    np.testing.assert_allclose(F.numpy(), [2.1 + 200.0, 8.1 + 200.0])
+    with pytest.raises(TypeError):
+        pes.value_and_grad(xp)
+
+
 def test_no_cpu_fallback(monkeypatch, tmp_path):
     """The product path fails loudly instead of falling back to CPU code:
     without the built library the loader raises, and without a GPU the

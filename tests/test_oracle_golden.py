@@ -252,3 +252,20 @@ def test_h54_oracle_run_obeys_translation_sum_rule():
     assert np.abs(g.sum(axis=0)).max() < 1e-6 < 1e-2 < np.abs(g).max()
     # 27 doubly occupied bands below the gap
     assert z["bands"][26] < z["bands"][27]
+
+
+def test_oracle_kpoint_gradient_at_gamma_equals_gamma_gradient():
+    """The oracle's complex (k-point) gradient at k = 0 reproduces its real
+    Gamma-point gradient (Hartree-Fock and PBE, H2 dzv on a 17^3 grid): the
+    conjugations of the Bloch form drop out when the phases are 1."""
+    from oracle.forces import electronic_gradient
+    n, rs = 2, 1.5
+    L = (4 / 3 * np.pi * n) ** (1 / 3)
+    xp = np.array([[0.3, 0.5, 0.4], [1.1, 0.9, 1.3]])
+    for kw in (dict(dft=False), dict(dft=True, xc="pbe")):
+        common = dict(n_grid=17, tol=1e-11, max_cycle=200, **kw)
+        s0 = Solver(n, L, rs, "gth-dzv", **common)
+        s0.solve(xp)
+        sk = Solver(n, L, rs, "gth-dzv", **common)
+        sk.solve(xp, np.zeros(3))
+        np.testing.assert_allclose(electronic_gradient(sk), electronic_gradient(s0), atol=1e-9)
