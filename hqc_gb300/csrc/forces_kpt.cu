@@ -1,4 +1,5 @@
-// Grid parts of the nuclear gradient at a single k-point (FP64, complex).
+// Grid parts of the nuclear gradient at a single k-point (complex; FP64
+// sums).
 //
 // The reference has no forces (doc/solver_algorithm.md:1210).  Its single-k
 // energy (hf_kpt / dft_kpt, hqc/pbc/solver.py:769-962) uses the Bloch AOs
@@ -16,8 +17,9 @@
 // unnormalised transforms of fft_fp64.cu): one forward transform of the four
 // fields X_p conj(psibar_i), d_c phibar_p conj(psibar_i) per AO and orbital
 // and no inverse transform (FP32 transforms with FP64 sums on the mixed
-// plan, as the Gamma-point exchange gradient).  grad phibar and hess phibar are recomputed from
-// the complex 1D factor table of the k-point plan, not stored.
+// plan, as the Gamma-point exchange gradient).  grad phibar and hess phibar
+// are recomputed from the complex 1D factor table of the k-point plan, not
+// stored.
 #include "common.cuh"
 #include "kernels.h"
 #include "zmath.cuh"
