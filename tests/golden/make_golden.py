@@ -98,6 +98,10 @@ SOLVER_CASES = {
                        dict(grid_length=0.2, tol=1e-8, dft=True, xc="lda,hl")),
     "dft_szv_lda_x": ("solver", 4, 1.5, "gth-szv", 7,
                       dict(grid_length=0.2, tol=1e-8, dft=True, xc="lda,")),
+    "dft_szv_lda_bh72": ("solver", 4, 1.5, "gth-szv", 7,
+                         dict(grid_length=0.2, tol=1e-8, dft=True, xc="lda,bh72")),
+    "dft_szv_lda_gl77": ("solver", 4, 1.5, "gth-szv", 7,
+                         dict(grid_length=0.2, tol=1e-8, dft=True, xc="lda,gl77")),
     "dft_dzvp_lda": ("solver", 4, 1.5, "gth-dzvp", 42,
                      dict(grid_length=0.25, tol=1e-8, dft=True, xc="lda,vwn")),
     "hf_h8_dzv_gauss_bisect": ("solver", 8, 1.4, "gth-dzv", 1,

@@ -13,7 +13,8 @@ from oracle.ewald import vpp
 
 CONVERGED = ["hf_szv_diis", "hf_dzv_diis", "hf_dzvp_diis", "hf_dzv_fp", "hf_dzv_fermi_bisect",
              "hf_dzv_fermi_newton", "hf_h8_szv_41", "dft_dzv_lda", "dft_dzv_lda_fermi",
-             "dft_szv_lda_gauss", "dft_szv_lda_hl", "dft_szv_lda_x", "dft_dzvp_lda"]
+             "dft_szv_lda_gauss", "dft_szv_lda_hl", "dft_szv_lda_x", "dft_dzvp_lda",
+             "dft_szv_lda_bh72", "dft_szv_lda_gl77"]
 
 
 def run_case(name):
