@@ -3,7 +3,8 @@
 (hqc/pbc/pes.py:10-153) is used.
 
 The energy and its adjoint gradient come from one XLA FFI call
-(``pes_ffi.cc``: the engine's batched SCF + forces + Ewald on XLA's stream)
+(``pes_ffi.cc``: the engine's batched SCF + forces + Ewald on XLA's stream;
+the Gamma point or a single k-point)
 wrapped in ``jax.custom_vjp``, so ``jax.grad(pes)`` runs the engine's
 adjoint instead of differentiating through the SCF (which the reference
 cannot do either: its ``lax.while_loop`` has no reverse-mode rule).  The
@@ -29,49 +30,78 @@ _registered = False
 
 
 def register(lib_path=os.path.join(HERE, "libhqcgb_jax.so")):
-    """Load the compiled handler and register it as the CUDA target
-    "hqcgb_pes" (once per process)."""
+    """Load the compiled handlers and register them as the CUDA targets
+    "hqcgb_pes" and "hqcgb_pes_kpt" (once per process)."""
     global _registered
     if _registered:
         return
     lib = ctypes.cdll.LoadLibrary(lib_path)
     jax.ffi.register_ffi_target("hqcgb_pes", jax.ffi.pycapsule(lib.HqcgbPes), platform="CUDA")
+    jax.ffi.register_ffi_target("hqcgb_pes_kpt", jax.ffi.pycapsule(lib.HqcgbPesKpt), platform="CUDA")
     _registered = True
 
 
-def make_pes_jax(n, L, rs, basis, Gmax=15, kappa=10, **kw):
+def make_pes_jax(n, L, rs, basis, Gmax=15, kappa=10, gamma=True, **kw):
     """``pes(xp)`` -> F + Vpp (Rydberg) for xp (n, 3) or (B, n, 3) in rs
-    units, differentiable with jax.grad (the engine's adjoint).  Other
+    units, differentiable with jax.grad (the engine's adjoint).  With
+    ``gamma=False``, ``pes(xp, kpt)`` at a single k-point (kpt (3,) or
+    (B, 3) in 1/Bohr, pes_kpt of hqc/pbc/pes.py:88-98); its gradient is
+    taken with respect to xp (the k-point's cotangent is zero).  Other
     keyword arguments as ``make_pes`` (precision, dft, xc, smearing, ...)."""
     register()
-    host = make_pes(n, L, rs, basis, forces=True, Gmax=Gmax, kappa=kappa, **kw)
+    host = make_pes(n, L, rs, basis, forces=True, Gmax=Gmax, kappa=kappa, gamma=gamma, **kw)
     plan = int(host.solver.plan.handle.value)
+    attrs = dict(plan=np.int64(plan), L_rs=np.float64(L), rs=np.float64(rs), kappa=np.float64(kappa),
+                 gmax=np.int64(Gmax))
 
-    def _call(xp):
-        shape = xp.shape
+    def _outs(shape):
         batch = shape[:-2]
         f64 = jnp.float64
-        outs = (jax.ShapeDtypeStruct(batch + (5,), f64), jax.ShapeDtypeStruct(batch, f64),
+        return (jax.ShapeDtypeStruct(batch + (5,), f64), jax.ShapeDtypeStruct(batch, f64),
                 jax.ShapeDtypeStruct(shape, f64), jax.ShapeDtypeStruct(batch, f64),
                 jax.ShapeDtypeStruct(shape, f64), jax.ShapeDtypeStruct(batch, jnp.int32))
-        call = jax.ffi.ffi_call("hqcgb_pes", outs, vmap_method="broadcast_all")
-        energies, free, grad, vpp, vpp_grad, conv = call(
-            xp, xp * rs, plan=np.int64(plan), L_rs=np.float64(L), rs=np.float64(rs),
-            kappa=np.float64(kappa), gmax=np.int64(Gmax))
+
+    def _finish(free, grad, vpp, vpp_grad):
         value = 2.0 * free + vpp                       # Hartree -> Rydberg, + Vpp
         g = 2.0 * rs * grad + vpp_grad                 # Hartree/Bohr -> Rydberg per rs unit
         return value, g
 
-    @jax.custom_vjp
-    def pes(xp):
-        return _call(xp)[0]
+    if gamma:
+        def _call(xp):
+            outs = _outs(xp.shape)
+            call = jax.ffi.ffi_call("hqcgb_pes", outs, vmap_method="broadcast_all")
+            energies, free, grad, vpp, vpp_grad, conv = call(xp, xp * rs, **attrs)
+            return _finish(free, grad, vpp, vpp_grad)
 
-    def fwd(xp):
-        value, g = _call(xp)
-        return value, g
+        @jax.custom_vjp
+        def pes(xp):
+            return _call(xp)[0]
 
-    def bwd(g, ct):
-        return (ct[..., None, None] * g,)
+        def fwd(xp):
+            value, g = _call(xp)
+            return value, g
+
+        def bwd(g, ct):
+            return (ct[..., None, None] * g,)
+    else:
+        def _call(xp, kpt):
+            kpt = jnp.broadcast_to(kpt, xp.shape[:-2] + (3,))
+            outs = _outs(xp.shape)
+            call = jax.ffi.ffi_call("hqcgb_pes_kpt", outs, vmap_method="broadcast_all")
+            energies, free, grad, vpp, vpp_grad, conv = call(xp, xp * rs, kpt, **attrs)
+            return _finish(free, grad, vpp, vpp_grad)
+
+        @jax.custom_vjp
+        def pes(xp, kpt):
+            return _call(xp, kpt)[0]
+
+        def fwd(xp, kpt):
+            value, g = _call(xp, kpt)
+            return value, (g, kpt)
+
+        def bwd(res, ct):
+            g, kpt = res
+            return ct[..., None, None] * g, jnp.zeros_like(kpt)
 
     pes.defvjp(fwd, bwd)
     pes.host = host

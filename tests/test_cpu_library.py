@@ -364,25 +364,28 @@ def test_plain_c_client_links_and_runs(tmp_path):
 
 
 def test_jax_ffi_handler_matches_its_python_wrapper():
-    """The XLA FFI handler (hqc_gb300/jax_ffi/pes_ffi.cc, compiled only where
-    jaxlib is installed) and the ffi_call in hqc_gb300/jax_ffi/__init__.py
+    """The XLA FFI handlers (hqc_gb300/jax_ffi/pes_ffi.cc, compiled only where
+    jaxlib is installed) and the ffi_calls in hqc_gb300/jax_ffi/__init__.py
     agree on the call signature: the same attribute names, as many results
-    as the wrapper declares, two positional arguments."""
+    as the wrapper declares, two positional arguments at the Gamma point and
+    three (with the k-points) for the single-k form."""
     import re
     src = open(os.path.join(ROOT, "hqc_gb300", "jax_ffi", "pes_ffi.cc")).read()
     py = open(os.path.join(ROOT, "hqc_gb300", "jax_ffi", "__init__.py")).read()
-    bind = src[src.index("XLA_FFI_DEFINE_HANDLER_SYMBOL"):]
-    attrs = re.findall(r'\.Attr<[^>]+>\("(\w+)"\)', bind)
-    assert attrs == ["plan", "L_rs", "rs", "kappa", "gmax"]
-    for a in attrs:
-        assert re.search(rf"\b{a}=np\.", py), a
-    n_ret = len(re.findall(r"\.Ret<", bind))
-    n_out = py[py.index("outs = ("):py.index("call = jax.ffi.ffi_call")].count("ShapeDtypeStruct(")
-    assert n_ret == n_out == 6
-    assert len(re.findall(r"\.Arg<", bind)) == 2
-    # the handler's results are the ABI's outputs: hqcgb_pes_batch + hqcgb_ewald
+    n_out = py[py.index("def _outs("):py.index("def _finish(")].count("ShapeDtypeStruct(")
+    for symbol, target, n_args in (("HqcgbPes", "hqcgb_pes", 2), ("HqcgbPesKpt", "hqcgb_pes_kpt", 3)):
+        start = src.index(f"XLA_FFI_DEFINE_HANDLER_SYMBOL({symbol},")
+        bind = src[start:src.index(");", start)]
+        attrs = re.findall(r'\.Attr<[^>]+>\("(\w+)"\)', bind)
+        assert attrs == ["plan", "L_rs", "rs", "kappa", "gmax"]
+        for a in attrs:
+            assert re.search(rf"\b{a}=np\.", py), a
+        assert len(re.findall(r"\.Ret<", bind)) == n_out == 6
+        assert len(re.findall(r"\.Arg<", bind)) == n_args
+        assert f'"{target}"' in py and f"lib.{symbol})" in py
+    # the handlers' results are the ABI's outputs: the PES batches + hqcgb_ewald
     hdr = open(os.path.join(ROOT, "include", "hqcgb.h")).read()
-    for fn in ("hqcgb_pes_batch", "hqcgb_ewald", "hqcgb_last_error"):
+    for fn in ("hqcgb_pes_batch", "hqcgb_pes_kpt_batch", "hqcgb_ewald", "hqcgb_last_error"):
         assert fn in src and fn in hdr
 
 
