@@ -218,6 +218,23 @@ def test_autograd_wrapper_chains_engine_gradient():
     torch.testing.assert_close(gb, w[:, None, None] * 3 * xb.detach() ** 2)
     assert FakePes.calls == 2  # one engine call per forward, none in backward
 
+    class FakeKpes:
+        def value_and_grad(self, xp, kpt):
+            x = torch.as_tensor(xp, dtype=torch.float64)
+            k = torch.as_tensor(kpt, dtype=torch.float64).reshape(-1, 3)[:, 0]
+            E = (x ** 3).sum(dim=(-2, -1)) * (1 + k)
+            g = 3 * x ** 2 * (1 + k)[:, None, None]
+            return (E[0], g[0]) if torch.as_tensor(kpt).dim() == 1 else (E, g)
+
+    kp = FakeKpes()
+    (gk,) = torch.autograd.grad(pes_energy(x1, kp, [0.5, 0.0, 0.0]), x1)
+    torch.testing.assert_close(gk, 1.5 * 3 * x1.detach() ** 2)
+    mesh = torch.tensor([[0.0, 0, 0], [1.0, 0, 0]], dtype=torch.float64)
+    Em = pes_energy(x1, kp, mesh)
+    assert Em.shape == (2,)
+    (gm,) = torch.autograd.grad(Em.sum(), x1)  # both k-points act on the same positions
+    torch.testing.assert_close(gm, (1.0 + 2.0) * 3 * x1.detach() ** 2)
+
 
 
 def test_pes_host_logic_with_stand_in_engine(monkeypatch):
