@@ -17,9 +17,10 @@ reference's rhoG/ERI formulation (``hqc/pbc/solver.py:391-479``).
 Parity pin: ``tests/golden/*.npz`` hold outputs of the reference's own
 unmodified source, executed by ``tests/golden/make_golden.py`` over a NumPy
 stand-in for the JAX API subset it uses.  ``tests/test_oracle_golden.py``
-checks this oracle against those vectors.  The features the reference lacks
-(GGA-PBE, analytic forces) are checked by internal identities only and are
-"parity unpinned": forces against central finite differences of the
-oracle's own energy, PBE against the constraints it was built to satisfy
-(``tests/test_oracle_xc.py``).
+checks this oracle against those vectors.  Analytic forces, which the
+reference lacks, are pinned to central finite differences of the
+reference's own energies (``pes_gamma`` and ``pes_kpt``, differenced by
+``make_golden.py``) and of the oracle's own energy.  GGA-PBE, also absent
+from the reference, is checked against the constraints it was built to
+satisfy (``tests/test_oracle_xc.py``): "parity unpinned".
 """

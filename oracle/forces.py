@@ -1,4 +1,5 @@
-"""Oracle: analytic nuclear gradient of the GPW SCF energy (Gamma point).
+"""Oracle: analytic nuclear gradient of the GPW SCF energy (Gamma point and
+single k-point).
 
 The reference has no forces (``doc/solver_algorithm.md:1210``); this is a new
 FP64 CPU restatement used to check the GPU adjoint (parity unpinned; pinned by
