@@ -36,6 +36,12 @@ def test_last_error_and_bad_args_without_gpu():
     st = lib.hqcgb_plan_create(ctypes.byref(P), ctypes.byref(h))
     assert st == 2  # HQCGB_BAD_ARG, validated before any device call
     assert b"n_atoms" in lib.hqcgb_last_error()
+    # the k-point force entry points refuse null plans and outputs the same way
+    assert lib.hqcgb_forces_kpt(None, None, None) == 2
+    assert b"null" in lib.hqcgb_last_error()
+    out = _lib.ScfOut()
+    assert lib.hqcgb_pes_kpt_batch(None, 1, None, None, ctypes.byref(out), None, None) == 2
+    assert b"null" in lib.hqcgb_last_error()
 
 
 @pytest.mark.parametrize("basis", ["gth-szv", "gth-dzv", "gth-dzvp", "gth-tzv2p", "gth-qzv2p"])
